@@ -1,0 +1,143 @@
+/* nlfem_gpu.h - C ABI of the GB300 nonlocal assembly library (libnlfem_gpu.so).
+ *
+ * Drop-in boundary for nlfem's assembly path. Every entry point takes plain pointers and
+ * sizes (row-major, int64 indices as the reference's `long`), returns an nlfem status code
+ * instead of aborting, and runs its arithmetic on the GPU (sm_103a). No CPU fallback exists:
+ * without a usable CUDA device every compute entry point returns NLFEM_ERR_CUDA.
+ *
+ * Reference interfaces replaced (cagau/nlfem):
+ *   nlfem_par_assemble        <- par_assemble         include/Cassemble.h:125-140,
+ *                                                      bound by include/Cassemble.pxd:12-25
+ *   nlfem_stiffness_matrix    <- par_system           include/Cassemble.h:171 (+ nlfem.pyx:128-274
+ *                                                      read-back, in memory instead of a file)
+ *   nlfem_load_vector         <- par_forcing          include/Cassemble.h:182 (+ nlfem.pyx:276-389)
+ *   nlfem_method_retriangulate<- method_retriangulate include/Cassemble.h:62-64, Cassemble.pxd:32-34
+ *   nlfem_toRef               <- toRef                include/Cassemble.h:68, Cassemble.pxd:38
+ *   nlfem_toPhys              <- toPhys(E,p,dim,out)  include/Cassemble.h:70, Cassemble.pxd:39
+ *   nlfem_solve2x2            <- solve2x2             include/Cassemble.h:71, Cassemble.pxd:40
+ *   nlfem_stiffness_batch     <- (no counterpart: many independent par_system calls in one pass)
+ *   nlfem_pair_list           <- (no counterpart: exposes the BFS interaction pairs of par_system,
+ *                                 src/Cassemble.cpp:595-783, for parity checks)
+ *   nlfem_pair_blocks         <- (no counterpart: the four local blocks integrate() returns,
+ *                                 src/integration.cpp:67-79, for explicit pairs)
+ */
+#ifndef NLFEM_GPU_H
+#define NLFEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NLFEM_OK 0
+#define NLFEM_ERR_INVALID 1     /* bad argument or configuration (the reference aborts) */
+#define NLFEM_ERR_CUDA 2        /* no device, launch or runtime failure */
+#define NLFEM_ERR_NOMEM 3       /* device or host allocation failed */
+#define NLFEM_ERR_UNSUPPORTED 4 /* option outside the implemented set */
+#define NLFEM_ERR_NUMERIC 5     /* degenerate element (solve2x2 would abort in the reference) */
+#define NLFEM_ERR_TIMEOUT 6     /* a bounded device wait ran out */
+
+/* arithmetic of the quadrature */
+#define NLFEM_PREC_FP64 0       /* all FP64, the reference's arithmetic */
+#define NLFEM_PREC_MIXED 1      /* FP32 quadrature, FP64 cut geometry and accumulation */
+
+/* One assembly problem. Arrays are borrowed host pointers, row-major. */
+typedef struct nlfem_problem {
+    int dim;                     /* 2 or 3 */
+    int outdim;                  /* 1 (vector-valued kernels are not implemented) */
+    int is_dg;                   /* 0: continuous P1 (K = nV), 1: discontinuous (K = nE*(dim+1)) */
+    long nE, nV;
+    const long *elements;        /* (nE, dim+1) vertex indices */
+    const long *elementLabels;   /* (nE,) >0 domain, <0 Dirichlet layer, 0 bridge only */
+    const double *vertices;      /* (nV, dim) */
+    const long *vertexLabels;    /* (nV,) rows with label <= 0 are not assembled (CG) */
+    const double *Px; int nPx; const double *dx;   /* outer rule on the reference element */
+    const double *Py; int nPy; const double *dy;   /* inner rule */
+    const double *Pg; int tensorGaussDegree; const double *dg; /* [-1,1]^4 tensor rule (singular) */
+    double sqdelta;              /* squared horizon */
+    double fractional_s;         /* s of the fractional kernel, -1 if unused */
+    const char *kernel;          /* "constant", "parabola", "fractional", "constant3D" */
+    const char *forcing;         /* "linear", "linear3D", "constant" */
+    const char *method_remote;   /* "retriangulate" or "baryCenter" */
+    const char *method_close;    /* "fractional" or NULL (= method_remote) */
+    int is_PlacePointOnCap;
+    int is_fullConnectedComponentSearch;
+    int precision;               /* NLFEM_PREC_FP64 or NLFEM_PREC_MIXED */
+    int verbose;
+} nlfem_problem;
+
+/* CSR matrix owned by the library; release with nlfem_csr_free. */
+typedef struct nlfem_csr {
+    long K;
+    long nnz;
+    long *indptr;   /* K+1 */
+    long *indices;  /* nnz, ascending within a row */
+    double *values; /* nnz */
+} nlfem_csr;
+
+/* Run statistics of the last assembly on this thread. */
+typedef struct nlfem_stats {
+    long n_pairs;        /* interacting ordered element pairs (contributing integrate() calls) */
+    long n_candidates;   /* integrate() calls of the BFS, interacting or not */
+    long n_close;        /* pairs integrated with the singular close-pair rule */
+    long nnz_structural; /* slots before exact zeros are dropped */
+    double ms_total;     /* device time of the assembly (CUDA events) */
+    double ms_bfs, ms_pattern, ms_quad, ms_finish;
+} nlfem_stats;
+
+const char *nlfem_last_error(void);
+int nlfem_device_count(void);
+int nlfem_get_stats(nlfem_stats *out);
+
+/* Stiffness matrix of one problem, host in / host out (the nlfem.stiffnessMatrix path). */
+int nlfem_stiffness_matrix(const nlfem_problem *prob, nlfem_csr *out);
+/* Load vector (K doubles written to fd; the nlfem.loadVector path). */
+int nlfem_load_vector(const nlfem_problem *prob, double *fd);
+/* Many independent problems in one pass; outs[i] receives problem i's matrix. */
+int nlfem_stiffness_batch(const nlfem_problem *probs, int n, nlfem_csr *outs);
+void nlfem_csr_free(nlfem_csr *m);
+
+/* Device-resident sessions: upload once, assemble many times (benchmarks, repeated solves). */
+typedef struct nlfem_session nlfem_session;
+int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out);
+int nlfem_session_assemble(nlfem_session *s);            /* inputs already in HBM */
+int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out);
+void nlfem_session_destroy(nlfem_session *s);
+
+/* The interacting pairs (aT, bT) of the BFS, sorted by (aT, bT). Free *pairs with free(). */
+int nlfem_pair_list(const nlfem_problem *prob, long *n_pairs, long **pairs);
+/* Local blocks (termLocal, termNonloc, termLocalPrime, termNonlocPrime) of explicit pairs:
+ * out (n, 4, dim+1, dim+1); does_interact (n,). close != 0 selects the close-pair rule. */
+int nlfem_pair_blocks(const nlfem_problem *prob, long n, const long *pairs, int close,
+                      double *out, int *does_interact);
+
+/* Geometry primitives of the Python debug hooks (cython/nlfem.pyx:712-771), on the GPU. */
+int nlfem_method_retriangulate(const double *x_center, const double *TE, double sqdelta,
+                               double *reTriangleList, int is_placePointOnCap);
+int nlfem_retriangulate_batch(long n, const double *x_center, const double *TE, double sqdelta,
+                              int is_placePointOnCap, int *counts, double *reTriangleList);
+int nlfem_toRef(const double *E, const double *phys_x, double *ref_p);
+int nlfem_toPhys(const double *E, const double *p, int dim, double *out_x);
+int nlfem_solve2x2(const double *A, const double *b, double *x);
+
+/* C twin of par_assemble (include/Cassemble.h:125-140) with C strings. Writes the arma binary
+ * files the unchanged nlfem.pyx reads back (ARMA_SPM_BIN_FN008 for "system" holding A^T in CSC,
+ * ARMA_MAT_BIN_FN008 for "forcing"). Returns a status instead of aborting. */
+int nlfem_par_assemble(const char *compute, const char *path_spAd, const char *path_fd,
+                       int K_Omega, int K, const long *ptrTriangles, const long *ptrLabelTriangles,
+                       const double *ptrVerts, const long *ptrLabelVerts, int nE, int nE_Omega,
+                       int nV, int nV_Omega, const double *Px, int nPx, const double *dx,
+                       const double *Py, int nPy, const double *dy, double sqdelta,
+                       int is_DiscontinuousGalerkin, int is_NeumannBoundary,
+                       const char *str_model_kernel, const char *str_model_f,
+                       const char *str_integration_method_remote,
+                       const char *str_integration_method_close, int is_PlacePointOnCap,
+                       int dim, int outdim, const long *ptrZetaIndicator_indices,
+                       const long *ptrZetaIndicator_indptr, long nZeta, const double *Pg,
+                       int degree, const double *dg, double maxDiameter, double fractional_s,
+                       int is_fullConnectedComponentSearch, int verbose);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NLFEM_GPU_H */

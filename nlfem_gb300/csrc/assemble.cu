@@ -1,0 +1,596 @@
+// GB300 (sm_103a) nonlocal stiffness-matrix / load-vector assembly.
+//
+// Pipeline of one assembly (all on the device, one stream):
+//   prep      int64 mesh -> int32 connectivity, element coordinates, |det| (FP64)
+//   dual      vertex->element incidence and vertex-sharing element adjacency (replaces
+//             METIS_MeshToDual(ncommon=1), src/Cassemble.cpp:391-417)
+//   bfs       one warp per outer element: breadth-first search over the dual graph with the
+//             bit-exact interaction predicate (src/Cassemble.cpp:595-783); emits the ordered
+//             interacting pairs (aT, bT)
+//   pairs     compaction into aT-major pair arrays; transposed (bT-major) lists
+//   pattern   CSR sparsity pattern: row u collects the vertices of every element touching an
+//             element incident to u (src/Cassemble.cpp:721-770 index rules)
+//   quad      per-pair quadrature of the four local blocks (src/integration.cpp) and their
+//             scatter into CSR slots through 128-bit fixed-point atomics (order independent,
+//             so run-to-run identical)
+//   finish    fixed point -> FP64, exact zeros dropped (arma::sp_mat semantics)
+#include "../../include/nlfem_gpu.h"
+#include "geometry.cuh"
+#include "primitives.cuh"
+#include "quadrature.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace nlg {
+
+// ======================================================================= device kernels
+__device__ __forceinline__ int find_prob(const int *off, int n, long long e) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if ((long long)off[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int DIM>
+__global__ void k_prep_elements(const long long *__restrict__ T64, const long long *__restrict__ lab64,
+                                const double *__restrict__ V, const int *__restrict__ eoff,
+                                const int *__restrict__ voff, int nProb, long long nE,
+                                int *__restrict__ T32, int *__restrict__ labT, int *__restrict__ eprob,
+                                double *__restrict__ EC, double *__restrict__ adet) {
+    constexpr int dV = DIM + 1;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    const int p = find_prob(eoff, nProb, e);
+    const int vo = voff[p];
+    double E[DIM * dV];
+#pragma unroll
+    for (int k = 0; k < dV; k++) {
+        int v = (int)T64[e * dV + k] + vo;
+        T32[e * dV + k] = v;
+#pragma unroll
+        for (int j = 0; j < DIM; j++) {
+            E[DIM * k + j] = V[(long long)v * DIM + j];
+            EC[e * DIM * dV + DIM * k + j] = E[DIM * k + j];
+        }
+    }
+    long long l = lab64[e];
+    labT[e] = (int)(l > 2147483647LL ? 2147483647LL : (l < -2147483647LL ? -2147483647LL : l));
+    eprob[e] = p;
+    // absDet(E, dim) with the cofactor determinant (mathhelpers.cpp:112-129)
+    double det;
+    if (DIM == 2) {
+        double a = xsub(E[2], E[0]), b = xsub(E[4], E[0]);
+        double c = xsub(E[3], E[1]), d = xsub(E[5], E[1]);
+        det = xsub(xmul(a, d), xmul(c, b));
+    } else {
+        double M[3][3];
+        for (int i = 1; i < 4; i++)
+            for (int j = 0; j < 3; j++) M[j][i - 1] = xsub(E[j + 3 * i], E[j]);
+        double c0 = xsub(xmul(M[1][1], M[2][2]), xmul(M[1][2], M[2][1]));
+        double c1 = xsub(xmul(M[1][0], M[2][2]), xmul(M[1][2], M[2][0]));
+        double c2 = xsub(xmul(M[1][0], M[2][1]), xmul(M[1][1], M[2][0]));
+        det = xadd(xsub(xmul(M[0][0], c0), xmul(M[0][1], c1)), xmul(M[0][2], c2));
+    }
+    adet[e] = fabs(det);
+}
+
+__global__ void k_prep_vertices(const long long *__restrict__ lab64, const int *__restrict__ voff,
+                                int nProb, long long nV, int *__restrict__ labV, int *__restrict__ vprob) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    long long l = lab64[v];
+    labV[v] = (int)(l > 2147483647LL ? 2147483647LL : (l < -2147483647LL ? -2147483647LL : l));
+    vprob[v] = find_prob(voff, nProb, v);
+}
+
+// ------------------------------------------------------------------ dual graph
+__global__ void k_vinc_count(const int *__restrict__ T32, long long n, int *__restrict__ vcnt) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&vcnt[T32[i]], 1);
+}
+__global__ void k_vinc_fill(const int *__restrict__ T32, long long n, int dV,
+                            const long long *__restrict__ vptr, int *__restrict__ vfill,
+                            int *__restrict__ vel) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int v = T32[i];
+    long long pos = vptr[v] + atomicAdd(&vfill[v], 1);
+    vel[pos] = (int)(i / dV);
+}
+__global__ void k_vinc_sort(const long long *__restrict__ vptr, long long nV, int *__restrict__ vel) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    long long b = vptr[v], e = vptr[v + 1];
+    for (long long i = b + 1; i < e; i++) {
+        int x = vel[i];
+        long long j = i - 1;
+        while (j >= b && vel[j] > x) { vel[j + 1] = vel[j]; j--; }
+        vel[j + 1] = x;
+    }
+}
+
+constexpr int MAX_ADJ_CAND = 320;
+
+template <int DIM>
+__global__ void k_adjacency(const int *__restrict__ T32, long long nE, const long long *__restrict__ vptr,
+                            const int *__restrict__ vel, const long long *__restrict__ xadj,
+                            int *__restrict__ cnt, int *__restrict__ adj, int *__restrict__ err) {
+    constexpr int dV = DIM + 1;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    int c[MAX_ADJ_CAND];
+    int n = 0;
+    for (int k = 0; k < dV; k++) {
+        int v = T32[e * dV + k];
+        for (long long j = vptr[v]; j < vptr[v + 1]; j++) {
+            int o = vel[j];
+            if (o == (int)e) continue;
+            if (n >= MAX_ADJ_CAND) { atomicOr(err, 1); return; }
+            // insertion into sorted unique list
+            int i = n - 1;
+            bool dup = false;
+            while (i >= 0 && c[i] >= o) { if (c[i] == o) { dup = true; break; } i--; }
+            if (dup) continue;
+            for (int t = n; t > i + 1; t--) c[t] = c[t - 1];
+            c[i + 1] = o;
+            n++;
+        }
+    }
+    if (!adj) { cnt[e] = n; return; }
+    long long o = xadj[e];
+    for (int i = 0; i < n; i++) adj[o + i] = c[i];
+}
+
+// ------------------------------------------------------------------ BFS pair search
+constexpr int BFS_THREADS = 256;
+constexpr int BFS_WARPS = BFS_THREADS / 32;
+
+struct BfsArgs {
+    const int *T32, *labT, *eprob, *adj;
+    const long long *xadj;
+    const double *EC;
+    const ProbParams *probs;
+    long long nE;
+    unsigned *visited;       // nwarps * vstride
+    long long vstride;
+    int *queue;              // nwarps * qcap
+    long long qcap;
+    int *pool;               // pool of bT per aT segment
+    long long pool_cap;
+    unsigned long long *pool_cursor;
+    long long *seg_start;
+    int *seg_cnt;
+    unsigned long long *n_cand;
+    int *err;                // [0] queue overflow, [1] pool overflow, [2] bad method
+    long long *qneed;
+};
+
+// Interaction predicate of integrate(aT, bT) for the configured method: the return value of
+// integrate_retriangulate / integrate_baryCenter / integrate_fractional (integration.cpp:539,
+// 1017, 287), OR'ed with is_fullConnectedComponentSearch.
+template <int DIM>
+__device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method, const double *xs,
+                                                int nPx, const double *Eb) {
+    if (P.full_search) return true;
+    if (method == MTH_FRACTIONAL) return true;
+    if (method == MTH_BARYCENTER) {
+        double b[DIM];
+        xbary<DIM>(Eb, b);
+        for (int k = 0; k < nPx; k++)
+            if (xbaryInside<DIM>(&xs[DIM * k], b, P.sqdelta)) return true;
+        return false;
+    }
+    if (DIM == 2) {
+        double R[18];
+        for (int k = 0; k < nPx; k++)
+            if (xretriangulate(&xs[2 * k], Eb, P.sqdelta, P.caps, R) >= 3) return true;
+    }
+    return false;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
+    constexpr int dV = DIM + 1;
+    __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * BFS_WARPS + wib;
+    const long long nw = (long long)gridDim.x * BFS_WARPS;
+    unsigned *visited = a.visited + gw * a.vstride;
+    int *queue = a.queue + gw * a.qcap;
+    double *xs = s_x[wib];
+    unsigned long long cand_local = 0;
+    for (long long aT = gw; aT < a.nE; aT += nw) {
+        const int lab = a.labT[aT];
+        if (lab == 0) {
+            if (lane == 0) { a.seg_cnt[aT] = 0; a.seg_start[aT] = 0; }
+            continue;
+        }
+        const ProbParams P = a.probs[a.eprob[aT]];
+        const long long eoff = P.elem_off;
+        const unsigned stamp = (unsigned)aT + 1u;   // unique over all problems
+        const double *Ea = &a.EC[aT * DIM * dV];
+        for (int k = lane; k < rule.nPx; k += 32) xtoPhys<DIM>(Ea, &rule.Px[DIM * k], &xs[DIM * k]);
+        __syncwarp();
+        // (aT, aT): the first candidate of the first dequeued element (Cassemble.cpp:621)
+        bool self_pair = false;
+        if (lane == 0) {
+            visited[aT - eoff] = stamp;
+            self_pair = interacts_exact<DIM>(P, P.singular ? P.close : P.remote, xs, rule.nPx, Ea);
+            queue[0] = (int)aT;
+        }
+        self_pair = __shfl_sync(FULL, self_pair, 0);
+        cand_local += (lane == 0);
+        long long qhead = 0, qtail = 1;
+        int level = 0;
+        bool overflow = false;
+        while (qhead < qtail) {
+            const long long lvl_end = qtail;
+            const int method = (P.singular && level == 0) ? P.close : P.remote;
+            for (long long g = qhead; g < lvl_end; g += 32) {
+                long long gi = g + lane;
+                int s = gi < lvl_end ? queue[gi] : -1;
+                if (s < -1) s = -s - 2;   // label-0 bridge stored as -(e+2)
+                long long beg = 0;
+                int deg = 0;
+                if (s >= 0) { beg = a.xadj[s]; deg = (int)(a.xadj[s + 1] - beg); }
+                const int incl = warp_incl_scan(deg, lane);
+                const int total = __shfl_sync(FULL, incl, 31);
+                const int excl = incl - deg;
+                for (int c0 = 0; c0 < total; c0 += 32) {
+                    const int c = c0 + lane;
+                    // owner lane j: largest j with excl_j <= c
+                    int lo = 0, hi = 31;
+#pragma unroll
+                    for (int it = 0; it < 5; it++) {
+                        int mid = (lo + hi + 1) >> 1;
+                        int em = __shfl_sync(FULL, excl, mid);
+                        if (em <= c) lo = mid; else hi = mid - 1;
+                    }
+                    const long long bj = __shfl_sync(FULL, beg, lo);
+                    const int ej = __shfl_sync(FULL, excl, lo);
+                    int cand = -1;
+                    if (c < total) cand = a.adj[bj + (c - ej)];
+                    bool push = false, pair = false, bridge = false;
+                    if (cand >= 0) {
+                        unsigned old = atomicExch(&visited[cand - eoff], stamp);
+                        if (old != stamp) {
+                            if (a.labT[cand] != 0) {
+                                cand_local++;
+                                pair = interacts_exact<DIM>(P, method, xs, rule.nPx, &a.EC[(long long)cand * DIM * dV]);
+                                push = pair;
+                            } else {
+                                push = true;
+                                bridge = true;
+                            }
+                        }
+                    }
+                    const unsigned m = __ballot_sync(FULL, push);
+                    const long long pos = qtail + __popc(m & lanemask_lt());
+                    if (push) {
+                        if (pos < a.qcap) queue[pos] = bridge ? -(cand + 2) : cand;
+                        else overflow = true;
+                    }
+                    qtail += __popc(m);
+                }
+                if (__any_sync(FULL, overflow)) break;
+            }
+            if (__any_sync(FULL, overflow)) break;
+            qhead = lvl_end;
+            level++;
+        }
+        overflow = __any_sync(FULL, overflow);
+        if (overflow) {
+            if (lane == 0) {
+                atomicOr(&a.err[0], 1);
+                atomicMax((unsigned long long *)a.qneed, (unsigned long long)(qtail + 1));
+                a.seg_cnt[aT] = 0;
+                a.seg_start[aT] = 0;
+            }
+            continue;
+        }
+        // pairs: queue entries that interacted (queue[0] = aT only if (aT, aT) interacts)
+        int npairs = 0;
+        for (long long g = 0; g < qtail; g += 32) {
+            long long gi = g + lane;
+            bool isp = false;
+            if (gi < qtail) {
+                int s = queue[gi];
+                isp = (gi == 0) ? self_pair : (s >= 0);
+            }
+            npairs += __popc(__ballot_sync(FULL, isp));
+        }
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.pool_cursor, (unsigned long long)npairs);
+        base = __shfl_sync(FULL, base, 0);
+        const bool fits = base + npairs <= (unsigned long long)a.pool_cap;
+        if (lane == 0) {
+            a.seg_cnt[aT] = npairs;
+            a.seg_start[aT] = (long long)base;
+            if (!fits) atomicOr(&a.err[1], 1);
+        }
+        if (fits) {
+            int w = 0;
+            for (long long g = 0; g < qtail; g += 32) {
+                long long gi = g + lane;
+                bool isp = false;
+                int s = -1;
+                if (gi < qtail) {
+                    s = queue[gi];
+                    isp = (gi == 0) ? self_pair : (s >= 0);
+                }
+                const unsigned m = __ballot_sync(FULL, isp);
+                if (isp) a.pool[base + w + __popc(m & lanemask_lt())] = s;
+                w += __popc(m);
+            }
+        }
+    }
+    cand_local = warp_sum(cand_local);
+    if (lane == 0 && cand_local) atomicAdd(a.n_cand, cand_local);
+}
+
+// aT-major compaction of the BFS segments.
+__global__ void k_compact_pairs(const long long *__restrict__ seg_start, const int *__restrict__ seg_cnt,
+                                const long long *__restrict__ out_ptr, const int *__restrict__ pool,
+                                long long nE, int *__restrict__ pA, int *__restrict__ pB) {
+    const int lane = threadIdx.x & 31;
+    long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (e >= nE) return;
+    const int n = seg_cnt[e];
+    const long long s = seg_start[e], o = out_ptr[e];
+    for (int i = lane; i < n; i += 32) {
+        pA[o + i] = (int)e;
+        pB[o + i] = pool[s + i];
+    }
+}
+
+__global__ void k_in_count(const int *__restrict__ pB, long long P, int *__restrict__ incnt) {
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) atomicAdd(&incnt[pB[p]], 1);
+}
+__global__ void k_in_fill(const int *__restrict__ pA, const int *__restrict__ pB, long long P,
+                          const long long *__restrict__ in_ptr, int *__restrict__ infill,
+                          int *__restrict__ inA) {
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    int b = pB[p];
+    long long pos = in_ptr[b] + atomicAdd(&infill[b], 1);
+    inA[pos] = pA[p];
+}
+
+// ------------------------------------------------------------------ CSR pattern
+struct RowArgs {
+    const int *T32, *labT, *labV, *vprob, *vel, *pB, *inA;
+    const long long *vptr, *out_ptr, *in_ptr;
+    const ProbParams *probs;
+    long long nV;
+    unsigned *marks;       // nwarps * mstride
+    long long mstride;
+    const long long *rowptr;   // fill mode
+    int *cols;                 // fill mode (null: count mode)
+    int *rowcnt;               // count mode
+};
+
+// One warp per row (vertex) u with label > 0: union of the vertices of every element that
+// shares a pair with an element incident to u.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_row_pattern(RowArgs a, int pass) {
+    constexpr int dV = DIM + 1;
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    unsigned *marks = a.marks + gw * a.mstride;
+    for (long long u = gw; u < a.nV; u += nw) {
+        const bool keep = a.labV[u] > 0;
+        if (!keep) {
+            if (!a.cols && lane == 0) a.rowcnt[u] = 0;
+            continue;
+        }
+        const int voff = a.probs[a.vprob[u]].vert_off;
+        const unsigned stamp = (unsigned)(2 * u + 1 + pass);   // unique per row and pass
+        long long w = 0;
+        const long long rbase = a.cols ? a.rowptr[u] : 0;
+        for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
+            const int T = a.vel[t];
+            const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
+            const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
+            if (oe == ob && ie == ib) continue;
+            const long long nEl = 1 + (oe - ob) + (ie - ib);
+            const long long nItems = nEl * dV;
+            for (long long i0 = 0; i0 < nItems; i0 += 32) {
+                const long long i = i0 + lane;
+                bool isnew = false;
+                int v = 0;
+                if (i < nItems) {
+                    const long long el_i = i / dV;
+                    const int k = (int)(i - el_i * dV);
+                    int el;
+                    if (el_i == 0) el = T;
+                    else if (el_i <= oe - ob) el = a.pB[ob + el_i - 1];
+                    else el = a.inA[ib + (el_i - 1 - (oe - ob))];
+                    v = a.T32[(long long)el * dV + k];
+                    unsigned old = atomicExch(&marks[v - voff], stamp);
+                    isnew = old != stamp;
+                }
+                const unsigned m = __ballot_sync(FULL, isnew);
+                if (a.cols && isnew) a.cols[rbase + w + __popc(m & lanemask_lt())] = v;
+                w += __popc(m);
+            }
+        }
+        if (!a.cols && lane == 0) a.rowcnt[u] = (int)w;
+    }
+}
+
+// Sort each row's columns (bitonic network in shared memory, padded with INT_MAX).
+__global__ void k_row_sort(const long long *__restrict__ rowptr, long long nV, int *__restrict__ cols,
+                           int cap) {
+    extern __shared__ int sh[];
+    for (long long u = blockIdx.x; u < nV; u += gridDim.x) {
+        const long long b = rowptr[u];
+        const int n = (int)(rowptr[u + 1] - b);
+        if (n <= 1) continue;
+        int n2 = 1;
+        while (n2 < n) n2 <<= 1;
+        int *s = (n2 <= cap) ? sh : nullptr;
+        if (!s) continue;  // longer rows are sorted by k_row_sort_global
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? cols[b + i] : 0x7fffffff;
+        __syncthreads();
+        for (int k = 2; k <= n2; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        int x = s[i], y = s[ixj];
+                        bool up = (i & k) == 0;
+                        if ((x > y) == up) { s[i] = y; s[ixj] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) cols[b + i] = s[i];
+        __syncthreads();
+    }
+}
+// Fallback for rows longer than the shared-memory cap: odd-even transposition in global memory.
+__global__ void k_row_sort_global(const long long *__restrict__ rowptr, long long nV,
+                                  int *__restrict__ cols, int cap) {
+    for (long long u = blockIdx.x; u < nV; u += gridDim.x) {
+        const long long b = rowptr[u];
+        const int n = (int)(rowptr[u + 1] - b);
+        int n2 = 1;
+        while (n2 < n) n2 <<= 1;
+        if (n <= 1 || n2 <= cap) continue;
+        for (int phase = 0; phase < n; phase++) {
+            for (int i = 2 * threadIdx.x + (phase & 1); i + 1 < n; i += 2 * blockDim.x) {
+                int x = cols[b + i], y = cols[b + i + 1];
+                if (x > y) { cols[b + i] = y; cols[b + i + 1] = x; }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ------------------------------------------------------------------ finish
+// Per row: fixed point -> FP64 and count of kept entries (nonzero sum, or a nonzero contribution
+// too small for the fixed-point grid).
+__global__ void k_finish_count(const long long *__restrict__ rowptr, long long nV,
+                               const unsigned long long *__restrict__ acc, const unsigned *__restrict__ tiny,
+                               const int *__restrict__ vprob, const ProbParams *__restrict__ probs,
+                               double *__restrict__ vals, int *__restrict__ keepcnt) {
+    const int lane = threadIdx.x & 31;
+    long long u = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= nV) return;
+    const int se = probs[vprob[u]].scale_exp;
+    const long long b = rowptr[u], e = rowptr[u + 1];
+    int cnt = 0;
+    for (long long i = b + lane; i < e; i += 32) {
+        unsigned long long lo = acc[2 * i], hi = acc[2 * i + 1];
+        double d = fx_to_double(lo, hi, se);
+        vals[i] = d;
+        cnt += ((lo | hi) != 0ULL) || tiny[i];
+    }
+    cnt = warp_sum(cnt);
+    if (lane == 0) keepcnt[u] = cnt;
+}
+__global__ void k_finish_compact(const long long *__restrict__ rowptr, long long nV,
+                                 const unsigned long long *__restrict__ acc, const unsigned *__restrict__ tiny,
+                                 const int *__restrict__ cols, const double *__restrict__ vals,
+                                 const long long *__restrict__ fptr, int *__restrict__ fcols,
+                                 double *__restrict__ fvals) {
+    const int lane = threadIdx.x & 31;
+    long long u = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= nV) return;
+    const long long b = rowptr[u], e = rowptr[u + 1];
+    long long w = fptr[u];
+    for (long long i0 = b; i0 < e; i0 += 32) {
+        long long i = i0 + lane;
+        bool k = false;
+        if (i < e) k = ((acc[2 * i] | acc[2 * i + 1]) != 0ULL) || tiny[i];
+        unsigned m = __ballot_sync(FULL, k);
+        if (k) {
+            long long o = w + __popc(m & lanemask_lt());
+            fcols[o] = cols[i];
+            fvals[o] = vals[i];
+        }
+        w += __popc(m);
+    }
+}
+
+// ------------------------------------------------------------------ load vector
+// par_forcing / compute_f (Cassemble.cpp:857-928, 149-164)
+template <int DIM>
+__global__ void k_forcing(const double *__restrict__ EC, const double *__restrict__ adet,
+                          const int *__restrict__ labT, const int *__restrict__ T32,
+                          const int *__restrict__ labV, const int *__restrict__ eprob,
+                          const ProbParams *__restrict__ probs, long long nE, Rule rule,
+                          unsigned long long *__restrict__ facc, unsigned *__restrict__ tiny) {
+    constexpr int dV = DIM + 1;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE || labT[e] <= 0) return;
+    const ProbParams &P = probs[eprob[e]];
+    const double *E = &EC[e * DIM * dV];
+    double termf[dV];
+#pragma unroll
+    for (int a = 0; a < dV; a++) termf[a] = 0;
+    for (int i = 0; i < rule.nPx; i++) {
+        double x[DIM];
+        xtoPhys<DIM>(E, &rule.Px[DIM * i], x);
+        const double fv = load_f64(P.load, x);
+#pragma unroll
+        for (int a = 0; a < dV; a++) termf[a] += rule.psix[dV * i + a] * fv * adet[e] * rule.dx[i];
+    }
+#pragma unroll
+    for (int a = 0; a < dV; a++) {
+        int v = T32[e * dV + a];
+        if (labV[v] > 0) fx_atomic_add(&facc[2 * (long long)v], termf[a], P.scale_exp, &tiny[v]);
+    }
+}
+__global__ void k_forcing_finish(const unsigned long long *__restrict__ facc, long long nV,
+                                 const int *__restrict__ vprob, const ProbParams *__restrict__ probs,
+                                 double *__restrict__ fd) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    fd[v] = fx_to_double(facc[2 * v], facc[2 * v + 1], probs[vprob[v]].scale_exp);
+}
+
+// ------------------------------------------------------------------ geometry debug hooks
+__global__ void k_retri_batch(long long n, const double *__restrict__ x, const double *__restrict__ TE,
+                              double sqdelta, int caps, int *__restrict__ counts, double *__restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double R[18];
+    double xc[2] = {x[2 * i], x[2 * i + 1]};
+    double E[6];
+    for (int j = 0; j < 6; j++) E[j] = TE[6 * i + j];
+    int Rdx = xretriangulate(xc, E, sqdelta, caps, R);
+    int nt = Rdx < 3 ? 0 : Rdx - 2;
+    counts[i] = nt;
+    double *o = &out[54 * i];
+    for (int k = 0; k < nt; k++)
+        for (int c = 0; c < 2; c++) {
+            o[2 * (3 * k + 0) + c] = R[c];
+            o[2 * (3 * k + 1) + c] = R[2 * (k + 1) + c];
+            o[2 * (3 * k + 2) + c] = R[2 * (k + 2) + c];
+        }
+}
+__global__ void k_geom_misc(int op, const double *__restrict__ A, const double *__restrict__ b, int dim,
+                            double *__restrict__ out, int *__restrict__ ok) {
+    if (threadIdx.x || blockIdx.x) return;
+    if (op == 0) { *ok = xtoRef(A, b, out); }
+    else if (op == 1) {
+        if (dim == 2) xtoPhys<2>(A, b, out); else xtoPhys<3>(A, b, out);
+        *ok = 1;
+    } else { *ok = xsolve2x2(A, b, out); }
+}
+
+}  // namespace nlg
+
+#include "pipeline.inl"

@@ -1,0 +1,251 @@
+// Device geometry and model functions of the nonlocal assembly.
+//
+// The "exact" functions reproduce the reference's FP64 arithmetic operation by operation
+// (src/mathhelpers.cpp, src/integration.cpp) with explicit round-to-nearest intrinsics, so that
+// no FMA contraction changes a rounding: the interaction predicate they feed decides the sparsity
+// pattern and must agree bit for bit with the reference's CPU build.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nlg {
+
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+
+// vec_dot / vec_sqL2dist of two 2-vectors (mathhelpers.cpp:255-279): ((0 + a0 b0) + a1 b1)
+__device__ __forceinline__ double xdot2(double a0, double a1, double b0, double b1) {
+    return xadd(xmul(a0, b0), xmul(a1, b1));
+}
+__device__ __forceinline__ double xsqdist2(const double *p, const double *x) {
+    double d0 = xsub(p[0], x[0]), d1 = xsub(p[1], x[1]);
+    return xadd(xmul(d0, d0), xmul(d1, d1));
+}
+
+// toPhys(E, p, dim, out) (mathhelpers.cpp:217-225)
+template <int DIM>
+__device__ __forceinline__ void xtoPhys(const double *E, const double *p, double *x) {
+#pragma unroll
+    for (int i = 0; i < DIM; i++) {
+        double s = xmul(p[0], xsub(E[DIM + i], E[i]));
+#pragma unroll
+        for (int j = 1; j < DIM; j++) s = xadd(s, xmul(p[j], xsub(E[DIM * (j + 1) + i], E[i])));
+        x[i] = xadd(s, E[i]);
+    }
+}
+
+// signDet(E) of a triangle (mathhelpers.cpp:131-147)
+__device__ __forceinline__ double xsignDet2(const double *E) {
+    double M00 = xsub(E[2], E[0]), M01 = xsub(E[4], E[0]);
+    double M10 = xsub(E[3], E[1]), M11 = xsub(E[5], E[1]);
+    double det = xsub(xmul(M00, M11), xmul(M01, M10));
+    return det > 0 ? 1.0 : (det < 0 ? -1.0 : 0.0);
+}
+
+// absDet(E) of a triangle (mathhelpers.cpp:101-109)
+__device__ __forceinline__ double xabsDet2(const double *E) {
+    double M00 = xsub(E[2], E[0]), M01 = xsub(E[4], E[0]);
+    double M10 = xsub(E[3], E[1]), M11 = xsub(E[5], E[1]);
+    return fabs(xsub(xmul(M00, M11), xmul(M01, M10)));
+}
+
+// inTriangle (integration.cpp:1283-1298)
+__device__ __forceinline__ bool xinTriangle(const double *y, const double *TE, const double *na,
+                                            const double *nb, const double *nc) {
+    bool a = xdot2(na[0], na[1], xsub(y[0], TE[0]), xsub(y[1], TE[1])) >= 0;
+    bool b = xdot2(nb[0], nb[1], xsub(y[0], TE[2]), xsub(y[1], TE[3])) >= 0;
+    bool c = xdot2(nc[0], nc[1], xsub(y[0], TE[4]), xsub(y[1], TE[5])) >= 0;
+    return a && b && c;
+}
+
+// placePointOnCap (integration.cpp:1353-1377); rightNormal (mathhelpers.cpp:74-78)
+__device__ __forceinline__ int xplaceCap(const double *ypred, const double *ycur, const double *xc,
+                                         double sqdelta, const double *TE, const double *na,
+                                         const double *nb, const double *nc, double orientation,
+                                         int Rdx, double *R) {
+    double n0 = xmul(xsub(ypred[1], ycur[1]), orientation);
+    double n1 = xmul(xsub(ycur[0], ypred[0]), orientation);
+    double s = xsqrt(xdiv(sqdelta, xdot2(n0, n1, n0, n1)));
+    double y[2] = {xadd(xc[0], xmul(n0, s)), xadd(xc[1], xmul(n1, s))};
+    if (xinTriangle(y, TE, na, nb, nc)) {
+        R[2 * Rdx] = y[0];
+        R[2 * Rdx + 1] = y[1];
+        return 1;
+    }
+    return 0;
+}
+
+// method_retriangulate (integration.cpp:1393-1512). Fills the polygon points R (<= 9) of
+// B_delta(xc) intersected with the triangle TE and returns their number; the sub-triangles are
+// the fan (R0, R[k+1], R[k+2]), k < n-2, present only if n >= 3.
+__device__ __forceinline__ int xretriangulate(const double *xc, const double *TE, double sqdelta,
+                                              int caps, double *R) {
+    int Rdx = 0;
+    bool is_onEdge = false, is_firstPointLiesOnVertex = true;
+    const double orientation = -xsignDet2(TE);
+    double na[2], nb[2], nc[2];
+    na[0] = xmul(xsub(TE[3], TE[1]), orientation); na[1] = xmul(xsub(TE[0], TE[2]), orientation);
+    nb[0] = xmul(xsub(TE[5], TE[3]), orientation); nb[1] = xmul(xsub(TE[2], TE[4]), orientation);
+    nc[0] = xmul(xsub(TE[1], TE[5]), orientation); nc[1] = xmul(xsub(TE[4], TE[0]), orientation);
+#pragma unroll 1
+    for (int k = 0; k < 3; k++) {
+        const double *p = &TE[2 * k];
+        const double *q = &TE[2 * (k == 2 ? 0 : k + 1)];
+        const double a0 = xsub(q[0], xc[0]), a1 = xsub(q[1], xc[1]);
+        const double b0 = xsub(p[0], q[0]), b1 = xsub(p[1], q[1]);
+        if (xsqdist2(p, xc) <= sqdelta) {
+            R[2 * Rdx] = p[0];
+            R[2 * Rdx + 1] = p[1];
+            is_onEdge = false;
+            Rdx += 1;
+        }
+        const double ab = xdot2(a0, a1, b0, b1);
+        const double aa = xdot2(a0, a1, a0, a1);
+        const double bb = xdot2(b0, b1, b0, b1);
+        const double aad = xsub(aa, sqdelta);
+        const double v = xsub(xmul(ab, ab), xmul(aad, bb));
+        if (v >= 0) {
+            const double term1 = xdiv(-ab, bb);
+            const double term2 = xdiv(xsqrt(v), bb);
+            double lam1, lam2;
+            if (term1 > 0) {
+                lam1 = xadd(term1, term2);
+                lam2 = xdiv(xmul(xdiv(1.0, lam1), aad), bb);
+            } else {
+                lam2 = xsub(term1, term2);
+                lam1 = xdiv(xmul(xdiv(1.0, lam2), aad), bb);
+            }
+            const double y1[2] = {xadd(xmul(lam1, b0), q[0]), xadd(xmul(lam1, b1), q[1])};
+            const double y2[2] = {xadd(xmul(lam2, b0), q[0]), xadd(xmul(lam2, b1), q[1])};
+            if ((0 <= lam1) && (lam1 <= 1)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
+                if (is_onEdge && caps)
+                    Rdx += xplaceCap(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+                R[2 * Rdx] = y1[0];
+                R[2 * Rdx + 1] = y1[1];
+                is_onEdge = true;
+                Rdx += 1;
+            }
+            const double dl = xsub(lam1, lam2);
+            if ((0 <= lam2) && (lam2 <= 1) && (xmul(dl, dl) > 0)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
+                if (is_onEdge && caps)
+                    Rdx += xplaceCap(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+                R[2 * Rdx] = y2[0];
+                R[2 * Rdx + 1] = y2[1];
+                is_onEdge = true;
+                Rdx += 1;
+            }
+        }
+    }
+    if (is_onEdge && (!is_firstPointLiesOnVertex && Rdx > 1) && caps)
+        Rdx += xplaceCap(&R[2 * (Rdx - 1)], &R[0], xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+    return Rdx;
+}
+
+// baryCenter(dim, E) (mathhelpers.cpp:184-196) and method_baryCenter (integration.cpp:1262-1280):
+// true iff |x - bary(T)|^2 <= delta^2.
+template <int DIM>
+__device__ __forceinline__ void xbary(const double *E, double *b) {
+#pragma unroll
+    for (int j = 0; j < DIM; j++) {
+        double s = E[j];
+#pragma unroll
+        for (int i = 1; i <= DIM; i++) s = xadd(s, E[DIM * i + j]);
+        b[j] = xdiv(s, (double)(DIM + 1));
+    }
+}
+template <int DIM>
+__device__ __forceinline__ bool xbaryInside(const double *x, const double *b, double sqdelta) {
+    double d = xsub(x[0], b[0]);
+    double r = xmul(d, d);
+#pragma unroll
+    for (int j = 1; j < DIM; j++) {
+        d = xsub(x[j], b[j]);
+        r = xadd(r, xmul(d, d));
+    }
+    return !(r > sqdelta);
+}
+
+// solve2x2 (mathhelpers.cpp:41-71). Returns false where the reference aborts.
+__device__ __forceinline__ bool xsolve2x2(const double *A, const double *b, double *x) {
+    int dx0 = 0, dx1 = 1;
+    if (fabs(A[0]) < fabs(A[2])) { dx0 = 1; dx1 = 0; }
+    if (fabs(A[2 * dx0]) < 1e-15) return false;
+    const double l = xdiv(A[2 * dx1], A[2 * dx0]);
+    const double u = xsub(A[2 * dx1 + 1], xmul(l, A[2 * dx0 + 1]));
+    if (u == 0) return false;
+    x[1] = xdiv(xsub(b[dx1], xmul(l, b[dx0])), u);
+    x[0] = xdiv(xsub(b[dx0], xmul(A[2 * dx0 + 1], x[1])), A[2 * dx0]);
+    return true;
+}
+
+// toRef (mathhelpers.cpp:227-240)
+__device__ __forceinline__ bool xtoRef(const double *E, const double *y, double *p) {
+    double M[4] = {xsub(E[2], E[0]), xsub(E[4], E[0]), xsub(E[3], E[1]), xsub(E[5], E[1])};
+    double b[2] = {xsub(y[0], E[0]), xsub(y[1], E[1])};
+    return xsolve2x2(M, b, p);
+}
+
+// ------------------------------------------------------------------- model (model.cpp)
+enum KernelId { KER_CONSTANT = 0, KER_PARABOLA = 1, KER_FRACTIONAL = 2, KER_CONSTANT3D = 3 };
+enum MethodId { MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2 };
+enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
+
+// Per-problem parameters (one entry per independent assembly).
+struct ProbParams {
+    double sqdelta, delta;
+    double kc;       // kernel constant (host-computed with the reference's formula)
+    double expo;     // fractional: dim + 2s
+    float sqdelta_f, kc_f, expo_f, pad_f;
+    int kernel, remote, close, caps;
+    int full_search, singular, load, scale_exp;
+    int elem_off, nE, vert_off, nV;
+};
+
+// FP64 kernel value k(x, y) (model.cpp:25-28, 52-60, 62-65, 126-138)
+template <int DIM>
+__device__ __forceinline__ double kernel_f64(const ProbParams &P, const double *x, const double *y) {
+    switch (P.kernel) {
+    case KER_PARABOLA: {
+        double z0 = x[0] - y[0], z1 = x[1] - y[1];
+        return P.kc * (P.sqdelta - (z0 * z0 + z1 * z1));
+    }
+    case KER_FRACTIONAL: {
+        double r = 0;
+#pragma unroll
+        for (int i = 0; i < DIM; i++) { double z = x[i] - y[i]; r += z * z; }
+        return P.kc * (1.0 / pow(sqrt(r), P.expo));
+    }
+    default:
+        return P.kc;
+    }
+}
+
+// FP32 kernel value from the difference z = x - y (local coordinates).
+__device__ __forceinline__ float kernel_f32(const ProbParams &P, float z0, float z1) {
+    switch (P.kernel) {
+    case KER_PARABOLA:
+        return P.kc_f * (P.sqdelta_f - (z0 * z0 + z1 * z1));
+    case KER_FRACTIONAL: {
+        float r2 = z0 * z0 + z1 * z1;
+        return P.kc_f * exp2f(-0.5f * P.expo_f * log2f(r2));
+    }
+    default:
+        return P.kc_f;
+    }
+}
+
+// Load functions (model.cpp:201-203, 240-242, 259-261)
+__device__ __forceinline__ double load_f64(int load, const double *x) {
+    switch (load) {
+    case LOAD_LINEAR: return -2. * (x[1] + 1.);
+    case LOAD_LINEAR3D: return -2. * (x[1] + 2.);
+    default: return 1.0;
+    }
+}
+
+}  // namespace nlg

@@ -1,0 +1,1003 @@
+// Host orchestration of the assembly pipeline and the C ABI (included by assemble.cu).
+#include <mutex>
+
+namespace nlg {
+
+static thread_local std::string g_err;
+static thread_local nlfem_stats g_stats;
+
+static int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(NLFEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+static inline unsigned grid_for(long long n, int threads) {
+    long long g = (n + threads - 1) / threads;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    template <typename T>
+    T *get() const { return (T *)p; }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+static int ensure(DevBuf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (bytes <= b.cap) return NLFEM_OK;
+    b.release();
+    size_t want = std::max(bytes, (size_t)(b.cap + b.cap / 4));
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaMalloc(&b.p, bytes);
+        want = bytes;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return fail(NLFEM_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    b.cap = want;
+    return NLFEM_OK;
+}
+#define ENS(buf, bytes) do { int r_ = ensure(buf, bytes); if (r_) return r_; } while (0)
+
+// ---------------------------------------------------------------- configuration parsing
+static int kernel_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "constant") return KER_CONSTANT;
+    if (k == "parabola") return KER_PARABOLA;
+    if (k == "fractional") return KER_FRACTIONAL;
+    if (k == "constant3D") return KER_CONSTANT3D;
+    return -1;
+}
+static int method_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "retriangulate") return MTH_RETRIANGULATE;
+    if (k == "baryCenter") return MTH_BARYCENTER;
+    if (k == "fractional") return MTH_FRACTIONAL;
+    return -1;
+}
+static int load_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "linear") return LOAD_LINEAR;
+    if (k == "linear3D") return LOAD_LINEAR3D;
+    if (k == "constant") return LOAD_CONSTANT;
+    return -1;
+}
+
+// Quadrature rule and the basis function check (Cassemble.cpp:509-517, checks.cpp:36-47).
+static int make_rule(const nlfem_problem &p, bool inner, Rule &r) {
+    memset(&r, 0, sizeof(r));
+    const int dim = p.dim, dV = dim + 1;
+    r.dim = dim;
+    r.nPx = p.nPx;
+    r.nPy = inner ? p.nPy : 0;
+    if (p.nPx <= 0 || p.nPx > MAXQ || !p.Px || !p.dx)
+        return fail(NLFEM_ERR_INVALID, "outer quadrature rule missing or longer than 32 points");
+    if (inner && (p.nPy <= 0 || p.nPy > MAXQ || !p.Py || !p.dy))
+        return fail(NLFEM_ERR_INVALID, "inner quadrature rule missing or longer than 32 points");
+    for (int k = 0; k < r.nPx; k++) {
+        double s = 1.0;
+        for (int j = 0; j < dim; j++) {
+            r.Px[dim * k + j] = p.Px[dim * k + j];
+            s -= p.Px[dim * k + j];
+            r.psix[dV * k + j + 1] = p.Px[dim * k + j];
+        }
+        r.psix[dV * k] = s;
+        r.dx[k] = p.dx[k];
+    }
+    for (int k = 0; k < r.nPy; k++) {
+        double s = 1.0;
+        for (int j = 0; j < dim; j++) {
+            r.Py[dim * k + j] = p.Py[dim * k + j];
+            s -= p.Py[dim * k + j];
+            r.psiy[dV * k + j + 1] = p.Py[dim * k + j];
+        }
+        r.psiy[dV * k] = s;
+        r.dy[k] = p.dy[k];
+        for (int j = 0; j < dim && j < 2; j++) r.Pyf[2 * k + j] = (float)p.Py[dim * k + j];
+        r.dyf[k] = (float)p.dy[k];
+        for (int a = 0; a < dV; a++) r.psiyf[dV * k + a] = (float)r.psiy[dV * k + a];
+    }
+    // chk_BasisFunction: sum_k w_k psi_0(P_k) == 1/(d+1)!
+    const double want = dim == 2 ? 1.0 / 6.0 : 1.0 / 24.0;
+    double sx = 0;
+    for (int k = 0; k < r.nPx; k++) sx += r.dx[k] * r.psix[dV * k];
+    if (fabs(sx - want) >= 1e-8) return fail(NLFEM_ERR_INVALID, "Wrong integral of basis function w.r.t. weights dx.");
+    if (inner) {
+        double sy = 0;
+        for (int k = 0; k < r.nPy; k++) sy += r.dy[k] * r.psiy[dV * k];
+        if (fabs(sy - want) >= 1e-8) return fail(NLFEM_ERR_INVALID, "Wrong integral of basis function w.r.t. weights dy.");
+    }
+    return NLFEM_OK;
+}
+
+// Per-problem parameters, checks (checks.cpp:87-113) and the fixed-point scale.
+static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
+    memset(&P, 0, sizeof(P));
+    if (p.dim != 2 && p.dim != 3) return fail(NLFEM_ERR_INVALID, "Dimension is not equal to 2 or 3.");
+    if (p.outdim != 1) return fail(NLFEM_ERR_UNSUPPORTED, "only outdim = 1 is implemented");
+    if (p.is_dg) return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz is not implemented");
+    if (p.nE <= 0 || p.nV <= 0 || !p.elements || !p.elementLabels || !p.vertices || !p.vertexLabels)
+        return fail(NLFEM_ERR_INVALID, "empty or missing mesh arrays");
+    if (p.nE >= (1LL << 31) || p.nV >= (1LL << 31)) return fail(NLFEM_ERR_UNSUPPORTED, "mesh too large");
+    P.sqdelta = p.sqdelta;
+    P.delta = sqrt(p.sqdelta);
+    P.sqdelta_f = (float)p.sqdelta;
+    if (system) {
+        P.kernel = kernel_id(p.kernel);
+        if (P.kernel < 0) return fail(NLFEM_ERR_UNSUPPORTED, std::string("unknown kernel: ") + (p.kernel ? p.kernel : "(null)"));
+        P.remote = method_id(p.method_remote);
+        P.close = (p.method_close && p.method_close[0]) ? method_id(p.method_close) : P.remote;
+        if (P.remote < 0 || P.close < 0) return fail(NLFEM_ERR_UNSUPPORTED, "unknown integration method");
+        if (p.dim == 3 && P.remote != MTH_BARYCENTER)
+            return fail(NLFEM_ERR_INVALID, "Only Bary-Center is currently implemented as integration method for 3D and 1D.");
+        if (P.remote == MTH_FRACTIONAL)
+            return fail(NLFEM_ERR_INVALID, "The fractional and fractional_weakSingular integration routines are meant for close elements only.");
+        std::string kn(p.kernel);
+        P.singular = (kn == "fractional");
+        if (P.singular && P.close == MTH_FRACTIONAL && (p.tensorGaussDegree <= 0 || !p.Pg || !p.dg))
+            return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
+        if (P.close == MTH_FRACTIONAL && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "fractional close pairs are 2D only");
+        if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
+        P.caps = p.is_PlacePointOnCap ? 1 : 0;
+        P.full_search = p.is_fullConnectedComponentSearch ? 1 : 0;
+        const double s = p.fractional_s;
+        switch (P.kernel) {
+        case KER_CONSTANT: P.kc = 4 / (M_PI * (p.sqdelta * p.sqdelta)); break;             // model.cpp:25-28
+        case KER_PARABOLA: P.kc = 12. / (M_PI * pow(p.sqdelta, 3)); break;                 // model.cpp:52-60
+        case KER_FRACTIONAL:                                                               // model.cpp:126-138
+            P.expo = p.dim + 2. * s;
+            P.kc = (2. - 2. * s) / (M_PI * pow(P.delta, 2. - 2. * s));
+            break;
+        case KER_CONSTANT3D: P.kc = 15 / (M_PI * 4 * pow(P.delta, 5)); break;              // model.cpp:62-65
+        }
+        P.kc_f = (float)P.kc;
+        P.expo_f = (float)P.expo;
+    } else {
+        P.load = load_id(p.forcing);
+        if (P.load < 0) return fail(NLFEM_ERR_UNSUPPORTED, std::string("unknown forcing: ") + (p.forcing ? p.forcing : "(null)"));
+    }
+    // fixed-point scale: typical magnitude of an entry
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (long v = 0; v < p.nV; v++)
+        for (int j = 0; j < p.dim; j++) {
+            double x = p.vertices[v * p.dim + j];
+            lo[j] = std::min(lo[j], x);
+            hi[j] = std::max(hi[j], x);
+        }
+    double vol = 1;
+    for (int j = 0; j < p.dim; j++) vol *= std::max(hi[j] - lo[j], 1e-300);
+    const double el = vol / (double)p.nE;
+    double mag;
+    if (system) {
+        const double h = pow(el, 1.0 / p.dim);
+        const double ball = p.dim == 2 ? M_PI * p.sqdelta : 4.0 / 3.0 * M_PI * p.sqdelta * P.delta;
+        double kmax = P.kc;
+        if (P.kernel == KER_PARABOLA) kmax = P.kc * p.sqdelta;
+        if (P.kernel == KER_FRACTIONAL) kmax = P.kc / pow(std::min(h, P.delta), P.expo);
+        mag = fabs(kmax) * el * std::max(ball, el);
+    } else {
+        double fm = 1.0;
+        for (int j = 0; j < p.dim; j++) fm = std::max(fm, std::max(fabs(lo[j]), fabs(hi[j])));
+        mag = 2.0 * (fm + 2.0) * el;
+    }
+    if (!(mag > 0) || !std::isfinite(mag)) mag = 1.0;
+    P.scale_exp = (int)std::ceil(std::log2(mag));
+    return NLFEM_OK;
+}
+
+// Duffy tables (MeshTypes.cpp:32-209, 252-327): scaled points, xi factored out of the transform
+// (alphaCanceled[0] = 1), determinant xi^(3-2s) * traffoDet * SCALEDET, mirrored.
+static double duffy_traffo(int c, int t, double *al) {
+    const double xi = al[0], e1 = al[1], e2 = al[2], e3 = al[3];
+    if (c == 0) {
+        if (t == 0) { al[0] = xi; al[1] = e1 * xi; al[2] = e2 * xi; al[3] = e2 * e3 * xi; }
+        else { al[0] = xi * e2; al[1] = xi * e2 * e3; al[2] = xi; al[3] = xi * e1; }
+        return pow(xi, 3) * e2;
+    }
+    if (c == 1) {
+        switch (t) {
+        case 0: al[0] = xi; al[1] = xi * e1 * e3; al[2] = xi * (1. - e1 * e2); al[3] = xi * e1 * (1. - e2);
+            return pow(xi, 3) * (e1 * e1);
+        case 1: al[0] = xi; al[1] = xi * e1; al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * e1 * e2 * (1. - e3); break;
+        case 2: al[0] = xi * (1. - e1 * e2); al[1] = xi * e1 * (1. - e2); al[2] = xi; al[3] = xi * e1 * e2 * e3; break;
+        case 3: al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * e2 * (1. - e3); al[2] = xi; al[3] = xi * e1; break;
+        default: al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * (1. - e2 * e3); al[2] = xi; al[3] = xi * e1 * e2; break;
+        }
+        return pow(xi, 3) * (e1 * e1) * e2;
+    }
+    switch (t) {
+    case 0: al[0] = xi; al[1] = xi * (1. - e1 + e1 * e2); al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * (1. - e1); break;
+    case 1: al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * (1. - e1); al[2] = xi; al[3] = xi * (1. - e1 + e1 * e2); break;
+    case 2: al[0] = xi; al[1] = xi * e1 * (1. - e2 + e2 * e3); al[2] = xi * (1. - e1 * e2); al[3] = xi * e1 * (1. - e2); break;
+    case 3: al[0] = xi * (1. - e1 * e2); al[1] = xi * e1 * (1. - e2); al[2] = xi; al[3] = xi * e1 * (1. - e2 + e2 * e3); break;
+    case 4: al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * (1. - e2 * e3); al[2] = xi; al[3] = xi * e1 * (1. - e2); break;
+    default: al[0] = xi; al[1] = xi * e1 * (1. - e2); al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * e1 * (1. - e2 * e3); break;
+    }
+    return pow(xi, 3) * (e1 * e1) * e2;
+}
+
+// ---------------------------------------------------------------- session
+struct Session {
+    int dim = 2, dV = 3, nProb = 0;
+    bool system = true;
+    long long nE = 0, nV = 0;
+    int maxNE = 0, maxNV = 0;
+    int nSM = 148;
+    std::vector<ProbParams> hprm;
+    std::vector<int> eoff, voff;   // nProb + 1
+    Rule rule;
+    int duffy_nPg = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[8];
+    // inputs
+    DevBuf T64, labT64, V, labV64, eoffd, voffd, prm, duffy;
+    // derived
+    DevBuf T32, labT, eprob, EC, adet, labV, vprob;
+    DevBuf vcnt, vptr, vel, adjcnt, xadj, adj;
+    DevBuf visited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
+    DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
+    DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
+    DevBuf out64a, out64b;
+    long long qcap = 0, pool_cap = 0;
+    long long P = 0, nnz_struct = 0, nnz = 0;
+    nlfem_stats stats;
+    ~Session() {
+        DevBuf *all[] = {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
+                         &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited,
+                         &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
+                         &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
+                         &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b};
+        for (DevBuf *b : all) b->release();
+        if (st) {
+            for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
+            cudaStreamDestroy(st);
+        }
+    }
+};
+
+// Exclusive scan of n inputs into n+1 outputs (out[n] = total), int64 results.
+template <typename TIn>
+static int scan_excl(Session &S, const TIn *in, long long n, long long *out) {
+    const long long n_out = n + 1;
+    std::vector<long long> sizes;
+    long long m = n_out;
+    // recursion over block sums kept in scan_tmp
+    long long nb = (m + SCAN_TILE - 1) / SCAN_TILE;
+    long long total_tmp = 0, t = nb;
+    while (true) {
+        total_tmp += 2 * t + 2;
+        if (t <= 1) break;
+        t = (t + SCAN_TILE - 1) / SCAN_TILE;
+    }
+    ENS(S.scan_tmp, (size_t)total_tmp * sizeof(long long));
+    long long *tmp = S.scan_tmp.get<long long>();
+    // level 0
+    struct Lvl { long long n; long long *bsum; long long *boff; long long nb; };
+    std::vector<Lvl> lv;
+    lv.push_back({m, tmp, tmp + nb + 1, nb});
+    k_scan_reduce<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, lv[0].bsum);
+    long long off = 2 * nb + 2;
+    while (lv.back().nb > 1) {
+        Lvl &pl = lv.back();
+        long long nb2 = (pl.nb + SCAN_TILE - 1) / SCAN_TILE;
+        Lvl l2{pl.nb, tmp + off, tmp + off + nb2 + 1, nb2};
+        off += 2 * nb2 + 2;
+        k_scan_reduce<long long><<<(unsigned)nb2, SCAN_THREADS, 0, S.st>>>(pl.bsum, pl.nb, l2.bsum);
+        lv.push_back(l2);
+    }
+    // top level: single block sum -> offset 0
+    CK(cudaMemsetAsync(lv.back().boff, 0, sizeof(long long), S.st));
+    for (int i = (int)lv.size() - 1; i >= 1; i--) {
+        // scan level i-1 block sums using level i offsets
+        k_scan_down<long long><<<(unsigned)lv[i].nb, SCAN_THREADS, 0, S.st>>>(lv[i - 1].bsum, lv[i - 1].nb, lv[i - 1].nb, lv[i].boff, lv[i - 1].boff);
+    }
+    // final: scan n inputs (+1 trailing zero) into out
+    (void)sizes;
+    k_scan_down<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, n_out, lv[0].boff, out);
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+template <typename T>
+static int d2h(Session &S, T *host, const T *dev, size_t n) {
+    CK(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, S.st));
+    CK(cudaStreamSynchronize(S.st));
+    return NLFEM_OK;
+}
+
+static int session_init(Session &S, const nlfem_problem *probs, int n, bool system) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&S.nSM, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
+    for (int i = 0; i < 8; i++) CK(cudaEventCreate(&S.ev[i]));
+    S.system = system;
+    S.nProb = n;
+    S.dim = probs[0].dim;
+    S.dV = S.dim + 1;
+    S.hprm.resize(n);
+    S.eoff.assign(n + 1, 0);
+    S.voff.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        const nlfem_problem &p = probs[i];
+        if (p.dim != S.dim) return fail(NLFEM_ERR_INVALID, "all problems of a batch must share the dimension");
+        int r = make_params(p, system, S.hprm[i]);
+        if (r) return r;
+        S.hprm[i].elem_off = (int)S.eoff[i];
+        S.hprm[i].vert_off = (int)S.voff[i];
+        S.hprm[i].nE = (int)p.nE;
+        S.hprm[i].nV = (int)p.nV;
+        if ((long long)S.eoff[i] + p.nE >= (1LL << 31) || (long long)S.voff[i] + p.nV >= (1LL << 31))
+            return fail(NLFEM_ERR_UNSUPPORTED, "batch too large (2^31 elements or vertices)");
+        S.eoff[i + 1] = S.eoff[i] + (int)p.nE;
+        S.voff[i + 1] = S.voff[i] + (int)p.nV;
+        S.maxNE = std::max(S.maxNE, (int)p.nE);
+        S.maxNV = std::max(S.maxNV, (int)p.nV);
+    }
+    S.nE = S.eoff[n];
+    S.nV = S.voff[n];
+    int r = make_rule(probs[0], system, S.rule);
+    if (r) return r;
+    for (int i = 1; i < n; i++) {
+        Rule r2;
+        int rr = make_rule(probs[i], system, r2);
+        if (rr) return rr;
+        if (memcmp(&r2, &S.rule, sizeof(Rule)) != 0)
+            return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the quadrature rules");
+    }
+    const int dV = S.dV, dim = S.dim;
+    ENS(S.T64, sizeof(long long) * S.nE * dV);
+    ENS(S.labT64, sizeof(long long) * S.nE);
+    ENS(S.V, sizeof(double) * S.nV * dim);
+    ENS(S.labV64, sizeof(long long) * S.nV);
+    ENS(S.eoffd, sizeof(int) * (n + 1));
+    ENS(S.voffd, sizeof(int) * (n + 1));
+    ENS(S.prm, sizeof(ProbParams) * n);
+    CK(cudaMemcpyAsync(S.eoffd.p, S.eoff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(S.voffd.p, S.voff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(S.prm.p, S.hprm.data(), sizeof(ProbParams) * n, cudaMemcpyHostToDevice, S.st));
+    // Duffy tables (shared by the batch: same tensor degree and s required)
+    if (system) {
+        bool need = false;
+        for (int i = 0; i < n; i++) need |= (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL);
+        if (need) {
+            const nlfem_problem &p = probs[0];
+            const int deg = p.tensorGaussDegree;
+            const int nPg = deg * deg * deg * deg;
+            for (int i = 1; i < n; i++)
+                if (probs[i].tensorGaussDegree != deg || probs[i].fractional_s != p.fractional_s)
+                    return fail(NLFEM_ERR_UNSUPPORTED, "batched singular problems must share degree and s");
+            S.duffy_nPg = nPg;
+            const int nTr[3] = {2, 5, 6};
+            std::vector<double> h;
+            for (int c = 0; c < 3; c++) {
+                std::vector<double> al((size_t)nTr[c] * nPg * 4), td((size_t)nTr[c] * nPg);
+                for (int t = 0; t < nTr[c]; t++)
+                    for (int k = 0; k < nPg; k++) {
+                        double *a = &al[((size_t)t * nPg + k) * 4];
+                        for (int j = 0; j < 4; j++) a[j] = p.Pg[4 * k + j] * 0.5 + 0.5;
+                        double tdf = pow(a[0], 3 - 2 * p.fractional_s);
+                        a[0] = 1.0;
+                        double det = duffy_traffo(c, t, a);
+                        tdf *= det * 0.0625;
+                        a[0] = a[0] - a[1];
+                        a[2] = a[2] - a[3];
+                        td[(size_t)t * nPg + k] = tdf;
+                    }
+                h.insert(h.end(), al.begin(), al.end());
+                h.insert(h.end(), td.begin(), td.end());
+            }
+            h.insert(h.end(), p.dg, p.dg + nPg);
+            ENS(S.duffy, sizeof(double) * h.size());
+            CK(cudaMemcpyAsync(S.duffy.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, S.st));
+            CK(cudaStreamSynchronize(S.st));
+        }
+    }
+    return NLFEM_OK;
+}
+
+// Host -> device copy of the meshes (the per-step input traffic of the end-to-end path).
+static int session_upload(Session &S, const nlfem_problem *probs) {
+    const int dV = S.dV, dim = S.dim;
+    for (int i = 0; i < S.nProb; i++) {
+        const nlfem_problem &p = probs[i];
+        CK(cudaMemcpyAsync(S.T64.get<long long>() + (long long)S.eoff[i] * dV, p.elements, sizeof(long long) * p.nE * dV, cudaMemcpyHostToDevice, S.st));
+        CK(cudaMemcpyAsync(S.labT64.get<long long>() + S.eoff[i], p.elementLabels, sizeof(long long) * p.nE, cudaMemcpyHostToDevice, S.st));
+        CK(cudaMemcpyAsync(S.V.get<double>() + (long long)S.voff[i] * dim, p.vertices, sizeof(double) * p.nV * dim, cudaMemcpyHostToDevice, S.st));
+        CK(cudaMemcpyAsync(S.labV64.get<long long>() + S.voff[i], p.vertexLabels, sizeof(long long) * p.nV, cudaMemcpyHostToDevice, S.st));
+    }
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_prep(Session &S) {
+    const long long nE = S.nE, nV = S.nV;
+    constexpr int dV = DIM + 1;
+    ENS(S.T32, sizeof(int) * nE * dV);
+    ENS(S.labT, sizeof(int) * nE);
+    ENS(S.eprob, sizeof(int) * nE);
+    ENS(S.EC, sizeof(double) * nE * DIM * dV);
+    ENS(S.adet, sizeof(double) * nE);
+    ENS(S.labV, sizeof(int) * nV);
+    ENS(S.vprob, sizeof(int) * nV);
+    ENS(S.counters, sizeof(unsigned long long) * 16);
+    ENS(S.err, sizeof(int) * 16);
+    CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 16, S.st));
+    CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 16, S.st));
+    k_prep_elements<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(
+        S.T64.get<long long>(), S.labT64.get<long long>(), S.V.get<double>(), S.eoffd.get<int>(),
+        S.voffd.get<int>(), S.nProb, nE, S.T32.get<int>(), S.labT.get<int>(), S.eprob.get<int>(),
+        S.EC.get<double>(), S.adet.get<double>());
+    k_prep_vertices<<<grid_for(nV, 256), 256, 0, S.st>>>(S.labV64.get<long long>(), S.voffd.get<int>(),
+        S.nProb, nV, S.labV.get<int>(), S.vprob.get<int>());
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_dual(Session &S) {
+    constexpr int dV = DIM + 1;
+    const long long nE = S.nE, nV = S.nV;
+    ENS(S.vcnt, sizeof(int) * (nV + 1));
+    ENS(S.vptr, sizeof(long long) * (nV + 1));
+    ENS(S.vel, sizeof(int) * nE * dV);
+    CK(cudaMemsetAsync(S.vcnt.p, 0, sizeof(int) * (nV + 1), S.st));
+    k_vinc_count<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, S.vcnt.get<int>());
+    int r = scan_excl<int>(S, S.vcnt.get<int>(), nV, S.vptr.get<long long>());
+    if (r) return r;
+    CK(cudaMemsetAsync(S.vcnt.p, 0, sizeof(int) * (nV + 1), S.st));
+    k_vinc_fill<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, dV, S.vptr.get<long long>(), S.vcnt.get<int>(), S.vel.get<int>());
+    k_vinc_sort<<<grid_for(nV, 256), 256, 0, S.st>>>(S.vptr.get<long long>(), nV, S.vel.get<int>());
+    ENS(S.adjcnt, sizeof(int) * (nE + 1));
+    ENS(S.xadj, sizeof(long long) * (nE + 1));
+    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), nullptr, S.adjcnt.get<int>(), nullptr, S.err.get<int>() + 8);
+    r = scan_excl<int>(S, S.adjcnt.get<int>(), nE, S.xadj.get<long long>());
+    if (r) return r;
+    long long nadj = 0;
+    r = d2h(S, &nadj, S.xadj.get<long long>() + nE, 1);
+    if (r) return r;
+    ENS(S.adj, sizeof(int) * (nadj + 1));
+    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), S.xadj.get<long long>(), S.adjcnt.get<int>(), S.adj.get<int>(), S.err.get<int>() + 8);
+    CK(cudaGetLastError());
+    int e8 = 0;
+    r = d2h(S, &e8, S.err.get<int>() + 8, 1);
+    if (r) return r;
+    if (e8) return fail(NLFEM_ERR_UNSUPPORTED, "element with more than 320 vertex neighbours");
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_bfs(Session &S) {
+    const long long nE = S.nE;
+    const int nwarps = S.nSM * 2 * BFS_WARPS;
+    if (S.qcap == 0) S.qcap = std::min<long long>(S.maxNE + 1, 8192);
+    if (S.pool_cap == 0) S.pool_cap = std::max<long long>(nE * 64, 1 << 20);
+    ENS(S.visited, sizeof(unsigned) * (size_t)nwarps * S.maxNE);
+    ENS(S.seg_start, sizeof(long long) * (nE + 1));
+    ENS(S.seg_cnt, sizeof(int) * (nE + 1));
+    for (int attempt = 0; attempt < 8; attempt++) {
+        ENS(S.queue, sizeof(int) * (size_t)nwarps * S.qcap);
+        ENS(S.pool, sizeof(int) * (size_t)S.pool_cap);
+        CK(cudaMemsetAsync(S.visited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNE, S.st));
+        CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 4, S.st));
+        CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
+        BfsArgs a;
+        a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>();
+        a.adj = S.adj.get<int>(); a.xadj = S.xadj.get<long long>(); a.EC = S.EC.get<double>();
+        a.probs = S.prm.get<ProbParams>(); a.nE = nE;
+        a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;
+        a.queue = S.queue.get<int>(); a.qcap = S.qcap;
+        a.pool = S.pool.get<int>(); a.pool_cap = S.pool_cap;
+        unsigned long long *cnt = S.counters.get<unsigned long long>();
+        a.pool_cursor = cnt + 0; a.n_cand = cnt + 1; a.qneed = (long long *)(cnt + 2);
+        a.seg_start = S.seg_start.get<long long>(); a.seg_cnt = S.seg_cnt.get<int>();
+        a.err = S.err.get<int>();
+        k_bfs<DIM><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
+        CK(cudaGetLastError());
+        unsigned long long hc[3];
+        int he[2];
+        int r = d2h(S, hc, cnt, 3);
+        if (r) return r;
+        r = d2h(S, he, S.err.get<int>(), 2);
+        if (r) return r;
+        if (he[0]) { S.qcap = std::max<long long>((long long)hc[2] * 3 / 2, S.qcap * 2); continue; }
+        if (he[1]) { S.pool_cap = (long long)hc[0] + (long long)hc[0] / 8 + 1024; continue; }
+        S.stats.n_candidates = (long)hc[1];
+        return NLFEM_OK;
+    }
+    return fail(NLFEM_ERR_NOMEM, "BFS capacity retries exhausted");
+}
+
+template <int DIM>
+static int run_pairs(Session &S) {
+    const long long nE = S.nE;
+    ENS(S.out_ptr, sizeof(long long) * (nE + 1));
+    int r = scan_excl<int>(S, S.seg_cnt.get<int>(), nE, S.out_ptr.get<long long>());
+    if (r) return r;
+    r = d2h(S, &S.P, S.out_ptr.get<long long>() + nE, 1);
+    if (r) return r;
+    const long long P = S.P;
+    ENS(S.pA, sizeof(int) * (P + 1));
+    ENS(S.pB, sizeof(int) * (P + 1));
+    k_compact_pairs<<<grid_for(nE * 32, 256), 256, 0, S.st>>>(S.seg_start.get<long long>(), S.seg_cnt.get<int>(), S.out_ptr.get<long long>(), S.pool.get<int>(), nE, S.pA.get<int>(), S.pB.get<int>());
+    ENS(S.incnt, sizeof(int) * (nE + 1));
+    ENS(S.in_ptr, sizeof(long long) * (nE + 1));
+    ENS(S.inA, sizeof(int) * (P + 1));
+    CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
+    k_in_count<<<grid_for(P, 256), 256, 0, S.st>>>(S.pB.get<int>(), P, S.incnt.get<int>());
+    r = scan_excl<int>(S, S.incnt.get<int>(), nE, S.in_ptr.get<long long>());
+    if (r) return r;
+    CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
+    k_in_fill<<<grid_for(P, 256), 256, 0, S.st>>>(S.pA.get<int>(), S.pB.get<int>(), P, S.in_ptr.get<long long>(), S.incnt.get<int>(), S.inA.get<int>());
+    CK(cudaGetLastError());
+    S.stats.n_pairs = (long)P;
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_pattern(Session &S) {
+    const long long nV = S.nV;
+    const int nwarps = S.nSM * 4 * 8;
+    ENS(S.marks, sizeof(unsigned) * (size_t)nwarps * S.maxNV);
+    ENS(S.rowcnt, sizeof(int) * (nV + 1));
+    ENS(S.rowptr, sizeof(long long) * (nV + 1));
+    CK(cudaMemsetAsync(S.marks.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNV, S.st));
+    RowArgs a;
+    a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
+    a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
+    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
+    a.probs = S.prm.get<ProbParams>(); a.nV = nV;
+    a.marks = S.marks.get<unsigned>(); a.mstride = S.maxNV;
+    a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
+    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 0);
+    int r = scan_excl<int>(S, S.rowcnt.get<int>(), nV, S.rowptr.get<long long>());
+    if (r) return r;
+    r = d2h(S, &S.nnz_struct, S.rowptr.get<long long>() + nV, 1);
+    if (r) return r;
+    ENS(S.cols, sizeof(int) * (S.nnz_struct + 1));
+    a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 1);
+    const int cap = 16384;
+    CK(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, cap * (int)sizeof(int)));
+    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap);
+    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap);
+    CK(cudaGetLastError());
+    S.stats.nnz_structural = (long)S.nnz_struct;
+    return NLFEM_OK;
+}
+
+static int check_errors(Session &S);
+
+static Duffy duffy_view(const Session &S) {
+    Duffy d;
+    const int nPg = S.duffy_nPg;
+    const int nTr[3] = {2, 5, 6};
+    const double *h = S.duffy.get<double>();
+    size_t o = 0;
+    for (int c = 0; c < 3; c++) {
+        d.alpha[c] = h + o; o += (size_t)nTr[c] * nPg * 4;
+        d.tdet[c] = h + o; o += (size_t)nTr[c] * nPg;
+    }
+    d.dg = h + o;
+    d.nPg = nPg;
+    return d;
+}
+
+__global__ void k_iota(int *l, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) l[i] = (int)i;
+}
+
+// Blocks of explicit pairs (no scatter): the kernel-level parity hook.
+template <int DIM>
+static int run_pair_blocks(Session &S, long long n, const long *pairs, int close, double *out, int *ret) {
+    constexpr int dV = DIM + 1;
+    int r = run_prep<DIM>(S);
+    if (r) return r;
+    std::vector<int> a32(n), b32(n);
+    for (long long i = 0; i < n; i++) {
+        if (pairs[2 * i] < 0 || pairs[2 * i] >= S.nE || pairs[2 * i + 1] < 0 || pairs[2 * i + 1] >= S.nE)
+            return fail(NLFEM_ERR_INVALID, "pair index out of range");
+        a32[i] = (int)pairs[2 * i];
+        b32[i] = (int)pairs[2 * i + 1];
+    }
+    ENS(S.pA, sizeof(int) * (n + 1));
+    ENS(S.pB, sizeof(int) * (n + 1));
+    ENS(S.vals, sizeof(double) * 4 * dV * dV * (n + 1));
+    ENS(S.keepcnt, sizeof(int) * (n + 1));
+    ENS(S.closelist, sizeof(int) * (n + 1));
+    CK(cudaMemcpyAsync(S.pA.p, a32.data(), sizeof(int) * n, cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(S.pB.p, b32.data(), sizeof(int) * n, cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemsetAsync(S.vals.p, 0, sizeof(double) * 4 * dV * dV * (n + 1), S.st));
+    QuadArgs a;
+    memset(&a, 0, sizeof(a));
+    a.pA = S.pA.get<int>(); a.pB = S.pB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
+    a.probs = S.prm.get<ProbParams>(); a.P = n; a.err = S.err.get<int>();
+    a.n_close = S.counters.get<unsigned long long>() + 4;
+    a.blocks_out = S.vals.get<double>(); a.ret_out = S.keepcnt.get<int>(); a.force_close = close;
+    const ProbParams &P0 = S.hprm[0];
+    const int method = close ? P0.close : P0.remote;
+    if (method == MTH_FRACTIONAL) {
+        if (DIM != 2 || S.duffy_nPg == 0) return fail(NLFEM_ERR_INVALID, "close rule needs a 2D mesh and a tensor Gauss rule");
+        k_iota<<<grid_for(n, 256), 256, 0, S.st>>>(S.closelist.get<int>(), n);
+        a.list = S.closelist.get<int>();
+        a.nlist = n;
+        k_quad_close<<<grid_for(n * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+    } else {
+        k_quad_fp64<DIM><<<grid_for(n, 128), 128, 0, S.st>>>(a, S.rule);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(S.st));
+    r = check_errors(S);
+    if (r) return r;
+    r = d2h(S, out, S.vals.get<double>(), (size_t)n * 4 * dV * dV);
+    if (r) return r;
+    return d2h(S, ret, S.keepcnt.get<int>(), (size_t)n);
+}
+
+template <int DIM>
+static int run_quad(Session &S) {
+    const long long P = S.P, nnz = S.nnz_struct;
+    ENS(S.acc, sizeof(unsigned long long) * 2 * (nnz + 1));
+    ENS(S.tiny, sizeof(unsigned) * (nnz + 1));
+    CK(cudaMemsetAsync(S.acc.p, 0, sizeof(unsigned long long) * 2 * (nnz + 1), S.st));
+    CK(cudaMemsetAsync(S.tiny.p, 0, sizeof(unsigned) * (nnz + 1), S.st));
+    QuadArgs a;
+    a.pA = S.pA.get<int>(); a.pB = S.pB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
+    a.probs = S.prm.get<ProbParams>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    a.acc = S.acc.get<unsigned long long>(); a.tiny = S.tiny.get<unsigned>(); a.P = P;
+    a.list = nullptr; a.nlist = 0; a.err = S.err.get<int>();
+    a.blocks_out = nullptr; a.ret_out = nullptr; a.force_close = 0;
+    unsigned long long *cnt = S.counters.get<unsigned long long>();
+    a.n_close = cnt + 4;
+    CK(cudaMemsetAsync(cnt + 3, 0, 2 * sizeof(unsigned long long), S.st));
+    if (P > 0) k_quad_fp64<DIM><<<grid_for(P, 128), 128, 0, S.st>>>(a, S.rule);
+    if (DIM == 2 && S.duffy_nPg > 0 && P > 0) {
+        ENS(S.closelist, sizeof(int) * (P + 1));
+        k_close_list<DIM><<<grid_for(P, 256), 256, 0, S.st>>>(a, S.closelist.get<int>(), cnt + 3);
+        unsigned long long ncl = 0;
+        int r = d2h(S, &ncl, cnt + 3, 1);
+        if (r) return r;
+        a.list = S.closelist.get<int>();
+        a.nlist = (long long)ncl;
+        Duffy d = duffy_view(S);
+        if (ncl) k_quad_close<<<grid_for((long long)ncl * 32, 128), 128, 0, S.st>>>(a, d);
+    }
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+static int run_finish(Session &S) {
+    const long long nV = S.nV;
+    ENS(S.vals, sizeof(double) * (S.nnz_struct + 1));
+    ENS(S.keepcnt, sizeof(int) * (nV + 1));
+    ENS(S.fptr, sizeof(long long) * (nV + 1));
+    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.acc.get<unsigned long long>(), S.tiny.get<unsigned>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.vals.get<double>(), S.keepcnt.get<int>());
+    int r = scan_excl<int>(S, S.keepcnt.get<int>(), nV, S.fptr.get<long long>());
+    if (r) return r;
+    r = d2h(S, &S.nnz, S.fptr.get<long long>() + nV, 1);
+    if (r) return r;
+    ENS(S.fcols, sizeof(int) * (S.nnz + 1));
+    ENS(S.fvals, sizeof(double) * (S.nnz + 1));
+    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.acc.get<unsigned long long>(), S.tiny.get<unsigned>(), S.cols.get<int>(), S.vals.get<double>(), S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+static int check_errors(Session &S) {
+    int he[8];
+    int r = d2h(S, he, S.err.get<int>(), 8);
+    if (r) return r;
+    if (he[3]) return fail(NLFEM_ERR_CUDA, "internal: CSR slot not found during scatter");
+    if (he[4]) return fail(NLFEM_ERR_NUMERIC, "in solve2x2. Matrix not invertible.");
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_system_t(Session &S) {
+    int r;
+    CK(cudaEventRecord(S.ev[0], S.st));
+    if ((r = run_prep<DIM>(S))) return r;
+    if ((r = run_dual<DIM>(S))) return r;
+    if ((r = run_bfs<DIM>(S))) return r;
+    if ((r = run_pairs<DIM>(S))) return r;
+    CK(cudaEventRecord(S.ev[1], S.st));
+    if ((r = run_pattern<DIM>(S))) return r;
+    CK(cudaEventRecord(S.ev[2], S.st));
+    if ((r = run_quad<DIM>(S))) return r;
+    CK(cudaEventRecord(S.ev[3], S.st));
+    if ((r = run_finish(S))) return r;
+    CK(cudaEventRecord(S.ev[4], S.st));
+    CK(cudaStreamSynchronize(S.st));
+    if ((r = check_errors(S))) return r;
+    float t[4];
+    for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]));
+    unsigned long long ncl = 0;
+    if ((r = d2h(S, &ncl, S.counters.get<unsigned long long>() + 4, 1))) return r;
+    S.stats.n_close = (long)ncl;
+    S.stats.ms_bfs = t[0];
+    S.stats.ms_pattern = t[1];
+    S.stats.ms_quad = t[2];
+    S.stats.ms_finish = t[3];
+    S.stats.ms_total = t[0] + t[1] + t[2] + t[3];
+    g_stats = S.stats;
+    return NLFEM_OK;
+}
+
+static int run_system(Session &S) { return S.dim == 2 ? run_system_t<2>(S) : run_system_t<3>(S); }
+
+template <int DIM>
+static int run_forcing_t(Session &S) {
+    int r;
+    if ((r = run_prep<DIM>(S))) return r;
+    const long long nV = S.nV;
+    ENS(S.facc, sizeof(unsigned long long) * 2 * (nV + 1));
+    ENS(S.ftiny, sizeof(unsigned) * (nV + 1));
+    ENS(S.fd, sizeof(double) * (nV + 1));
+    CK(cudaMemsetAsync(S.facc.p, 0, sizeof(unsigned long long) * 2 * (nV + 1), S.st));
+    CK(cudaMemsetAsync(S.ftiny.p, 0, sizeof(unsigned) * (nV + 1), S.st));
+    k_forcing<DIM><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>());
+    k_forcing_finish<<<grid_for(nV, 256), 256, 0, S.st>>>(S.facc.get<unsigned long long>(), nV, S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fd.get<double>());
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(S.st));
+    return NLFEM_OK;
+}
+
+__global__ void k_export(const long long *__restrict__ fptr, const int *__restrict__ fcols, long long r0,
+                         long long nrows, long long c0, long long *__restrict__ indptr,
+                         long long *__restrict__ indices) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long base = fptr[r0];
+    if (i <= nrows) indptr[i] = fptr[r0 + i] - base;
+    const long long n = fptr[r0 + nrows] - base;
+    for (long long j = i; j < n; j += (long long)gridDim.x * blockDim.x) indices[j] = (long long)fcols[base + j] - c0;
+}
+
+static int download(Session &S, int i, nlfem_csr *out) {
+    const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
+    long long b[2];
+    int r = d2h(S, &b[0], S.fptr.get<long long>() + r0, 1);
+    if (r) return r;
+    r = d2h(S, &b[1], S.fptr.get<long long>() + r0 + nrows, 1);
+    if (r) return r;
+    const long long nnz = b[1] - b[0];
+    ENS(S.out64a, sizeof(long long) * (nrows + 1));
+    ENS(S.out64b, sizeof(long long) * (nnz + 1));
+    k_export<<<grid_for(std::max(nrows + 1, nnz), 256), 256, 0, S.st>>>(S.fptr.get<long long>(), S.fcols.get<int>(), r0, nrows, r0, S.out64a.get<long long>(), S.out64b.get<long long>());
+    CK(cudaGetLastError());
+    out->K = (long)nrows;
+    out->nnz = (long)nnz;
+    out->indptr = (long *)malloc(sizeof(long) * (nrows + 1));
+    out->indices = (long *)malloc(sizeof(long) * (nnz ? nnz : 1));
+    out->values = (double *)malloc(sizeof(double) * (nnz ? nnz : 1));
+    if (!out->indptr || !out->indices || !out->values) {
+        nlfem_csr_free(out);
+        return fail(NLFEM_ERR_NOMEM, "host allocation failed");
+    }
+    CK(cudaMemcpyAsync(out->indptr, S.out64a.p, sizeof(long long) * (nrows + 1), cudaMemcpyDeviceToHost, S.st));
+    if (nnz) {
+        CK(cudaMemcpyAsync(out->indices, S.out64b.p, sizeof(long long) * nnz, cudaMemcpyDeviceToHost, S.st));
+        CK(cudaMemcpyAsync(out->values, S.fvals.get<double>() + b[0], sizeof(double) * nnz, cudaMemcpyDeviceToHost, S.st));
+    }
+    CK(cudaStreamSynchronize(S.st));
+    return NLFEM_OK;
+}
+
+static int device_ok() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(NLFEM_ERR_CUDA, "no CUDA device available (the library has no CPU path)");
+    }
+    return NLFEM_OK;
+}
+
+}  // namespace nlg
+
+// ======================================================================= C ABI
+using namespace nlg;
+
+struct nlfem_session {
+    Session S;
+    std::vector<nlfem_problem> probs;
+};
+
+extern "C" {
+
+const char *nlfem_last_error(void) { return g_err.c_str(); }
+
+int nlfem_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return n;
+}
+
+int nlfem_get_stats(nlfem_stats *out) {
+    if (!out) return NLFEM_ERR_INVALID;
+    *out = g_stats;
+    return NLFEM_OK;
+}
+
+void nlfem_csr_free(nlfem_csr *m) {
+    if (!m) return;
+    free(m->indptr); free(m->indices); free(m->values);
+    m->indptr = nullptr; m->indices = nullptr; m->values = nullptr;
+}
+
+int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out) {
+    if (!probs || n <= 0 || !out) return fail(NLFEM_ERR_INVALID, "no problems");
+    int r = device_ok();
+    if (r) return r;
+    nlfem_session *s = new nlfem_session();
+    s->probs.assign(probs, probs + n);
+    r = session_init(s->S, probs, n, true);
+    if (!r) r = session_upload(s->S, probs);
+    if (!r) { cudaError_t e = cudaStreamSynchronize(s->S.st); if (e != cudaSuccess) r = fail(NLFEM_ERR_CUDA, cudaGetErrorString(e)); }
+    if (r) { delete s; return r; }
+    *out = s;
+    return NLFEM_OK;
+}
+
+int nlfem_session_assemble(nlfem_session *s) {
+    if (!s) return fail(NLFEM_ERR_INVALID, "null session");
+    return run_system(s->S);
+}
+
+int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out) {
+    if (!s || !out || i < 0 || i >= s->S.nProb) return fail(NLFEM_ERR_INVALID, "bad session download");
+    return download(s->S, i, out);
+}
+
+void nlfem_session_destroy(nlfem_session *s) { delete s; }
+
+int nlfem_stiffness_batch(const nlfem_problem *probs, int n, nlfem_csr *outs) {
+    if (!outs) return fail(NLFEM_ERR_INVALID, "null output");
+    nlfem_session *s = nullptr;
+    int r = nlfem_session_create(probs, n, &s);
+    if (r) return r;
+    r = run_system(s->S);
+    for (int i = 0; !r && i < n; i++) r = download(s->S, i, &outs[i]);
+    nlfem_session_destroy(s);
+    return r;
+}
+
+int nlfem_stiffness_matrix(const nlfem_problem *prob, nlfem_csr *out) {
+    return nlfem_stiffness_batch(prob, 1, out);
+}
+
+int nlfem_load_vector(const nlfem_problem *prob, double *fd) {
+    if (!prob || !fd) return fail(NLFEM_ERR_INVALID, "null argument");
+    int r = device_ok();
+    if (r) return r;
+    Session S;
+    r = session_init(S, prob, 1, false);
+    if (!r) r = session_upload(S, prob);
+    if (!r) r = (S.dim == 2) ? run_forcing_t<2>(S) : run_forcing_t<3>(S);
+    if (!r) r = d2h(S, fd, S.fd.get<double>(), (size_t)S.nV);
+    return r;
+}
+
+int nlfem_pair_list(const nlfem_problem *prob, long *n_pairs, long **pairs) {
+    if (!prob || !n_pairs || !pairs) return fail(NLFEM_ERR_INVALID, "null argument");
+    nlfem_session *s = nullptr;
+    int r = nlfem_session_create(prob, 1, &s);
+    if (r) return r;
+    Session &S = s->S;
+    r = S.dim == 2 ? (run_prep<2>(S) || run_dual<2>(S) || run_bfs<2>(S) || run_pairs<2>(S))
+                   : (run_prep<3>(S) || run_dual<3>(S) || run_bfs<3>(S) || run_pairs<3>(S));
+    if (r) { r = g_err.empty() ? NLFEM_ERR_CUDA : r; nlfem_session_destroy(s); return r ? r : NLFEM_ERR_CUDA; }
+    const long long P = S.P;
+    std::vector<int> a(P), b(P);
+    if (P) {
+        r = d2h(S, a.data(), S.pA.get<int>(), P);
+        if (!r) r = d2h(S, b.data(), S.pB.get<int>(), P);
+    }
+    nlfem_session_destroy(s);
+    if (r) return r;
+    std::vector<long long> key(P);
+    for (long long i = 0; i < P; i++) key[i] = ((long long)a[i] << 32) | (unsigned)b[i];
+    std::sort(key.begin(), key.end());
+    long *o = (long *)malloc(sizeof(long) * 2 * (P ? P : 1));
+    for (long long i = 0; i < P; i++) { o[2 * i] = (long)(key[i] >> 32); o[2 * i + 1] = (long)(key[i] & 0xffffffffLL); }
+    *n_pairs = (long)P;
+    *pairs = o;
+    return NLFEM_OK;
+}
+
+int nlfem_pair_blocks(const nlfem_problem *prob, long n, const long *pairs, int close,
+                      double *out, int *does_interact) {
+    if (!prob || n < 0 || (n && (!pairs || !out || !does_interact))) return fail(NLFEM_ERR_INVALID, "null argument");
+    if (n == 0) return NLFEM_OK;
+    nlfem_session *s = nullptr;
+    int r = nlfem_session_create(prob, 1, &s);
+    if (r) return r;
+    r = s->S.dim == 2 ? run_pair_blocks<2>(s->S, n, pairs, close, out, does_interact)
+                      : run_pair_blocks<3>(s->S, n, pairs, close, out, does_interact);
+    nlfem_session_destroy(s);
+    return r;
+}
+
+int nlfem_retriangulate_batch(long n, const double *x_center, const double *TE, double sqdelta,
+                              int caps, int *counts, double *out) {
+    if (n < 0 || (n && (!x_center || !TE || !counts || !out))) return fail(NLFEM_ERR_INVALID, "null argument");
+    if (n == 0) return NLFEM_OK;
+    int r = device_ok();
+    if (r) return r;
+    double *dx = nullptr, *dT = nullptr, *dO = nullptr;
+    int *dc = nullptr;
+    CK(cudaMalloc(&dx, sizeof(double) * 2 * n));
+    CK(cudaMalloc(&dT, sizeof(double) * 6 * n));
+    CK(cudaMalloc(&dO, sizeof(double) * 54 * n));
+    CK(cudaMalloc(&dc, sizeof(int) * n));
+    CK(cudaMemcpy(dx, x_center, sizeof(double) * 2 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dT, TE, sizeof(double) * 6 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dO, 0, sizeof(double) * 54 * n));
+    k_retri_batch<<<grid_for(n, 128), 128>>>(n, dx, dT, sqdelta, caps, dc, dO);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(counts, dc, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out, dO, sizeof(double) * 54 * n, cudaMemcpyDeviceToHost));
+    cudaFree(dx); cudaFree(dT); cudaFree(dO); cudaFree(dc);
+    return NLFEM_OK;
+}
+
+int nlfem_method_retriangulate(const double *x_center, const double *TE, double sqdelta,
+                               double *reTriangleList, int is_placePointOnCap) {
+    int cnt = 0;
+    int r = nlfem_retriangulate_batch(1, x_center, TE, sqdelta, is_placePointOnCap, &cnt, reTriangleList);
+    return r ? -r : cnt;
+}
+
+static int geom_misc(int op, const double *A, int na, const double *b, int nb, int dim, double *out, int nout) {
+    int r = device_ok();
+    if (r) return r;
+    double *dA, *db, *dO;
+    int *dok, ok = 0;
+    CK(cudaMalloc(&dA, sizeof(double) * na));
+    CK(cudaMalloc(&db, sizeof(double) * nb));
+    CK(cudaMalloc(&dO, sizeof(double) * nout));
+    CK(cudaMalloc(&dok, sizeof(int)));
+    CK(cudaMemcpy(dA, A, sizeof(double) * na, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(db, b, sizeof(double) * nb, cudaMemcpyHostToDevice));
+    k_geom_misc<<<1, 32>>>(op, dA, db, dim, dO, dok);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out, dO, sizeof(double) * nout, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ok, dok, sizeof(int), cudaMemcpyDeviceToHost));
+    cudaFree(dA); cudaFree(db); cudaFree(dO); cudaFree(dok);
+    return ok ? NLFEM_OK : fail(NLFEM_ERR_NUMERIC, "in solve2x2. Matrix not invertible.");
+}
+
+int nlfem_toRef(const double *E, const double *phys_x, double *ref_p) {
+    if (!E || !phys_x || !ref_p) return fail(NLFEM_ERR_INVALID, "null argument");
+    return geom_misc(0, E, 6, phys_x, 2, 2, ref_p, 2);
+}
+int nlfem_toPhys(const double *E, const double *p, int dim, double *out_x) {
+    if (!E || !p || !out_x || (dim != 2 && dim != 3)) return fail(NLFEM_ERR_INVALID, "bad argument");
+    return geom_misc(1, E, dim * (dim + 1), p, dim, dim, out_x, dim);
+}
+int nlfem_solve2x2(const double *A, const double *b, double *x) {
+    if (!A || !b || !x) return fail(NLFEM_ERR_INVALID, "null argument");
+    return geom_misc(2, A, 4, b, 2, 2, x, 2);
+}
+
+}  // extern "C"

@@ -1,0 +1,347 @@
+// Per-pair quadrature of the four local blocks and their scatter into the CSR accumulators.
+//
+//   termLocal[a][b]       -> A[aV[a], aV[b]]   (+), row kept if label(aV[a]) > 0
+//   termNonloc[a][b]      -> A[aV[a], bV[b]]   (-)
+//   termLocalPrime[a][b]  -> A[bV[b], bV[a]]   (+), row kept if label(bV[b]) > 0
+//   termNonlocPrime[a][b] -> A[bV[b], aV[a]]   (-)
+// (src/Cassemble.cpp:721-770, outdim = 1, no domain-decomposition weight).
+#pragma once
+#include "geometry.cuh"
+#include "primitives.cuh"
+
+namespace nlg {
+
+constexpr int MAXQ = 32;   // points per outer/inner rule
+
+// Quadrature rule on the reference element; passed by value (kernel parameter space).
+struct Rule {
+    int nPx, nPy, dim, pad;
+    double Px[MAXQ * 3], dx[MAXQ], Py[MAXQ * 3], dy[MAXQ];
+    double psix[MAXQ * 4], psiy[MAXQ * 4];   // [k * dV + a]
+    float Pyf[MAXQ * 2], dyf[MAXQ], psiyf[MAXQ * 4];
+};
+
+// Duffy tables of the singular close-pair rule (MeshTypes.cpp:252-327), device pointers.
+struct Duffy {
+    int nPg;
+    const double *alpha[3];   // [case][(t * nPg + k) * 4 + j]
+    const double *tdet[3];    // [case][t * nPg + k]
+    const double *dg;         // [k]
+};
+
+struct QuadArgs {
+    const int *pA, *pB, *T32, *labV, *eprob;
+    const double *EC, *adet;
+    const ProbParams *probs;
+    const long long *rowptr;
+    const int *cols;
+    unsigned long long *acc;
+    unsigned *tiny;
+    long long P;
+    const int *list;          // optional index list into the pairs
+    long long nlist;
+    int *err;                 // [3] slot not found, [4] singular toRef
+    unsigned long long *n_close;
+    double *blocks_out;       // explicit-pair mode: (P, 4, dV, dV) blocks instead of scatter
+    int *ret_out;             // explicit-pair mode: doesInteract
+    int force_close;          // explicit-pair mode: use the close-pair rule
+};
+
+__device__ __forceinline__ long long find_slot(const long long *__restrict__ rowptr,
+                                               const int *__restrict__ cols, int row, int col) {
+    long long lo = rowptr[row], hi = rowptr[row + 1] - 1;
+    while (lo <= hi) {
+        long long mid = (lo + hi) >> 1;
+        int c = cols[mid];
+        if (c == col) return mid;
+        if (c < col) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void add_entry(const QuadArgs &a, int row, int col, double val, int se) {
+    long long s = find_slot(a.rowptr, a.cols, row, col);
+    if (s < 0) { atomicOr(&a.err[3], 1); return; }
+    fx_atomic_add(&a.acc[2 * s], val, se, &a.tiny[s]);
+}
+
+template <int dV>
+__device__ __forceinline__ void scatter_blocks(const QuadArgs &a, const int *aV, const int *bV,
+                                               const double *L, const double *N, const double *LP,
+                                               const double *NP, int se, bool prime) {
+#pragma unroll 1
+    for (int i = 0; i < dV; i++) {
+        if (a.labV[aV[i]] > 0) {
+            for (int j = 0; j < dV; j++) {
+                add_entry(a, aV[i], aV[j], L[dV * i + j], se);
+                add_entry(a, aV[i], bV[j], -N[dV * i + j], se);
+            }
+        }
+    }
+    if (!prime) return;
+#pragma unroll 1
+    for (int j = 0; j < dV; j++) {
+        if (a.labV[bV[j]] > 0) {
+            for (int i = 0; i < dV; i++) {
+                add_entry(a, bV[j], bV[i], LP[dV * i + j], se);
+                add_entry(a, bV[j], aV[i], -NP[dV * i + j], se);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ bool share_vertex(const int *aV, const int *bV, int dV) {
+    for (int i = 0; i < dV; i++)
+        for (int j = 0; j < dV; j++)
+            if (aV[i] == bV[j]) return true;
+    return false;
+}
+
+// FP64 integrate_retriangulate (integration.cpp:345-540) of one pair.
+__device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, const double *Ea,
+                                      const double *Eb, double adet_a, double *L, double *N,
+                                      double *LP, double *NP, int *err) {
+    double R[18];
+    int interacts = 0;
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2];
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        const int Rdx = xretriangulate(x, Eb, P.sqdelta, P.caps, R);
+        interacts |= (Rdx >= 3);
+        double innerLocal = 0, iN[3] = {0, 0, 0}, iNP[3] = {0, 0, 0};
+        for (int r = 0; r + 2 < Rdx; r++) {
+            const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
+            const double rTdet = xabsDet2(tri);
+            for (int i = 0; i < rule.nPy; i++) {
+                double y[2];
+                // toPhys(E, p, out) of the sub-triangle (mathhelpers.cpp:210-215)
+                y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
+                y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
+                const double ker = kernel_f64<2>(P, x, y);
+                const double w = rule.dy[i] * rTdet;
+                innerLocal += ker * w;
+                double ref[2];
+                if (!xtoRef(Eb, y, ref)) atomicOr(&err[4], 1);
+                const double kerP = kernel_f64<2>(P, y, x);
+                const double psi[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
+                const double wl = kerP * w * rule.dx[k] * adet_a;
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    iN[b] += psi[b] * ker * w;
+                    iNP[b] += psi[b] * kerP * w;
+                }
+#pragma unroll
+                for (int aa = 0; aa < 3; aa++)
+#pragma unroll
+                    for (int b = 0; b < 3; b++) LP[3 * aa + b] += psi[aa] * psi[b] * wl;
+            }
+        }
+        const double wx = adet_a * rule.dx[k];
+#pragma unroll
+        for (int aa = 0; aa < 3; aa++) {
+            const double pa = rule.psix[3 * k + aa] * wx;
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                L[3 * aa + b] += pa * rule.psix[3 * k + b] * innerLocal;
+                N[3 * aa + b] += pa * iN[b];
+                NP[3 * aa + b] += pa * iNP[b];
+            }
+        }
+    }
+    return interacts | P.full_search;
+}
+
+// FP64 integrate_baryCenter (integration.cpp:910-1018) of one pair (2D or 3D).
+template <int DIM>
+__device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const double *Ea,
+                                   const double *Eb, double adet_a, double adet_b, double *L,
+                                   double *N) {
+    constexpr int dV = DIM + 1;
+    double b[DIM];
+    xbary<DIM>(Eb, b);
+    int interacts = 0;
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[DIM];
+        xtoPhys<DIM>(Ea, &rule.Px[DIM * k], x);
+        if (!xbaryInside<DIM>(x, b, P.sqdelta)) continue;
+        interacts = 1;
+        double innerLocal = 0, iN[dV];
+#pragma unroll
+        for (int j = 0; j < dV; j++) iN[j] = 0;
+        for (int i = 0; i < rule.nPy; i++) {
+            double y[DIM];
+            xtoPhys<DIM>(Eb, &rule.Py[DIM * i], y);
+            const double ker = kernel_f64<DIM>(P, x, y);
+            innerLocal += adet_b * ker * rule.dy[i];
+            const double kerP = kernel_f64<DIM>(P, y, x);
+#pragma unroll
+            for (int j = 0; j < dV; j++) iN[j] += rule.psiy[dV * i + j] * kerP * rule.dy[i] * adet_b;
+        }
+        const double wx = 2.0 * adet_a * rule.dx[k];
+#pragma unroll
+        for (int aa = 0; aa < dV; aa++) {
+            const double pa = rule.psix[dV * k + aa] * wx;
+#pragma unroll
+            for (int j = 0; j < dV; j++) {
+                L[dV * aa + j] += pa * rule.psix[dV * k + j] * innerLocal;
+                N[dV * aa + j] += pa * iN[j];
+            }
+        }
+    }
+    return interacts | P.full_search;
+}
+
+// One thread per (non-close) pair: FP64 quadrature and scatter.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
+    constexpr int dV = DIM + 1;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const int aT = a.pA[p], bT = a.pB[p];
+    const ProbParams P = a.probs[a.eprob[aT]];
+    int aV[dV], bV[dV];
+#pragma unroll
+    for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
+    const bool close = a.blocks_out ? (a.force_close != 0) : (P.singular && share_vertex(aV, bV, dV));
+    const int method = close ? P.close : P.remote;
+    if (method == MTH_FRACTIONAL) return;   // handled by k_quad_close
+    double Ea[DIM * dV], Eb[DIM * dV];
+#pragma unroll
+    for (int i = 0; i < DIM * dV; i++) { Ea[i] = a.EC[(long long)aT * DIM * dV + i]; Eb[i] = a.EC[(long long)bT * DIM * dV + i]; }
+    double L[dV * dV], N[dV * dV], LP[dV * dV], NP[dV * dV];
+#pragma unroll
+    for (int i = 0; i < dV * dV; i++) { L[i] = 0; N[i] = 0; LP[i] = 0; NP[i] = 0; }
+    bool prime = false;
+    int interacts = 0;
+    if (method == MTH_BARYCENTER) {
+        interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.adet[aT], a.adet[bT], L, N);
+    } else if (DIM == 2) {
+        interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.adet[aT], L, N, LP, NP, a.err);
+        prime = true;
+    }
+    if (a.blocks_out) {
+        double *o = &a.blocks_out[p * 4 * dV * dV];
+        for (int i = 0; i < dV * dV; i++) {
+            o[i] = L[i]; o[dV * dV + i] = N[i]; o[2 * dV * dV + i] = LP[i]; o[3 * dV * dV + i] = NP[i];
+        }
+        a.ret_out[p] = interacts;
+        return;
+    }
+    scatter_blocks<dV>(a, aV, bV, L, N, LP, NP, P.scale_exp, prime);
+}
+
+// Flags and lists the close pairs (singular kernel, shared vertex, fractional close rule).
+template <int DIM>
+__global__ void k_close_list(QuadArgs a, int *list, unsigned long long *count) {
+    constexpr int dV = DIM + 1;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const int aT = a.pA[p], bT = a.pB[p];
+    const ProbParams &P = a.probs[a.eprob[aT]];
+    if (!P.singular || P.close != MTH_FRACTIONAL) return;
+    int aV[dV], bV[dV];
+    for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
+    if (!share_vertex(aV, bV, dV)) return;
+    unsigned long long i = atomicAdd(count, 1ULL);
+    list[i] = (int)p;
+}
+
+// One warp per close pair: integrate_fractional (integration.cpp:187-288) with join()
+// (:1913-1958), FP64 throughout; lanes stride over the Duffy points, warp-reduce the blocks.
+__global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
+    const int lane = threadIdx.x & 31;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= a.nlist) return;
+    const long long p = a.list[w];
+    const int aT = a.pA[p], bT = a.pB[p];
+    const ProbParams P = a.probs[a.eprob[aT]];
+    const int *aV = &a.T32[(long long)aT * 3];
+    const int *bV = &a.T32[(long long)bT * 3];
+    // join
+    int nEqual = 0, AinB[3] = {0, 0, 0}, BinA[3] = {0, 0, 0}, argA[3], argB[3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            if (aV[i] == bV[j]) {
+                AinB[i] += 1; BinA[j] += 1;
+                argA[nEqual] = i;
+                argB[nEqual] = j;
+                nEqual++;
+            }
+    int ia = 0, ib = 0;
+    for (int i = 0; i < 3; i++) {
+        if (!AinB[i]) { argA[nEqual + ia] = i; ia++; }
+        if (!BinA[i]) { argB[nEqual + ib] = i; ib++; }
+    }
+    double EA[6], EB[6];
+    const double *Ea = &a.EC[(long long)aT * 6], *Eb = &a.EC[(long long)bT * 6];
+    for (int k = 0; k < 3; k++) {
+        int ka = argA[k], kb = argB[k];
+        EA[2 * k] = Ea[2 * ka]; EA[2 * k + 1] = Ea[2 * ka + 1];
+        EB[2 * k] = Eb[2 * kb]; EB[2 * k + 1] = Eb[2 * kb + 1];
+    }
+    const double dA = fabs(xsub(xmul(xsub(EA[2], EA[0]), xsub(EA[5], EA[1])), xmul(xsub(EA[3], EA[1]), xsub(EA[4], EA[0]))));
+    const double dB = fabs(xsub(xmul(xsub(EB[2], EB[0]), xsub(EB[5], EB[1])), xmul(xsub(EB[3], EB[1]), xsub(EB[4], EB[0]))));
+    const int c = nEqual - 1;
+    if (c < 0) return;
+    const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    const int nLocal = 6 - nEqual, shift = 3 - nEqual;
+    // target of (a, b) in the 4 x 9 block vector and its sign
+    int tgt[36];
+    double sgn[36];
+    for (int aa = 0; aa < nLocal; aa++)
+        for (int b = 0; b < nLocal; b++) {
+            int t;
+            double s;
+            if (aa < 3) {
+                if (b < 3) { t = 0 * 9 + 3 * argA[aa] + argA[b]; s = 1.0; }
+                else { t = 1 * 9 + 3 * argA[aa] + argB[b - shift]; s = -1.0; }
+            } else {
+                if (b < 3) { t = 3 * 9 + 3 * argA[b] + argB[aa - shift]; s = -1.0; }
+                else { t = 2 * 9 + 3 * argB[aa - shift] + argB[b - shift]; s = 1.0; }
+            }
+            tgt[aa * 6 + b] = t;
+            sgn[aa * 6 + b] = s;
+        }
+    double acc[36];
+    for (int i = 0; i < 36; i++) acc[i] = 0;
+    const int total = nT * d.nPg;
+    const double *al_base = d.alpha[c];
+    const double *td_base = d.tdet[c];
+    for (int idx = lane; idx < total; idx += 32) {
+        const int k = idx % d.nPg;
+        const double *al = &al_base[(long long)idx * 4];
+        const double tf = td_base[idx];
+        double x[2], y[2];
+        x[0] = al[0] * (EA[2] - EA[0]) + al[1] * (EA[4] - EA[0]) + EA[0];
+        x[1] = al[0] * (EA[3] - EA[1]) + al[1] * (EA[5] - EA[1]) + EA[1];
+        y[0] = al[2] * (EB[2] - EB[0]) + al[3] * (EB[4] - EB[0]) + EB[0];
+        y[1] = al[2] * (EB[3] - EB[1]) + al[3] * (EB[5] - EB[1]) + EB[1];
+        const double ker = kernel_f64<2>(P, x, y);
+        const double px[3] = {1.0 - al[0] - al[1], al[0], al[1]};
+        const double py[3] = {1.0 - al[2] - al[3], al[2], al[3]};
+        double pxy[6];
+        for (int i = 0; i < nEqual; i++) pxy[i] = px[i] - py[i];
+        for (int i = nEqual; i < 3; i++) { pxy[i] = px[i]; pxy[i + shift] = -py[i]; }
+        const double base = ker * tf * d.dg[k] * dA * dB;
+        for (int aa = 0; aa < nLocal; aa++) {
+            const double fa = base * pxy[aa];
+            for (int b = 0; b < nLocal; b++) acc[tgt[aa * 6 + b]] += sgn[aa * 6 + b] * fa * pxy[b];
+        }
+    }
+    for (int i = 0; i < 36; i++) acc[i] = warp_sum(acc[i]);
+    if (a.blocks_out) {
+        if (lane == 0) {
+            double *o = &a.blocks_out[p * 36];
+            for (int i = 0; i < 36; i++) o[i] = acc[i];
+            a.ret_out[p] = 1;
+        }
+        return;
+    }
+    if (lane == 0) {
+        int aVl[3] = {aV[0], aV[1], aV[2]}, bVl[3] = {bV[0], bV[1], bV[2]};
+        scatter_blocks<3>(a, aVl, bVl, &acc[0], &acc[9], &acc[18], &acc[27], P.scale_exp, true);
+        atomicAdd(a.n_close, 1ULL);
+    }
+}
+
+}  // namespace nlg

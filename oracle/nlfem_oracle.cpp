@@ -1,0 +1,896 @@
+// nlfem oracle: CPU restatement of the reference assembly path (TEST INFRASTRUCTURE ONLY).
+//
+// This file is the checker for the GPU library, never a product path. Only tests/, the smoke
+// check and bench.py's CPU-baseline / reference arm load it. It restates, function by function,
+// the reference's FP64 algorithm for nonlocal stiffness-matrix and load-vector assembly
+// (cagau/nlfem). Every function cites the reference file:line it follows. Arithmetic keeps the
+// reference's operation order; it is compiled with -ffp-contract=off so no FMA contraction
+// changes a rounding (the reference's x86 build has none either).
+//
+// Parity status: the reference's own tests hold no golden vectors for the assembled matrix or
+// load vector, and the reference itself cannot be built here (it needs Armadillo, METIS and
+// CGAL, none of which exist in this image). Parity of this restatement is therefore UNPINNED
+// for the assembled values; it is pinned only where fixtures exist (quadrature tables, tensor
+// Gauss rule, vertex labels, arma file format, 6-tet split). See the oracle tests.
+//
+// Differences from the reference that cannot change results beyond rounding:
+//  * arma::det is replaced by the cofactor formula (feeds |det| only, never a predicate).
+//  * METIS_MeshToDual is replaced by a sorted vertex-sharing adjacency (the BFS pair set does
+//    not depend on adjacency order; only the map's summation order may).
+//  * METIS_PartMeshDual (thread split) is replaced by contiguous element blocks.
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <queue>
+#include <string>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const double EPSILON = 1e-15;        // mathhelpers.h:11
+const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
+
+enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_NONE = -1 };
+enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_NONE = -1 };
+enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_NONE = -1 };
+
+struct Mesh {
+    int dim, dV, outdim, is_dg;
+    long nE, nV, K;
+    const long *T, *labT, *labV;
+    const double *V;
+    double sqdelta, delta, frac_s;
+    int kernel, load;
+    int remote, close;   // MethodId of integrate_remote / integrate_close
+    int is_singular;
+    int caps, full_search;
+};
+
+struct Quad {
+    const double *Px, *dx, *Py, *dy;
+    int nPx, nPy;
+    std::vector<double> psix, psiy;  // column-major (dV, nP): psi[dV*k + a]
+    int nPg;
+    const double *dg;
+    // Duffy tables of the fractional close-pair rule, index [case][ (t*nPg + k)*4 + j ]
+    std::vector<double> alphaC[3], tdetFrac[3];
+};
+
+struct Elem {
+    double E[12];
+    double absDet;
+    long label;
+    long Tdx;
+};
+
+// ---------------------------------------------------------------- math helpers (mathhelpers.cpp)
+inline double absolute(double v) { return v < 0 ? -v : v; }                // mathhelpers.cpp:362-368
+inline bool double_eq(double x, double y, double eps = EPSILON) {           // mathhelpers.cpp:370-373
+    return absolute(x - y) < eps;
+}
+inline double sq(double v) { return v * v; }  // pow(v, 2): gcc folds pow(x, 2.0) to x*x
+
+double vec_dot(const double *x, const double *y, int len) {                 // mathhelpers.cpp:255-263
+    double r = 0;
+    for (int i = 0; i < len; i++) r += x[i] * y[i];
+    return r;
+}
+double vec_sqL2dist(const double *x, const double *y, int len) {            // mathhelpers.cpp:272-279
+    double r = 0;
+    for (int i = 0; i < len; i++) r += sq(x[i] - y[i]);
+    return r;
+}
+
+int solve2x2(const double *A, const double *b, double *x) {                 // mathhelpers.cpp:41-71
+    int dx0 = 0, dx1 = 1;
+    if (absolute(A[0]) < absolute(A[2])) { dx0 = 1; dx1 = 0; }
+    if (double_eq(A[2 * dx0], 0)) return -1;  // reference aborts
+    double l = A[2 * dx1] / A[2 * dx0];
+    double u = A[2 * dx1 + 1] - l * A[2 * dx0 + 1];
+    if (u == 0) return -1;                     // reference aborts
+    x[1] = (b[dx1] - l * b[dx0]) / u;
+    x[0] = (b[dx0] - A[2 * dx0 + 1] * x[1]) / A[2 * dx0];
+    return 0;
+}
+
+void rightNormal(const double *y0, const double *y1, double orientation, double *n) {  // :74-78
+    n[0] = y1[1] - y0[1];
+    n[1] = y0[0] - y1[0];
+    n[0] = n[0] * orientation;
+    n[1] = n[1] * orientation;
+}
+
+double absDet2(const double *E) {                                          // mathhelpers.cpp:101-109
+    double M00 = E[2] - E[0], M01 = E[4] - E[0];
+    double M10 = E[3] - E[1], M11 = E[5] - E[1];
+    return absolute(M00 * M11 - M01 * M10);
+}
+
+double detDim(const double *E, int dim) {
+    // mathhelpers.cpp:112-129: M(j, i-1) = E[j + dim*i] - E[j]; arma::det(M) (cofactor form here)
+    if (dim == 2) {
+        double a = E[2] - E[0], b = E[4] - E[0];
+        double c = E[3] - E[1], d = E[5] - E[1];
+        return a * d - c * b;
+    }
+    double M[3][3];
+    for (int i = 1; i < 4; i++)
+        for (int j = 0; j < 3; j++) M[j][i - 1] = E[j + 3 * i] - E[j];
+    return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1])
+         - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0])
+         + M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+}
+double absDetDim(const double *E, int dim) { return absolute(detDim(E, dim)); }
+
+double signDet2(const double *E) {                                         // mathhelpers.cpp:131-147
+    double M00 = E[2] - E[0], M01 = E[4] - E[0];
+    double M10 = E[3] - E[1], M11 = E[5] - E[1];
+    double det = M00 * M11 - M01 * M10;
+    if (det > 0) return 1.;
+    if (det < 0) return -1.;
+    return 0.0;
+}
+
+void baryCenter(int dim, const double *E, double *bary) {                  // mathhelpers.cpp:184-196
+    int dVert = dim + 1;
+    for (int j = 0; j < dim; j++) {
+        bary[j] = 0;
+        for (int i = 0; i < dVert; i++) bary[j] += E[dim * i + j];
+        bary[j] = bary[j] / static_cast<double>(dVert);
+    }
+}
+
+void toPhys3(const double *E, const double *p, double *x) {                // mathhelpers.cpp:210-215
+    for (int i = 0; i < 2; i++)
+        x[i] = (E[2 + i] - E[i]) * p[0] + (E[4 + i] - E[i]) * p[1] + E[i];
+}
+void toPhys(const double *E, const double *p, int dim, double *x) {        // mathhelpers.cpp:217-225
+    for (int i = 0; i < dim; i++) {
+        x[i] = 0;
+        for (int j = 0; j < dim; j++) x[i] += p[j] * (E[dim * (j + 1) + i] - E[i]);
+        x[i] += E[i];
+    }
+}
+int toRef(const double *E, const double *x, double *p) {                   // mathhelpers.cpp:227-240
+    double M[4], b[2];
+    M[0] = E[2] - E[0];
+    M[1] = E[4] - E[0];
+    M[2] = E[3] - E[1];
+    M[3] = E[5] - E[1];
+    b[0] = x[0] - E[0];
+    b[1] = x[1] - E[1];
+    return solve2x2(M, b, p);
+}
+
+void basis(const double *p, int dim, double *psi) {                        // MeshTypes.cpp:16-24
+    psi[0] = 1;
+    for (int i = 0; i < dim; i++) {
+        psi[0] -= p[i];
+        psi[i + 1] = p[i];
+    }
+}
+
+// ---------------------------------------------------------------- model (model.cpp)
+double kernel_value(const Mesh &m, const double *x, const double *y) {
+    switch (m.kernel) {
+    case K_CONSTANT:   // model.cpp:25-28
+        return 4 / (M_PI * sq(m.sqdelta));
+    case K_PARABOLA: { // model.cpp:52-60
+        double z[2] = {x[0] - y[0], x[1] - y[1]};
+        const double value = m.sqdelta - vec_dot(z, z, 2);
+        const double c = 12. / (M_PI * pow(m.sqdelta, 3));
+        return c * value;
+    }
+    case K_FRACTIONAL: { // model.cpp:126-138
+        const double exponent = m.dim + 2. * m.frac_s;
+        const double constant_exponent = 2. - 2. * m.frac_s;
+        double z[3];
+        for (int i = 0; i < m.dim; i++) z[i] = x[i] - y[i];
+        const double denominator = 1.0 / pow(sqrt(vec_dot(z, z, m.dim)), exponent);
+        const double c = (constant_exponent) / (M_PI * pow(m.delta, constant_exponent));
+        return c * denominator;
+    }
+    case K_CONSTANT3D: // model.cpp:62-65
+        return 15 / (M_PI * 4 * pow(m.delta, 5));
+    }
+    return NAN;
+}
+
+double load_value(const Mesh &m, const double *x) {
+    switch (m.load) {
+    case F_LINEAR: return -2. * (x[1] + 1.);     // model.cpp:240-242
+    case F_LINEAR3D: return -2. * (x[1] + 2.);   // model.cpp:259-261
+    case F_CONSTANT: return 1.0;                 // model.cpp:201-203
+    }
+    return NAN;
+}
+
+// ---------------------------------------------------------------- elements (MeshTypes.cpp:216-250)
+void initializeElement(long Tdx, const Mesh &m, Elem &T) {
+    for (int k = 0; k < m.dV; k++) {
+        long Vdx = m.T[m.dV * Tdx + k];
+        for (int j = 0; j < m.dim; j++) T.E[m.dim * k + j] = m.V[m.dim * Vdx + j];
+    }
+    T.absDet = absDetDim(T.E, m.dim);
+    T.label = m.labT[Tdx];
+    T.Tdx = Tdx;
+}
+
+// ---------------------------------------------------------------- ball truncation (integration.cpp)
+bool inTriangle(const double *y, const double *p, const double *q, const double *r,
+                const double *na, const double *nb, const double *nc) {   // integration.cpp:1283-1298
+    double v[2];
+    v[0] = y[0] - p[0]; v[1] = y[1] - p[1];
+    bool a = vec_dot(na, v, 2) >= 0;
+    v[0] = y[0] - q[0]; v[1] = y[1] - q[1];
+    bool b = vec_dot(nb, v, 2) >= 0;
+    v[0] = y[0] - r[0]; v[1] = y[1] - r[1];
+    bool c = vec_dot(nc, v, 2) >= 0;
+    return a && b && c;
+}
+
+int placePointOnCap(const double *ypred, const double *ycur, const double *x, double sqdelta,
+                    const double *TE, const double *na, const double *nb, const double *nc,
+                    double orientation, int Rdx, double *R) {             // integration.cpp:1353-1377
+    double n[2], ynew[2];
+    rightNormal(ycur, ypred, orientation, n);
+    double s = sqrt(sqdelta / vec_dot(n, n, 2));
+    n[0] = n[0] * s;
+    n[1] = n[1] * s;
+    ynew[0] = x[0] + n[0];
+    ynew[1] = x[1] + n[1];
+    if (inTriangle(ynew, &TE[0], &TE[2], &TE[4], na, nb, nc)) {
+        R[2 * Rdx] = ynew[0];
+        R[2 * Rdx + 1] = ynew[1];
+        return 1;
+    }
+    return 0;
+}
+
+int method_retriangulate(const double *xc, const double *TE, double sqdelta, double *out,
+                         int caps) {                                       // integration.cpp:1393-1512
+    int Rdx = 0;
+    double na[2], nb[2], nc[2];
+    bool is_onEdge = false, is_firstPointLiesOnVertex = true;
+    double R[9 * 2];
+    for (int i = 0; i < 18; i++) R[i] = 0;
+    double orientation = -signDet2(TE);
+    rightNormal(&TE[0], &TE[2], orientation, na);
+    rightNormal(&TE[2], &TE[4], orientation, nb);
+    rightNormal(&TE[4], &TE[0], orientation, nc);
+    for (int k = 0; k < 3; k++) {
+        const double *p = &TE[2 * k];
+        const double *q = &TE[2 * ((k + 1) % 3)];
+        double a[2] = {q[0] - xc[0], q[1] - xc[1]};
+        double b[2] = {p[0] - q[0], p[1] - q[1]};
+        if (vec_sqL2dist(p, xc, 2) <= sqdelta) {
+            R[2 * Rdx] = p[0];
+            R[2 * Rdx + 1] = p[1];
+            is_onEdge = false;
+            Rdx += 1;
+        }
+        // arma::dot of two 2-vectors: a0*b0 + a1*b1
+        double ab = a[0] * b[0] + a[1] * b[1];
+        double aa = a[0] * a[0] + a[1] * a[1];
+        double bb = b[0] * b[0] + b[1] * b[1];
+        double v = sq(ab) - (aa - sqdelta) * bb;
+        if (v >= 0) {
+            double term1 = -ab / bb;
+            double term2 = sqrt(v) / bb;
+            double lam1, lam2;
+            if (term1 > 0) {
+                lam1 = term1 + term2;
+                lam2 = 1 / lam1 * (aa - sqdelta) / bb;
+            } else {
+                lam2 = term1 - term2;
+                lam1 = 1 / lam2 * (aa - sqdelta) / bb;
+            }
+            double y1[2] = {lam1 * b[0] + q[0], lam1 * b[1] + q[1]};
+            double y2[2] = {lam2 * b[0] + q[0], lam2 * b[1] + q[1]};
+            if ((0 <= lam1) && (lam1 <= 1)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
+                if (is_onEdge && caps)
+                    Rdx += placePointOnCap(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+                R[2 * Rdx] = y1[0];
+                R[2 * Rdx + 1] = y1[1];
+                is_onEdge = true;
+                Rdx += 1;
+            }
+            if ((0 <= lam2) && (lam2 <= 1) && (sq(lam1 - lam2) > 0)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
+                if (is_onEdge && caps)
+                    Rdx += placePointOnCap(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+                R[2 * Rdx] = y2[0];
+                R[2 * Rdx + 1] = y2[1];
+                is_onEdge = true;
+                Rdx += 1;
+            }
+        }
+    }
+    if (is_onEdge && (!is_firstPointLiesOnVertex && Rdx > 1) && caps)
+        Rdx += placePointOnCap(&R[2 * (Rdx - 1)], &R[0], xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+    if (Rdx < 3) return 0;
+    for (int k = 0; k < Rdx - 2; k++) {
+        for (int i = 0; i < 2; i++) {
+            out[2 * (3 * k + 0) + i] = R[i];
+            out[2 * (3 * k + 1) + i] = R[2 * (k + 1) + i];
+            out[2 * (3 * k + 2) + i] = R[2 * (k + 2) + i];
+        }
+    }
+    return Rdx - 2;
+}
+
+int method_baryCenter(const double *x, const Elem &T, const Mesh &m) {    // integration.cpp:1262-1280
+    double b[3];
+    baryCenter(m.dim, T.E, b);
+    double distance = vec_sqL2dist(x, b, m.dim);
+    return (distance > m.sqdelta) ? 0 : -1;
+}
+
+// ---------------------------------------------------------------- integration routines
+// All four local blocks are (dV x dV) row-major, outdim = 1.
+int integrate_retriangulate(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                            double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:345-540
+    const int dV = 3;
+    double x[2], y[2], ref[2], psi[3];
+    double innerLocal, innerNonloc[3], innerNonlocPrime[3];
+    double reTri[9 * 3 * 2];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[2 * k], 2, x);
+        int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        doesInteract += Rdx;
+        innerLocal = 0;
+        for (int b = 0; b < dV; b++) { innerNonloc[b] = 0; innerNonlocPrime[b] = 0; }
+        for (int r = 0; r < Rdx; r++) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys3(&reTri[6 * r], &q.Py[2 * i], y);
+                double rTdet = absDet2(&reTri[6 * r]);
+                double ker = kernel_value(m, x, y);
+                innerLocal += ker * q.dy[i] * rTdet;
+                toRef(bT.E, y, ref);
+                double kerP = kernel_value(m, y, x);
+                basis(ref, 2, psi);
+                for (int b = 0; b < dV; b++) {
+                    innerNonloc[b] += psi[b] * ker * q.dy[i] * rTdet;
+                    innerNonlocPrime[b] += psi[b] * kerP * q.dy[i] * rTdet;
+                }
+                for (int a = 0; a < dV; a++)
+                    for (int b = 0; b < dV; b++)
+                        tLP[dV * a + b] += psi[a] * psi[b] * kerP * q.dy[i] * q.dx[k] * rTdet * aT.absDet;
+            }
+        }
+        for (int a = 0; a < dV; a++) {
+            for (int b = 0; b < dV; b++) {
+                tL[dV * a + b] += aT.absDet * q.psix[dV * k + a] * q.psix[dV * k + b] * q.dx[k] * innerLocal;
+                tN[dV * a + b] += aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonloc[b];
+                tNP[dV * a + b] += aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonlocPrime[b];
+            }
+        }
+    }
+    return (doesInteract || m.full_search);
+}
+
+int integrate_baryCenter(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                         double *tL, double *tN) {                        // integration.cpp:910-1018
+    const int dim = m.dim, dV = m.dV;
+    double x[3], y[3];
+    double innerLocal, innerNonloc[4];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[dim * k], dim, x);
+        innerLocal = 0;
+        for (int b = 0; b < dV; b++) innerNonloc[b] = 0;
+        int Rdx = method_baryCenter(x, bT, m);
+        doesInteract += Rdx;
+        if (Rdx) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys(bT.E, &q.Py[dim * i], dim, y);
+                double rTdet = absDetDim(bT.E, dim);
+                double ker = kernel_value(m, x, y);
+                innerLocal += rTdet * ker * q.dy[i];
+                ker = kernel_value(m, y, x);
+                for (int b = 0; b < dV; b++) innerNonloc[b] += q.psiy[dV * i + b] * ker * q.dy[i] * rTdet;
+            }
+        }
+        for (int a = 0; a < dV; a++) {
+            for (int b = 0; b < dV; b++) {
+                tL[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.psix[dV * k + b] * q.dx[k] * innerLocal;
+                tN[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonloc[b];
+            }
+        }
+    }
+    return (doesInteract || m.full_search);
+}
+
+// join + setupElement: integration.cpp:1897-1958
+int join(const Elem &aT, const Elem &bT, const Mesh &m, Elem &aS, Elem &bS, int *argA, int *argB) {
+    int nEqual = 0;
+    int AinB[3] = {0, 0, 0}, BinA[3] = {0, 0, 0};
+    const long *aV = &m.T[3 * aT.Tdx];
+    const long *bV = &m.T[3 * bT.Tdx];
+    long aS_v[3], bS_v[3];
+    for (int a = 0; a < 3; a++) {
+        for (int b = 0; b < 3; b++) {
+            if (aV[a] == bV[b]) {
+                AinB[a] += 1;
+                BinA[b] += 1;
+                aS_v[nEqual] = aV[a];
+                argA[nEqual] = a;
+                bS_v[nEqual] = bV[b];
+                argB[nEqual] = b;
+                nEqual += 1;
+            }
+        }
+    }
+    int ia = 0, ib = 0;
+    for (int i = 0; i < 3; i++) {
+        if (!AinB[i]) { aS_v[nEqual + ia] = aV[i]; argA[nEqual + ia] = i; ia++; }
+        if (!BinA[i]) { bS_v[nEqual + ib] = bV[i]; argB[nEqual + ib] = i; ib++; }
+    }
+    for (int k = 0; k < 3; k++)
+        for (int j = 0; j < 2; j++) {
+            aS.E[2 * k + j] = m.V[2 * aS_v[k] + j];
+            bS.E[2 * k + j] = m.V[2 * bS_v[k] + j];
+        }
+    aS.absDet = absDetDim(aS.E, 2);
+    bS.absDet = absDetDim(bS.E, 2);
+    return nEqual;
+}
+
+int integrate_fractional(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                         double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:187-288
+    Elem aS, bS;
+    int argA[3], argB[3];
+    const int nEqual = join(aT, bT, m, aS, bS, argA, argB);
+    if (nEqual < 1 || nEqual > 3) return -1;  // reference aborts
+    const int c = nEqual - 1;
+    const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    const int dV = 3;
+    const int nLocal = 2 * dV - nEqual;
+    double x[2], y[2], psix[3], psiy[3], psixy[6];
+    for (int t = 0; t < nT; t++) {
+        for (int k = 0; k < q.nPg; k++) {
+            const double tf = q.tdetFrac[c][t * q.nPg + k];
+            const double *al = &q.alphaC[c][(t * q.nPg + k) * 4];
+            toPhys(aS.E, &al[0], 2, x);
+            toPhys(bS.E, &al[2], 2, y);
+            double ker = kernel_value(m, x, y);
+            basis(&al[0], 2, psix);
+            basis(&al[2], 2, psiy);
+            int shift = dV - nEqual;
+            for (int a = 0; a < nEqual; a++) psixy[a] = psix[a] - psiy[a];
+            for (int a = nEqual; a < dV; a++) {
+                psixy[a] = psix[a];
+                psixy[a + shift] = -psiy[a];
+            }
+            for (int a = 0; a < nLocal; a++) {
+                for (int b = 0; b < nLocal; b++) {
+                    double f = ker * tf * psixy[a] * psixy[b] * q.dg[k] * aS.absDet * bS.absDet;
+                    if (a < dV) {
+                        if (b < dV) tL[dV * argA[a] + argA[b]] += f;
+                        else tN[dV * argA[a] + argB[b - shift]] -= f;
+                    } else {
+                        if (b < dV) tNP[dV * argA[b] + argB[a - shift]] -= f;
+                        else tLP[dV * argB[a - shift] + argB[b - shift]] += f;
+                    }
+                }
+            }
+        }
+    }
+    return 1;
+}
+
+// Duffy tables: MeshTypes.cpp:32-209 (traffo*), :252-327 (initializeQuadrule), mathhelpers.cpp:88-97
+double traffo(int c, int t, double *al) {
+    const double xi = al[0], e1 = al[1], e2 = al[2], e3 = al[3];
+    if (c == 0) {
+        if (t == 0) { al[0] = xi; al[1] = e1 * xi; al[2] = e2 * xi; al[3] = e2 * e3 * xi; }
+        else { al[0] = xi * e2; al[1] = xi * e2 * e3; al[2] = xi; al[3] = xi * e1; }
+        return pow(xi, 3) * e2;
+    }
+    if (c == 1) {
+        switch (t) {
+        case 0:
+            al[0] = xi; al[1] = xi * e1 * e3; al[2] = xi * (1. - e1 * e2); al[3] = xi * e1 * (1. - e2);
+            return pow(xi, 3) * sq(e1);
+        case 1:
+            al[0] = xi; al[1] = xi * e1; al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * e1 * e2 * (1. - e3);
+            break;
+        case 2:
+            al[0] = xi * (1. - e1 * e2); al[1] = xi * e1 * (1. - e2); al[2] = xi; al[3] = xi * e1 * e2 * e3;
+            break;
+        case 3:
+            al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * e2 * (1. - e3); al[2] = xi; al[3] = xi * e1;
+            break;
+        default:
+            al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * (1. - e2 * e3); al[2] = xi; al[3] = xi * e1 * e2;
+            break;
+        }
+        return pow(xi, 3) * sq(e1) * e2;
+    }
+    switch (t) {
+    case 0:
+        al[0] = xi; al[1] = xi * (1. - e1 + e1 * e2); al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * (1. - e1);
+        break;
+    case 1:
+        al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * (1. - e1); al[2] = xi; al[3] = xi * (1. - e1 + e1 * e2);
+        break;
+    case 2:
+        al[0] = xi; al[1] = xi * e1 * (1. - e2 + e2 * e3); al[2] = xi * (1. - e1 * e2); al[3] = xi * e1 * (1. - e2);
+        break;
+    case 3:
+        al[0] = xi * (1. - e1 * e2); al[1] = xi * e1 * (1. - e2); al[2] = xi; al[3] = xi * e1 * (1. - e2 + e2 * e3);
+        break;
+    case 4:
+        al[0] = xi * (1. - e1 * e2 * e3); al[1] = xi * e1 * (1. - e2 * e3); al[2] = xi; al[3] = xi * e1 * (1. - e2);
+        break;
+    default:
+        al[0] = xi; al[1] = xi * e1 * (1. - e2); al[2] = xi * (1. - e1 * e2 * e3); al[3] = xi * e1 * (1. - e2 * e3);
+        break;
+    }
+    return pow(xi, 3) * sq(e1) * e2;
+}
+
+void initializeQuadrule(Quad &q, const Mesh &m, const double *Pg) {
+    const int nTr[3] = {2, 5, 6};
+    for (int c = 0; c < 3; c++) {
+        q.alphaC[c].assign((size_t)nTr[c] * q.nPg * 4, 0.0);
+        q.tdetFrac[c].assign((size_t)nTr[c] * q.nPg, 0.0);
+        for (int t = 0; t < nTr[c]; t++) {
+            for (int k = 0; k < q.nPg; k++) {
+                double *al = &q.alphaC[c][((size_t)t * q.nPg + k) * 4];
+                for (int j = 0; j < 4; j++) al[j] = Pg[4 * k + j];
+                for (int j = 0; j < 4; j++) al[j] = al[j] * 0.5 + 0.5;        // scale()
+                double tdf = pow(al[0], 3 - 2 * m.frac_s);
+                al[0] = 1.0;
+                double det = traffo(c, t, al);
+                tdf *= det * SCALEDET;
+                al[0] = al[0] - al[1];                                         // mirror()
+                al[2] = al[2] - al[3];
+                q.tdetFrac[c][(size_t)t * q.nPg + k] = tdf;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- dual graph (METIS_MeshToDual, ncommon=1)
+void dual_graph(const Mesh &m, std::vector<long> &xadj, std::vector<long> &adj) {
+    std::vector<long> vcnt(m.nV + 1, 0);
+    for (long e = 0; e < m.nE; e++)
+        for (int k = 0; k < m.dV; k++) vcnt[m.T[m.dV * e + k] + 1]++;
+    for (long v = 0; v < m.nV; v++) vcnt[v + 1] += vcnt[v];
+    std::vector<long> vel(vcnt[m.nV]);
+    std::vector<long> fill(vcnt.begin(), vcnt.end() - 1);
+    for (long e = 0; e < m.nE; e++)
+        for (int k = 0; k < m.dV; k++) vel[fill[m.T[m.dV * e + k]]++] = e;
+    xadj.assign(m.nE + 1, 0);
+    adj.clear();
+    std::vector<long> nb;
+    for (long e = 0; e < m.nE; e++) {
+        nb.clear();
+        for (int k = 0; k < m.dV; k++) {
+            long v = m.T[m.dV * e + k];
+            for (long j = vcnt[v]; j < vcnt[v + 1]; j++)
+                if (vel[j] != e) nb.push_back(vel[j]);
+        }
+        std::sort(nb.begin(), nb.end());
+        nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+        adj.insert(adj.end(), nb.begin(), nb.end());
+        xadj[e + 1] = (long)adj.size();
+    }
+}
+
+// ---------------------------------------------------------------- integrate dispatch (integration.cpp:67-79)
+int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                     double *tL, double *tN, double *tLP, double *tNP) {
+    switch (method) {
+    case M_RETRIANGULATE: return integrate_retriangulate(aT, bT, q, m, tL, tN, tLP, tNP);
+    case M_BARYCENTER: return integrate_baryCenter(aT, bT, q, m, tL, tN);
+    case M_FRACTIONAL: return integrate_fractional(aT, bT, q, m, tL, tN, tLP, tNP);
+    }
+    return -1;
+}
+int integrate(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m, bool first,
+              double *tL, double *tN, double *tLP, double *tNP) {
+    return integrate_method(first ? m.close : m.remote, aT, bT, q, m, tL, tN, tLP, tNP);
+}
+
+struct Counters {
+    long n_pairs = 0, n_cand = 0, n_close = 0, err = 0;
+};
+
+// One outer element: BFS over the dual graph, integrate each candidate, scatter the four local
+// blocks into the map. Cassemble.cpp:555-784 (outdim = 1, weight = 1: no domain decomposition).
+void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<long> &xadj,
+                    const std::vector<long> &adj, std::vector<int> &visited,
+                    std::map<unsigned long, double> &Ad, Counters &cnt, std::vector<long> *pairs) {
+    const int dV = m.dV;
+    const unsigned long K = (unsigned long)m.K;
+    long aDG[4], bDG[4];
+    const long *aAdx, *bAdx;
+    Elem aT, bT;
+    double tL[16], tN[16], tLP[16], tNP[16];
+    if (m.is_dg) { for (int j = 0; j < dV; j++) aDG[j] = dV * aTdx + j; aAdx = aDG; }
+    else aAdx = &m.T[dV * aTdx];
+    initializeElement(aTdx, m, aT);
+    std::queue<long> queue;
+    queue.push(aTdx);
+    std::fill(visited.begin(), visited.end(), 0);                        // Cassemble.cpp:597
+    bool first = m.is_singular;                                           // :600
+    while (!queue.empty()) {
+        long s = queue.front();
+        queue.pop();
+        long start = xadj[s], end = xadj[s + 1];
+        for (long nT = -1; start + nT != end; nT++) {                     // :613-622
+            long bTdx = (nT == -1) ? aTdx : adj[start + nT];
+            if (!visited[bTdx]) {
+                if (m.labT[bTdx]) {
+                    initializeElement(bTdx, m, bT);
+                    if (m.is_dg) { for (int j = 0; j < dV; j++) bDG[j] = dV * bTdx + j; bAdx = bDG; }
+                    else bAdx = &m.T[dV * bTdx];
+                    for (int i = 0; i < dV * dV; i++) { tL[i] = 0; tN[i] = 0; tLP[i] = 0; tNP[i] = 0; }
+                    cnt.n_cand++;
+                    if (first) cnt.n_close++;
+                    int does = integrate(aT, bT, q, m, first, tL, tN, tLP, tNP);
+                    if (does < 0) { cnt.err++; does = 0; }
+                    if (does) {
+                        queue.push(bTdx);                                 // :713
+                        cnt.n_pairs++;
+                        if (pairs) { pairs->push_back(aTdx); pairs->push_back(bTdx); }
+                        for (int a = 0; a < dV; a++) {                    // :721-770
+                            for (int b = 0; b < dV; b++) {
+                                if (m.is_dg || m.labV[aAdx[a]] > 0) {
+                                    Ad[(unsigned long)aAdx[a] * K + aAdx[b]] += tL[dV * a + b];
+                                    Ad[(unsigned long)aAdx[a] * K + bAdx[b]] += -tN[dV * a + b];
+                                }
+                                if (m.is_dg || m.labV[bAdx[b]] > 0) {
+                                    Ad[(unsigned long)bAdx[b] * K + bAdx[a]] += tLP[dV * a + b];
+                                    Ad[(unsigned long)bAdx[b] * K + aAdx[a]] += -tNP[dV * a + b];
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    queue.push(bTdx);                                     // :773-775
+                }
+            }
+            visited[bTdx] = 1;                                            // :778
+        }
+        first = false;                                                    // :782
+    }
+}
+
+int kernel_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "constant") return K_CONSTANT;
+    if (k == "parabola") return K_PARABOLA;
+    if (k == "fractional") return K_FRACTIONAL;
+    if (k == "constant3D") return K_CONSTANT3D;
+    return K_NONE;
+}
+int load_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "linear") return F_LINEAR;
+    if (k == "linear3D") return F_LINEAR3D;
+    if (k == "constant") return F_CONSTANT;
+    return F_NONE;
+}
+int method_id(const char *s) {
+    std::string k(s ? s : "");
+    if (k == "retriangulate") return M_RETRIANGULATE;
+    if (k == "baryCenter") return M_BARYCENTER;
+    if (k == "fractional") return M_FRACTIONAL;
+    return M_NONE;
+}
+
+}  // namespace
+
+// ====================================================================== C interface (ctypes)
+extern "C" {
+
+struct oracle_result {
+    long K, nnz;
+    long *indptr, *indices;
+    double *values;
+    double *fd;
+    long n_pairs, n_candidates, n_close, n_errors;
+    long *pairs;   // (n_pairs, 2) in BFS order per outer element, outer elements ascending
+    double seconds;
+};
+
+void oracle_free(oracle_result *r) {
+    if (!r) return;
+    free(r->indptr); free(r->indices); free(r->values); free(r->fd); free(r->pairs);
+    free(r);
+}
+
+// Method retriangulation of one ball center against one triangle (integration.cpp:1775-1894).
+int oracle_retriangulate(const double *x, const double *TE, double sqdelta, double *out, int caps) {
+    return method_retriangulate(x, TE, sqdelta, out, caps);
+}
+int oracle_toRef(const double *E, const double *x, double *p) { return toRef(E, x, p); }
+
+// Twin of par_assemble (Cassemble.cpp:360-462 -> par_system :464-855 / par_forcing :857-928),
+// returning CSR and the load vector in memory. compute: "system" or "forcing".
+// subset (optional): only these outer elements are processed (CPU baseline sampling).
+// nthreads <= 1: canonical single-threaded order (one map, as the reference's 1-thread run).
+oracle_result *oracle_par_assemble(
+    const char *compute, int K, const long *ptrTriangles, const long *ptrLabelTriangles,
+    const double *ptrVerts, const long *ptrLabelVerts, int nE, int nV,
+    const double *Px, int nPx, const double *dx, const double *Py, int nPy, const double *dy,
+    double sqdelta, int is_DG, const char *kernel, const char *f, const char *method_remote,
+    const char *method_close, int is_PlacePointOnCap, int dim, int outdim,
+    const double *Pg, int degree, const double *dg, double fractional_s,
+    int is_fullConnectedComponentSearch, int nthreads, const long *subset, long n_subset,
+    int want_pairs) {
+    Mesh m;
+    m.dim = dim; m.dV = dim + 1; m.outdim = outdim; m.is_dg = is_DG;
+    m.nE = nE; m.nV = nV; m.K = K;
+    m.T = ptrTriangles; m.labT = ptrLabelTriangles; m.labV = ptrLabelVerts; m.V = ptrVerts;
+    m.sqdelta = sqdelta; m.delta = sqrt(sqdelta); m.frac_s = fractional_s;
+    m.kernel = kernel_id(kernel); m.load = load_id(f);
+    m.remote = method_id(method_remote);
+    m.close = method_id(method_close && method_close[0] ? method_close : method_remote);
+    std::string kn(kernel ? kernel : "");
+    m.is_singular = (kn == "fractional" || kn == "linearPrototypeMicroelastic" ||
+                     kn == "linearPrototypeMicroelasticField");               // Cassemble.cpp:89-94
+    m.caps = is_PlacePointOnCap; m.full_search = is_fullConnectedComponentSearch;
+    if (outdim != 1) return nullptr;
+
+    Quad q;
+    q.Px = Px; q.dx = dx; q.Py = Py; q.dy = dy; q.nPx = nPx; q.nPy = nPy;
+    q.nPg = degree > 0 ? (int)pow(degree, dim * 2) : 0;                     // MeshTypes.h:155
+    q.dg = dg;
+    q.psix.resize((size_t)m.dV * nPx);
+    q.psiy.resize((size_t)m.dV * (nPy > 0 ? nPy : 1));
+    for (int h = 0; h < nPx; h++) basis(&Px[dim * h], dim, &q.psix[m.dV * h]);   // Cassemble.cpp:509-516
+    for (int h = 0; h < nPy; h++) basis(&Py[dim * h], dim, &q.psiy[m.dV * h]);
+    if (q.nPg > 0 && Pg) initializeQuadrule(q, m, Pg);
+
+    oracle_result *r = (oracle_result *)calloc(1, sizeof(oracle_result));
+    r->K = K;
+    double t0 = 0;
+#ifdef _OPENMP
+    t0 = omp_get_wtime();
+#endif
+    std::string comp(compute ? compute : "");
+    if (comp == "forcing") {
+        // par_forcing (Cassemble.cpp:857-928), compute_f (:149-164)
+        std::vector<double> fd(K, 0.0);
+        for (long aTdx = 0; aTdx < nE; aTdx++) {
+            if (m.labT[aTdx] > 0) {
+                Elem aT;
+                initializeElement(aTdx, m, aT);
+                long aDG[4];
+                const long *aAdx;
+                if (m.is_dg) { for (int j = 0; j < m.dV; j++) aDG[j] = m.dV * aTdx + j; aAdx = aDG; }
+                else aAdx = &m.T[m.dV * aTdx];
+                double termf[4] = {0, 0, 0, 0};
+                double x[3];
+                for (int a = 0; a < m.dV; a++) {
+                    for (int i = 0; i < nPx; i++) {
+                        toPhys(aT.E, &Px[dim * i], dim, x);
+                        double fv = load_value(m, x);
+                        termf[a] += q.psix[m.dV * i + a] * fv * aT.absDet * dx[i];
+                    }
+                }
+                for (int a = 0; a < m.dV; a++)
+                    if (m.is_dg || m.labV[aAdx[a]] > 0) fd[aAdx[a]] += termf[a] * 1.;
+            }
+        }
+        r->fd = (double *)malloc(sizeof(double) * K);
+        memcpy(r->fd, fd.data(), sizeof(double) * K);
+    } else {
+        std::vector<long> xadj, adj;
+        dual_graph(m, xadj, adj);
+        std::vector<long> outer;
+        if (subset) outer.assign(subset, subset + n_subset);
+        else for (long e = 0; e < nE; e++) outer.push_back(e);
+        int nt = nthreads > 1 ? nthreads : 1;
+        std::vector<std::map<unsigned long, double>> maps(nt);
+        std::vector<Counters> cnts(nt);
+        std::vector<std::vector<long>> pairs(nt);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nt)
+#endif
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+            std::vector<int> visited(nE, 0);
+            long n = (long)outer.size();
+            long lo = n * tid / nt, hi = n * (tid + 1) / nt;  // contiguous element blocks
+            for (long i = lo; i < hi; i++) {
+                long aTdx = outer[i];
+                if (m.labT[aTdx])                                          // Cassemble.cpp:559
+                    system_element(aTdx, m, q, xadj, adj, visited, maps[tid], cnts[tid],
+                                   want_pairs ? &pairs[tid] : nullptr);
+            }
+        }
+        // merge thread maps, sum duplicates in thread order, drop exact zeros (arma::sp_mat)
+        std::map<unsigned long, double> &all = maps[0];
+        for (int t = 1; t < nt; t++)
+            for (auto &it : maps[t]) all[it.first] += it.second;
+        long nnz = 0;
+        for (auto &it : all) if (it.second != 0.0) nnz++;
+        r->nnz = nnz;
+        r->indptr = (long *)calloc(K + 1, sizeof(long));
+        r->indices = (long *)malloc(sizeof(long) * (nnz ? nnz : 1));
+        r->values = (double *)malloc(sizeof(double) * (nnz ? nnz : 1));
+        long k = 0;
+        for (auto &it : all) {
+            if (it.second == 0.0) continue;
+            long row = (long)(it.first / (unsigned long)K), col = (long)(it.first % (unsigned long)K);
+            r->indices[k] = col;
+            r->values[k] = it.second;
+            r->indptr[row + 1]++;
+            k++;
+        }
+        for (long i = 0; i < K; i++) r->indptr[i + 1] += r->indptr[i];
+        for (int t = 0; t < nt; t++) {
+            r->n_pairs += cnts[t].n_pairs;
+            r->n_candidates += cnts[t].n_cand;
+            r->n_close += cnts[t].n_close;
+            r->n_errors += cnts[t].err;
+        }
+        if (want_pairs) {
+            r->pairs = (long *)malloc(sizeof(long) * 2 * (r->n_pairs ? r->n_pairs : 1));
+            long o = 0;
+            for (int t = 0; t < nt; t++) {
+                memcpy(r->pairs + o, pairs[t].data(), sizeof(long) * pairs[t].size());
+                o += (long)pairs[t].size();
+            }
+        }
+    }
+#ifdef _OPENMP
+    r->seconds = omp_get_wtime() - t0;
+#endif
+    return r;
+}
+
+// Local blocks of explicit (aT, bT) pairs, for kernel-level parity tests.
+// out: (n, 4, dV, dV) = termLocal, termNonloc, termLocalPrime, termNonlocPrime; ret[i] = doesInteract.
+int oracle_pair_blocks(
+    const long *ptrTriangles, const long *ptrLabelTriangles, const double *ptrVerts, int nE, int nV,
+    const double *Px, int nPx, const double *dx, const double *Py, int nPy, const double *dy,
+    double sqdelta, const char *kernel, const char *method, int is_PlacePointOnCap, int dim,
+    const double *Pg, int degree, const double *dg, double fractional_s,
+    const long *pairs, long n, double *out, int *ret) {
+    Mesh m;
+    memset(&m, 0, sizeof(m));
+    m.dim = dim; m.dV = dim + 1; m.outdim = 1;
+    m.nE = nE; m.nV = nV; m.T = ptrTriangles; m.labT = ptrLabelTriangles; m.V = ptrVerts;
+    m.sqdelta = sqdelta; m.delta = sqrt(sqdelta); m.frac_s = fractional_s;
+    m.kernel = kernel_id(kernel); m.caps = is_PlacePointOnCap;
+    int meth = method_id(method);
+    Quad q;
+    q.Px = Px; q.dx = dx; q.Py = Py; q.dy = dy; q.nPx = nPx; q.nPy = nPy;
+    q.nPg = degree > 0 ? (int)pow(degree, dim * 2) : 0;
+    q.dg = dg;
+    q.psix.resize((size_t)m.dV * nPx);
+    q.psiy.resize((size_t)m.dV * (nPy > 0 ? nPy : 1));
+    for (int h = 0; h < nPx; h++) basis(&Px[dim * h], dim, &q.psix[m.dV * h]);
+    for (int h = 0; h < nPy; h++) basis(&Py[dim * h], dim, &q.psiy[m.dV * h]);
+    if (q.nPg > 0 && Pg) initializeQuadrule(q, m, Pg);
+    const int bs = m.dV * m.dV;
+    for (long i = 0; i < n; i++) {
+        Elem aT, bT;
+        initializeElement(pairs[2 * i], m, aT);
+        initializeElement(pairs[2 * i + 1], m, bT);
+        double *o = &out[i * 4 * bs];
+        for (int j = 0; j < 4 * bs; j++) o[j] = 0;
+        ret[i] = integrate_method(meth, aT, bT, q, m, o, o + bs, o + 2 * bs, o + 3 * bs);
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+"""CPU checks of the oracle and of the host-side helpers against the reference's fixtures."""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import conf2d, conf3d, square_mesh, cube_mesh
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_quadrules_match_reference_configuration():
+    from nlfem_gb300 import quadrules
+    ref = json.load(open(os.path.join(GOLD, "quadrules_ref.json")))
+    P, w = quadrules.dunavant7()
+    np.testing.assert_allclose(P, ref["7point"]["points"], atol=1e-13)
+    np.testing.assert_allclose(w, ref["7point"]["weights"], atol=1e-13)
+    P, w = quadrules.dunavant16()
+    np.testing.assert_allclose(P, ref["16point"]["points"], atol=1e-8)
+    np.testing.assert_allclose(w, ref["16point"]["weights"], atol=1e-13)
+
+
+def test_keast_rule_is_degree_4_exact():
+    from math import factorial
+    from nlfem_gb300 import quadrules
+    P, w = quadrules.keast11()
+    assert abs(w.sum() - 1.0 / 6.0) < 1e-15
+    for a in range(5):
+        for b in range(5 - a):
+            for c in range(5 - a - b):
+                exact = factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 3)
+                got = np.sum(w * P[:, 0] ** a * P[:, 1] ** b * P[:, 2] ** c)
+                assert abs(got - exact) < 1e-14
+
+
+def test_tensorgauss_matches_reference_class():
+    from nlfem_gb300.quadrules import tensorgauss
+    ref = np.load(os.path.join(GOLD, "tensorgauss_ref.npz"))
+    for deg in (2, 5):
+        tg = tensorgauss(deg)
+        np.testing.assert_array_equal(tg.points, ref[f"points{deg}"])
+        np.testing.assert_array_equal(tg.weights, ref[f"weights{deg}"])
+
+
+def test_vertex_labels_match_reference():
+    from nlfem_gb300.meshes import get_vertexLabel
+    d = json.load(open(os.path.join(GOLD, "vertexlabels_ref.json")))
+    got = get_vertexLabel(np.array(d["elements"]), np.array(d["elementLabels"]), np.array(d["vertices"]))
+    np.testing.assert_array_equal(got, d["vertexLabels"])
+
+
+def test_cube_split_matches_reference_golden_list():
+    from nlfem_gb300.meshes import regular_cube
+    d = json.load(open(os.path.join(GOLD, "tets_ref.json")))
+    v, e, l = regular_cube(d["n_cells"], 0.1)
+    np.testing.assert_array_equal(e, np.array(d["tets"]))
+
+
+def test_arma_writer_matches_reference_reader():
+    ref = np.load(os.path.join(GOLD, "arma_ref.npz"))
+    np.testing.assert_array_equal(ref["A_dense"], ref["B_dense"])
+    np.testing.assert_array_equal(ref["f"], ref["g"])
+
+
+def test_arma_roundtrip(tmp_path):
+    from nlfem_gb300.nlfem import write_arma_spMat, read_arma_spMat, write_arma_mat, read_arma_mat
+    A = sp.random(13, 13, density=0.3, random_state=np.random.RandomState(1), format="csr")
+    write_arma_spMat(tmp_path / "A", A)
+    B = read_arma_spMat(tmp_path / "A")
+    assert abs(A - B).max() == 0
+    f = np.arange(13.0)
+    write_arma_mat(tmp_path / "f", f)
+    np.testing.assert_array_equal(read_arma_mat(tmp_path / "f")[:, 0], f)
+    with pytest.raises(ValueError):
+        read_arma_mat(tmp_path / "A")
+
+
+def test_oracle_constant_kernel_invariants():
+    from oracle import oracle
+    m = square_mesh(12, 0.1)
+    ker = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    r = oracle.assemble(m, ker, conf2d(), want_pairs=True)
+    A = r["A"]
+    assert r["n_errors"] == 0
+    assert r["n_pairs"] == len(r["pairs"])
+    # the operator annihilates constants on rows whose full stencil is assembled
+    keep = m["vertexLabels"] > 0
+    assert np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()
+    # Dirichlet rows are empty
+    assert np.all(np.diff(A.indptr)[~keep] == 0)
+    # every outer element interacts with itself
+    pairs = set(map(tuple, r["pairs"]))
+    for e in range(m["elements"].shape[0]):
+        assert (e, e) in pairs
+
+
+def test_oracle_thread_split_is_rounding_only():
+    from oracle import oracle
+    m = square_mesh(10, 0.1, jitter=0.2, seed=1)
+    ker = {"function": "parabola", "horizon": 0.15, "outputdim": 1}
+    a = oracle.assemble(m, ker, conf2d())["A"]
+    b = oracle.assemble(m, ker, conf2d(), nthreads=4)["A"]
+    assert (a != 0).nnz == (b != 0).nnz
+    assert abs(a - b).max() <= 1e-13 * abs(a).max()
+
+
+def test_oracle_retriangulate_area_and_caps():
+    from oracle import oracle
+    # a ball deep inside a large triangle: no polygon point -> no interaction (reference quirk)
+    T = np.array([0.0, 0.0, 10.0, 0.0, 0.0, 10.0])
+    n, tri = oracle.retriangulate(np.array([2.0, 2.0]), T, 0.5)
+    assert n == 0
+    # triangle fully inside the ball: one sub-triangle, the triangle itself
+    T = np.array([0.0, 0.0, 0.1, 0.0, 0.0, 0.1])
+    n, tri = oracle.retriangulate(np.array([0.02, 0.02]), T, 1.0)
+    assert n == 1 and np.allclose(tri[0].ravel(), T)
+    # ball center at a vertex of a large triangle: area close to a quarter disc with caps
+    T = np.array([0.0, 0.0, 1.0, 0.0, 0.0, 1.0])
+    areas = []
+    for caps in (0, 1):
+        n, tri = oracle.retriangulate(np.array([0.0, 0.0]), T, 0.3, caps)
+        a = sum(abs(np.linalg.det(np.array([t[1] - t[0], t[2] - t[0]]))) / 2 for t in tri)
+        areas.append(a)
+    assert areas[0] < areas[1] < np.pi * 0.09 / 4
+
+
+def test_oracle_fractional_and_3d_run():
+    from oracle import oracle
+    m = square_mesh(6, 0.2)
+    ker = {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4}
+    r = oracle.assemble(m, ker, conf2d(rule="16", close="fractional", deg=3))
+    assert r["n_close"] > 0 and r["n_errors"] == 0
+    A = r["A"]
+    assert np.all(np.isfinite(A.data))
+    m3 = cube_mesh(3, 0.1)
+    ker3 = {"function": "constant3D", "horizon": 0.3, "outputdim": 1}
+    r3 = oracle.assemble(m3, ker3, conf3d())
+    assert r3["A"].nnz > 0
+
+
+def test_oracle_load_vector_linear():
+    from oracle import oracle
+    m = square_mesh(8, 0.1)
+    f = oracle.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
+    keep = m["vertexLabels"] > 0
+    assert np.all(f[~keep] == 0)
+    # sum of the load over all basis functions of label>0 elements = integral of f over them
+    assert np.all(f[keep] < 0)

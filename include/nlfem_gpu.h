@@ -81,6 +81,7 @@ typedef struct nlfem_stats {
     long n_candidates;   /* integrate() calls of the BFS, interacting or not */
     long n_close;        /* pairs integrated with the singular close-pair rule */
     long nnz_structural; /* slots before exact zeros are dropped */
+    long n_subtri;       /* (pair, outer point, sub-triangle) integrations of the remote rule */
     double ms_total;     /* device time of the assembly (CUDA events) */
     double ms_bfs, ms_pattern, ms_quad, ms_finish;
 } nlfem_stats;

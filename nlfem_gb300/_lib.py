@@ -44,6 +44,7 @@ class CSR(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_long), ("n_candidates", ctypes.c_long),
                 ("n_close", ctypes.c_long), ("nnz_structural", ctypes.c_long),
+                ("n_subtri", ctypes.c_long),
                 ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double),
                 ("ms_pattern", ctypes.c_double), ("ms_quad", ctypes.c_double),
                 ("ms_finish", ctypes.c_double)]

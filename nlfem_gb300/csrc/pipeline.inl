@@ -670,7 +670,8 @@ static int run_quad(Session &S) {
     a.blocks_out = nullptr; a.ret_out = nullptr; a.force_close = 0;
     unsigned long long *cnt = S.counters.get<unsigned long long>();
     a.n_close = cnt + 4;
-    CK(cudaMemsetAsync(cnt + 3, 0, 2 * sizeof(unsigned long long), S.st));
+    a.n_subtri = cnt + 5;
+    CK(cudaMemsetAsync(cnt + 3, 0, 3 * sizeof(unsigned long long), S.st));
     if (P > 0) k_quad_fp64<DIM><<<grid_for(P, 128), 128, 0, S.st>>>(a, S.rule);
     if (DIM == 2 && S.duffy_nPg > 0 && P > 0) {
         ENS(S.closelist, sizeof(int) * (P + 1));
@@ -732,9 +733,10 @@ static int run_system_t(Session &S) {
     if ((r = check_errors(S))) return r;
     float t[4];
     for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]));
-    unsigned long long ncl = 0;
-    if ((r = d2h(S, &ncl, S.counters.get<unsigned long long>() + 4, 1))) return r;
-    S.stats.n_close = (long)ncl;
+    unsigned long long ncl[2] = {0, 0};
+    if ((r = d2h(S, ncl, S.counters.get<unsigned long long>() + 4, 2))) return r;
+    S.stats.n_close = (long)ncl[0];
+    S.stats.n_subtri = (long)ncl[1];
     S.stats.ms_bfs = t[0];
     S.stats.ms_pattern = t[1];
     S.stats.ms_quad = t[2];

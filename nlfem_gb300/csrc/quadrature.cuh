@@ -45,6 +45,7 @@ struct QuadArgs {
     double *blocks_out;       // explicit-pair mode: (P, 4, dV, dV) blocks instead of scatter
     int *ret_out;             // explicit-pair mode: doesInteract
     int force_close;          // explicit-pair mode: use the close-pair rule
+    unsigned long long *n_subtri;
 };
 
 __device__ __forceinline__ long long find_slot(const long long *__restrict__ rowptr,
@@ -100,7 +101,7 @@ __device__ __forceinline__ bool share_vertex(const int *aV, const int *bV, int d
 // FP64 integrate_retriangulate (integration.cpp:345-540) of one pair.
 __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, const double *Ea,
                                       const double *Eb, double adet_a, double *L, double *N,
-                                      double *LP, double *NP, int *err) {
+                                      double *LP, double *NP, int *err, int &nsub) {
     double R[18];
     int interacts = 0;
     for (int k = 0; k < rule.nPx; k++) {
@@ -108,6 +109,7 @@ __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, con
         xtoPhys<2>(Ea, &rule.Px[2 * k], x);
         const int Rdx = xretriangulate(x, Eb, P.sqdelta, P.caps, R);
         interacts |= (Rdx >= 3);
+        nsub += Rdx >= 3 ? Rdx - 2 : 0;
         double innerLocal = 0, iN[3] = {0, 0, 0}, iNP[3] = {0, 0, 0};
         for (int r = 0; r + 2 < Rdx; r++) {
             const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
@@ -155,7 +157,7 @@ __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, con
 template <int DIM>
 __device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const double *Ea,
                                    const double *Eb, double adet_a, double adet_b, double *L,
-                                   double *N) {
+                                   double *N, int &nsub) {
     constexpr int dV = DIM + 1;
     double b[DIM];
     xbary<DIM>(Eb, b);
@@ -165,6 +167,7 @@ __device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const 
         xtoPhys<DIM>(Ea, &rule.Px[DIM * k], x);
         if (!xbaryInside<DIM>(x, b, P.sqdelta)) continue;
         interacts = 1;
+        nsub++;
         double innerLocal = 0, iN[dV];
 #pragma unroll
         for (int j = 0; j < dV; j++) iN[j] = 0;
@@ -196,38 +199,43 @@ template <int DIM>
 __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
     constexpr int dV = DIM + 1;
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.P) return;
-    const int aT = a.pA[p], bT = a.pB[p];
-    const ProbParams P = a.probs[a.eprob[aT]];
-    int aV[dV], bV[dV];
+    int nsub = 0;
+    if (p < a.P) {
+        const int aT = a.pA[p], bT = a.pB[p];
+        const ProbParams P = a.probs[a.eprob[aT]];
+        int aV[dV], bV[dV];
 #pragma unroll
-    for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
-    const bool close = a.blocks_out ? (a.force_close != 0) : (P.singular && share_vertex(aV, bV, dV));
-    const int method = close ? P.close : P.remote;
-    if (method == MTH_FRACTIONAL) return;   // handled by k_quad_close
-    double Ea[DIM * dV], Eb[DIM * dV];
+        for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
+        const bool close = a.blocks_out ? (a.force_close != 0) : (P.singular && share_vertex(aV, bV, dV));
+        const int method = close ? P.close : P.remote;
+        if (method != MTH_FRACTIONAL) {   // fractional close pairs: k_quad_close
+            double Ea[DIM * dV], Eb[DIM * dV];
 #pragma unroll
-    for (int i = 0; i < DIM * dV; i++) { Ea[i] = a.EC[(long long)aT * DIM * dV + i]; Eb[i] = a.EC[(long long)bT * DIM * dV + i]; }
-    double L[dV * dV], N[dV * dV], LP[dV * dV], NP[dV * dV];
+            for (int i = 0; i < DIM * dV; i++) { Ea[i] = a.EC[(long long)aT * DIM * dV + i]; Eb[i] = a.EC[(long long)bT * DIM * dV + i]; }
+            double L[dV * dV], N[dV * dV], LP[dV * dV], NP[dV * dV];
 #pragma unroll
-    for (int i = 0; i < dV * dV; i++) { L[i] = 0; N[i] = 0; LP[i] = 0; NP[i] = 0; }
-    bool prime = false;
-    int interacts = 0;
-    if (method == MTH_BARYCENTER) {
-        interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.adet[aT], a.adet[bT], L, N);
-    } else if (DIM == 2) {
-        interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.adet[aT], L, N, LP, NP, a.err);
-        prime = true;
-    }
-    if (a.blocks_out) {
-        double *o = &a.blocks_out[p * 4 * dV * dV];
-        for (int i = 0; i < dV * dV; i++) {
-            o[i] = L[i]; o[dV * dV + i] = N[i]; o[2 * dV * dV + i] = LP[i]; o[3 * dV * dV + i] = NP[i];
+            for (int i = 0; i < dV * dV; i++) { L[i] = 0; N[i] = 0; LP[i] = 0; NP[i] = 0; }
+            bool prime = false;
+            int interacts = 0;
+            if (method == MTH_BARYCENTER) {
+                interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.adet[aT], a.adet[bT], L, N, nsub);
+            } else if (DIM == 2) {
+                interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.adet[aT], L, N, LP, NP, a.err, nsub);
+                prime = true;
+            }
+            if (a.blocks_out) {
+                double *o = &a.blocks_out[p * 4 * dV * dV];
+                for (int i = 0; i < dV * dV; i++) {
+                    o[i] = L[i]; o[dV * dV + i] = N[i]; o[2 * dV * dV + i] = LP[i]; o[3 * dV * dV + i] = NP[i];
+                }
+                a.ret_out[p] = interacts;
+            } else {
+                scatter_blocks<dV>(a, aV, bV, L, N, LP, NP, P.scale_exp, prime);
+            }
         }
-        a.ret_out[p] = interacts;
-        return;
     }
-    scatter_blocks<dV>(a, aV, bV, L, N, LP, NP, P.scale_exp, prime);
+    const unsigned tot = __reduce_add_sync(FULL, (unsigned)nsub);
+    if ((threadIdx.x & 31) == 0 && tot && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)tot);
 }
 
 // Flags and lists the close pairs (singular kernel, shared vertex, fractional close rule).

@@ -203,7 +203,8 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": config_dict(args, mesh),
-        "pairs_per_step": int(pairs[-1]), "nnz": int(A.nnz),
+        "pairs_per_step": int(pairs[-1]), "nnz": int(A.nnz), "nnz_structural": int(st["nnz_structural"]),
+        "fp64_fallbacks": int(st["n_ambiguous"]), "subtriangles": int(st["n_subtri"]),
         "phase_ms": {"dual+bfs+pairs": st["ms_bfs"], "pattern": st["ms_pattern"],
                      "quadrature+scatter": st["ms_quad"], "finish": st["ms_finish"]},
         "roofline": {"bound": args.fp_bound, "kernel": "k_quad (quadrature + scatter)",

@@ -81,7 +81,8 @@ typedef struct nlfem_stats {
     long n_candidates;   /* integrate() calls of the BFS, interacting or not */
     long n_close;        /* pairs integrated with the singular close-pair rule */
     long nnz_structural; /* slots before exact zeros are dropped */
-    long n_subtri;       /* (pair, outer point, sub-triangle) integrations of the remote rule */
+    long n_subtri;       /* (pair side, outer point, sub-triangle) integrations of the remote rule */
+    long n_ambiguous;    /* outer points whose FP32 geometry fell back to FP64 (mixed precision) */
     double ms_total;     /* device time of the assembly (CUDA events) */
     double ms_bfs, ms_pattern, ms_quad, ms_finish;
 } nlfem_stats;
@@ -117,6 +118,11 @@ int nlfem_method_retriangulate(const double *x_center, const double *TE, double 
                                double *reTriangleList, int is_placePointOnCap);
 int nlfem_retriangulate_batch(long n, const double *x_center, const double *TE, double sqdelta,
                               int is_placePointOnCap, int *counts, double *reTriangleList);
+/* Test hook (no counterpart in the reference): the certified FP32 retriangulation of the mixed
+ * path on the same cases; ambiguous[i] != 0 marks cases it hands to the FP64 routine. points
+ * (n, 9, 2) relative to the center. */
+int nlfem_retriangulate_certified_batch(long n, const double *x_center, const double *TE, double sqdelta,
+                                        int caps, int *counts, int *ambiguous, double *points);
 int nlfem_toRef(const double *E, const double *phys_x, double *ref_p);
 int nlfem_toPhys(const double *E, const double *p, int dim, double *out_x);
 int nlfem_solve2x2(const double *A, const double *b, double *x);

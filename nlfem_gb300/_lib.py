@@ -44,7 +44,7 @@ class CSR(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_long), ("n_candidates", ctypes.c_long),
                 ("n_close", ctypes.c_long), ("nnz_structural", ctypes.c_long),
-                ("n_subtri", ctypes.c_long),
+                ("n_subtri", ctypes.c_long), ("n_ambiguous", ctypes.c_long),
                 ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double),
                 ("ms_pattern", ctypes.c_double), ("ms_quad", ctypes.c_double),
                 ("ms_finish", ctypes.c_double)]
@@ -88,6 +88,7 @@ def load():
     l.nlfem_pair_blocks.argtypes = [P, ctypes.c_long, _lp, ctypes.c_int, _dp, _ip]
     l.nlfem_method_retriangulate.argtypes = [_dp, _dp, ctypes.c_double, _dp, ctypes.c_int]
     l.nlfem_retriangulate_batch.argtypes = [ctypes.c_long, _dp, _dp, ctypes.c_double, ctypes.c_int, _ip, _dp]
+    l.nlfem_retriangulate_certified_batch.argtypes = [ctypes.c_long, _dp, _dp, ctypes.c_double, ctypes.c_int, _ip, _ip, _dp]
     l.nlfem_toRef.argtypes = [_dp, _dp, _dp]
     l.nlfem_toPhys.argtypes = [_dp, _dp, ctypes.c_int, _dp]
     l.nlfem_solve2x2.argtypes = [_dp, _dp, _dp]
@@ -112,6 +113,6 @@ EXPORTED = [
     "nlfem_load_vector", "nlfem_stiffness_batch", "nlfem_csr_free", "nlfem_session_create",
     "nlfem_session_assemble", "nlfem_session_download", "nlfem_session_destroy",
     "nlfem_pair_list", "nlfem_pair_blocks", "nlfem_method_retriangulate",
-    "nlfem_retriangulate_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
+    "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
     "nlfem_par_assemble",
 ]

@@ -18,6 +18,8 @@
 #include "geometry.cuh"
 #include "primitives.cuh"
 #include "quadrature.cuh"
+#include "passes.cuh"
+#include "passes_mix.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -44,7 +46,9 @@ __global__ void k_prep_elements(const long long *__restrict__ T64, const long lo
                                 const double *__restrict__ V, const int *__restrict__ eoff,
                                 const int *__restrict__ voff, int nProb, long long nE,
                                 int *__restrict__ T32, int *__restrict__ labT, int *__restrict__ eprob,
-                                double *__restrict__ EC, double *__restrict__ adet) {
+                                double *__restrict__ EC, double *__restrict__ adet,
+                                float *__restrict__ EChi, float *__restrict__ EClo,
+                                float *__restrict__ adetf) {
     constexpr int dV = DIM + 1;
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nE) return;
@@ -59,6 +63,9 @@ __global__ void k_prep_elements(const long long *__restrict__ T64, const long lo
         for (int j = 0; j < DIM; j++) {
             E[DIM * k + j] = V[(long long)v * DIM + j];
             EC[e * DIM * dV + DIM * k + j] = E[DIM * k + j];
+            const float hi = (float)E[DIM * k + j];
+            EChi[e * DIM * dV + DIM * k + j] = hi;
+            EClo[e * DIM * dV + DIM * k + j] = (float)(E[DIM * k + j] - (double)hi);
         }
     }
     long long l = lab64[e];
@@ -80,6 +87,7 @@ __global__ void k_prep_elements(const long long *__restrict__ T64, const long lo
         det = xadd(xsub(xmul(M[0][0], c0), xmul(M[0][1], c1)), xmul(M[0][2], c2));
     }
     adet[e] = fabs(det);
+    adetf[e] = (float)fabs(det);
 }
 
 __global__ void k_prep_vertices(const long long *__restrict__ lab64, const int *__restrict__ voff,
@@ -157,6 +165,8 @@ struct BfsArgs {
     const int *T32, *labT, *eprob, *adj;
     const long long *xadj;
     const double *EC;
+    const float *EChi, *EClo;
+    unsigned long long *n_amb;
     const ProbParams *probs;
     long long nE;
     unsigned *visited;       // nwarps * vstride
@@ -196,10 +206,69 @@ __device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method,
     return false;
 }
 
+// The same predicate with the certified FP32 geometry (certified.cuh); the exact FP64 routine
+// runs only for outer points whose FP32 decisions are within their margins.
 template <int DIM>
+__device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int method, const double *xs,
+                                                   const float *xsf, int nPx, const double *Eb,
+                                                   const float *pb, unsigned &namb) {
+    if (P.full_search) return true;
+    if (method == MTH_FRACTIONAL) return true;
+    const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
+    if (method == MTH_BARYCENTER) {
+        float bf[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; j++) {
+            float s = pb[j];
+#pragma unroll
+            for (int i = 1; i <= DIM; i++) s += pb[DIM * i + j];
+            bf[j] = s / (float)(DIM + 1);
+        }
+        double b64[DIM];
+        bool have_b64 = false;
+        for (int k = 0; k < nPx; k++) {
+            float d2 = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; j++) { float d = xsf[DIM * k + j] - bf[j]; d2 = fmaf(d, d, d2); }
+            if (d2 < sqlo) return true;
+            if (d2 > sqhi) continue;
+            namb++;
+            if (!have_b64) { xbary<DIM>(Eb, b64); have_b64 = true; }
+            if (xbaryInside<DIM>(&xs[DIM * k], b64, P.sqdelta)) return true;
+        }
+        return false;
+    }
+    if (DIM != 2) return false;
+    const F2 p[3] = {f2(pb[0], pb[1]), f2(pb[2], pb[3]), f2(pb[4], pb[5])};
+    for (int k = 0; k < nPx; k++) {
+        const F2 x = f2(xsf[2 * k], xsf[2 * k + 1]);
+        const F2 Q[3] = {p[0] - x, p[1] - x, p[2] - x};
+        const float d0 = dot(Q[0], Q[0]), d1 = dot(Q[1], Q[1]), d2 = dot(Q[2], Q[2]);
+        const bool clear = (d0 < sqlo || d0 > sqhi) && (d1 < sqlo || d1 > sqhi) && (d2 < sqlo || d2 > sqhi);
+        // one vertex strictly inside and none on the sphere: both edges through it cross once,
+        // so the polygon has at least three points
+        if (clear && (d0 < sqlo || d1 < sqlo || d2 < sqlo)) return true;
+        if (fclassify(Q, P.sqdelta_f) == CLS_OUT) continue;
+        F2 R[9];
+        bool amb = false;
+        const int n = fretriangulate(Q, P.sqdelta_f, P.caps, R, amb);
+        if (!amb) {
+            if (n >= 3) return true;
+            continue;
+        }
+        namb++;
+        double R64[18];
+        if (xretriangulate(&xs[2 * k], Eb, P.sqdelta, P.caps, R64) >= 3) return true;
+    }
+    return false;
+}
+
+template <int DIM, int PREC>
 __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
     constexpr int dV = DIM + 1;
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
+    __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];
+    unsigned namb = 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const long long gw = (long long)blockIdx.x * BFS_WARPS + wib;
     const long long nw = (long long)gridDim.x * BFS_WARPS;
@@ -217,7 +286,15 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
         const long long eoff = P.elem_off;
         const unsigned stamp = (unsigned)aT + 1u;   // unique over all problems
         const double *Ea = &a.EC[aT * DIM * dV];
-        for (int k = lane; k < rule.nPx; k += 32) xtoPhys<DIM>(Ea, &rule.Px[DIM * k], &xs[DIM * k]);
+        float ohi[DIM], olo[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; j++) { ohi[j] = a.EChi[aT * DIM * dV + j]; olo[j] = a.EClo[aT * DIM * dV + j]; }
+        float *xsf = s_xf[wib];
+        for (int k = lane; k < rule.nPx; k += 32) {
+            xtoPhys<DIM>(Ea, &rule.Px[DIM * k], &xs[DIM * k]);
+#pragma unroll
+            for (int j = 0; j < DIM; j++) xsf[DIM * k + j] = (float)(xs[DIM * k + j] - Ea[j]);
+        }
         __syncwarp();
         // (aT, aT): the first candidate of the first dequeued element (Cassemble.cpp:621)
         bool self_pair = false;
@@ -264,7 +341,16 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                         if (old != stamp) {
                             if (a.labT[cand] != 0) {
                                 cand_local++;
-                                pair = interacts_exact<DIM>(P, method, xs, rule.nPx, &a.EC[(long long)cand * DIM * dV]);
+                                const double *Eb = &a.EC[(long long)cand * DIM * dV];
+                                if (PREC == PREC_F64) {
+                                    pair = interacts_exact<DIM>(P, method, xs, rule.nPx, Eb);
+                                } else {
+                                    float pb[DIM * dV];
+#pragma unroll
+                                    for (int j = 0; j < DIM * dV; j++)
+                                        pb[j] = (a.EChi[(long long)cand * DIM * dV + j] - ohi[j % DIM]) + (a.EClo[(long long)cand * DIM * dV + j] - olo[j % DIM]);
+                                    pair = interacts_filtered<DIM>(P, method, xs, xsf, rule.nPx, Eb, pb, namb);
+                                }
                                 push = pair;
                             } else {
                                 push = true;
@@ -334,6 +420,8 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
     }
     cand_local = warp_sum(cand_local);
     if (lane == 0 && cand_local) atomicAdd(a.n_cand, cand_local);
+    namb = warp_sum(namb);
+    if (lane == 0 && namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
 }
 
 // aT-major compaction of the BFS segments.
@@ -479,30 +567,31 @@ __global__ void k_row_sort_global(const long long *__restrict__ rowptr, long lon
 }
 
 // ------------------------------------------------------------------ finish
-// Per row: fixed point -> FP64 and count of kept entries (nonzero sum, or a nonzero contribution
-// too small for the fixed-point grid).
+// Per row: number of entries whose FP64 sum is not exactly zero (arma::sp_mat drops the zeros).
+// With touched (mixed precision) a slot that received a contribution is kept even when its
+// FP32-derived sum cancelled to exactly zero: its exact value is a nonzero below FP32 resolution.
 __global__ void k_finish_count(const long long *__restrict__ rowptr, long long nV,
-                               const unsigned long long *__restrict__ acc, const unsigned *__restrict__ tiny,
-                               const int *__restrict__ vprob, const ProbParams *__restrict__ probs,
-                               double *__restrict__ vals, int *__restrict__ keepcnt) {
+                               const double *__restrict__ vals, const unsigned char *__restrict__ touched,
+                               int *__restrict__ keepcnt) {
     const int lane = threadIdx.x & 31;
     long long u = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (u >= nV) return;
-    const int se = probs[vprob[u]].scale_exp;
     const long long b = rowptr[u], e = rowptr[u + 1];
     int cnt = 0;
     for (long long i = b + lane; i < e; i += 32) {
-        unsigned long long lo = acc[2 * i], hi = acc[2 * i + 1];
-        double d = fx_to_double(lo, hi, se);
-        vals[i] = d;
-        cnt += ((lo | hi) != 0ULL) || tiny[i];
+        double v = vals[i];
+        if (touched) {   // mixed precision: the slot holds a double-float pair
+            const DF d = reinterpret_cast<const DF *>(vals)[i];
+            v = df_to_double(d);
+        }
+        cnt += (v != 0.0) || (touched && touched[i]);
     }
     cnt = warp_sum(cnt);
     if (lane == 0) keepcnt[u] = cnt;
 }
 __global__ void k_finish_compact(const long long *__restrict__ rowptr, long long nV,
-                                 const unsigned long long *__restrict__ acc, const unsigned *__restrict__ tiny,
                                  const int *__restrict__ cols, const double *__restrict__ vals,
+                                 const unsigned char *__restrict__ touched,
                                  const long long *__restrict__ fptr, int *__restrict__ fcols,
                                  double *__restrict__ fvals) {
     const int lane = threadIdx.x & 31;
@@ -513,12 +602,16 @@ __global__ void k_finish_compact(const long long *__restrict__ rowptr, long long
     for (long long i0 = b; i0 < e; i0 += 32) {
         long long i = i0 + lane;
         bool k = false;
-        if (i < e) k = ((acc[2 * i] | acc[2 * i + 1]) != 0ULL) || tiny[i];
+        double v = 0.0;
+        if (i < e) {
+            v = touched ? df_to_double(reinterpret_cast<const DF *>(vals)[i]) : vals[i];
+            k = (v != 0.0) || (touched && touched[i]);
+        }
         unsigned m = __ballot_sync(FULL, k);
         if (k) {
             long long o = w + __popc(m & lanemask_lt());
             fcols[o] = cols[i];
-            fvals[o] = vals[i];
+            fvals[o] = v;
         }
         w += __popc(m);
     }
@@ -581,6 +674,27 @@ __global__ void k_retri_batch(long long n, const double *__restrict__ x, const d
             o[2 * (3 * k + 2) + c] = R[2 * (k + 2) + c];
         }
 }
+// Certified FP32 retriangulation on the same cases (test hook): count, ambiguity flag, points
+// relative to the center.
+__global__ void k_retri_cert_batch(long long n, const double *__restrict__ x, const double *__restrict__ TE,
+                                   double sqdelta, int caps, int *__restrict__ counts,
+                                   int *__restrict__ amb, double *__restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    F2 Q[3];
+    for (int j = 0; j < 3; j++) Q[j] = f2((float)(TE[6 * i + 2 * j] - x[2 * i]), (float)(TE[6 * i + 2 * j + 1] - x[2 * i + 1]));
+    F2 R[9];
+    bool a = false;
+    unsigned why = 0;
+    const int c = fretriangulate(Q, (float)sqdelta, caps, R, a, &why);
+    counts[i] = c;
+    amb[i] = a ? (int)why | (int)0x100 : 0;
+    for (int j = 0; j < c && j < 9; j++) {
+        out[18 * i + 2 * j] = R[j].x;
+        out[18 * i + 2 * j + 1] = R[j].y;
+    }
+}
+
 __global__ void k_geom_misc(int op, const double *__restrict__ A, const double *__restrict__ b, int dim,
                             double *__restrict__ out, int *__restrict__ ok) {
     if (threadIdx.x || blockIdx.x) return;

@@ -1,0 +1,212 @@
+// Certified FP32 ball-triangle geometry.
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so the interaction geometry runs in
+// FP32 on coordinates relative to the ball center, and every discrete decision of the
+// reference's method_retriangulate (integration.cpp:1393-1512) - vertex inside the ball,
+// discriminant sign, root in [0, 1], cap point inside the triangle, orientation - is checked
+// against a margin far above the FP32 rounding error of its operands. When every decision clears
+// its margin, the FP32 run takes exactly the branches the FP64 reference takes (same polygon,
+// same point count) and its points agree to FP32 accuracy; otherwise the caller reruns the
+// exact FP64 routine (geometry.cuh). The sparsity pattern therefore stays bit-exact while FP64
+// runs only for near-tangent and near-degenerate cuts.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace nlg {
+
+// Margins, relative to the magnitude of each decision's operands. The FP32 rounding error of every
+// tested quantity is a few units of 2^-24 of that magnitude (coordinates are local to the ball
+// center, built from double-float differences), so each margin is at least 256 times larger.
+// Which roots of |q + l (p - q) - x|^2 = delta^2 lie in [0, 1] is fixed by the signs of its values
+// at 0 and 1 (vertex distances, MARG_D) and of the discriminant (MARG_V, flagged only when the
+// tangent point lies near the segment); MARG_L additionally guards the computed roots.
+constexpr float MARG_D = 1.0f / 65536.0f;  // |d^2 - delta^2| <= MARG_D * delta^2: vertex on the sphere
+constexpr float MARG_V = 1.0f / 16384.0f;  // |disc| <= MARG_V * (ab^2 + aa*bb): near-tangent line
+constexpr float MARG_L = 1.0f / 16384.0f;  // root within MARG_L of 0 or 1
+constexpr float MARG_C = 1.0f / 65536.0f;  // cap point near a triangle edge line
+constexpr float MARG_O = 1.0f / 4096.0f;   // near-degenerate triangle
+
+struct F2 {
+    float x, y;
+};
+__device__ __forceinline__ F2 f2(float x, float y) { return F2{x, y}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2{a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2{a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ float dot(F2 a, F2 b) { return fmaf(a.x, b.x, a.y * b.y); }
+
+constexpr float U32 = 5.9604645e-8f;      // 2^-24
+
+// inTriangle with margin: y carries a position error bound ey; a sign test is ambiguous when its
+// value is within twice the bound on its error.
+__device__ __forceinline__ bool fin_triangle(F2 y, float ey, const F2 *P, const F2 *nu, bool &amb, unsigned *why = nullptr) {
+    bool in = true;
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        F2 w = y - P[e];
+        float s = dot(nu[e], w);
+        const float nn = fabsf(nu[e].x) + fabsf(nu[e].y);
+        const float err = nn * (ey + 8.f * U32 * (fabsf(w.x) + fabsf(w.y) + fabsf(y.x) + fabsf(y.y)));
+        if (fabsf(s) <= fmaxf(2.f * err, MARG_C * nn * (fabsf(w.x) + fabsf(w.y)))) { amb = true; if (why) *why |= (ey > 16.f * U32 * (fabsf(y.x) + fabsf(y.y)) ? 64u : 32u); }
+        in = in && (s >= 0.f);
+    }
+    return in;
+}
+
+// Polygon point bookkeeping: position, edge it lies on (-1: a vertex or a cap point), error of
+// its position across its edge line (rounding) and along it (root error, large near tangency).
+struct FPoly {
+    F2 R[9];
+    float eperp[9], ealong[9];
+    signed char edge[9];
+    int n;
+};
+
+struct FPt {
+    F2 y;
+    float eperp, ealong;
+    int edge;
+};
+
+__device__ __forceinline__ FPt fpt_of(const FPoly &Y, int i) {
+    return FPt{Y.R[i], Y.eperp[i], Y.ealong[i], (int)Y.edge[i]};
+}
+
+__device__ __forceinline__ void fpush(FPoly &Y, const FPt &p, bool &amb) {
+    if (Y.n >= 9) { amb = true; return; }
+    Y.R[Y.n] = p.y; Y.eperp[Y.n] = p.eperp; Y.ealong[Y.n] = p.ealong; Y.edge[Y.n] = (signed char)p.edge;
+    Y.n++;
+}
+
+// Cap point between two consecutive polygon points (placePointOnCap, integration.cpp:1353-1377),
+// appended when it lies in the triangle. The reference places it at x + delta * n / |n| with n the
+// oriented normal of the chord. Both chord ends are cut points on the sphere, so in exact
+// arithmetic that point is also delta * m / |m| with m the chord midpoint (the perpendicular
+// bisector of a chord passes through the center), on the side sign(n . m). This form turns the
+// chord ends' position errors into a cap error of the same size instead of amplifying them by
+// delta / |chord|.
+__device__ __forceinline__ void fplace_cap(FPoly &Y, const FPt &a, const FPt &b, float sq, const F2 *P,
+                                           const F2 *nu, float orientation, bool &amb, unsigned *why = nullptr) {
+    const F2 n = f2((a.y.y - b.y.y) * orientation, (b.y.x - a.y.x) * orientation);
+    const F2 m = f2(0.5f * (a.y.x + b.y.x), 0.5f * (a.y.y + b.y.y));
+    const float mm = dot(m, m), nn = dot(n, n);
+    const float nm = dot(n, m);
+    const float delta = sqrtf(sq);
+    // n and m are parallel up to rounding; a near-diametral chord (m ~ 0) is left to FP64
+    if (!(nm * nm > 0.25f * nn * mm) || mm <= 1e-6f * sq) { amb = true; if (why) *why |= 128u; return; }
+    const float s = (nm > 0.f ? delta : -delta) * rsqrtf(mm);
+    const F2 y = f2(m.x * s, m.y * s);
+    const float em = 0.5f * (a.eperp + a.ealong + b.eperp + b.ealong);
+    const float ey = delta * em * rsqrtf(mm) + em + 8.f * U32 * delta;
+    if (fin_triangle(y, ey, P, nu, amb, why)) fpush(Y, FPt{y, ey, 0.f, -1}, amb);
+}
+
+// FP32 method_retriangulate with the triangle P given relative to the ball center. Returns the
+// polygon point count (sub-triangles: fan (R0, R[j+1], R[j+2])); amb = true when a decision was
+// within its margin (the result must then be recomputed in FP64).
+__device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F2 *R, bool &amb,
+                                              unsigned *why = nullptr) {
+    FPoly Y;
+    Y.n = 0;
+    bool is_onEdge = false, is_firstPointLiesOnVertex = true;
+    const F2 e1 = P[1] - P[0], e2 = P[2] - P[0];
+    const float det = e1.x * e2.y - e1.y * e2.x;
+    if (fabsf(det) <= MARG_O * (fabsf(e1.x) + fabsf(e1.y)) * (fabsf(e2.x) + fabsf(e2.y))) { amb = true; if (why) *why |= 1u; }
+    const float orientation = det > 0 ? -1.f : 1.f;
+    F2 nu[3];
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        F2 a = P[e], b = P[e == 2 ? 0 : e + 1];
+        nu[e] = f2((b.y - a.y) * orientation, (a.x - b.x) * orientation);
+    }
+    const float sqlo = sq * (1.f - MARG_D), sqhi = sq * (1.f + MARG_D);
+#pragma unroll 1
+    for (int k = 0; k < 3; k++) {
+        const F2 p = P[k], q = P[k == 2 ? 0 : k + 1];
+        const F2 b = p - q;
+        const float dp = dot(p, p);
+        if (dp > sqlo && dp < sqhi) { amb = true; if (why) *why |= 2u; }
+        if (dp <= sq) {
+            fpush(Y, FPt{p, 4.f * U32 * (fabsf(p.x) + fabsf(p.y)), 0.f, -1}, amb);
+            is_onEdge = false;
+        }
+        const float ab = dot(q, b), aa = dot(q, q), bb = dot(b, b);
+        const float aad = aa - sq;
+        if (fabsf(aad) <= MARG_D * sq) { amb = true; if (why) *why |= 2u; }   // q on the sphere (f(0) ~ 0)
+        const float v = ab * ab - aad * bb;
+        const float vscale = ab * ab + aa * bb;
+        if (fabsf(v) <= MARG_V * vscale) {
+            // near-tangent line: only ambiguous if a root can fall near the segment [0, 1]
+            const float t = -ab / bb;
+            const float r = sqrtf(2.f * MARG_V * vscale) / bb;
+            if (t + r >= -MARG_L && t - r <= 1.f + MARG_L) { amb = true; if (why) *why |= 4u; }
+        }
+        if (v >= 0.f) {
+            const float sv = sqrtf(v);
+            const float term1 = -ab / bb;
+            const float term2 = sv / bb;
+            float lam1, lam2;
+            if (term1 > 0.f) {
+                lam1 = term1 + term2;
+                lam2 = aad / (bb * lam1);
+            } else {
+                lam2 = term1 - term2;
+                lam1 = aad / (bb * lam2);
+            }
+            // cut point error: across the edge line only rounding; along it the root moves by
+            // err(v) / (2 sqrt(v) |b|), and err(v) <= 10 u (ab^2 + aa bb) (two products of dot
+            // products, each within a few u of its magnitude); bound taken twice
+            const float eperp = 8.f * U32 * (fabsf(q.x) + fabsf(q.y) + fabsf(b.x) + fabsf(b.y));
+            const float ealong = 10.f * U32 * vscale / fmaxf(sv * sqrtf(bb), 1e-30f);
+            if (fabsf(lam1) <= MARG_L || fabsf(lam1 - 1.f) <= MARG_L) { amb = true; if (why) *why |= 8u; }
+            if (fabsf(lam2) <= MARG_L || fabsf(lam2 - 1.f) <= MARG_L) { amb = true; if (why) *why |= 16u; }
+            if (lam1 >= 0.f && lam1 <= 1.f) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
+                const FPt y1{f2(fmaf(lam1, b.x, q.x), fmaf(lam1, b.y, q.y)), eperp, ealong, k};
+                if (is_onEdge && caps) fplace_cap(Y, fpt_of(Y, Y.n - 1), y1, sq, P, nu, orientation, amb, why);
+                fpush(Y, y1, amb);
+                is_onEdge = true;
+            }
+            if (lam2 >= 0.f && lam2 <= 1.f && v > 0.f) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
+                const FPt y2{f2(fmaf(lam2, b.x, q.x), fmaf(lam2, b.y, q.y)), eperp, ealong, k};
+                if (is_onEdge && caps) fplace_cap(Y, fpt_of(Y, Y.n - 1), y2, sq, P, nu, orientation, amb, why);
+                fpush(Y, y2, amb);
+                is_onEdge = true;
+            }
+        }
+    }
+    if (is_onEdge && (!is_firstPointLiesOnVertex && Y.n > 1) && caps)
+        fplace_cap(Y, fpt_of(Y, Y.n - 1), fpt_of(Y, 0), sq, P, nu, orientation, amb, why);
+    for (int i = 0; i < Y.n; i++) R[i] = Y.R[i];
+    return Y.n;
+}
+
+// Squared distance from the origin to the segment [p, q] and a bound on its FP32 error.
+__device__ __forceinline__ float fseg_dist2(F2 p, F2 q) {
+    const F2 u = q - p;
+    const float uu = dot(u, u);
+    float t = uu > 0.f ? -dot(p, u) / uu : 0.f;
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    const F2 c = f2(fmaf(t, u.x, p.x), fmaf(t, u.y, p.y));
+    return dot(c, c);
+}
+
+enum { CLS_OUT = 0, CLS_IN = 1, CLS_CUT = 2 };
+
+// Fast classes of one outer point against a triangle (relative to the ball center):
+//   CLS_IN   all vertices inside with margin: the polygon is the triangle itself
+//   CLS_OUT  every edge farther than delta with margin: no polygon point at all
+//   CLS_CUT  anything else
+__device__ __forceinline__ int fclassify(const F2 *P, float sq) {
+    const float sqlo = sq * (1.f - MARG_D), sqhi = sq * (1.f + MARG_D);
+    const float d0 = dot(P[0], P[0]), d1 = dot(P[1], P[1]), d2 = dot(P[2], P[2]);
+    if (d0 < sqlo && d1 < sqlo && d2 < sqlo) return CLS_IN;
+    const float m = fminf(fminf(d0, d1), d2);
+    if (m > sqhi) {
+        const float s0 = fseg_dist2(P[0], P[1]), s1 = fseg_dist2(P[1], P[2]), s2 = fseg_dist2(P[2], P[0]);
+        if (fminf(fminf(s0, s1), s2) > sqhi) return CLS_OUT;
+    }
+    return CLS_CUT;
+}
+
+}  // namespace nlg

@@ -71,6 +71,7 @@ __device__ __forceinline__ int xplaceCap(const double *ypred, const double *ycur
     double s = xsqrt(xdiv(sqdelta, xdot2(n0, n1, n0, n1)));
     double y[2] = {xadd(xc[0], xmul(n0, s)), xadd(xc[1], xmul(n1, s))};
     if (xinTriangle(y, TE, na, nb, nc)) {
+        if (Rdx >= 9) return 0;   // at most 9 polygon points exist; never reached
         R[2 * Rdx] = y[0];
         R[2 * Rdx + 1] = y[1];
         return 1;
@@ -97,10 +98,8 @@ __device__ __forceinline__ int xretriangulate(const double *xc, const double *TE
         const double a0 = xsub(q[0], xc[0]), a1 = xsub(q[1], xc[1]);
         const double b0 = xsub(p[0], q[0]), b1 = xsub(p[1], q[1]);
         if (xsqdist2(p, xc) <= sqdelta) {
-            R[2 * Rdx] = p[0];
-            R[2 * Rdx + 1] = p[1];
+            if (Rdx < 9) { R[2 * Rdx] = p[0]; R[2 * Rdx + 1] = p[1]; Rdx += 1; }
             is_onEdge = false;
-            Rdx += 1;
         }
         const double ab = xdot2(a0, a1, b0, b1);
         const double aa = xdot2(a0, a1, a0, a1);
@@ -124,20 +123,16 @@ __device__ __forceinline__ int xretriangulate(const double *xc, const double *TE
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
                 if (is_onEdge && caps)
                     Rdx += xplaceCap(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                R[2 * Rdx] = y1[0];
-                R[2 * Rdx + 1] = y1[1];
+                if (Rdx < 9) { R[2 * Rdx] = y1[0]; R[2 * Rdx + 1] = y1[1]; Rdx += 1; }
                 is_onEdge = true;
-                Rdx += 1;
             }
             const double dl = xsub(lam1, lam2);
             if ((0 <= lam2) && (lam2 <= 1) && (xmul(dl, dl) > 0)) {
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
                 if (is_onEdge && caps)
                     Rdx += xplaceCap(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                R[2 * Rdx] = y2[0];
-                R[2 * Rdx + 1] = y2[1];
+                if (Rdx < 9) { R[2 * Rdx] = y2[0]; R[2 * Rdx + 1] = y2[1]; Rdx += 1; }
                 is_onEdge = true;
-                Rdx += 1;
             }
         }
     }

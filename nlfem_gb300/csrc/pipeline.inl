@@ -98,6 +98,7 @@ static int make_rule(const nlfem_problem &p, bool inner, Rule &r) {
             r.Px[dim * k + j] = p.Px[dim * k + j];
             s -= p.Px[dim * k + j];
             r.psix[dV * k + j + 1] = p.Px[dim * k + j];
+            r.Pxf[dim * k + j] = (float)p.Px[dim * k + j];
         }
         r.psix[dV * k] = s;
         r.dx[k] = p.dx[k];
@@ -250,7 +251,10 @@ struct Session {
     // inputs
     DevBuf T64, labT64, V, labV64, eoffd, voffd, prm, duffy;
     // derived
-    DevBuf T32, labT, eprob, EC, adet, labV, vprob;
+    DevBuf T32, labT, eprob, EC, adet, labV, vprob, EChi, EClo, adetf;
+    DevBuf color, color2, colorlist, closeA, closeB, closebuf, touched;
+    std::vector<int> color_off;
+    int prec = 0;
     DevBuf vcnt, vptr, vel, adjcnt, xadj, adj;
     DevBuf visited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
@@ -264,7 +268,8 @@ struct Session {
                          &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited,
                          &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                          &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
-                         &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b};
+                         &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
+                         &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched};
         for (DevBuf *b : all) b->release();
         if (st) {
             for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
@@ -354,6 +359,10 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     }
     S.nE = S.eoff[n];
     S.nV = S.voff[n];
+    S.prec = probs[0].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64;
+    for (int i = 1; i < n; i++)
+        if ((probs[i].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64) != S.prec)
+            return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the precision");
     int r = make_rule(probs[0], system, S.rule);
     if (r) return r;
     for (int i = 1; i < n; i++) {
@@ -436,6 +445,9 @@ static int run_prep(Session &S) {
     ENS(S.eprob, sizeof(int) * nE);
     ENS(S.EC, sizeof(double) * nE * DIM * dV);
     ENS(S.adet, sizeof(double) * nE);
+    ENS(S.EChi, sizeof(float) * nE * DIM * dV);
+    ENS(S.adetf, sizeof(float) * nE);
+    ENS(S.EClo, sizeof(float) * nE * DIM * dV);
     ENS(S.labV, sizeof(int) * nV);
     ENS(S.vprob, sizeof(int) * nV);
     ENS(S.counters, sizeof(unsigned long long) * 16);
@@ -445,7 +457,7 @@ static int run_prep(Session &S) {
     k_prep_elements<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(
         S.T64.get<long long>(), S.labT64.get<long long>(), S.V.get<double>(), S.eoffd.get<int>(),
         S.voffd.get<int>(), S.nProb, nE, S.T32.get<int>(), S.labT.get<int>(), S.eprob.get<int>(),
-        S.EC.get<double>(), S.adet.get<double>());
+        S.EC.get<double>(), S.adet.get<double>(), S.EChi.get<float>(), S.EClo.get<float>(), S.adetf.get<float>());
     k_prep_vertices<<<grid_for(nV, 256), 256, 0, S.st>>>(S.labV64.get<long long>(), S.voffd.get<int>(),
         S.nProb, nV, S.labV.get<int>(), S.vprob.get<int>());
     CK(cudaGetLastError());
@@ -497,11 +509,12 @@ static int run_bfs(Session &S) {
         ENS(S.queue, sizeof(int) * (size_t)nwarps * S.qcap);
         ENS(S.pool, sizeof(int) * (size_t)S.pool_cap);
         CK(cudaMemsetAsync(S.visited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNE, S.st));
-        CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 4, S.st));
+        CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 8, S.st));
         CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
         BfsArgs a;
         a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>();
         a.adj = S.adj.get<int>(); a.xadj = S.xadj.get<long long>(); a.EC = S.EC.get<double>();
+        a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
         a.probs = S.prm.get<ProbParams>(); a.nE = nE;
         a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;
         a.queue = S.queue.get<int>(); a.qcap = S.qcap;
@@ -510,7 +523,9 @@ static int run_bfs(Session &S) {
         a.pool_cursor = cnt + 0; a.n_cand = cnt + 1; a.qneed = (long long *)(cnt + 2);
         a.seg_start = S.seg_start.get<long long>(); a.seg_cnt = S.seg_cnt.get<int>();
         a.err = S.err.get<int>();
-        k_bfs<DIM><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
+        a.n_amb = cnt + 7;
+        if (S.prec == PREC_MIX) k_bfs<DIM, PREC_MIX><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
+        else k_bfs<DIM, PREC_F64><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
         CK(cudaGetLastError());
         unsigned long long hc[3];
         int he[2];
@@ -524,6 +539,15 @@ static int run_bfs(Session &S) {
         return NLFEM_OK;
     }
     return fail(NLFEM_ERR_NOMEM, "BFS capacity retries exhausted");
+}
+
+static int sort_segments(Session &S, const long long *ptr, long long nseg, int *data) {
+    const int cap = 16384;
+    CK(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, cap * (int)sizeof(int)));
+    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(ptr, nseg, data, cap);
+    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(ptr, nseg, data, cap);
+    CK(cudaGetLastError());
+    return NLFEM_OK;
 }
 
 template <int DIM>
@@ -548,7 +572,54 @@ static int run_pairs(Session &S) {
     CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
     k_in_fill<<<grid_for(P, 256), 256, 0, S.st>>>(S.pA.get<int>(), S.pB.get<int>(), P, S.in_ptr.get<long long>(), S.incnt.get<int>(), S.inA.get<int>());
     CK(cudaGetLastError());
+    // sorted out- and in-lists: a fixed processing order, hence a fixed summation order
+    r = sort_segments(S, S.out_ptr.get<long long>(), nE, S.pB.get<int>());
+    if (r) return r;
+    r = sort_segments(S, S.in_ptr.get<long long>(), nE, S.inA.get<int>());
+    if (r) return r;
     S.stats.n_pairs = (long)P;
+    return NLFEM_OK;
+}
+
+// Deterministic element coloring (Jones-Plassmann rounds, ping-pong buffers) and color lists.
+static int run_color(Session &S) {
+    const long long nE = S.nE;
+    ENS(S.color, sizeof(int) * (nE + 1));
+    ENS(S.color2, sizeof(int) * (nE + 1));
+    ENS(S.colorlist, sizeof(int) * (nE + 1));
+    CK(cudaMemsetAsync(S.color.p, 0xff, sizeof(int) * (nE + 1), S.st));
+    unsigned long long *rem = S.counters.get<unsigned long long>() + 8;
+    int *cur = S.color.get<int>(), *nxt = S.color2.get<int>();
+    for (int round = 0; round < 1000; round++) {
+        CK(cudaMemsetAsync(rem, 0, sizeof(unsigned long long), S.st));
+        k_color_round<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), nE, S.eprob.get<int>(), S.prm.get<ProbParams>(), cur, nxt, rem, S.err.get<int>() + 9);
+        std::swap(cur, nxt);
+        unsigned long long left = 0;
+        int r = d2h(S, &left, rem, 1);
+        if (r) return r;
+        if (left == 0) break;
+    }
+    if (cur != S.color.get<int>()) CK(cudaMemcpyAsync(S.color.p, cur, sizeof(int) * nE, cudaMemcpyDeviceToDevice, S.st));
+    int e9 = 0;
+    int r = d2h(S, &e9, S.err.get<int>() + 9, 1);
+    if (r) return r;
+    if (e9) return fail(NLFEM_ERR_UNSUPPORTED, "more than 256 element colors");
+    ENS(S.keepcnt, sizeof(int) * 520);
+    int *cnt = S.keepcnt.get<int>();
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 520, S.st));
+    k_color_count<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt);
+    std::vector<int> h(256);
+    r = d2h(S, h.data(), cnt, 256);
+    if (r) return r;
+    int nc = 0;
+    for (int c = 0; c < 256; c++) if (h[c]) nc = c + 1;
+    S.color_off.assign(nc + 1, 0);
+    for (int c = 0; c < nc; c++) S.color_off[c + 1] = S.color_off[c] + h[c];
+    CK(cudaMemcpyAsync(cnt + 260, S.color_off.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 256, S.st));
+    k_color_fill<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt + 260, cnt, S.colorlist.get<int>());
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(S.st));
     return NLFEM_OK;
 }
 
@@ -654,35 +725,103 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
     return d2h(S, ret, S.keepcnt.get<int>(), (size_t)n);
 }
 
-template <int DIM>
-static int run_quad(Session &S) {
-    const long long P = S.P, nnz = S.nnz_struct;
-    ENS(S.acc, sizeof(unsigned long long) * 2 * (nnz + 1));
-    ENS(S.tiny, sizeof(unsigned) * (nnz + 1));
-    CK(cudaMemsetAsync(S.acc.p, 0, sizeof(unsigned long long) * 2 * (nnz + 1), S.st));
-    CK(cudaMemsetAsync(S.tiny.p, 0, sizeof(unsigned) * (nnz + 1), S.st));
+static PassRule make_pass_rule(const Rule &r, int dim) {
+    PassRule pr;
+    memset(&pr, 0, sizeof(pr));
+    const int dV = dim + 1, NS = dV * (dV + 1) / 2;
+    for (int k = 0; k < r.nPx; k++) {
+        pr.dxf[k] = (float)r.dx[k];
+        int t = 0;
+        for (int a = 0; a < dV; a++) {
+            pr.cx[dV * k + a] = (float)(r.dx[k] * r.psix[dV * k + a]);
+            for (int b = a; b < dV; b++) pr.cxx[NS * k + t++] = (float)(r.dx[k] * r.psix[dV * k + a] * r.psix[dV * k + b]);
+        }
+    }
+    for (int i = 0; i < r.nPy; i++) {
+        int t = 0;
+        for (int a = 0; a < dV; a++) {
+            pr.cy[dV * i + a] = (float)(r.dy[i] * r.psiy[dV * i + a]);
+            for (int b = a; b < dV; b++) pr.cyy[NS * i + t++] = (float)(r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b]);
+        }
+    }
+    return pr;
+}
+
+// Close pairs of the singular kernel: Duffy blocks into closebuf (FP64, one warp per pair).
+static int run_close(Session &S) {
+    if (S.dim != 2 || S.duffy_nPg == 0) return NLFEM_OK;
+    const long long nE = S.nE;
+    long long nadj = 0;
+    int r = d2h(S, &nadj, S.xadj.get<long long>() + nE, 1);
+    if (r) return r;
+    const long long nslot = nadj + nE;
+    ENS(S.closeA, sizeof(int) * (nslot + 1));
+    ENS(S.closeB, sizeof(int) * (nslot + 1));
+    ENS(S.closebuf, sizeof(double) * 36 * (nslot + 1));
+    ENS(S.closelist, sizeof(int) * (nslot + 1));
+    k_close_pairs<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), S.labT.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), nE, S.closeA.get<int>(), S.closeB.get<int>());
     QuadArgs a;
-    a.pA = S.pA.get<int>(); a.pB = S.pB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    memset(&a, 0, sizeof(a));
+    a.pA = S.closeA.get<int>(); a.pB = S.closeB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
     a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
-    a.probs = S.prm.get<ProbParams>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
-    a.acc = S.acc.get<unsigned long long>(); a.tiny = S.tiny.get<unsigned>(); a.P = P;
-    a.list = nullptr; a.nlist = 0; a.err = S.err.get<int>();
-    a.blocks_out = nullptr; a.ret_out = nullptr; a.force_close = 0;
+    a.probs = S.prm.get<ProbParams>(); a.P = nslot; a.err = S.err.get<int>();
+    a.n_close = S.counters.get<unsigned long long>() + 4;
+    a.blocks_out = S.closebuf.get<double>(); a.ret_out = S.closelist.get<int>(); a.force_close = 1;
+    k_iota<<<grid_for(nslot, 256), 256, 0, S.st>>>(S.closelist.get<int>(), nslot);
+    a.list = S.closelist.get<int>();
+    a.nlist = nslot;
+    k_quad_close<<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+template <int DIM>
+static int run_passes(Session &S) {
+    constexpr int dV = DIM + 1;
+    const long long nnz = S.nnz_struct;
+    ENS(S.vals, sizeof(double) * (nnz + 1));
+    CK(cudaMemsetAsync(S.vals.p, 0, sizeof(double) * (nnz + 1), S.st));
+    if (S.prec == PREC_MIX) {
+        ENS(S.touched, (size_t)nnz + 16);
+        CK(cudaMemsetAsync(S.touched.p, 0, (size_t)nnz + 16, S.st));
+    }
     unsigned long long *cnt = S.counters.get<unsigned long long>();
-    a.n_close = cnt + 4;
-    a.n_subtri = cnt + 5;
-    CK(cudaMemsetAsync(cnt + 3, 0, 3 * sizeof(unsigned long long), S.st));
-    if (P > 0) k_quad_fp64<DIM><<<grid_for(P, 128), 128, 0, S.st>>>(a, S.rule);
-    if (DIM == 2 && S.duffy_nPg > 0 && P > 0) {
-        ENS(S.closelist, sizeof(int) * (P + 1));
-        k_close_list<DIM><<<grid_for(P, 256), 256, 0, S.st>>>(a, S.closelist.get<int>(), cnt + 3);
-        unsigned long long ncl = 0;
-        int r = d2h(S, &ncl, cnt + 3, 1);
-        if (r) return r;
-        a.list = S.closelist.get<int>();
-        a.nlist = (long long)ncl;
-        Duffy d = duffy_view(S);
-        if (ncl) k_quad_close<<<grid_for((long long)ncl * 32, 128), 128, 0, S.st>>>(a, d);
+    CK(cudaMemsetAsync(cnt + 4, 0, 3 * sizeof(unsigned long long), S.st));
+    int r = run_close(S);
+    if (r) return r;
+    PassArgs a;
+    memset(&a, 0, sizeof(a));
+    a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>(); a.eprob = S.eprob.get<int>(); a.labT = S.labT.get<int>();
+    a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>(); a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
+    a.adetf = S.adetf.get<float>();
+    a.probs = S.prm.get<ProbParams>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
+    a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
+    a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
+    a.n_subtri = cnt + 5; a.n_amb = cnt + 6;
+    a.touched = S.prec == PREC_MIX ? S.touched.get<unsigned char>() : nullptr;
+    const PassRule pr = make_pass_rule(S.rule, DIM);
+    bool all_retri = true;
+    for (const ProbParams &q : S.hprm) all_retri &= (q.remote == MTH_RETRIANGULATE);
+    const bool use_mix2d = DIM == 2 && S.prec == PREC_MIX && all_retri;
+    const size_t smem2d = mix_warp_bytes(S.rule.nPx) * MIX_WARPS;
+    if (use_mix2d) CK(cudaFuncSetAttribute(k_pass_mix2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2d));
+    const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
+    if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    else CK(cudaFuncSetAttribute(k_pass<DIM, PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int ncol = (int)S.color_off.size() - 1;
+    for (int c = 0; c < ncol; c++) {
+        a.list = S.colorlist.get<int>() + S.color_off[c];
+        a.count = S.color_off[c + 1] - S.color_off[c];
+        if (!a.count) continue;
+        if (use_mix2d) {
+            const unsigned g2 = (unsigned)std::min<long long>((a.count + MIX_WARPS - 1) / MIX_WARPS, (long long)S.nSM * 8);
+            k_pass_mix2d<<<g2, MIX_THREADS, smem2d, S.st>>>(a, S.rule, pr);
+            continue;
+        }
+        const unsigned grid = (unsigned)std::min<long long>((a.count + PASS_WARPS - 1) / PASS_WARPS, (long long)S.nSM * 8);
+        if (S.prec == PREC_MIX) k_pass<DIM, PREC_MIX><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
+        else k_pass<DIM, PREC_F64><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
     }
     CK(cudaGetLastError());
     return NLFEM_OK;
@@ -690,17 +829,17 @@ static int run_quad(Session &S) {
 
 static int run_finish(Session &S) {
     const long long nV = S.nV;
-    ENS(S.vals, sizeof(double) * (S.nnz_struct + 1));
     ENS(S.keepcnt, sizeof(int) * (nV + 1));
     ENS(S.fptr, sizeof(long long) * (nV + 1));
-    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.acc.get<unsigned long long>(), S.tiny.get<unsigned>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.vals.get<double>(), S.keepcnt.get<int>());
+    const unsigned char *tch = S.prec == PREC_MIX ? S.touched.get<unsigned char>() : nullptr;
+    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), tch, S.keepcnt.get<int>());
     int r = scan_excl<int>(S, S.keepcnt.get<int>(), nV, S.fptr.get<long long>());
     if (r) return r;
     r = d2h(S, &S.nnz, S.fptr.get<long long>() + nV, 1);
     if (r) return r;
     ENS(S.fcols, sizeof(int) * (S.nnz + 1));
     ENS(S.fvals, sizeof(double) * (S.nnz + 1));
-    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.acc.get<unsigned long long>(), S.tiny.get<unsigned>(), S.cols.get<int>(), S.vals.get<double>(), S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
+    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), S.vals.get<double>(), tch, S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -722,10 +861,11 @@ static int run_system_t(Session &S) {
     if ((r = run_dual<DIM>(S))) return r;
     if ((r = run_bfs<DIM>(S))) return r;
     if ((r = run_pairs<DIM>(S))) return r;
+    if ((r = run_color(S))) return r;
     CK(cudaEventRecord(S.ev[1], S.st));
     if ((r = run_pattern<DIM>(S))) return r;
     CK(cudaEventRecord(S.ev[2], S.st));
-    if ((r = run_quad<DIM>(S))) return r;
+    if ((r = run_passes<DIM>(S))) return r;
     CK(cudaEventRecord(S.ev[3], S.st));
     if ((r = run_finish(S))) return r;
     CK(cudaEventRecord(S.ev[4], S.st));
@@ -733,10 +873,11 @@ static int run_system_t(Session &S) {
     if ((r = check_errors(S))) return r;
     float t[4];
     for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]));
-    unsigned long long ncl[2] = {0, 0};
-    if ((r = d2h(S, ncl, S.counters.get<unsigned long long>() + 4, 2))) return r;
+    unsigned long long ncl[4] = {0, 0, 0, 0};
+    if ((r = d2h(S, ncl, S.counters.get<unsigned long long>() + 4, 4))) return r;
     S.stats.n_close = (long)ncl[0];
     S.stats.n_subtri = (long)ncl[1];
+    S.stats.n_ambiguous = (long)(ncl[2] + ncl[3]);
     S.stats.ms_bfs = t[0];
     S.stats.ms_pattern = t[1];
     S.stats.ms_quad = t[2];
@@ -960,6 +1101,31 @@ int nlfem_retriangulate_batch(long n, const double *x_center, const double *TE, 
     CK(cudaMemcpy(counts, dc, sizeof(int) * n, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(out, dO, sizeof(double) * 54 * n, cudaMemcpyDeviceToHost));
     cudaFree(dx); cudaFree(dT); cudaFree(dO); cudaFree(dc);
+    return NLFEM_OK;
+}
+
+int nlfem_retriangulate_certified_batch(long n, const double *x_center, const double *TE, double sqdelta,
+                                        int caps, int *counts, int *ambiguous, double *points) {
+    if (n < 0 || (n && (!x_center || !TE || !counts || !ambiguous || !points))) return fail(NLFEM_ERR_INVALID, "null argument");
+    if (n == 0) return NLFEM_OK;
+    int r = device_ok();
+    if (r) return r;
+    double *dx = nullptr, *dT = nullptr, *dO = nullptr;
+    int *dc = nullptr, *da = nullptr;
+    CK(cudaMalloc(&dx, sizeof(double) * 2 * n));
+    CK(cudaMalloc(&dT, sizeof(double) * 6 * n));
+    CK(cudaMalloc(&dO, sizeof(double) * 18 * n));
+    CK(cudaMalloc(&dc, sizeof(int) * n));
+    CK(cudaMalloc(&da, sizeof(int) * n));
+    CK(cudaMemcpy(dx, x_center, sizeof(double) * 2 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dT, TE, sizeof(double) * 6 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dO, 0, sizeof(double) * 18 * n));
+    k_retri_cert_batch<<<grid_for(n, 128), 128>>>(n, dx, dT, sqdelta, caps, dc, da, dO);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(counts, dc, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ambiguous, da, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(points, dO, sizeof(double) * 18 * n, cudaMemcpyDeviceToHost));
+    cudaFree(dx); cudaFree(dT); cudaFree(dO); cudaFree(dc); cudaFree(da);
     return NLFEM_OK;
 }
 

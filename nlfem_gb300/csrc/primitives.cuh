@@ -87,6 +87,36 @@ __global__ void k_scan_down(const TIn *in, long long n_in, long long n_out,
     }
 }
 
+// ---------------------------------------------------------------- double-float accumulation
+// An unevaluated sum hi + lo of two floats, updated with error-free transforms (Knuth two-sum):
+// about 48 significant bits from FP32 adds only. Used where GB300's FP64 rate would otherwise
+// bound the accumulation of per-element blocks and CSR values.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_zero() { return DF{0.f, 0.f}; }
+__device__ __forceinline__ DF df_add(DF a, float b) {
+    const float s = a.hi + b;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b - bb);
+    e += a.lo;
+    const float hi = s + e;
+    return DF{hi, e - (hi - s)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return DF{hi, e - (hi - s)};
+}
+__device__ __forceinline__ DF df_from_double(double x) {
+    const float hi = (float)x;
+    return DF{hi, (float)(x - (double)hi)};
+}
+__device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
+
 // ---------------------------------------------------------------- 128-bit fixed point
 // A value x of problem scale 2^e is stored as round-toward-zero(x * 2^(FX_FRAC - e)) in a
 // two's-complement 128-bit integer split over two uint64 words (lo, hi). Integer addition is

@@ -19,6 +19,7 @@ struct Rule {
     double Px[MAXQ * 3], dx[MAXQ], Py[MAXQ * 3], dy[MAXQ];
     double psix[MAXQ * 4], psiy[MAXQ * 4];   // [k * dV + a]
     float Pyf[MAXQ * 2], dyf[MAXQ], psiyf[MAXQ * 4];
+    float Pxf[MAXQ * 3];
 };
 
 // Duffy tables of the singular close-pair rule (MeshTypes.cpp:252-327), device pointers.

@@ -327,6 +327,21 @@ def retriangulate_batch(x_centers, TEs, sqdelta, caps=1):
     return cnt, out
 
 
+def retriangulate_certified_batch(x_centers, TEs, sqdelta, caps=1):
+    """FP32 certified retriangulation: counts (n,), ambiguous (n,), points (n, 9, 2) relative to x."""
+    lib = _lib.load()
+    x = np.ascontiguousarray(x_centers, dtype=np.float64).reshape(-1, 2)
+    T = np.ascontiguousarray(TEs, dtype=np.float64).reshape(-1, 6)
+    n = x.shape[0]
+    pts = np.zeros((n, 9, 2))
+    cnt = np.zeros(n, dtype=np.int32)
+    amb = np.zeros(n, dtype=np.int32)
+    _lib.check(lib.nlfem_retriangulate_certified_batch(n, x.ctypes.data_as(_dp), T.ctypes.data_as(_dp),
+                                                       float(sqdelta), int(caps), cnt.ctypes.data_as(_ip),
+                                                       amb.ctypes.data_as(_ip), pts.ctypes.data_as(_dp)))
+    return cnt, amb, pts
+
+
 def py_toRef(TE, phys_x):
     lib = _lib.load()
     T = np.ascontiguousarray(TE, dtype=np.float64); x = np.ascontiguousarray(phys_x, dtype=np.float64)

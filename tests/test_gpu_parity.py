@@ -234,3 +234,153 @@ def test_par_assemble_file_protocol(nl, tmp_path):
     assert r == 0, lib.nlfem_last_error()
     B = nl.read_arma_spMat(tmp_path / "spAd")
     assert same_pattern(A, B) and abs(A - B).max() == 0
+
+
+# ---------------------------------------------------------------- mixed precision
+MIX_TOL = 1e-6   # relative Frobenius / max-entry error of the mixed path against the FP64 oracle
+
+
+def test_certified_geometry_small_triangles(nl, orc):
+    """Mesh regime: triangles of size ~delta/20 straddling the sphere, incl. near-tangent edges
+    and vertices close to it. Certified FP32 cases must match the exact polygon exactly."""
+    rng = np.random.Generator(np.random.PCG64(23))
+    delta = 0.1
+    n = 60000
+    ang = rng.uniform(0, 2 * np.pi, n)
+    rad = delta + rng.normal(0, 0.004, n)
+    rad[::5] = delta + rng.normal(0, 1e-6, n)[::5]          # vertex near the sphere
+    c = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1)
+    h = delta / 20 * rng.uniform(0.5, 1.5, n)
+    th = rng.uniform(0, 2 * np.pi, (n, 3))
+    T = np.zeros((n, 6))
+    T[:, 0:2] = c
+    T[:, 2:4] = c + h[:, None] * np.stack([np.cos(th[:, 1]), np.sin(th[:, 1])], 1)
+    T[:, 4:6] = c + h[:, None] * np.stack([np.cos(th[:, 2]), np.sin(th[:, 2])], 1)
+    T[1::7, 2:4] = T[1::7, 0:2] + (T[1::7, 0:2] / np.linalg.norm(T[1::7, 0:2], axis=1)[:, None])[:, ::-1] * [1, -1] * h[1::7, None]
+    x0 = np.array([0.3, -0.2])
+    X = np.tile(x0, (n, 1))
+    T = T + np.tile(x0, 3)
+    for caps in (1, 0):
+        cnt, amb, pts = nl.retriangulate_certified_batch(X, T, delta ** 2, caps)
+        namb = 0
+        for j in range(n):
+            if amb[j]:
+                namb += 1
+                continue
+            m, tri = orc.retriangulate_sq(X[j], T[j], delta ** 2, caps)
+            exact_pts = 0 if m == 0 else m + 2
+            got = cnt[j] if cnt[j] >= 3 else 0
+            assert got == exact_pts, (caps, j, cnt[j], m)
+            if m:
+                R = np.concatenate([tri[0, :1], tri[:, 1], tri[-1:, 2]], axis=0) - X[j]
+                # positions: FP32 accuracy, looser along near-tangent edges (values only)
+                np.testing.assert_allclose(pts[j, :exact_pts], R, atol=1e-3 * delta)
+        # about a third of the cases are built on a decision boundary
+        assert namb < 0.45 * n
+
+
+def test_certified_geometry_mesh_regime(nl, orc):
+    """Outer points of mesh elements against the elements near their ball boundary (the cases the
+    assembly meets): certified FP32 results equal the exact polygon counts; few fall back."""
+    from nlfem_gb300 import meshes, quadrules
+    v, e, l = meshes.regular_square(64, 0.1, jitter=0.2, seed=3)
+    P, w = quadrules.dunavant7()
+    rng = np.random.Generator(np.random.PCG64(4))
+    E = v[e]
+    bary = E.mean(axis=1)
+    X, T = [], []
+    for a in rng.choice(len(e), 60, replace=False):
+        xs = E[a][0] + (E[a][1] - E[a][0]) * P[:, :1] + (E[a][2] - E[a][0]) * P[:, 1:2]
+        d = np.linalg.norm(bary - bary[a], axis=1)
+        cand = np.where(np.abs(d - 0.1) < 0.04)[0]
+        for x in xs:
+            X.append(np.repeat(x[None], len(cand), 0)); T.append(E[cand].reshape(-1, 6))
+    X = np.concatenate(X); T = np.concatenate(T)
+    cnt, amb, pts = nl.retriangulate_certified_batch(X, T, 0.01, 1)
+    ex, _ = nl.retriangulate_batch(X, T, 0.01, 1)
+    ok = amb == 0
+    got = np.where(cnt >= 3, cnt - 2, 0)
+    np.testing.assert_array_equal(got[ok], ex[ok])
+    assert (~ok).sum() < 0.01 * (ex > 0).sum()
+
+
+def test_certified_geometry_never_disagrees(nl, orc):
+    """Where the FP32 geometry does not flag a decision as ambiguous, it reproduces the exact
+    polygon point count and its points to FP32 accuracy. Half of the cases are built to sit on a
+    decision boundary (tangent edges, vertices on the sphere); random cases rarely do."""
+    rng = np.random.Generator(np.random.PCG64(17))
+    cases = _cases_retri(rng, 4000)
+    amb_random = 0
+    for j, (x, T, sq, caps) in enumerate(cases):
+        c, a, pts = nl.retriangulate_certified_batch(x[None], T[None], sq, caps)
+        n, tri = orc.retriangulate_sq(x, T, sq, caps)
+        if a[0]:
+            amb_random += (j % 4 == 0)
+            continue
+        exact_pts = 0 if n == 0 else n + 2
+        got = c[0] if c[0] >= 3 else 0
+        assert got == exact_pts, (j, c[0], n)
+        if n:
+            R = np.concatenate([tri[0, :1], tri[:, 1], tri[-1:, 2]], axis=0) - x
+            np.testing.assert_allclose(pts[0, :exact_pts], R, atol=1e-3 * np.sqrt(sq) + 1e-6)
+    assert amb_random < 0.05 * len(cases) / 4
+
+
+@pytest.mark.parametrize("n,delta,kern,jit", [(32, 0.1, "constant", 0.0), (24, 0.12, "parabola", 0.2),
+                                              (20, 0.15, "constant", 0.2)])
+def test_mixed_matches_oracle(nl, orc, n, delta, kern, jit):
+    m = square_mesh(n, delta, jitter=jit, seed=n)
+    k = {"function": kern, "horizon": delta, "outputdim": 1}
+    A = nl.stiffnessMatrix(m, k, conf2d(precision="mixed"))
+    B = orc.assemble(m, k, conf2d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_pair_list_exact(nl, orc):
+    m = square_mesh(24, 0.13, jitter=0.2, seed=3)
+    k = {"function": "constant", "horizon": 0.13, "outputdim": 1}
+    ref = orc.assemble(m, k, conf2d(), want_pairs=True)
+    got = nl.pair_list(m, k, conf2d(precision="mixed"))
+    rp = ref["pairs"][np.lexsort((ref["pairs"][:, 1], ref["pairs"][:, 0]))]
+    np.testing.assert_array_equal(got, rp)
+
+
+def test_mixed_fractional(nl, orc):
+    m = square_mesh(12, 0.2, jitter=0.1, seed=5)
+    k = {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4}
+    A = nl.stiffnessMatrix(m, k, conf2d(rule="16", close="fractional", deg=3, precision="mixed"))
+    B = orc.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_3d(nl, orc):
+    m = cube_mesh(5, 0.1, jitter=0.15, seed=2)
+    k = {"function": "constant3D", "horizon": 0.3, "outputdim": 1}
+    A = nl.stiffnessMatrix(m, k, conf3d(precision="mixed"))
+    B = orc.assemble(m, k, conf3d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_deterministic(nl):
+    m = square_mesh(28, 0.1, jitter=0.2, seed=6)
+    k = {"function": "parabola", "horizon": 0.1, "outputdim": 1}
+    A = nl.stiffnessMatrix(m, k, conf2d(precision="mixed"))
+    B = nl.stiffnessMatrix(m, k, conf2d(precision="mixed"))
+    assert same_pattern(A, B) and np.array_equal(A.data, B.data)
+
+
+def test_mixed_pattern_equals_fp64_at_scale(nl):
+    """On a mesh too large for the oracle the mixed pattern still equals the FP64 GPU pattern
+    (itself bit-exact against the oracle on the smaller meshes above)."""
+    m = square_mesh(96, 0.1, jitter=0.2, seed=1)
+    A = nl.stiffnessMatrix(m, KC, conf2d(precision="mixed"))
+    B = nl.stiffnessMatrix(m, KC, conf2d())
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)

@@ -144,6 +144,21 @@ int nlfem_par_assemble(const char *compute, const char *path_spAd, const char *p
                        int degree, const double *dg, double maxDiameter, double fractional_s,
                        int is_fullConnectedComponentSearch, int verbose);
 
+/* Allocation-free load vector (no counterpart in the reference). The same result as
+ * nlfem_load_vector (continuous P1, bit-identical) for callers that must not let a library allocate
+ * device memory: the mesh arrays and d_fd (nV doubles) are caller-owned DEVICE pointers, Px/dx
+ * and forcing are host data, and the only scratch is a static 16 MiB device array inside the
+ * library, so no cudaMalloc or cudaFree happens. At most 1,048,576 vertices (NLFEM_ERR_INVALID
+ * above). The first call on each device does a one-time set-up (it looks up the array's address
+ * with that device current) and should come before any stream capture. Calls share the array:
+ * overlapping calls (two streams or threads) race and must be serialized by the caller. Work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream); returns once d_fd holds the
+ * result. */
+int nlfem_load_vector_noalloc(int dim, long nE, long nV, const long *d_elements,
+                              const long *d_elementLabels, const double *d_vertices,
+                              const long *d_vertexLabels, const double *Px, int nPx,
+                              const double *dx, const char *forcing, double *d_fd, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

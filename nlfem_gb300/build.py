@@ -1,4 +1,4 @@
-"""Builds libnlfem_gpu.so in-tree with nvcc for sm_103a (two translation units in parallel)."""
+"""Builds libnlfem_gpu.so in-tree with nvcc for sm_103a (three translation units in parallel)."""
 import os
 import subprocess
 import sys
@@ -36,6 +36,8 @@ def build(force=False, verbose=False):
                                   "-o", os.path.join(objdir, "assemble.o")],
         [NVCC] + common + ["-x", "cu", "-c", os.path.join(CSRC, "compat.cpp"),
                            "-o", os.path.join(objdir, "compat.o")] + ARCH,
+        [NVCC] + ARCH + common + ["-c", os.path.join(CSRC, "noalloc.cu"),
+                                  "-o", os.path.join(objdir, "noalloc.o")],
     ]
 
     def run(cmd):
@@ -46,7 +48,7 @@ def build(force=False, verbose=False):
             raise RuntimeError("nvcc failed:\n" + p.stdout + p.stderr)
         return p.stdout + p.stderr
 
-    with ThreadPoolExecutor(2) as ex:
+    with ThreadPoolExecutor(len(jobs)) as ex:
         logs = list(ex.map(run, jobs))
     if verbose:
         for l in logs:
@@ -54,7 +56,7 @@ def build(force=False, verbose=False):
                 print(l)
     tmp = LIB + ".tmp"
     run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(objdir, "assemble.o"),
-                         os.path.join(objdir, "compat.o"), "-lcudart"])
+                         os.path.join(objdir, "compat.o"), os.path.join(objdir, "noalloc.o"), "-lcudart"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -958,6 +958,11 @@ static int device_ok() {
 
 }  // namespace nlg
 
+// Error reporting for the entry points compiled in other translation units (not exported).
+__attribute__((visibility("hidden"))) int nlfem_fail_internal(int code, const char *msg) {
+    return nlg::fail(code, msg ? msg : "");
+}
+
 // ======================================================================= C ABI
 using namespace nlg;
 

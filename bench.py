@@ -7,9 +7,16 @@ right-diagonal triangulation with 2*256^2 triangles, interior vertices jittered 
 stiffness-matrix assembly (dual graph, BFS pair search, pattern, quadrature, deterministic
 scatter, zero dropping) from the mesh in HBM to the CSR matrix in HBM.
 
-metric: element-pair quadratures/s = interacting ordered element pairs / assembly time.
-Prints one JSON line (rank 0). --impl reference times the CPU restatement of the reference
-(oracle, OpenMP, all host cores) on a bounded sample of the same workload instead.
+metric: element-pair quadratures/s = interacting ordered element pairs (reference integrate()
+calls that contribute) / assembly time. The headline runs the mixed FP32/FP64 path; the all-FP64
+GPU path is timed on the same workload beside it, and the relative Frobenius / max-entry error
+of the mixed matrix against the FP64 one is reported (the FP64 path itself matches the CPU
+oracle to 1e-12 in the parity tests).
+
+--impl reference times the CPU restatement of the reference algorithm (oracle, OpenMP, all host
+cores) on a bounded sample of the same workload. --gpus N runs N independent replicas (one per
+GPU; the assembly of one problem is not partitioned), value = all pairs / max time over ranks.
+Prints one JSON line (rank 0).
 """
 import argparse
 import json
@@ -24,26 +31,31 @@ sys.path.insert(0, ROOT)
 
 import numpy as np
 
-METRIC = "element-pair quadratures/s"
+METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel err"
+
+# DRAM traffic of one k_pass_mix2d launch (one color) of the default workload, from the ncu
+# capture summarised in profiles/ (read + write bytes; None when the workload differs from the
+# captured one).
+PASS_TRAFFIC_BYTES = {(256, 0.1): None}
 
 
-def workload(args):
+def workload(args, precision):
     from nlfem_gb300 import meshes, quadrules
     v, e, l = meshes.regular_square(args.n, args.delta, jitter=0.2, seed=1)
     mesh = meshes.mesh_dict(v, e, l)
     P, w = quadrules.dunavant7()
     conf = {"ansatz": "CG", "approxBalls": {"method": "retriangulate", "is_PlacePointOnCap": 1},
             "quadrature": {"outer": {"points": P, "weights": w}, "inner": {"points": P, "weights": w}},
-            "precision": args.precision}
+            "precision": precision}
     kernel = {"function": "constant", "horizon": args.delta, "outputdim": 1}
     return mesh, kernel, conf
 
 
 def config_dict(args, mesh):
-    return {"workload": f"2D constant kernel, 2*{args.n}^2 triangles jittered +-0.2h, delta={args.delta}, "
+    return {"workload": f"2D constant kernel, 2*{args.n}^2 triangles jittered +-0.2h (seed 1), delta={args.delta}, "
                         f"retriangulate+caps, 7-pt Dunavant outer/inner, P1 CG",
             "n": args.n, "delta": args.delta, "nE": int(mesh["elements"].shape[0]),
-            "nV": int(mesh["vertices"].shape[0]), "precision": args.precision,
+            "nV": int(mesh["vertices"].shape[0]), "precision": "mixed (headline) and fp64",
             "l2": "flushed between steps (256 MiB write)"}
 
 
@@ -53,7 +65,8 @@ class Clocks:
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, index=0):
+        self.index = index
         self.samples = []
         self.stop = threading.Event()
         self.t = threading.Thread(target=self.run, daemon=True)
@@ -61,7 +74,7 @@ class Clocks:
     def run(self):
         while not self.stop.is_set():
             try:
-                out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={self.FIELDS}",
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                       "--format=csv,noheader,nounits"], capture_output=True,
                                      text=True, timeout=5).stdout.strip()
                 if out:
@@ -98,6 +111,24 @@ def measured_peaks():
         return {}
 
 
+def algorithmic_flops(st, conf, kernel):
+    """Floating-point operations the reference algorithm needs for one assembly (retriangulate,
+    2D, outdim 1), counted from integration.cpp:345-540 and :1393-1512 with loop invariants
+    hoisted (an FMA counts 2):
+      per pair:                         12  (toRef factorisation of bT)
+      per (pair, outer point):         198  (toPhys 8, method_retriangulate 133, outer fold
+                                             of termLocal/termNonloc/termNonlocPrime 57)
+      per (pair, outer pt, sub-tri):    11  (edge vectors, |det|)
+      per inner point of a sub-tri: 51 + k (toPhys 8, toRef 10, basis 2, weight 1, innerLocal 2,
+                                             innerNonloc 6, innerNonlocPrime 6, termLocalPrime 16;
+                                             k = 0 constant kernel, 7 parabola)
+    n_subtri counts each (pair, outer point, sub-triangle) unit once."""
+    nPx = len(conf["quadrature"]["outer"]["weights"])
+    nPy = len(conf["quadrature"]["inner"]["weights"])
+    kf = {"constant": 0, "parabola": 7}.get(kernel["function"], 0)
+    return st["n_pairs"] * (12 + nPx * 198) + st["n_subtri"] * (11 + nPy * (51 + kf))
+
+
 def cpu_sample(mesh, kernel, conf, seconds, threads):
     """Oracle (CPU restatement, OpenMP) on a bounded sample of outer elements."""
     from oracle import oracle
@@ -114,11 +145,10 @@ def cpu_sample(mesh, kernel, conf, seconds, threads):
 
 
 def run_reference(args):
-    mesh, kernel, conf = workload(args)
+    mesh, kernel, conf = workload(args, "fp64")
     threads = os.cpu_count() or 1
-    vals = []
     per_step = max(2.0, args.cpu_seconds / max(args.steps, 1))
-    for _ in range(args.warmup if args.warmup < 1 else 1):
+    for _ in range(min(args.warmup, 1)):
         cpu_sample(mesh, kernel, conf, 1.0, threads)
     tot_p = tot_s = 0.0
     ns = 0
@@ -126,9 +156,9 @@ def run_reference(args):
         p, s, ns = cpu_sample(mesh, kernel, conf, per_step, threads)
         tot_p += p
         tot_s += s
-        vals.append(p / s)
     value = tot_p / tot_s
-    sample = f"{ns} outer elements drawn uniformly (seed 0) of {mesh['elements'].shape[0]}, BFS + quadrature + map scatter per element"
+    sample = (f"{ns} outer elements drawn uniformly (seed 0) of {mesh['elements'].shape[0]} per step: "
+              f"BFS + quadrature + map scatter of those rows, FP64, {threads} OpenMP threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
@@ -140,33 +170,78 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args):
+def timed_session(mesh, kernel, conf, steps, warmup, flush, clocks_index=0, dist=None):
+    """W untimed + K timed assemblies from HBM-resident inputs; L2 flushed before each step.
+    Returns (pairs, seconds, last stats, per-step stats, clocks, session)."""
+    import torch
+    from nlfem_gb300 import nlfem
+    sess = nlfem.Session([(mesh, kernel, conf)])
+    for _ in range(warmup):
+        sess.assemble()
+    stats = []
+    with Clocks(clocks_index) as clk:
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            stats.append(sess.assemble())   # device time of the step: CUDA events on its stream
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+    pairs = float(sum(s["n_pairs"] for s in stats))
+    secs = float(sum(s["ms_total"] for s in stats)) / 1000.0
+    return pairs, secs, stats[-1], stats, clk.summary(), sess
+
+
+def rel_err(A, B):
+    """Relative Frobenius and max-entry error of A against B."""
+    A = A.tocsr(); B = B.tocsr()
+    A.sort_indices(); B.sort_indices()
+    same = (A.shape == B.shape and np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices))
+    if same:
+        d, b = A.data - B.data, B.data
+    else:
+        d, b = (A - B).tocsr().data, B.data
+    return same, float(np.sqrt(np.sum(d * d)) / np.sqrt(np.sum(b * b))), float(np.max(np.abs(d)) / np.max(np.abs(b)))
+
+
+def run_gpu(args, rank=0, world=1, dist=None):
+    import ctypes
     import torch
     from nlfem_gb300 import nlfem, _lib
     lib = _lib.load()
     if lib.nlfem_device_count() == 0:
         raise SystemExit("no CUDA device")
     torch.cuda.init()
-    mesh, kernel, conf = workload(args)
+    dev = torch.cuda.current_device()
+    mesh, kernel, conf = workload(args, "mixed")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    sess = nlfem.Session([(mesh, kernel, conf)])
-    for _ in range(args.warmup):
-        st = sess.assemble()
-    ms, pairs, stats = [], [], []
-    with Clocks() as clk:
-        for _ in range(args.steps):
-            flush.fill_(1)
-            torch.cuda.synchronize()
-            st = sess.assemble()
-            ms.append(st["ms_total"])
-            pairs.append(st["n_pairs"])
-            stats.append(st)
-    clocks = clk.summary()
-    A = sess.download(0)
+
+    pairs, secs, st, all_st, clocks, sess = timed_session(mesh, kernel, conf, args.steps, args.warmup,
+                                                          flush, dev, dist)
+    launches = int(sum(s["n_launches"] for s in all_st))
+    if dist is not None:
+        t = torch.tensor([secs], dtype=torch.float64, device="cuda")
+        p = torch.tensor([pairs], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(p, op=dist.ReduceOp.SUM)
+        secs, pairs = float(t.item()), float(p.item())
+    value = pairs / secs
+    A_mixed = sess.download(0)
     sess.close()
-    t_ms = float(np.sum(ms))
-    value = float(np.sum(pairs)) / (t_ms / 1000.0)
-    st = stats[-1]
+    if rank != 0:
+        return
+
+    # roofline of the dominant kernel (k_pass_mix2d, one launch per color): algorithmic flops
+    # of the step / device time of the quadrature phase (all its launches), against the FP32
+    # FMA peak measured in this run
+    f32, f64 = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    _lib.check(lib.nlfem_measure_peaks(ctypes.byref(f32), ctypes.byref(f64)))
+    peak32, peak64 = f32.value, f64.value
+    flops = algorithmic_flops(st, conf, kernel)
+    achieved = flops / (st["ms_quad"] / 1000.0) / 1e12
 
     # end to end through the public API: pinned host inputs, host CSR out
     pin = {}
@@ -178,11 +253,8 @@ def run_gpu(args):
     pmesh = dict(mesh)
     pmesh.update(pin)
     h2d = sum(pin[k].nbytes for k in pin)
-    for _ in range(1):
-        nlfem.stiffnessMatrix(pmesh, kernel, conf)
-    e2e_t = []
-    e2e_p = 0
-    d2h = 0
+    nlfem.stiffnessMatrix(pmesh, kernel, conf)
+    e2e_t, e2e_p, d2h = [], 0, 0
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -192,50 +264,49 @@ def run_gpu(args):
         d2h = B.data.nbytes + B.indices.nbytes + B.indptr.nbytes
     e2e = e2e_p / float(np.sum(e2e_t))
 
-    # roofline: the quadrature kernel, algorithmic FP64 flops per launch / its device time
-    flops = algorithmic_flops(st, conf)
-    achieved = flops / (st["ms_quad"] / 1000.0) / 1e12
-    peaks = measured_peaks()
-    peak = args.fp_peak_tflops
     line = {
-        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": config_dict(args, mesh),
-        "pairs_per_step": int(pairs[-1]), "nnz": int(A.nnz), "nnz_structural": int(st["nnz_structural"]),
+        "pairs_per_step": int(st["n_pairs"]), "nnz": int(A_mixed.nnz), "nnz_structural": int(st["nnz_structural"]),
         "fp64_fallbacks": int(st["n_ambiguous"]), "subtriangles": int(st["n_subtri"]),
-        "phase_ms": {"dual+bfs+pairs": st["ms_bfs"], "pattern": st["ms_pattern"],
+        "phase_ms": {"dual+bfs+pairs+color": st["ms_bfs"], "pattern": st["ms_pattern"],
                      "quadrature+scatter": st["ms_quad"], "finish": st["ms_finish"]},
-        "roofline": {"bound": args.fp_bound, "kernel": "k_quad (quadrature + scatter)",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
-                     "note": "algorithmic FP64 flops of the reference arithmetic per step / quadrature phase time; "
-                             "peak = nominal CUDA-core FP64 rate (no tensor-core or HBM bound applies)"},
-        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp32", "kernel": "k_pass_mix2d (quadrature + deterministic scatter, one launch per color)",
+                     "achieved": achieved, "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
+                     "traffic": PASS_TRAFFIC_BYTES.get((args.n, args.delta)),
+                     "note": "achieved = algorithmic flops of the reference algorithm for the step (FLOP model in "
+                             "bench.algorithmic_flops) / device time of the quadrature phase; peak = FP32 FMA "
+                             "throughput measured in this run (of measured); CUDA-core bound path with no "
+                             "GEMM-shaped work, so neither the tensor-core nor the HBM peak applies"},
+        "peaks_measured": {"fp32_tflops": peak32, "fp64_tflops": peak64,
+                           "hbm_gbs": measured_peaks().get("hbm_gbs")},
+        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "clocks": clocks,
-        "gpu_launches": int(args.launches_per_step * args.steps),
-        "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        "gpu_launches": launches,
     }
-    if not args.no_cpu:
+
+    if world == 1 and not args.no_fp64:
+        mesh64, kernel64, conf64 = workload(args, "fp64")
+        p64, s64, st64, _, clk64, sess64 = timed_session(mesh64, kernel64, conf64, args.fp64_steps, 1, flush, dev)
+        A64 = sess64.download(0)
+        sess64.close()
+        same, fro, mx = rel_err(A_mixed, A64)
+        a64 = algorithmic_flops(st64, conf64, kernel64) / (st64["ms_quad"] / 1000.0) / 1e12
+        line["fp64"] = {"value": p64 / s64, "unit": "pairs/s", "steps": args.fp64_steps,
+                        "ms_per_step": 1000.0 * s64 / args.fp64_steps, "mixed_over_fp64": value / (p64 / s64),
+                        "roofline": {"bound": "fp64", "achieved": a64, "peak": peak64, "unit": "TFLOP/s",
+                                     "frac": a64 / peak64},
+                        "clocks": clk64}
+        line["rel_err_vs_fp64"] = {"pattern_identical": bool(same), "fro": fro, "max": mx, "bound": 1e-6}
+    if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        p, s, ns = cpu_sample(mesh, kernel, conf, args.cpu_seconds, threads)
+        p, s, ns = cpu_sample(mesh, kernel, dict(conf, precision="fp64"), args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": p / s, "unit": "pairs/s", "cores": threads, "kind": "port",
-                                "sample": f"{ns} outer elements (uniform, seed 0) of {mesh['elements'].shape[0]}"}
+                                "sample": f"{ns} outer elements (uniform, seed 0) of {mesh['elements'].shape[0]}: "
+                                          f"BFS + FP64 quadrature + map scatter of their rows"}
     print(json.dumps(line), flush=True)
-
-
-def algorithmic_flops(st, conf):
-    """FP64 operations of the reference arithmetic for one assembly (counted from the code):
-    per (pair, outer point): toPhys 8 + method_retriangulate ~150; per (sub-triangle, inner
-    point): toPhys 10, two kernel values 2, toRef 14, basis 2, inner sums 4 + 2*3*4,
-    termLocalPrime 9*7; per (pair, outer point) the outer accumulation 3*3*(5+4+4)."""
-    nPx = len(conf["quadrature"]["outer"]["weights"])
-    nPy = len(conf["quadrature"]["inner"]["weights"])
-    per_outer = 8 + 150 + 9 * 13
-    per_inner = 10 + 2 + 14 + 2 + 4 + 24 + 63
-    return st["n_pairs"] * nPx * per_outer + st["n_subtri"] * nPy * per_inner
 
 
 def main():
@@ -246,40 +317,31 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--delta", type=float, default=0.1)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--fp-peak-tflops", type=float, default=1.25)
-    ap.add_argument("--fp-bound", default="fp64")
-    ap.add_argument("--launches-per-step", type=int, default=40)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
         return
-    if args.gpus > 1:
-        # replicas only: the assembly of one problem is not partitioned across GPUs
+    if world > 1:
+        # replicas only: each rank assembles the full workload on its own GPU, no collective on
+        # the data path; the barrier and the max over ranks bracket the timed steps
         import torch
         import torch.distributed as dist
-        local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-        dist.barrier()
-        if rank != 0:
-            args.no_cpu = True
-        run_gpu(args) if rank == 0 else run_gpu_silent(args)
-        dist.barrier()
-        dist.destroy_process_group()
+        try:
+            run_gpu(args, rank, world, dist)
+        finally:
+            dist.barrier()
+            dist.destroy_process_group()
         return
     run_gpu(args)
-
-
-def run_gpu_silent(args):
-    import contextlib
-    import io
-    with contextlib.redirect_stdout(io.StringIO()):
-        run_gpu(args)
 
 
 if __name__ == "__main__":

@@ -81,10 +81,11 @@ typedef struct nlfem_stats {
     long n_candidates;   /* integrate() calls of the BFS, interacting or not */
     long n_close;        /* pairs integrated with the singular close-pair rule */
     long nnz_structural; /* slots before exact zeros are dropped */
-    long n_subtri;       /* (pair side, outer point, sub-triangle) integrations of the remote rule */
+    long n_subtri;       /* (pair, outer point, sub-triangle) units of the remote rule, each once */
     long n_ambiguous;    /* outer points whose FP32 geometry fell back to FP64 (mixed precision) */
     double ms_total;     /* device time of the assembly (CUDA events) */
     double ms_bfs, ms_pattern, ms_quad, ms_finish;
+    long n_launches;     /* kernels the library launched for the assembly */
 } nlfem_stats;
 
 const char *nlfem_last_error(void);
@@ -143,6 +144,10 @@ int nlfem_par_assemble(const char *compute, const char *path_spAd, const char *p
                        const long *ptrZetaIndicator_indptr, long nZeta, const double *Pg,
                        int degree, const double *dg, double maxDiameter, double fractional_s,
                        int is_fullConnectedComponentSearch, int verbose);
+
+/* Benchmark helper (no counterpart in the reference): measured FP32 and FP64 FMA throughput of
+ * the current device in TFLOP/s, the roofline denominators of the quadrature kernels. */
+int nlfem_measure_peaks(double *fp32_tflops, double *fp64_tflops);
 
 /* Allocation-free load vector (no counterpart in the reference). The same result as
  * nlfem_load_vector (continuous P1, bit-identical) for callers that must not let a library allocate

@@ -47,7 +47,7 @@ class Stats(ctypes.Structure):
                 ("n_subtri", ctypes.c_long), ("n_ambiguous", ctypes.c_long),
                 ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double),
                 ("ms_pattern", ctypes.c_double), ("ms_quad", ctypes.c_double),
-                ("ms_finish", ctypes.c_double)]
+                ("ms_finish", ctypes.c_double), ("n_launches", ctypes.c_long)]
 
 
 class NlfemError(RuntimeError):
@@ -92,6 +92,7 @@ def load():
     l.nlfem_toRef.argtypes = [_dp, _dp, _dp]
     l.nlfem_toPhys.argtypes = [_dp, _dp, ctypes.c_int, _dp]
     l.nlfem_solve2x2.argtypes = [_dp, _dp, _dp]
+    l.nlfem_measure_peaks.argtypes = [_dp, _dp]
     vp = ctypes.c_void_p   # device pointers and the stream are passed as raw addresses
     l.nlfem_load_vector_noalloc.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, vp, vp, vp, vp,
                                             _dp, ctypes.c_int, _dp, ctypes.c_char_p, vp, vp]
@@ -117,5 +118,5 @@ EXPORTED = [
     "nlfem_session_assemble", "nlfem_session_download", "nlfem_session_destroy",
     "nlfem_pair_list", "nlfem_pair_blocks", "nlfem_method_retriangulate",
     "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
-    "nlfem_par_assemble", "nlfem_load_vector_noalloc",
+    "nlfem_par_assemble", "nlfem_load_vector_noalloc", "nlfem_measure_peaks",
 ]

@@ -354,7 +354,6 @@ __device__ void in_retri_mix(const ProbParams &P, const Rule &rule, const PassRu
         float i0 = 0.f, i1 = 0.f, i2 = 0.f;
         float lp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (cls == CLS_IN) {
-            nsub++;
             for (int i = 0; i < rule.nPy; i++) {
                 const F2 y = yT[i] - x;
                 const float kw = kernel_f32(P, -y.x, -y.y) * rTT;
@@ -370,7 +369,6 @@ __device__ void in_retri_mix(const ProbParams &P, const Rule &rule, const PassRu
             F2 R[9];
             const int n = cut_polygon(Q, sqf, P, x64, ET64, R, namb);
             for (int r = 0; r + 2 < n; r++) {
-                nsub++;
                 const F2 A = R[0], B = R[r + 1] - R[0], C = R[r + 2] - R[0];
                 const float rT = fabsf(B.x * C.y - B.y * C.x);
                 for (int i = 0; i < rule.nPy; i++) {
@@ -447,7 +445,6 @@ __device__ void in_retri_f64(const ProbParams &P, const Rule &rule, const double
         const int Rdx = xretriangulate(x, ET, P.sqdelta, P.caps, R);
         double iNP[3] = {0, 0, 0};
         for (int r = 0; r + 2 < Rdx; r++) {
-            nsub++;
             const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
             const double rTdet = xabsDet2(tri);
             for (int i = 0; i < rule.nPy; i++) {

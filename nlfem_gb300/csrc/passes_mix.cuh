@@ -119,7 +119,6 @@ __device__ __forceinline__ void item_in_cut(const ProbParams &P, const Rule &rul
     float i0 = 0.f, i1 = 0.f, i2 = 0.f;
     float lp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int r = 0; r + 2 < n; r++) {
-        nsub++;
         const F2 A = R[0], B = R[r + 1] - R[0], C = R[r + 2] - R[0];
         const float rT = fabsf(B.x * C.y - B.y * C.x);
         for (int i = 0; i < rule.nPy; i++) {
@@ -279,7 +278,6 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(PassArgs a, Rule rul
                             nsub++;
                             item_out_in(P, rule, pr, W.pc[j], W.prt[j], W.xf[k], rr);
                         } else {
-                            nsub++;
                             const float *q = W.pc[j];
                             const float px = rule.Pxf[2 * k], py = rule.Pxf[2 * k + 1];
                             const F2 x = f2(q[0] + (q[2] - q[0]) * px + (q[4] - q[0]) * py, q[1] + (q[3] - q[1]) * px + (q[5] - q[1]) * py);

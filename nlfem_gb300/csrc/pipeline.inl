@@ -262,6 +262,7 @@ struct Session {
     DevBuf out64a, out64b;
     long long qcap = 0, pool_cap = 0;
     long long P = 0, nnz_struct = 0, nnz = 0;
+    long long nlaunch = 0;   // kernels launched by the current assembly
     nlfem_stats stats;
     ~Session() {
         DevBuf *all[] = {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
@@ -298,25 +299,25 @@ static int scan_excl(Session &S, const TIn *in, long long n, long long *out) {
     struct Lvl { long long n; long long *bsum; long long *boff; long long nb; };
     std::vector<Lvl> lv;
     lv.push_back({m, tmp, tmp + nb + 1, nb});
-    k_scan_reduce<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, lv[0].bsum);
+    k_scan_reduce<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, lv[0].bsum); ++S.nlaunch;
     long long off = 2 * nb + 2;
     while (lv.back().nb > 1) {
         Lvl &pl = lv.back();
         long long nb2 = (pl.nb + SCAN_TILE - 1) / SCAN_TILE;
         Lvl l2{pl.nb, tmp + off, tmp + off + nb2 + 1, nb2};
         off += 2 * nb2 + 2;
-        k_scan_reduce<long long><<<(unsigned)nb2, SCAN_THREADS, 0, S.st>>>(pl.bsum, pl.nb, l2.bsum);
+        k_scan_reduce<long long><<<(unsigned)nb2, SCAN_THREADS, 0, S.st>>>(pl.bsum, pl.nb, l2.bsum); ++S.nlaunch;
         lv.push_back(l2);
     }
     // top level: single block sum -> offset 0
     CK(cudaMemsetAsync(lv.back().boff, 0, sizeof(long long), S.st));
     for (int i = (int)lv.size() - 1; i >= 1; i--) {
         // scan level i-1 block sums using level i offsets
-        k_scan_down<long long><<<(unsigned)lv[i].nb, SCAN_THREADS, 0, S.st>>>(lv[i - 1].bsum, lv[i - 1].nb, lv[i - 1].nb, lv[i].boff, lv[i - 1].boff);
+        k_scan_down<long long><<<(unsigned)lv[i].nb, SCAN_THREADS, 0, S.st>>>(lv[i - 1].bsum, lv[i - 1].nb, lv[i - 1].nb, lv[i].boff, lv[i - 1].boff); ++S.nlaunch;
     }
     // final: scan n inputs (+1 trailing zero) into out
     (void)sizes;
-    k_scan_down<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, n_out, lv[0].boff, out);
+    k_scan_down<TIn><<<(unsigned)nb, SCAN_THREADS, 0, S.st>>>(in, n, n_out, lv[0].boff, out); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -457,9 +458,9 @@ static int run_prep(Session &S) {
     k_prep_elements<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(
         S.T64.get<long long>(), S.labT64.get<long long>(), S.V.get<double>(), S.eoffd.get<int>(),
         S.voffd.get<int>(), S.nProb, nE, S.T32.get<int>(), S.labT.get<int>(), S.eprob.get<int>(),
-        S.EC.get<double>(), S.adet.get<double>(), S.EChi.get<float>(), S.EClo.get<float>(), S.adetf.get<float>());
+        S.EC.get<double>(), S.adet.get<double>(), S.EChi.get<float>(), S.EClo.get<float>(), S.adetf.get<float>()); ++S.nlaunch;
     k_prep_vertices<<<grid_for(nV, 256), 256, 0, S.st>>>(S.labV64.get<long long>(), S.voffd.get<int>(),
-        S.nProb, nV, S.labV.get<int>(), S.vprob.get<int>());
+        S.nProb, nV, S.labV.get<int>(), S.vprob.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -472,22 +473,22 @@ static int run_dual(Session &S) {
     ENS(S.vptr, sizeof(long long) * (nV + 1));
     ENS(S.vel, sizeof(int) * nE * dV);
     CK(cudaMemsetAsync(S.vcnt.p, 0, sizeof(int) * (nV + 1), S.st));
-    k_vinc_count<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, S.vcnt.get<int>());
+    k_vinc_count<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, S.vcnt.get<int>()); ++S.nlaunch;
     int r = scan_excl<int>(S, S.vcnt.get<int>(), nV, S.vptr.get<long long>());
     if (r) return r;
     CK(cudaMemsetAsync(S.vcnt.p, 0, sizeof(int) * (nV + 1), S.st));
-    k_vinc_fill<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, dV, S.vptr.get<long long>(), S.vcnt.get<int>(), S.vel.get<int>());
-    k_vinc_sort<<<grid_for(nV, 256), 256, 0, S.st>>>(S.vptr.get<long long>(), nV, S.vel.get<int>());
+    k_vinc_fill<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, dV, S.vptr.get<long long>(), S.vcnt.get<int>(), S.vel.get<int>()); ++S.nlaunch;
+    k_vinc_sort<<<grid_for(nV, 256), 256, 0, S.st>>>(S.vptr.get<long long>(), nV, S.vel.get<int>()); ++S.nlaunch;
     ENS(S.adjcnt, sizeof(int) * (nE + 1));
     ENS(S.xadj, sizeof(long long) * (nE + 1));
-    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), nullptr, S.adjcnt.get<int>(), nullptr, S.err.get<int>() + 8);
+    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), nullptr, S.adjcnt.get<int>(), nullptr, S.err.get<int>() + 8); ++S.nlaunch;
     r = scan_excl<int>(S, S.adjcnt.get<int>(), nE, S.xadj.get<long long>());
     if (r) return r;
     long long nadj = 0;
     r = d2h(S, &nadj, S.xadj.get<long long>() + nE, 1);
     if (r) return r;
     ENS(S.adj, sizeof(int) * (nadj + 1));
-    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), S.xadj.get<long long>(), S.adjcnt.get<int>(), S.adj.get<int>(), S.err.get<int>() + 8);
+    k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), S.xadj.get<long long>(), S.adjcnt.get<int>(), S.adj.get<int>(), S.err.get<int>() + 8); ++S.nlaunch;
     CK(cudaGetLastError());
     int e8 = 0;
     r = d2h(S, &e8, S.err.get<int>() + 8, 1);
@@ -526,6 +527,7 @@ static int run_bfs(Session &S) {
         a.n_amb = cnt + 7;
         if (S.prec == PREC_MIX) k_bfs<DIM, PREC_MIX><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
         else k_bfs<DIM, PREC_F64><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
+        ++S.nlaunch;
         CK(cudaGetLastError());
         unsigned long long hc[3];
         int he[2];
@@ -544,8 +546,8 @@ static int run_bfs(Session &S) {
 static int sort_segments(Session &S, const long long *ptr, long long nseg, int *data) {
     const int cap = 16384;
     CK(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, cap * (int)sizeof(int)));
-    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(ptr, nseg, data, cap);
-    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(ptr, nseg, data, cap);
+    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(ptr, nseg, data, cap); ++S.nlaunch;
+    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(ptr, nseg, data, cap); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -561,16 +563,16 @@ static int run_pairs(Session &S) {
     const long long P = S.P;
     ENS(S.pA, sizeof(int) * (P + 1));
     ENS(S.pB, sizeof(int) * (P + 1));
-    k_compact_pairs<<<grid_for(nE * 32, 256), 256, 0, S.st>>>(S.seg_start.get<long long>(), S.seg_cnt.get<int>(), S.out_ptr.get<long long>(), S.pool.get<int>(), nE, S.pA.get<int>(), S.pB.get<int>());
+    k_compact_pairs<<<grid_for(nE * 32, 256), 256, 0, S.st>>>(S.seg_start.get<long long>(), S.seg_cnt.get<int>(), S.out_ptr.get<long long>(), S.pool.get<int>(), nE, S.pA.get<int>(), S.pB.get<int>()); ++S.nlaunch;
     ENS(S.incnt, sizeof(int) * (nE + 1));
     ENS(S.in_ptr, sizeof(long long) * (nE + 1));
     ENS(S.inA, sizeof(int) * (P + 1));
     CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
-    k_in_count<<<grid_for(P, 256), 256, 0, S.st>>>(S.pB.get<int>(), P, S.incnt.get<int>());
+    k_in_count<<<grid_for(P, 256), 256, 0, S.st>>>(S.pB.get<int>(), P, S.incnt.get<int>()); ++S.nlaunch;
     r = scan_excl<int>(S, S.incnt.get<int>(), nE, S.in_ptr.get<long long>());
     if (r) return r;
     CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
-    k_in_fill<<<grid_for(P, 256), 256, 0, S.st>>>(S.pA.get<int>(), S.pB.get<int>(), P, S.in_ptr.get<long long>(), S.incnt.get<int>(), S.inA.get<int>());
+    k_in_fill<<<grid_for(P, 256), 256, 0, S.st>>>(S.pA.get<int>(), S.pB.get<int>(), P, S.in_ptr.get<long long>(), S.incnt.get<int>(), S.inA.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
     // sorted out- and in-lists: a fixed processing order, hence a fixed summation order
     r = sort_segments(S, S.out_ptr.get<long long>(), nE, S.pB.get<int>());
@@ -592,7 +594,7 @@ static int run_color(Session &S) {
     int *cur = S.color.get<int>(), *nxt = S.color2.get<int>();
     for (int round = 0; round < 1000; round++) {
         CK(cudaMemsetAsync(rem, 0, sizeof(unsigned long long), S.st));
-        k_color_round<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), nE, S.eprob.get<int>(), S.prm.get<ProbParams>(), cur, nxt, rem, S.err.get<int>() + 9);
+        k_color_round<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), nE, S.eprob.get<int>(), S.prm.get<ProbParams>(), cur, nxt, rem, S.err.get<int>() + 9); ++S.nlaunch;
         std::swap(cur, nxt);
         unsigned long long left = 0;
         int r = d2h(S, &left, rem, 1);
@@ -607,7 +609,7 @@ static int run_color(Session &S) {
     ENS(S.keepcnt, sizeof(int) * 520);
     int *cnt = S.keepcnt.get<int>();
     CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 520, S.st));
-    k_color_count<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt);
+    k_color_count<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt); ++S.nlaunch;
     std::vector<int> h(256);
     r = d2h(S, h.data(), cnt, 256);
     if (r) return r;
@@ -617,7 +619,7 @@ static int run_color(Session &S) {
     for (int c = 0; c < nc; c++) S.color_off[c + 1] = S.color_off[c] + h[c];
     CK(cudaMemcpyAsync(cnt + 260, S.color_off.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice, S.st));
     CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 256, S.st));
-    k_color_fill<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt + 260, cnt, S.colorlist.get<int>());
+    k_color_fill<<<grid_for(nE, 256), 256, 0, S.st>>>(S.color.get<int>(), nE, cnt + 260, cnt, S.colorlist.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(S.st));
     return NLFEM_OK;
@@ -638,18 +640,18 @@ static int run_pattern(Session &S) {
     a.probs = S.prm.get<ProbParams>(); a.nV = nV;
     a.marks = S.marks.get<unsigned>(); a.mstride = S.maxNV;
     a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
-    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 0);
+    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 0); ++S.nlaunch;
     int r = scan_excl<int>(S, S.rowcnt.get<int>(), nV, S.rowptr.get<long long>());
     if (r) return r;
     r = d2h(S, &S.nnz_struct, S.rowptr.get<long long>() + nV, 1);
     if (r) return r;
     ENS(S.cols, sizeof(int) * (S.nnz_struct + 1));
     a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
-    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 1);
+    k_row_pattern<DIM><<<S.nSM * 4, 256, 0, S.st>>>(a, 1); ++S.nlaunch;
     const int cap = 16384;
     CK(cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, cap * (int)sizeof(int)));
-    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap);
-    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap);
+    k_row_sort<<<S.nSM * 4, 256, cap * sizeof(int), S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap); ++S.nlaunch;
+    k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
     return NLFEM_OK;
@@ -709,12 +711,12 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
     const int method = close ? P0.close : P0.remote;
     if (method == MTH_FRACTIONAL) {
         if (DIM != 2 || S.duffy_nPg == 0) return fail(NLFEM_ERR_INVALID, "close rule needs a 2D mesh and a tensor Gauss rule");
-        k_iota<<<grid_for(n, 256), 256, 0, S.st>>>(S.closelist.get<int>(), n);
+        k_iota<<<grid_for(n, 256), 256, 0, S.st>>>(S.closelist.get<int>(), n); ++S.nlaunch;
         a.list = S.closelist.get<int>();
         a.nlist = n;
-        k_quad_close<<<grid_for(n * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+        k_quad_close<<<grid_for(n * 32, 128), 128, 0, S.st>>>(a, duffy_view(S)); ++S.nlaunch;
     } else {
-        k_quad_fp64<DIM><<<grid_for(n, 128), 128, 0, S.st>>>(a, S.rule);
+        k_quad_fp64<DIM><<<grid_for(n, 128), 128, 0, S.st>>>(a, S.rule); ++S.nlaunch;
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(S.st));
@@ -759,7 +761,7 @@ static int run_close(Session &S) {
     ENS(S.closeB, sizeof(int) * (nslot + 1));
     ENS(S.closebuf, sizeof(double) * 36 * (nslot + 1));
     ENS(S.closelist, sizeof(int) * (nslot + 1));
-    k_close_pairs<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), S.labT.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), nE, S.closeA.get<int>(), S.closeB.get<int>());
+    k_close_pairs<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), S.labT.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), nE, S.closeA.get<int>(), S.closeB.get<int>()); ++S.nlaunch;
     QuadArgs a;
     memset(&a, 0, sizeof(a));
     a.pA = S.closeA.get<int>(); a.pB = S.closeB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
@@ -767,10 +769,10 @@ static int run_close(Session &S) {
     a.probs = S.prm.get<ProbParams>(); a.P = nslot; a.err = S.err.get<int>();
     a.n_close = S.counters.get<unsigned long long>() + 4;
     a.blocks_out = S.closebuf.get<double>(); a.ret_out = S.closelist.get<int>(); a.force_close = 1;
-    k_iota<<<grid_for(nslot, 256), 256, 0, S.st>>>(S.closelist.get<int>(), nslot);
+    k_iota<<<grid_for(nslot, 256), 256, 0, S.st>>>(S.closelist.get<int>(), nslot); ++S.nlaunch;
     a.list = S.closelist.get<int>();
     a.nlist = nslot;
-    k_quad_close<<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+    k_quad_close<<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S)); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -816,12 +818,13 @@ static int run_passes(Session &S) {
         if (!a.count) continue;
         if (use_mix2d) {
             const unsigned g2 = (unsigned)std::min<long long>((a.count + MIX_WARPS - 1) / MIX_WARPS, (long long)S.nSM * 8);
-            k_pass_mix2d<<<g2, MIX_THREADS, smem2d, S.st>>>(a, S.rule, pr);
+            k_pass_mix2d<<<g2, MIX_THREADS, smem2d, S.st>>>(a, S.rule, pr); ++S.nlaunch;
             continue;
         }
         const unsigned grid = (unsigned)std::min<long long>((a.count + PASS_WARPS - 1) / PASS_WARPS, (long long)S.nSM * 8);
         if (S.prec == PREC_MIX) k_pass<DIM, PREC_MIX><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
         else k_pass<DIM, PREC_F64><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
+        ++S.nlaunch;
     }
     CK(cudaGetLastError());
     return NLFEM_OK;
@@ -832,14 +835,14 @@ static int run_finish(Session &S) {
     ENS(S.keepcnt, sizeof(int) * (nV + 1));
     ENS(S.fptr, sizeof(long long) * (nV + 1));
     const unsigned char *tch = S.prec == PREC_MIX ? S.touched.get<unsigned char>() : nullptr;
-    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), tch, S.keepcnt.get<int>());
+    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), tch, S.keepcnt.get<int>()); ++S.nlaunch;
     int r = scan_excl<int>(S, S.keepcnt.get<int>(), nV, S.fptr.get<long long>());
     if (r) return r;
     r = d2h(S, &S.nnz, S.fptr.get<long long>() + nV, 1);
     if (r) return r;
     ENS(S.fcols, sizeof(int) * (S.nnz + 1));
     ENS(S.fvals, sizeof(double) * (S.nnz + 1));
-    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), S.vals.get<double>(), tch, S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
+    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), S.vals.get<double>(), tch, S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>()); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -856,6 +859,7 @@ static int check_errors(Session &S) {
 template <int DIM>
 static int run_system_t(Session &S) {
     int r;
+    S.nlaunch = 0;
     CK(cudaEventRecord(S.ev[0], S.st));
     if ((r = run_prep<DIM>(S))) return r;
     if ((r = run_dual<DIM>(S))) return r;
@@ -883,6 +887,7 @@ static int run_system_t(Session &S) {
     S.stats.ms_quad = t[2];
     S.stats.ms_finish = t[3];
     S.stats.ms_total = t[0] + t[1] + t[2] + t[3];
+    S.stats.n_launches = (long)S.nlaunch;
     g_stats = S.stats;
     return NLFEM_OK;
 }
@@ -899,8 +904,8 @@ static int run_forcing_t(Session &S) {
     ENS(S.fd, sizeof(double) * (nV + 1));
     CK(cudaMemsetAsync(S.facc.p, 0, sizeof(unsigned long long) * 2 * (nV + 1), S.st));
     CK(cudaMemsetAsync(S.ftiny.p, 0, sizeof(unsigned) * (nV + 1), S.st));
-    k_forcing<DIM><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>());
-    k_forcing_finish<<<grid_for(nV, 256), 256, 0, S.st>>>(S.facc.get<unsigned long long>(), nV, S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fd.get<double>());
+    k_forcing<DIM><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>()); ++S.nlaunch;
+    k_forcing_finish<<<grid_for(nV, 256), 256, 0, S.st>>>(S.facc.get<unsigned long long>(), nV, S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fd.get<double>()); ++S.nlaunch;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(S.st));
     return NLFEM_OK;
@@ -926,7 +931,7 @@ static int download(Session &S, int i, nlfem_csr *out) {
     const long long nnz = b[1] - b[0];
     ENS(S.out64a, sizeof(long long) * (nrows + 1));
     ENS(S.out64b, sizeof(long long) * (nnz + 1));
-    k_export<<<grid_for(std::max(nrows + 1, nnz), 256), 256, 0, S.st>>>(S.fptr.get<long long>(), S.fcols.get<int>(), r0, nrows, r0, S.out64a.get<long long>(), S.out64b.get<long long>());
+    k_export<<<grid_for(std::max(nrows + 1, nnz), 256), 256, 0, S.st>>>(S.fptr.get<long long>(), S.fcols.get<int>(), r0, nrows, r0, S.out64a.get<long long>(), S.out64b.get<long long>()); ++S.nlaunch;
     CK(cudaGetLastError());
     out->K = (long)nrows;
     out->nnz = (long)nnz;

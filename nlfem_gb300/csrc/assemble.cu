@@ -570,29 +570,48 @@ __global__ void k_row_sort_global(const long long *__restrict__ rowptr, long lon
 // Per row: number of entries whose FP64 sum is not exactly zero (arma::sp_mat drops the zeros).
 // With touched (mixed precision) a slot that received a contribution is kept even when its
 // FP32-derived sum cancelled to exactly zero: its exact value is a nonzero below FP32 resolution.
+enum { VAL_F64 = 0, VAL_DF = 1, VAL_FX = 2 };
+struct FinishArgs {
+    int vmode;                       // how the slots hold their sums
+    const unsigned char *touched;    // VAL_DF: slots that received a contribution
+    const int *vprob;                // VAL_FX: problem of each row (fixed-point unit)
+    const ProbParams *probs;
+};
+// Value of slot i of row u; keep says whether the slot survives (the reference drops exact
+// zeros; slots of the mixed passes are kept when they received any contribution).
+__device__ __forceinline__ double slot_value(const FinishArgs &f, const double *vals, long long u, long long i,
+                                             bool &keep) {
+    double v;
+    if (f.vmode == VAL_FX) {
+        v = (double)reinterpret_cast<const long long *>(vals)[i] * f.probs[f.vprob[u]].fx_unit;
+        keep = true;
+    } else if (f.vmode == VAL_DF) {
+        v = df_to_double(reinterpret_cast<const DF *>(vals)[i]);
+        keep = (v != 0.0) || f.touched[i];
+    } else {
+        v = vals[i];
+        keep = v != 0.0;
+    }
+    return v;
+}
 __global__ void k_finish_count(const long long *__restrict__ rowptr, long long nV,
-                               const double *__restrict__ vals, const unsigned char *__restrict__ touched,
-                               int *__restrict__ keepcnt) {
+                               const double *__restrict__ vals, FinishArgs f, int *__restrict__ keepcnt) {
     const int lane = threadIdx.x & 31;
     long long u = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (u >= nV) return;
     const long long b = rowptr[u], e = rowptr[u + 1];
     int cnt = 0;
     for (long long i = b + lane; i < e; i += 32) {
-        double v = vals[i];
-        if (touched) {   // mixed precision: the slot holds a double-float pair
-            const DF d = reinterpret_cast<const DF *>(vals)[i];
-            v = df_to_double(d);
-        }
-        cnt += (v != 0.0) || (touched && touched[i]);
+        bool k;
+        slot_value(f, vals, u, i, k);
+        cnt += k;
     }
     cnt = warp_sum(cnt);
     if (lane == 0) keepcnt[u] = cnt;
 }
 __global__ void k_finish_compact(const long long *__restrict__ rowptr, long long nV,
                                  const int *__restrict__ cols, const double *__restrict__ vals,
-                                 const unsigned char *__restrict__ touched,
-                                 const long long *__restrict__ fptr, int *__restrict__ fcols,
+                                 FinishArgs f, const long long *__restrict__ fptr, int *__restrict__ fcols,
                                  double *__restrict__ fvals) {
     const int lane = threadIdx.x & 31;
     long long u = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -603,10 +622,7 @@ __global__ void k_finish_compact(const long long *__restrict__ rowptr, long long
         long long i = i0 + lane;
         bool k = false;
         double v = 0.0;
-        if (i < e) {
-            v = touched ? df_to_double(reinterpret_cast<const DF *>(vals)[i]) : vals[i];
-            k = (v != 0.0) || (touched && touched[i]);
-        }
+        if (i < e) v = slot_value(f, vals, u, i, k);
         unsigned m = __ballot_sync(FULL, k);
         if (k) {
             long long o = w + __popc(m & lanemask_lt());

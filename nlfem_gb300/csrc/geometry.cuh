@@ -199,6 +199,9 @@ struct ProbParams {
     int kernel, remote, close, caps;
     int full_search, singular, load, scale_exp;
     int elem_off, nE, vert_off, nV;
+    double fx_unit;   // value of one unit of the 64-bit fixed-point CSR sums: 2^fx_ue
+    float fx_mul;     // 2^-fx_ue
+    int fx_ue;        // scale_exp + guard bits - 62
 };
 
 // FP64 kernel value k(x, y) (model.cpp:25-28, 52-60, 62-65, 126-138)

@@ -130,6 +130,17 @@ static int make_rule(const nlfem_problem &p, bool inner, Rule &r) {
 }
 
 // Per-problem parameters, checks (checks.cpp:87-113) and the fixed-point scale.
+// Unit of the 64-bit fixed-point CSR sums of the one-sided pass: entries up to 2^(scale_exp +
+// FX_GUARD) fit; widen moves the unit up when a pass reported an out-of-range contribution.
+static int set_fx_unit(ProbParams &P, int widen) {
+    P.fx_ue = P.scale_exp + FX_GUARD - 62 + widen;
+    if (P.fx_ue <= -120 || P.fx_ue >= 120)
+        return fail(NLFEM_ERR_UNSUPPORTED, "matrix entries outside the range of the fixed-point accumulation");
+    P.fx_unit = std::ldexp(1.0, P.fx_ue);
+    P.fx_mul = std::ldexp(1.0f, -P.fx_ue);
+    return NLFEM_OK;
+}
+
 static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     memset(&P, 0, sizeof(P));
     if (p.dim != 2 && p.dim != 3) return fail(NLFEM_ERR_INVALID, "Dimension is not equal to 2 or 3.");
@@ -201,7 +212,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     }
     if (!(mag > 0) || !std::isfinite(mag)) mag = 1.0;
     P.scale_exp = (int)std::ceil(std::log2(mag));
-    return NLFEM_OK;
+    return set_fx_unit(P, 0);
 }
 
 // Duffy tables (MeshTypes.cpp:32-209, 252-327): scaled points, xi factored out of the transform
@@ -260,6 +271,8 @@ struct Session {
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
     DevBuf out64a, out64b;
+    DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided pass
+    bool one_sided = false;                 // 2D, mixed precision, retriangulate remote rule
     long long qcap = 0, pool_cap = 0;
     long long P = 0, nnz_struct = 0, nnz = 0;
     long long nlaunch = 0;   // kernels launched by the current assembly
@@ -270,7 +283,8 @@ struct Session {
                          &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                          &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                          &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
-                         &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched};
+                         &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
+                         &hcap, &hptr, &htab, &tpos, &dslot};
         for (DevBuf *b : all) b->release();
         if (st) {
             for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
@@ -372,6 +386,11 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
         if (rr) return rr;
         if (memcmp(&r2, &S.rule, sizeof(Rule)) != 0)
             return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the quadrature rules");
+    }
+    {
+        bool all_retri = system;
+        for (const ProbParams &q : S.hprm) all_retri &= (q.remote == MTH_RETRIANGULATE);
+        S.one_sided = S.dim == 2 && S.prec == PREC_MIX && all_retri;
     }
     const int dV = S.dV, dim = S.dim;
     ENS(S.T64, sizeof(long long) * S.nE * dV);
@@ -625,6 +644,41 @@ static int run_color(Session &S) {
     return NLFEM_OK;
 }
 
+static SlotMap slot_map(Session &S) {
+    SlotMap m;
+    m.rowptr = S.rowptr.get<long long>();
+    m.hptr = S.hptr.get<long long>();
+    m.htab = S.htab.get<unsigned long long>();
+    m.tpos = S.tpos.get<int>();
+    m.dslot = S.dslot.get<long long>();
+    return m;
+}
+
+// Row hash tables, transposed positions and diagonal-block slots (slots.cuh) of the pattern.
+template <int DIM>
+static int run_slot_maps(Session &S) {
+    constexpr int dV = DIM + 1;
+    const long long nV = S.nV, nE = S.nE, nnz = S.nnz_struct;
+    ENS(S.hcap, sizeof(long long) * (nV + 1));
+    ENS(S.hptr, sizeof(long long) * (nV + 1));
+    k_hash_cap<<<grid_for(nV, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.hcap.get<long long>()); ++S.nlaunch;
+    int r = scan_excl<long long>(S, S.hcap.get<long long>(), nV, S.hptr.get<long long>());
+    if (r) return r;
+    long long htot = 0;
+    r = d2h(S, &htot, S.hptr.get<long long>() + nV, 1);
+    if (r) return r;
+    ENS(S.htab, sizeof(unsigned long long) * (htot + 1));
+    CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (htot + 1), S.st));
+    k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
+    ENS(S.tpos, sizeof(int) * (nnz + 1));
+    ENS(S.dslot, sizeof(long long) * (nE * dV * dV + 1));
+    const SlotMap m = slot_map(S);
+    k_tpos<<<S.nSM * 8, 256, 0, S.st>>>(m, S.cols.get<int>(), S.labV.get<int>(), nV, S.tpos.get<int>(), S.err.get<int>()); ++S.nlaunch;
+    k_dslot<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(m, S.T32.get<int>(), S.labV.get<int>(), nE, S.dslot.get<long long>()); ++S.nlaunch;
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
 template <int DIM>
 static int run_pattern(Session &S) {
     const long long nV = S.nV;
@@ -654,6 +708,7 @@ static int run_pattern(Session &S) {
     k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
+    if (S.one_sided) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
 
@@ -777,13 +832,49 @@ static int run_close(Session &S) {
     return NLFEM_OK;
 }
 
+// One-sided mixed 2D pass (passes_mix.cuh): one persistent launch over all elements. A
+// contribution outside the fixed-point range sets err[5]; the pass is then redone with a unit
+// 2^16 times coarser.
+static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr) {
+    const long long nnz = S.nnz_struct;
+    const size_t smem = mix_warp_bytes(S.rule.nPx) * MIX_WARPS;
+    CK(cudaFuncSetAttribute(k_pass_mix2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_mix2d, MIX_THREADS, smem));
+    if (per_sm < 1) return fail(NLFEM_ERR_UNSUPPORTED, "quadrature rule too large for the pass's shared memory");
+    MixArgs ma;
+    ma.p = pa;
+    ma.p.list = nullptr;
+    ma.p.count = (int)S.nE;
+    ma.m = slot_map(S);
+    ma.work = reinterpret_cast<int *>(S.counters.get<unsigned long long>() + 10);
+    for (int attempt = 0; attempt < 4; attempt++) {
+        CK(cudaMemsetAsync(S.vals.p, 0, sizeof(long long) * (nnz + 1), S.st));
+        CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
+        CK(cudaMemsetAsync(S.err.get<int>() + 5, 0, sizeof(int), S.st));
+        CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 5, 0, 2 * sizeof(unsigned long long), S.st));
+        k_pass_mix2d<<<(unsigned)(S.nSM * per_sm), MIX_THREADS, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
+        CK(cudaGetLastError());
+        int ovf = 0;
+        int r = d2h(S, &ovf, S.err.get<int>() + 5, 1);
+        if (r) return r;
+        if (!ovf) return NLFEM_OK;
+        for (ProbParams &q : S.hprm) {
+            r = set_fx_unit(q, q.fx_ue - (q.scale_exp + FX_GUARD - 62) + 16);
+            if (r) return r;
+        }
+        CK(cudaMemcpyAsync(S.prm.p, S.hprm.data(), sizeof(ProbParams) * S.hprm.size(), cudaMemcpyHostToDevice, S.st));
+    }
+    return fail(NLFEM_ERR_NUMERIC, "contribution outside the fixed-point range (non-finite value?)");
+}
+
 template <int DIM>
 static int run_passes(Session &S) {
     constexpr int dV = DIM + 1;
     const long long nnz = S.nnz_struct;
     ENS(S.vals, sizeof(double) * (nnz + 1));
     CK(cudaMemsetAsync(S.vals.p, 0, sizeof(double) * (nnz + 1), S.st));
-    if (S.prec == PREC_MIX) {
+    if (S.prec == PREC_MIX && !S.one_sided) {
         ENS(S.touched, (size_t)nnz + 16);
         CK(cudaMemsetAsync(S.touched.p, 0, (size_t)nnz + 16, S.st));
     }
@@ -801,13 +892,9 @@ static int run_passes(Session &S) {
     a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
     a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6;
-    a.touched = S.prec == PREC_MIX ? S.touched.get<unsigned char>() : nullptr;
+    a.touched = S.prec == PREC_MIX && !S.one_sided ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);
-    bool all_retri = true;
-    for (const ProbParams &q : S.hprm) all_retri &= (q.remote == MTH_RETRIANGULATE);
-    const bool use_mix2d = DIM == 2 && S.prec == PREC_MIX && all_retri;
-    const size_t smem2d = mix_warp_bytes(S.rule.nPx) * MIX_WARPS;
-    if (use_mix2d) CK(cudaFuncSetAttribute(k_pass_mix2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2d));
+    if (S.one_sided) return run_pass_one_sided(S, a, pr);
     const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
     if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else CK(cudaFuncSetAttribute(k_pass<DIM, PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -816,11 +903,6 @@ static int run_passes(Session &S) {
         a.list = S.colorlist.get<int>() + S.color_off[c];
         a.count = S.color_off[c + 1] - S.color_off[c];
         if (!a.count) continue;
-        if (use_mix2d) {
-            const unsigned g2 = (unsigned)std::min<long long>((a.count + MIX_WARPS - 1) / MIX_WARPS, (long long)S.nSM * 8);
-            k_pass_mix2d<<<g2, MIX_THREADS, smem2d, S.st>>>(a, S.rule, pr); ++S.nlaunch;
-            continue;
-        }
         const unsigned grid = (unsigned)std::min<long long>((a.count + PASS_WARPS - 1) / PASS_WARPS, (long long)S.nSM * 8);
         if (S.prec == PREC_MIX) k_pass<DIM, PREC_MIX><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
         else k_pass<DIM, PREC_F64><<<grid, PASS_THREADS, smem, S.st>>>(a, S.rule, pr);
@@ -834,15 +916,19 @@ static int run_finish(Session &S) {
     const long long nV = S.nV;
     ENS(S.keepcnt, sizeof(int) * (nV + 1));
     ENS(S.fptr, sizeof(long long) * (nV + 1));
-    const unsigned char *tch = S.prec == PREC_MIX ? S.touched.get<unsigned char>() : nullptr;
-    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), tch, S.keepcnt.get<int>()); ++S.nlaunch;
+    // values: FP64 sums, double-float sums with touched flags (two-sided mixed passes), or
+    // fixed-point sums of the one-sided pass (every structural slot received a contribution)
+    const int vmode = S.one_sided ? VAL_FX : (S.prec == PREC_MIX ? VAL_DF : VAL_F64);
+    const unsigned char *tch = vmode == VAL_DF ? S.touched.get<unsigned char>() : nullptr;
+    const FinishArgs fa{vmode, tch, S.vprob.get<int>(), S.prm.get<ProbParams>()};
+    k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), fa, S.keepcnt.get<int>()); ++S.nlaunch;
     int r = scan_excl<int>(S, S.keepcnt.get<int>(), nV, S.fptr.get<long long>());
     if (r) return r;
     r = d2h(S, &S.nnz, S.fptr.get<long long>() + nV, 1);
     if (r) return r;
     ENS(S.fcols, sizeof(int) * (S.nnz + 1));
     ENS(S.fvals, sizeof(double) * (S.nnz + 1));
-    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), S.vals.get<double>(), tch, S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>()); ++S.nlaunch;
+    k_finish_compact<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), S.vals.get<double>(), fa, S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>()); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }
@@ -865,7 +951,7 @@ static int run_system_t(Session &S) {
     if ((r = run_dual<DIM>(S))) return r;
     if ((r = run_bfs<DIM>(S))) return r;
     if ((r = run_pairs<DIM>(S))) return r;
-    if ((r = run_color(S))) return r;
+    if (!S.one_sided && (r = run_color(S))) return r;   // the one-sided pass needs no colors
     CK(cudaEventRecord(S.ev[1], S.st));
     if ((r = run_pattern<DIM>(S))) return r;
     CK(cudaEventRecord(S.ev[2], S.st));

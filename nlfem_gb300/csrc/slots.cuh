@@ -1,0 +1,147 @@
+// CSR slot lookup and fixed-point accumulation for the one-sided pass.
+//
+// The pass adds every element pair's blocks into the rows of both elements (the reference adds
+// termNonloc / termLocal into the outer element's rows and termNonlocPrime / termLocalPrime into
+// the inner element's rows, Cassemble.cpp:737-766), from many warps at once. To keep the result
+// independent of the order those additions land in, each contribution is first rounded to a
+// 64-bit fixed-point integer (unit 2^fx_ue of its problem) and added with an integer atomic:
+// integer addition is associative, so the sums are identical run to run.
+//
+// Slots are found without binary search: every CSR row gets an open-addressing hash table
+// (capacity a power of two >= 2 x row length, linear probing) mapping a column to its position in
+// the sorted row; tpos[s] gives, for the slot s = (i, j), the position of column i in row j (the
+// pattern is symmetric on kept rows), and dslot lists the slots of each element's diagonal block.
+#pragma once
+#include "passes.cuh"
+
+namespace nlg {
+
+constexpr unsigned long long HEMPTY = ~0ULL;
+constexpr int FX_GUARD = 10;   // bits of headroom above the problem's entry magnitude
+
+struct SlotMap {
+    const long long *rowptr;          // CSR row starts (rows of vertices with label <= 0 are empty)
+    const long long *hptr;            // per row: start of its hash table; capacity = hptr[u+1]-hptr[u]
+    const unsigned long long *htab;   // entries (position << 32) | column, HEMPTY when free
+    const int *tpos;                  // per slot (i, j): position of column i in row j, -1 if row j is empty
+    const long long *dslot;           // per element: (dim+1)^2 slots of its diagonal block, -1 if the row is empty
+};
+
+// Slot of (u, col), or -1 when the row has no such column. At most capacity probes.
+__device__ __forceinline__ long long slot_find(const SlotMap &m, int u, int col) {
+    const long long hb = m.hptr[u];
+    const unsigned cap = (unsigned)(m.hptr[u + 1] - hb);
+    if (cap == 0) return -1;
+    const unsigned mask = cap - 1;
+    unsigned h = hash32((unsigned)col) & mask;
+    for (unsigned probe = 0; probe < cap; probe++) {
+        const unsigned long long e = m.htab[hb + h];
+        if (e == HEMPTY) return -1;
+        if ((unsigned)(e & 0xffffffffULL) == (unsigned)col) return m.rowptr[u] + (long long)(e >> 32);
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// Fixed-point value of a contribution: round(v * 2^-fx_ue); out of range (or not finite) sets
+// the overflow flag, which makes the host redo the pass with a coarser unit.
+__device__ __forceinline__ long long fx64(float v, float mul, int *ovf) {
+    const float t = v * mul;
+    if (!(fabsf(t) < 4.0e18f)) {
+        atomicOr(ovf, 1);
+        return 0;
+    }
+    return __float2ll_rn(t);
+}
+__device__ __forceinline__ long long fx64d(double v, double mul, int *ovf) {
+    const double t = v * mul;
+    if (!(fabs(t) < 4.0e18)) {
+        atomicOr(ovf, 1);
+        return 0;
+    }
+    return __double2ll_rn(t);
+}
+__device__ __forceinline__ void red_add(long long *vals, long long s, long long v) {
+    if (v) atomicAdd(reinterpret_cast<unsigned long long *>(vals) + s, (unsigned long long)v);
+}
+
+// ------------------------------------------------------------------ construction
+// Capacity of each row's table: the smallest power of two >= 2 x row length (0 for empty rows).
+__global__ void k_hash_cap(const long long *__restrict__ rowptr, long long nV, long long *__restrict__ cap) {
+    const long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nV) return;
+    const long long n = rowptr[u + 1] - rowptr[u];
+    long long c = 0;
+    if (n > 0) {
+        c = 2;
+        while (c < 2 * n) c <<= 1;
+    }
+    cap[u] = c;
+}
+
+// One warp per row: insert (position, column) of every slot. A free entry always exists within
+// capacity probes (load factor <= 1/2).
+__global__ void k_hash_fill(const long long *__restrict__ rowptr, const int *__restrict__ cols, long long nV,
+                            const long long *__restrict__ hptr, unsigned long long *__restrict__ htab) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long u = gw; u < nV; u += nw) {
+        const long long b = rowptr[u];
+        const int n = (int)(rowptr[u + 1] - b);
+        const long long hb = hptr[u];
+        const unsigned cap = (unsigned)(hptr[u + 1] - hb);
+        if (n == 0 || cap == 0) continue;
+        const unsigned mask = cap - 1;
+        for (int i = lane; i < n; i += 32) {
+            const int col = cols[b + i];
+            const unsigned long long e = ((unsigned long long)(unsigned)i << 32) | (unsigned)col;
+            unsigned h = hash32((unsigned)col) & mask;
+            for (unsigned probe = 0; probe < cap; probe++) {
+                if (atomicCAS(&htab[hb + h], HEMPTY, e) == HEMPTY) break;
+                h = (h + 1) & mask;
+            }
+        }
+    }
+}
+
+// One warp per row i: tpos of each slot (i, j).
+__global__ void k_tpos(SlotMap m, const int *__restrict__ cols, const int *__restrict__ labV, long long nV,
+                       int *__restrict__ tpos, int *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = gw; i < nV; i += nw) {
+        const long long b = m.rowptr[i], e = m.rowptr[i + 1];
+        for (long long s = b + lane; s < e; s += 32) {
+            const int j = cols[s];
+            int p = -1;
+            if (labV[j] > 0) {
+                const long long t = slot_find(m, j, (int)i);
+                if (t < 0) atomicOr(&err[3], 1);
+                else p = (int)(t - m.rowptr[j]);
+            }
+            tpos[s] = p;
+        }
+    }
+}
+
+// Diagonal-block slots of every element (-1 where the row is empty or, for an element without
+// any pair, where the pattern has no such slot).
+template <int DIM>
+__global__ void k_dslot(SlotMap m, const int *__restrict__ T32, const int *__restrict__ labV, long long nE,
+                        long long *__restrict__ dslot) {
+    constexpr int dV = DIM + 1;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+#pragma unroll
+    for (int r = 0; r < dV; r++) {
+        const int u = T32[e * dV + r];
+        const bool keep = labV[u] > 0;
+#pragma unroll
+        for (int c = 0; c < dV; c++)
+            dslot[e * dV * dV + r * dV + c] = keep ? slot_find(m, u, T32[e * dV + c]) : -1;
+    }
+}
+
+}  // namespace nlg

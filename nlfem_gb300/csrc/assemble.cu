@@ -335,6 +335,10 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                     const int ej = __shfl_sync(FULL, excl, lo);
                     int cand = -1;
                     if (c < total) cand = a.adj[bj + (c - ej)];
+                    // lanes holding the same candidate: the lowest one tests it, so the queue
+                    // order (and every order derived from it) does not depend on atomic timing
+                    const unsigned same = __match_any_sync(FULL, cand);
+                    if ((__ffs(same) - 1) != lane) cand = -1;
                     bool push = false, pair = false, bridge = false;
                     if (cand >= 0) {
                         unsigned old = atomicExch(&visited[cand - eoff], stamp);

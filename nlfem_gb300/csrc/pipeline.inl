@@ -593,11 +593,15 @@ static int run_pairs(Session &S) {
     CK(cudaMemsetAsync(S.incnt.p, 0, sizeof(int) * (nE + 1), S.st));
     k_in_fill<<<grid_for(P, 256), 256, 0, S.st>>>(S.pA.get<int>(), S.pB.get<int>(), P, S.in_ptr.get<long long>(), S.incnt.get<int>(), S.inA.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
-    // sorted out- and in-lists: a fixed processing order, hence a fixed summation order
-    r = sort_segments(S, S.out_ptr.get<long long>(), nE, S.pB.get<int>());
-    if (r) return r;
-    r = sort_segments(S, S.in_ptr.get<long long>(), nE, S.inA.get<int>());
-    if (r) return r;
+    // The out-lists come from the BFS in its (deterministic) discovery order. The colored
+    // two-sided passes sum the in-lists, which k_in_fill fills in atomic order, so those are
+    // sorted; the one-sided pass reads no in-list and the pattern sorts its rows itself.
+    if (!S.one_sided) {
+        r = sort_segments(S, S.out_ptr.get<long long>(), nE, S.pB.get<int>());
+        if (r) return r;
+        r = sort_segments(S, S.in_ptr.get<long long>(), nE, S.inA.get<int>());
+        if (r) return r;
+    }
     S.stats.n_pairs = (long)P;
     return NLFEM_OK;
 }

@@ -263,16 +263,47 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
     return false;
 }
 
+// Appends val for every lane with push, in lane order.
+__device__ __forceinline__ void queue_push(bool push, int val, int *queue, long long qcap, long long &qtail,
+                                           bool &overflow) {
+    const unsigned m = __ballot_sync(FULL, push);
+    if (push) {
+        const long long pos = qtail + __popc(m & lanemask_lt());
+        if (pos < qcap) queue[pos] = val;
+        else overflow = true;
+    }
+    qtail += __popc(m);
+}
+
+// Interaction test of candidate b against the outer element's points (doesInteract of the
+// integrate routines, integration.cpp:539,1017).
+template <int DIM, int PREC>
+__device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, int method, const double *xs,
+                                         const float *xsf, int nPx, const float *ohi, const float *olo, int b,
+                                         unsigned &namb) {
+    constexpr int dV = DIM + 1;
+    const double *Eb = &a.EC[(long long)b * DIM * dV];
+    if (PREC == PREC_F64) return interacts_exact<DIM>(P, method, xs, nPx, Eb);
+    float pb[DIM * dV];
+#pragma unroll
+    for (int j = 0; j < DIM * dV; j++)
+        pb[j] = (a.EChi[(long long)b * DIM * dV + j] - ohi[j % DIM]) + (a.EClo[(long long)b * DIM * dV + j] - olo[j % DIM]);
+    return interacts_filtered<DIM>(P, method, xs, xsf, nPx, Eb, pb, namb);
+}
+
 template <int DIM, int PREC>
 __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
     constexpr int dV = DIM + 1;
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
     __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];
+    __shared__ int s_buf[BFS_WARPS][64];   // candidates waiting for the interaction test
     unsigned namb = 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const long long gw = (long long)blockIdx.x * BFS_WARPS + wib;
-    const long long nw = (long long)gridDim.x * BFS_WARPS;
+    const int wpb = blockDim.x >> 5;   // at most BFS_WARPS
+    const long long gw = (long long)blockIdx.x * wpb + wib;
+    const long long nw = (long long)gridDim.x * wpb;
     unsigned *visited = a.visited + gw * a.vstride;
+    int *buf = s_buf[wib];
     int *queue = a.queue + gw * a.qcap;
     double *xs = s_x[wib];
     unsigned long long cand_local = 0;
@@ -304,6 +335,7 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
             queue[0] = (int)aT;
         }
         self_pair = __shfl_sync(FULL, self_pair, 0);
+        __syncwarp();   // aT's visited mark before any lane tests a candidate
         cand_local += (lane == 0);
         long long qhead = 0, qtail = 1;
         int level = 0;
@@ -311,6 +343,7 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
         while (qhead < qtail) {
             const long long lvl_end = qtail;
             const int method = (P.singular && level == 0) ? P.close : P.remote;
+            int nbuf = 0;
             for (long long g = qhead; g < lvl_end; g += 32) {
                 long long gi = g + lane;
                 int s = gi < lvl_end ? queue[gi] : -1;
@@ -335,42 +368,44 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                     const int ej = __shfl_sync(FULL, excl, lo);
                     int cand = -1;
                     if (c < total) cand = a.adj[bj + (c - ej)];
-                    // lanes holding the same candidate: the lowest one tests it, so the queue
+                    // lanes holding the same candidate: the lowest one takes it, so the queue
                     // order (and every order derived from it) does not depend on atomic timing
                     const unsigned same = __match_any_sync(FULL, cand);
                     if ((__ffs(same) - 1) != lane) cand = -1;
-                    bool push = false, pair = false, bridge = false;
-                    if (cand >= 0) {
-                        unsigned old = atomicExch(&visited[cand - eoff], stamp);
-                        if (old != stamp) {
-                            if (a.labT[cand] != 0) {
-                                cand_local++;
-                                const double *Eb = &a.EC[(long long)cand * DIM * dV];
-                                if (PREC == PREC_F64) {
-                                    pair = interacts_exact<DIM>(P, method, xs, rule.nPx, Eb);
-                                } else {
-                                    float pb[DIM * dV];
-#pragma unroll
-                                    for (int j = 0; j < DIM * dV; j++)
-                                        pb[j] = (a.EChi[(long long)cand * DIM * dV + j] - ohi[j % DIM]) + (a.EClo[(long long)cand * DIM * dV + j] - olo[j % DIM]);
-                                    pair = interacts_filtered<DIM>(P, method, xs, xsf, rule.nPx, Eb, pb, namb);
-                                }
-                                push = pair;
-                            } else {
-                                push = true;
-                                bridge = true;
-                            }
-                        }
+                    bool fresh = false;
+                    if (cand >= 0) fresh = atomicExch(&visited[cand - eoff], stamp) != stamp;
+                    const bool bridge = fresh && a.labT[cand] == 0;
+                    queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
+                    // candidates to test are compacted, so the test runs on full warps
+                    const bool totest = fresh && !bridge;
+                    const unsigned m = __ballot_sync(FULL, totest);
+                    if (totest) buf[nbuf + __popc(m & lanemask_lt())] = cand;
+                    nbuf += __popc(m);
+                    __syncwarp();
+                    if (nbuf >= 32) {
+                        const int b = buf[lane];
+                        const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
+                        cand_local++;
+                        queue_push(pair, b, queue, a.qcap, qtail, overflow);
+                        const int rest = nbuf - 32;
+                        const int v = lane < rest ? buf[32 + lane] : 0;
+                        __syncwarp();
+                        if (lane < rest) buf[lane] = v;
+                        nbuf = rest;
+                        __syncwarp();
                     }
-                    const unsigned m = __ballot_sync(FULL, push);
-                    const long long pos = qtail + __popc(m & lanemask_lt());
-                    if (push) {
-                        if (pos < a.qcap) queue[pos] = bridge ? -(cand + 2) : cand;
-                        else overflow = true;
-                    }
-                    qtail += __popc(m);
                 }
                 if (__any_sync(FULL, overflow)) break;
+            }
+            if (nbuf > 0 && !__any_sync(FULL, overflow)) {
+                const int b = lane < nbuf ? buf[lane] : -1;
+                bool pair = false;
+                if (b >= 0) {
+                    pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
+                    cand_local++;
+                }
+                queue_push(pair, b, queue, a.qcap, qtail, overflow);
+                __syncwarp();
             }
             if (__any_sync(FULL, overflow)) break;
             qhead = lvl_end;
@@ -517,6 +552,73 @@ __global__ void __launch_bounds__(256) k_row_pattern(RowArgs a, int pass) {
             }
         }
         if (!a.cols && lane == 0) a.rowcnt[u] = (int)w;
+    }
+}
+
+// Same row sets with the marks as a bitmap over the problem's vertices in shared memory (words
+// 32-bit words per warp): a shared-memory atomicOr replaces the global exchange, and the set
+// bits come out in increasing order, so the rows need no sort. pass 0 counts, pass 1 writes.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int words) {
+    extern __shared__ unsigned s_bm[];
+    constexpr int dV = DIM + 1;
+    const int lane = threadIdx.x & 31;
+    unsigned *bm = s_bm + (size_t)(threadIdx.x >> 5) * words;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long u = gw; u < a.nV; u += nw) {
+        if (a.labV[u] <= 0) {
+            if (pass == 0 && lane == 0) a.rowcnt[u] = 0;
+            continue;
+        }
+        const ProbParams &P = a.probs[a.vprob[u]];
+        const int voff = P.vert_off;
+        const int wu = (P.nV + 31) >> 5;
+        for (int i = lane; i < wu; i += 32) bm[i] = 0u;
+        __syncwarp();
+        int lo = 0x7fffffff, hi = -1;
+        for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
+            const int T = a.vel[t];
+            const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
+            const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
+            if (oe == ob && ie == ib) continue;
+            const long long nItems = (1 + (oe - ob) + (ie - ib)) * dV;
+            for (long long i = lane; i < nItems; i += 32) {
+                const long long el_i = i / dV;
+                const int k = (int)(i - el_i * dV);
+                int el;
+                if (el_i == 0) el = T;
+                else if (el_i <= oe - ob) el = a.pB[ob + el_i - 1];
+                else el = a.inA[ib + (el_i - 1 - (oe - ob))];
+                const int v = a.T32[(long long)el * dV + k] - voff;
+                atomicOr(&bm[v >> 5], 1u << (v & 31));
+                lo = min(lo, v);
+                hi = max(hi, v);
+            }
+        }
+        __syncwarp();
+        lo = __reduce_min_sync(FULL, lo);
+        hi = __reduce_max_sync(FULL, hi);
+        long long w = pass ? a.rowptr[u] : 0;
+        if (hi >= 0) {
+            for (int w0 = lo >> 5; w0 <= (hi >> 5); w0 += 32) {
+                const int wi = w0 + lane;
+                unsigned bits = wi <= (hi >> 5) ? bm[wi] : 0u;
+                const int c = __popc(bits);
+                const int incl = warp_incl_scan(c, lane);
+                if (pass) {
+                    long long o = w + incl - c;
+                    while (bits) {
+                        const int b = __ffs(bits) - 1;
+                        a.cols[o++] = voff + wi * 32 + b;
+                        bits &= bits - 1;
+                    }
+                }
+                w += __shfl_sync(FULL, incl, 31);
+            }
+        }
+        if (pass == 0 && lane == 0) a.rowcnt[u] = (int)w;
+        __syncwarp();
     }
 }
 

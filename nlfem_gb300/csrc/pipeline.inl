@@ -519,7 +519,14 @@ static int run_dual(Session &S) {
 template <int DIM>
 static int run_bfs(Session &S) {
     const long long nE = S.nE;
-    const int nwarps = S.nSM * 2 * BFS_WARPS;
+    // visited set: per-warp stamp arrays in global memory. (A shared-memory bitmap over the
+    // problem's elements was measured slower: neighbouring candidates share a word, so the
+    // shared-memory atomics serialise, and the bitmaps cap the occupancy.)
+    auto kfn = S.prec == PREC_MIX ? k_bfs<DIM, PREC_MIX> : k_bfs<DIM, PREC_F64>;
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BFS_THREADS, 0));
+    const int nblocks = S.nSM * std::max(per_sm, 1);
+    const int nwarps = nblocks * BFS_WARPS;
     if (S.qcap == 0) S.qcap = std::min<long long>(S.maxNE + 1, 8192);
     if (S.pool_cap == 0) S.pool_cap = std::max<long long>(nE * 64, 1 << 20);
     ENS(S.visited, sizeof(unsigned) * (size_t)nwarps * S.maxNE);
@@ -544,8 +551,7 @@ static int run_bfs(Session &S) {
         a.seg_start = S.seg_start.get<long long>(); a.seg_cnt = S.seg_cnt.get<int>();
         a.err = S.err.get<int>();
         a.n_amb = cnt + 7;
-        if (S.prec == PREC_MIX) k_bfs<DIM, PREC_MIX><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
-        else k_bfs<DIM, PREC_F64><<<S.nSM * 2, BFS_THREADS, 0, S.st>>>(a, S.rule);
+        kfn<<<nblocks, BFS_THREADS, 0, S.st>>>(a, S.rule);
         ++S.nlaunch;
         CK(cudaGetLastError());
         unsigned long long hc[3];
@@ -684,8 +690,45 @@ static int run_slot_maps(Session &S) {
 }
 
 template <int DIM>
+static int run_pattern_bm(Session &S, int words, int threads) {
+    const long long nV = S.nV;
+    ENS(S.rowcnt, sizeof(int) * (nV + 1));
+    ENS(S.rowptr, sizeof(long long) * (nV + 1));
+    RowArgs a;
+    a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
+    a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
+    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
+    a.probs = S.prm.get<ProbParams>(); a.nV = nV;
+    a.marks = nullptr; a.mstride = 0;
+    a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
+    const size_t smem = (size_t)words * 4 * (threads / 32);
+    CK(cudaFuncSetAttribute(k_row_pattern_bm<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pattern_bm<DIM>, threads, smem));
+    const unsigned grid = (unsigned)(S.nSM * std::max(per_sm, 1));
+    k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 0, words); ++S.nlaunch;
+    int r = scan_excl<int>(S, S.rowcnt.get<int>(), nV, S.rowptr.get<long long>());
+    if (r) return r;
+    r = d2h(S, &S.nnz_struct, S.rowptr.get<long long>() + nV, 1);
+    if (r) return r;
+    ENS(S.cols, sizeof(int) * (S.nnz_struct + 1));
+    a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 1, words); ++S.nlaunch;
+    CK(cudaGetLastError());
+    S.stats.nnz_structural = (long)S.nnz_struct;
+    if (S.one_sided) return run_slot_maps<DIM>(S);
+    return NLFEM_OK;
+}
+
+template <int DIM>
 static int run_pattern(Session &S) {
     const long long nV = S.nV;
+    // bitmap marks in shared memory when a problem's vertex bitmap is small enough
+    const int words = (S.maxNV + 31) / 32;
+    int bm_threads = 0;
+    if ((size_t)words * 4 * 8 <= 200 * 1024) bm_threads = 256;
+    else if ((size_t)words * 4 * 2 <= 200 * 1024) bm_threads = 64;
+    if (bm_threads) return run_pattern_bm<DIM>(S, words, bm_threads);
     const int nwarps = S.nSM * 4 * 8;
     ENS(S.marks, sizeof(unsigned) * (size_t)nwarps * S.maxNV);
     ENS(S.rowcnt, sizeof(int) * (nV + 1));

@@ -122,6 +122,12 @@ __device__ __forceinline__ int build_list(const unsigned char *mycls, int nPx, i
     return n;
 }
 
+// a[i] for i in {0, 1, 2} as register selects (no dynamic indexing of register arrays)
+template <typename X>
+__device__ __forceinline__ X sel3(const X *v, int i) {
+    return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
+}
+
 __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }
@@ -290,56 +296,51 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
             }
             // termNonloc into A[T, b] and its mirror into A[b, T] (both with the minus sign);
             // lanes sharing a partner vertex first add their integers, the first of them stores
+            // (rolled loops with register selects keep one copy of the hash probes in the code)
             const bool anyclose = __any_sync(FULL, close);
-#pragma unroll
+#pragma unroll 1
             for (int c = 0; c < 3; c++) {
-                const int col = act ? pv[c] : -1;
+                const int col = act ? sel3(pv, c) : -1;
                 const unsigned grp = __match_any_sync(FULL, col);
                 const bool leader = (__ffs(grp) - 1) == lane;
                 const int maxn = __reduce_max_sync(FULL, (unsigned)__popc(grp));
-                long long sn[3], sq[3];
-#pragma unroll
-                for (int r = 0; r < 3; r++) { sn[r] = nx[3 * r + c]; sq[r] = mx[3 * r + c]; }
+                const long long o0 = sel3(&nx[0], c), o1 = sel3(&nx[3], c), o2 = sel3(&nx[6], c);
+                const long long p0v = sel3(&mx[0], c), p1v = sel3(&mx[3], c), p2v = sel3(&mx[6], c);
+                long long sn0 = o0, sn1 = o1, sn2 = o2, sq0 = p0v, sq1 = p1v, sq2 = p2v;
                 unsigned rest = grp & ~(1u << lane);
                 for (int it = 1; it < maxn; it++) {
                     const int src = rest ? __ffs(rest) - 1 : lane;
                     const bool use = rest != 0;
                     if (rest) rest &= rest - 1;
-#pragma unroll
-                    for (int r = 0; r < 3; r++) {
-                        const long long t = shfl64(nx[3 * r + c], src);
-                        if (use) sn[r] += t;
-                    }
+                    const long long t0 = shfl64(o0, src), t1 = shfl64(o1, src), t2 = shfl64(o2, src);
+                    if (use) { sn0 += t0; sn1 += t1; sn2 += t2; }
                     if (anyclose) {
-#pragma unroll
-                        for (int r = 0; r < 3; r++) {
-                            const long long t = shfl64(mx[3 * r + c], src);
-                            if (use) sq[r] += t;
-                        }
+                        const long long u0 = shfl64(p0v, src), u1 = shfl64(p1v, src), u2 = shfl64(p2v, src);
+                        if (use) { sq0 += u0; sq1 += u1; sq2 += u2; }
                     }
                 }
-                if (!anyclose) {
-#pragma unroll
-                    for (int r = 0; r < 3; r++) sq[r] = sn[r];
-                }
+                if (!anyclose) { sq0 = sn0; sq1 = sn1; sq2 = sn2; }
                 if (leader && col >= 0) {
                     const bool keepc = a.labV[col] > 0;
                     const long long rb = keepc ? sm.rowptr[col] : 0;
-#pragma unroll
+#pragma unroll 1
                     for (int r = 0; r < 3; r++) {
-                        if (keep[r]) {
-                            const long long s = slot_find(sm, tv[r], col);
+                        const int t = sel3(tv, r);
+                        const long long sn = r == 0 ? sn0 : (r == 1 ? sn1 : sn2);
+                        const long long sq = r == 0 ? sq0 : (r == 1 ? sq1 : sq2);
+                        if (sel3(keep, r)) {
+                            const long long s = slot_find(sm, t, col);
                             if (s < 0) { atomicOr(&a.err[3], 1); continue; }
-                            red_add(vals, s, -sn[r]);
+                            red_add(vals, s, -sn);
                             if (keepc) {
                                 const int tp = sm.tpos[s];
                                 if (tp < 0) atomicOr(&a.err[3], 1);
-                                else red_add(vals, rb + tp, -sq[r]);
+                                else red_add(vals, rb + tp, -sq);
                             }
                         } else if (keepc) {
-                            const long long t = slot_find(sm, col, tv[r]);
-                            if (t < 0) atomicOr(&a.err[3], 1);
-                            else red_add(vals, t, -sq[r]);
+                            const long long q = slot_find(sm, col, t);
+                            if (q < 0) atomicOr(&a.err[3], 1);
+                            else red_add(vals, q, -sq);
                         }
                     }
                 }

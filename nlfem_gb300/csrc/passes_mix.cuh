@@ -31,11 +31,31 @@ struct MixWarp {
     float pc[32][6];        // partner element, local coordinates
     float prt[32];          // partner |det|
     int pid[32];            // partner element
+    int ds[32][9];          // partner's diagonal-block slots (prefetched at the start of a batch)
+    long long rhb[3], rrb[3];   // T's rows: hash table start, CSR row start
+    unsigned rmask[3];          // T's rows: hash capacity - 1 (0xffffffff: no row)
+    int tvs[3];                 // T's vertices
 };
-__host__ __device__ constexpr size_t mix_warp_bytes(int nPx) {
-    // MixWarp + res[32][nPx][RES_N] floats + lists[2][32 * nPx] shorts
-    return ((sizeof(MixWarp) + 15) / 16) * 16 + (size_t)32 * nPx * RES_N * 4 + (size_t)2 * 32 * nPx * 2 + 16;
+// One column group of a batch: the partner vertex and the integer sums of its three rows
+// (termNonloc into A[T, v], termNonlocPrime into A[v, T]). Stored over the item results.
+struct ScatEntry {
+    int col, pad;
+    long long v[6];
+};
+__host__ __device__ constexpr size_t mix_res_bytes(int nPx) {
+    return (size_t)32 * nPx * RES_N * 4 > 96 * sizeof(ScatEntry) ? (size_t)32 * nPx * RES_N * 4 : 96 * sizeof(ScatEntry);
 }
+__host__ __device__ constexpr size_t mix_warp_bytes(int nPx) {
+    // MixWarp + res[32][nPx][RES_N] floats (or the scatter list) + lists[2][32 * nPx] shorts
+    return ((sizeof(MixWarp) + 15) / 16) * 16 + mix_res_bytes(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
+}
+
+__device__ __forceinline__ void cp_async4(void *dst_smem, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 struct MixArgs {
     PassArgs p;
@@ -141,7 +161,8 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
     unsigned char *wbase = s_raw + (size_t)wib * mix_warp_bytes(nPx);
     MixWarp &W = *reinterpret_cast<MixWarp *>(wbase);
     float *res = reinterpret_cast<float *>(wbase + ((sizeof(MixWarp) + 15) / 16) * 16);   // [32][nPx][RES_N]
-    unsigned short *lst = reinterpret_cast<unsigned short *>(res + 32 * nPx * RES_N);     // [2][32*nPx]
+    unsigned short *lst = reinterpret_cast<unsigned short *>(reinterpret_cast<unsigned char *>(res) + mix_res_bytes(nPx));   // [2][32*nPx]
+    ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
     unsigned nsub = 0, namb = 0;
@@ -155,11 +176,22 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
         const long long lb = a.out_ptr[T], le = a.out_ptr[T + 1];
         if (lb == le || a.labT[T] == 0) continue;
         int tv[3];
-        bool keep[3];
+        unsigned keepmask = 0;   // bit r: the row of T's vertex r exists
 #pragma unroll
         for (int r = 0; r < 3; r++) {
             tv[r] = a.T32[(long long)T * 3 + r];
-            keep[r] = a.labV[tv[r]] > 0;
+            if (a.labV[tv[r]] > 0) keepmask |= 1u << r;
+        }
+        if (lane < 3) {   // T's rows, for the lookups of every batch
+            const int u = sel3(tv, lane);
+            RowHash h;
+            h.hb = h.rb = 0;
+            h.mask = 0xffffffffu;
+            if (keepmask & (1u << lane)) h = row_hash(sm, u);
+            W.rhb[lane] = h.hb;
+            W.rrb[lane] = h.rb;
+            W.rmask[lane] = h.mask;
+            W.tvs[lane] = u;
         }
         const ProbParams P = a.probs[a.eprob[T]];
         const double *ET64 = &a.EC[(long long)T * 6];
@@ -200,6 +232,11 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
             for (int j = 0; j < 6; j++) W.pc[lane][j] = pc[j];
             W.prt[lane] = a.adetf[part];
             W.pid[lane] = part;
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 9; q++) cp_async4(&W.ds[lane][q], &sm.dslot[(long long)part * 9 + q]);
+            }
+            cp_async_commit();
             for (int k = 0; k < nPx; k++) {
                 unsigned char c = CLS_OUT;
                 if (act && !close) {
@@ -283,21 +320,24 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
                     for (int i = 0; i < 6; i++) lpx[i] = fx64(LP[i] * rTT, P.fx_mul, ovf);
                 }
                 // termLocalPrime into the partner's diagonal block
-                const long long *ds = &sm.dslot[(long long)part * 9];
+                cp_async_wait_all();
+                const int *ds = W.ds[lane];
 #pragma unroll
                 for (int r = 0; r < 3; r++) {
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
-                        const long long s = ds[3 * r + c];
+                        const int s = ds[3 * r + c];
                         if (s >= 0) red_add(vals, s, lpx[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)]);
                         else if (a.labV[pv[r]] > 0) atomicOr(&a.err[3], 1);
                     }
                 }
             }
-            // termNonloc into A[T, b] and its mirror into A[b, T] (both with the minus sign);
-            // lanes sharing a partner vertex first add their integers, the first of them stores
-            // (rolled loops with register selects keep one copy of the hash probes in the code)
+            // termNonloc into A[T, b] and its mirror into A[b, T] (both with the minus sign):
+            // lanes sharing a partner vertex add their integers, the first of them lists the sums
+            // (over the item results, read by now); then all lanes share the (vertex, row) lookups
+            __syncwarp();
             const bool anyclose = __any_sync(FULL, close);
+            int nent = 0;
 #pragma unroll 1
             for (int c = 0; c < 3; c++) {
                 const int col = act ? sel3(pv, c) : -1;
@@ -320,29 +360,37 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
                     }
                 }
                 if (!anyclose) { sq0 = sn0; sq1 = sn1; sq2 = sn2; }
-                if (leader && col >= 0) {
-                    const bool keepc = a.labV[col] > 0;
-                    const long long rb = keepc ? sm.rowptr[col] : 0;
-#pragma unroll 1
-                    for (int r = 0; r < 3; r++) {
-                        const int t = sel3(tv, r);
-                        const long long sn = r == 0 ? sn0 : (r == 1 ? sn1 : sn2);
-                        const long long sq = r == 0 ? sq0 : (r == 1 ? sq1 : sq2);
-                        if (sel3(keep, r)) {
-                            const long long s = slot_find(sm, t, col);
-                            if (s < 0) { atomicOr(&a.err[3], 1); continue; }
-                            red_add(vals, s, -sn);
-                            if (keepc) {
-                                const int tp = sm.tpos[s];
-                                if (tp < 0) atomicOr(&a.err[3], 1);
-                                else red_add(vals, rb + tp, -sq);
-                            }
-                        } else if (keepc) {
-                            const long long q = slot_find(sm, col, t);
-                            if (q < 0) atomicOr(&a.err[3], 1);
-                            else red_add(vals, q, -sq);
-                        }
+                const bool put = leader && col >= 0;
+                const unsigned m = __ballot_sync(FULL, put);
+                if (put) {
+                    ScatEntry &e = slist[nent + __popc(m & lanemask_lt())];
+                    e.col = col;
+                    e.v[0] = sn0; e.v[1] = sn1; e.v[2] = sn2;
+                    e.v[3] = sq0; e.v[4] = sq1; e.v[5] = sq2;
+                }
+                nent += __popc(m);
+            }
+            __syncwarp();
+            for (int w = lane; w < 3 * nent; w += 32) {
+                const int e = w / 3, r = w - 3 * e;
+                const int col = slist[e].col;
+                const long long sn = slist[e].v[r], sq = slist[e].v[3 + r];
+                const bool keepc = a.labV[col] > 0;
+                RowHash h;
+                h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
+                if (h.mask != 0xffffffffu) {
+                    const long long s = slot_find_row(sm, h, col);
+                    if (s < 0) { atomicOr(&a.err[3], 1); continue; }
+                    red_add(vals, s, -sn);
+                    if (keepc) {
+                        const int tp = sm.tpos[s];
+                        if (tp < 0) atomicOr(&a.err[3], 1);
+                        else red_add(vals, sm.rowptr[col] + tp, -sq);
                     }
+                } else if (keepc) {
+                    const long long q = slot_find(sm, col, W.tvs[r]);
+                    if (q < 0) atomicOr(&a.err[3], 1);
+                    else red_add(vals, q, -sq);
                 }
             }
             __syncwarp();
@@ -352,10 +400,10 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
         for (int i = 0; i < 6; i++) D[i] = warp_sum_df(D[i]);
         if (lane < 9) {
             const int r = lane / 3, c = lane % 3;
-            const long long s = sm.dslot[(long long)T * 9 + lane];
+            const int s = sm.dslot[(long long)T * 9 + lane];
             const DF d = D[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)];
             if (s >= 0) red_add(vals, s, fx64(d.hi, P.fx_mul, ovf) + fx64(d.lo, P.fx_mul, ovf));
-            else if (keep[r]) atomicOr(&a.err[3], 1);
+            else if (keepmask & (1u << r)) atomicOr(&a.err[3], 1);
         }
         __syncwarp();
     }

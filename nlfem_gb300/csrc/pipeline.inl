@@ -660,7 +660,7 @@ static SlotMap slot_map(Session &S) {
     m.hptr = S.hptr.get<long long>();
     m.htab = S.htab.get<unsigned long long>();
     m.tpos = S.tpos.get<int>();
-    m.dslot = S.dslot.get<long long>();
+    m.dslot = S.dslot.get<int>();
     return m;
 }
 
@@ -681,10 +681,12 @@ static int run_slot_maps(Session &S) {
     CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (htot + 1), S.st));
     k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
     ENS(S.tpos, sizeof(int) * (nnz + 1));
-    ENS(S.dslot, sizeof(long long) * (nE * dV * dV + 1));
+    if (nnz >= 0x7fffffffLL)
+        return fail(NLFEM_ERR_UNSUPPORTED, "the one-sided pass indexes matrix slots with 32-bit integers (2^31 - 1 slots at most)");
+    ENS(S.dslot, sizeof(int) * (nE * dV * dV + 1));
     const SlotMap m = slot_map(S);
     k_tpos<<<S.nSM * 8, 256, 0, S.st>>>(m, S.cols.get<int>(), S.labV.get<int>(), nV, S.tpos.get<int>(), S.err.get<int>()); ++S.nlaunch;
-    k_dslot<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(m, S.T32.get<int>(), S.labV.get<int>(), nE, S.dslot.get<long long>()); ++S.nlaunch;
+    k_dslot<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(m, S.T32.get<int>(), S.labV.get<int>(), nE, S.dslot.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }

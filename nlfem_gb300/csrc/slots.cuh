@@ -24,7 +24,7 @@ struct SlotMap {
     const long long *hptr;            // per row: start of its hash table; capacity = hptr[u+1]-hptr[u]
     const unsigned long long *htab;   // entries (position << 32) | column, HEMPTY when free
     const int *tpos;                  // per slot (i, j): position of column i in row j, -1 if row j is empty
-    const long long *dslot;           // per element: (dim+1)^2 slots of its diagonal block, -1 if the row is empty
+    const int *dslot;                 // per element: (dim+1)^2 slots of its diagonal block, -1 if the row is empty
 };
 
 // Slot of (u, col), or -1 when the row has no such column. At most capacity probes.
@@ -39,6 +39,32 @@ __device__ __forceinline__ long long slot_find(const SlotMap &m, int u, int col)
         if (e == HEMPTY) return -1;
         if ((unsigned)(e & 0xffffffffULL) == (unsigned)col) return m.rowptr[u] + (long long)(e >> 32);
         h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// The hash table of one row, loaded once for many lookups (mask = capacity - 1; an empty row
+// has mask 0xffffffff and never matches).
+struct RowHash {
+    long long hb, rb;   // table start, CSR row start
+    unsigned mask;
+};
+__device__ __forceinline__ RowHash row_hash(const SlotMap &m, int u) {
+    RowHash h;
+    h.hb = m.hptr[u];
+    const unsigned cap = (unsigned)(m.hptr[u + 1] - h.hb);
+    h.mask = cap ? cap - 1 : 0xffffffffu;
+    h.rb = m.rowptr[u];
+    return h;
+}
+__device__ __forceinline__ long long slot_find_row(const SlotMap &m, const RowHash &h, int col) {
+    if (h.mask == 0xffffffffu) return -1;
+    unsigned i = hash32((unsigned)col) & h.mask;
+    for (unsigned probe = 0; probe <= h.mask; probe++) {
+        const unsigned long long e = m.htab[h.hb + i];
+        if (e == HEMPTY) return -1;
+        if ((unsigned)(e & 0xffffffffULL) == (unsigned)col) return h.rb + (long long)(e >> 32);
+        i = (i + 1) & h.mask;
     }
     return -1;
 }
@@ -130,7 +156,7 @@ __global__ void k_tpos(SlotMap m, const int *__restrict__ cols, const int *__res
 // any pair, where the pattern has no such slot).
 template <int DIM>
 __global__ void k_dslot(SlotMap m, const int *__restrict__ T32, const int *__restrict__ labV, long long nE,
-                        long long *__restrict__ dslot) {
+                        int *__restrict__ dslot) {
     constexpr int dV = DIM + 1;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nE) return;
@@ -140,7 +166,7 @@ __global__ void k_dslot(SlotMap m, const int *__restrict__ T32, const int *__res
         const bool keep = labV[u] > 0;
 #pragma unroll
         for (int c = 0; c < dV; c++)
-            dslot[e * dV * dV + r * dV + c] = keep ? slot_find(m, u, T32[e * dV + c]) : -1;
+            dslot[e * dV * dV + r * dV + c] = keep ? (int)slot_find(m, u, T32[e * dV + c]) : -1;
     }
 }
 

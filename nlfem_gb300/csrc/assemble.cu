@@ -582,18 +582,19 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
             const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
             const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
             if (oe == ob && ie == ib) continue;
-            const long long nItems = (1 + (oe - ob) + (ie - ib)) * dV;
-            for (long long i = lane; i < nItems; i += 32) {
-                const long long el_i = i / dV;
-                const int k = (int)(i - el_i * dV);
+            const int nout = (int)(oe - ob), nEl = 1 + nout + (int)(ie - ib);
+            for (int el_i = lane; el_i < nEl; el_i += 32) {   // one partner element per lane
                 int el;
                 if (el_i == 0) el = T;
-                else if (el_i <= oe - ob) el = a.pB[ob + el_i - 1];
-                else el = a.inA[ib + (el_i - 1 - (oe - ob))];
-                const int v = a.T32[(long long)el * dV + k] - voff;
-                atomicOr(&bm[v >> 5], 1u << (v & 31));
-                lo = min(lo, v);
-                hi = max(hi, v);
+                else if (el_i <= nout) el = a.pB[ob + el_i - 1];
+                else el = a.inA[ib + (el_i - 1 - nout)];
+#pragma unroll
+                for (int k = 0; k < dV; k++) {
+                    const int v = a.T32[(long long)el * dV + k] - voff;
+                    atomicOr(&bm[v >> 5], 1u << (v & 31));
+                    lo = min(lo, v);
+                    hi = max(hi, v);
+                }
             }
         }
         __syncwarp();

@@ -20,6 +20,7 @@
 #include "quadrature.cuh"
 #include "passes.cuh"
 #include "passes_mix.cuh"
+#include "passes_bary.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -527,7 +528,7 @@ __global__ void __launch_bounds__(256) k_row_pattern(RowArgs a, int pass) {
         for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
             const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
-            const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
+            const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
             if (oe == ob && ie == ib) continue;
             const long long nEl = 1 + (oe - ob) + (ie - ib);
             const long long nItems = nEl * dV;
@@ -580,7 +581,7 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
             const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
-            const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
+            const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
             if (oe == ob && ie == ib) continue;
             const int nout = (int)(oe - ob), nEl = 1 + nout + (int)(ie - ib);
             for (int el_i = lane; el_i < nEl; el_i += 32) {   // one partner element per lane

@@ -133,6 +133,7 @@ struct PassArgs {
     const double *closebuf;     // (slots, 4, 3, 3)
     int *err;                   // [3] slot missing
     unsigned long long *n_subtri, *n_amb;
+    unsigned long long *n_close;   // pairs integrated with the close-pair rule (from closebuf)
     unsigned char *touched;     // mixed precision: slots that received a contribution
 };
 
@@ -251,6 +252,7 @@ struct PassRule {
     float cyy[MAXQ * 10];   // dy_i * psi_a psi_b (P_i), upper triangle
     float cy[MAXQ * 4];     // dy_i * psi_a (P_i)
     float dxf[MAXQ];
+    float pyf[MAXQ * 3];    // inner points P_i (FP32, any dimension)
 };
 
 template <int dV>
@@ -562,7 +564,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
     int *s_cols = s_dyn + wib * dV * ROWCACHE;
     const long long gw = (long long)blockIdx.x * PASS_WARPS + wib;
     const long long nw = (long long)gridDim.x * PASS_WARPS;
-    unsigned nsub = 0, namb = 0;
+    unsigned nsub = 0, namb = 0, nclose = 0;
     for (long long idx = gw; idx < a.count; idx += nw) {
         const int T = a.list[idx];
         int tv[dV];
@@ -637,6 +639,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                     for (int i = 0; i < dV; i++)
                         for (int j = 0; j < dV; j++) close |= (tv[i] == bv[j]);
                     if (close) {
+                        nclose++;
                         const long long cs = close_slot(a.xadj, a.adj, T, bT);
                         if (cs < 0) { atomicOr(&a.err[3], 1); }
                         else {
@@ -795,9 +798,11 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
     }
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
+    nclose = warp_sum(nclose);
     if (lane == 0) {
         if (nsub && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)nsub);
         if (namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
+        if (nclose && a.n_close) atomicAdd(a.n_close, (unsigned long long)nclose);
     }
 }
 

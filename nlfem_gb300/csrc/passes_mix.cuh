@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
     ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
-    unsigned nsub = 0, namb = 0;
+    unsigned nsub = 0, namb = 0, nclose = 0;
     unsigned char mycls[MAXQ];
     for (;;) {
         int idx = 0;
@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
             for (int i = 0; i < 6; i++) lpx[i] = 0;
             if (act) {
                 if (close) {
+                    nclose++;
                     const long long cs = close_slot(a.xadj, a.adj, T, part);
                     if (cs < 0) {
                         atomicOr(&a.err[3], 1);
@@ -409,9 +410,11 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
     }
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
+    nclose = warp_sum(nclose);
     if (lane == 0) {
         if (nsub && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)nsub);
         if (namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
+        if (nclose && a.n_close) atomicAdd(a.n_close, (unsigned long long)nclose);
     }
 }
 

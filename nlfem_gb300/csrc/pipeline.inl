@@ -247,6 +247,10 @@ static double duffy_traffo(int c, int t, double *al) {
 }
 
 // ---------------------------------------------------------------- session
+// How the quadrature pass adds into the matrix: colored two-sided passes (FP64, and mixed rules
+// without a one-sided kernel), or one persistent one-sided pass with fixed-point atomics.
+enum { PM_COLORED = 0, PM_RETRI = 1, PM_BARY = 2 };
+
 struct Session {
     int dim = 2, dV = 3, nProb = 0;
     bool system = true;
@@ -271,8 +275,8 @@ struct Session {
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
     DevBuf out64a, out64b;
-    DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided pass
-    bool one_sided = false;                 // 2D, mixed precision, retriangulate remote rule
+    DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
+    int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
     long long qcap = 0, pool_cap = 0;
     long long P = 0, nnz_struct = 0, nnz = 0;
     long long nlaunch = 0;   // kernels launched by the current assembly
@@ -388,9 +392,16 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
             return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the quadrature rules");
     }
     {
-        bool all_retri = system;
-        for (const ProbParams &q : S.hprm) all_retri &= (q.remote == MTH_RETRIANGULATE);
-        S.one_sided = S.dim == 2 && S.prec == PREC_MIX && all_retri;
+        // one-sided fixed-point passes for the mixed precision; colored passes otherwise
+        bool all_retri = system, all_bary = system, any_singular = false;
+        for (const ProbParams &q : S.hprm) {
+            all_retri &= (q.remote == MTH_RETRIANGULATE);
+            all_bary &= (q.remote == MTH_BARYCENTER);
+            any_singular |= q.singular != 0;
+        }
+        S.pmode = PM_COLORED;
+        if (S.prec == PREC_MIX && S.dim == 2 && all_retri) S.pmode = PM_RETRI;
+        if (S.prec == PREC_MIX && all_bary && !any_singular) S.pmode = PM_BARY;
     }
     const int dV = S.dV, dim = S.dim;
     ENS(S.T64, sizeof(long long) * S.nE * dV);
@@ -589,6 +600,11 @@ static int run_pairs(Session &S) {
     ENS(S.pA, sizeof(int) * (P + 1));
     ENS(S.pB, sizeof(int) * (P + 1));
     k_compact_pairs<<<grid_for(nE * 32, 256), 256, 0, S.st>>>(S.seg_start.get<long long>(), S.seg_cnt.get<int>(), S.out_ptr.get<long long>(), S.pool.get<int>(), nE, S.pA.get<int>(), S.pB.get<int>()); ++S.nlaunch;
+    S.stats.n_pairs = (long)P;
+    if (S.pmode == PM_BARY) {   // barycenter pairs write the outer element's rows only: no in-lists
+        CK(cudaGetLastError());
+        return NLFEM_OK;
+    }
     ENS(S.incnt, sizeof(int) * (nE + 1));
     ENS(S.in_ptr, sizeof(long long) * (nE + 1));
     ENS(S.inA, sizeof(int) * (P + 1));
@@ -602,7 +618,7 @@ static int run_pairs(Session &S) {
     // The out-lists come from the BFS in its (deterministic) discovery order. The colored
     // two-sided passes sum the in-lists, which k_in_fill fills in atomic order, so those are
     // sorted; the one-sided pass reads no in-list and the pattern sorts its rows itself.
-    if (!S.one_sided) {
+    if (S.pmode == PM_COLORED) {
         r = sort_segments(S, S.out_ptr.get<long long>(), nE, S.pB.get<int>());
         if (r) return r;
         r = sort_segments(S, S.in_ptr.get<long long>(), nE, S.inA.get<int>());
@@ -680,6 +696,10 @@ static int run_slot_maps(Session &S) {
     ENS(S.htab, sizeof(unsigned long long) * (htot + 1));
     CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (htot + 1), S.st));
     k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
+    if (S.pmode != PM_RETRI) {   // the barycenter pass writes its own rows only: no mirror slots
+        CK(cudaGetLastError());
+        return NLFEM_OK;
+    }
     ENS(S.tpos, sizeof(int) * (nnz + 1));
     if (nnz >= 0x7fffffffLL)
         return fail(NLFEM_ERR_UNSUPPORTED, "the one-sided pass indexes matrix slots with 32-bit integers (2^31 - 1 slots at most)");
@@ -699,7 +719,8 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     RowArgs a;
     a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
     a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
-    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
+    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>();
+    a.in_ptr = S.pmode == PM_BARY ? nullptr : S.in_ptr.get<long long>();   // rows of one-sided rules: out-pairs only
     a.probs = S.prm.get<ProbParams>(); a.nV = nV;
     a.marks = nullptr; a.mstride = 0;
     a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
@@ -718,7 +739,7 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 1, words); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
-    if (S.one_sided) return run_slot_maps<DIM>(S);
+    if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
 
@@ -739,7 +760,8 @@ static int run_pattern(Session &S) {
     RowArgs a;
     a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
     a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
-    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
+    a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>();
+    a.in_ptr = S.pmode == PM_BARY ? nullptr : S.in_ptr.get<long long>();   // rows of one-sided rules: out-pairs only
     a.probs = S.prm.get<ProbParams>(); a.nV = nV;
     a.marks = S.marks.get<unsigned>(); a.mstride = S.maxNV;
     a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
@@ -757,7 +779,7 @@ static int run_pattern(Session &S) {
     k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
-    if (S.one_sided) return run_slot_maps<DIM>(S);
+    if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
 
@@ -844,6 +866,7 @@ static PassRule make_pass_rule(const Rule &r, int dim) {
         }
     }
     for (int i = 0; i < r.nPy; i++) {
+        for (int c = 0; c < dim; c++) pr.pyf[dim * i + c] = (float)r.Py[dim * i + c];
         int t = 0;
         for (int a = 0; a < dV; a++) {
             pr.cy[dV * i + a] = (float)(r.dy[i] * r.psiy[dV * i + a]);
@@ -884,12 +907,13 @@ static int run_close(Session &S) {
 // One-sided mixed 2D pass (passes_mix.cuh): one persistent launch over all elements. A
 // contribution outside the fixed-point range sets err[5]; the pass is then redone with a unit
 // 2^16 times coarser.
-static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr) {
+typedef void (*OneSidedKernel)(MixArgs, Rule, PassRule);
+static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, OneSidedKernel kfn, int threads,
+                              size_t smem) {
     const long long nnz = S.nnz_struct;
-    const size_t smem = mix_warp_bytes(S.rule.nPx) * MIX_WARPS;
-    CK(cudaFuncSetAttribute(k_pass_mix2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_mix2d, MIX_THREADS, smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem));
     if (per_sm < 1) return fail(NLFEM_ERR_UNSUPPORTED, "quadrature rule too large for the pass's shared memory");
     MixArgs ma;
     ma.p = pa;
@@ -901,8 +925,8 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr
         CK(cudaMemsetAsync(S.vals.p, 0, sizeof(long long) * (nnz + 1), S.st));
         CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.err.get<int>() + 5, 0, sizeof(int), S.st));
-        CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 5, 0, 2 * sizeof(unsigned long long), S.st));
-        k_pass_mix2d<<<(unsigned)(S.nSM * per_sm), MIX_THREADS, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
+        CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 4, 0, 3 * sizeof(unsigned long long), S.st));
+        kfn<<<(unsigned)(S.nSM * per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
         CK(cudaGetLastError());
         int ovf = 0;
         int r = d2h(S, &ovf, S.err.get<int>() + 5, 1);
@@ -923,7 +947,7 @@ static int run_passes(Session &S) {
     const long long nnz = S.nnz_struct;
     ENS(S.vals, sizeof(double) * (nnz + 1));
     CK(cudaMemsetAsync(S.vals.p, 0, sizeof(double) * (nnz + 1), S.st));
-    if (S.prec == PREC_MIX && !S.one_sided) {
+    if (S.prec == PREC_MIX && S.pmode == PM_COLORED) {
         ENS(S.touched, (size_t)nnz + 16);
         CK(cudaMemsetAsync(S.touched.p, 0, (size_t)nnz + 16, S.st));
     }
@@ -940,10 +964,12 @@ static int run_passes(Session &S) {
     a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
     a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
     a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
-    a.n_subtri = cnt + 5; a.n_amb = cnt + 6;
-    a.touched = S.prec == PREC_MIX && !S.one_sided ? S.touched.get<unsigned char>() : nullptr;
+    a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4;
+    a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);
-    if (S.one_sided) return run_pass_one_sided(S, a, pr);
+    if (S.pmode == PM_RETRI) return run_pass_one_sided(S, a, pr, k_pass_mix2d, MIX_THREADS, mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
+    if (S.pmode == PM_BARY)
+        return run_pass_one_sided(S, a, pr, k_pass_bary<DIM>, BARY_THREADS, bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
     const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
     if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else CK(cudaFuncSetAttribute(k_pass<DIM, PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -967,7 +993,7 @@ static int run_finish(Session &S) {
     ENS(S.fptr, sizeof(long long) * (nV + 1));
     // values: FP64 sums, double-float sums with touched flags (two-sided mixed passes), or
     // fixed-point sums of the one-sided pass (every structural slot received a contribution)
-    const int vmode = S.one_sided ? VAL_FX : (S.prec == PREC_MIX ? VAL_DF : VAL_F64);
+    const int vmode = S.pmode != PM_COLORED ? VAL_FX : (S.prec == PREC_MIX ? VAL_DF : VAL_F64);
     const unsigned char *tch = vmode == VAL_DF ? S.touched.get<unsigned char>() : nullptr;
     const FinishArgs fa{vmode, tch, S.vprob.get<int>(), S.prm.get<ProbParams>()};
     k_finish_count<<<grid_for(nV * 32, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.vals.get<double>(), fa, S.keepcnt.get<int>()); ++S.nlaunch;
@@ -1000,7 +1026,7 @@ static int run_system_t(Session &S) {
     if ((r = run_dual<DIM>(S))) return r;
     if ((r = run_bfs<DIM>(S))) return r;
     if ((r = run_pairs<DIM>(S))) return r;
-    if (!S.one_sided && (r = run_color(S))) return r;   // the one-sided pass needs no colors
+    if (S.pmode == PM_COLORED && (r = run_color(S))) return r;   // the one-sided passes need no colors
     CK(cudaEventRecord(S.ev[1], S.st));
     if ((r = run_pattern<DIM>(S))) return r;
     CK(cudaEventRecord(S.ev[2], S.st));

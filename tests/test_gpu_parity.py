@@ -384,3 +384,25 @@ def test_mixed_pattern_equals_fp64_at_scale(nl):
     assert same_pattern(A, B)
     fro, mx = rel_errors(A, B)
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_barycenter_2d(nl, orc):
+    m = square_mesh(16, 0.15, jitter=0.2, seed=4)
+    k = {"function": "parabola", "horizon": 0.15, "outputdim": 1}
+    A = nl.stiffnessMatrix(m, k, conf2d(method="baryCenter", precision="mixed"))
+    B = orc.assemble(m, k, conf2d(method="baryCenter"))["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_3d_deterministic_and_fp64_pattern(nl):
+    m = cube_mesh(7, 0.1, jitter=0.1, seed=3)
+    k = {"function": "constant3D", "horizon": 0.25, "outputdim": 1}
+    A1 = nl.stiffnessMatrix(m, k, conf3d(precision="mixed"))
+    A2 = nl.stiffnessMatrix(m, k, conf3d(precision="mixed"))
+    assert same_pattern(A1, A2) and np.array_equal(A1.data, A2.data)
+    B = nl.stiffnessMatrix(m, k, conf3d())
+    assert same_pattern(A1, B)
+    fro, mx = rel_errors(A1, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)

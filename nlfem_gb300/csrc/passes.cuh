@@ -255,10 +255,6 @@ struct PassRule {
     float pyf[MAXQ * 3];    // inner points P_i (FP32, any dimension)
 };
 
-template <int dV>
-__device__ __forceinline__ int sym_idx(int a, int b) {   // upper-triangle index, a <= b
-    return a * dV - (a * (a - 1)) / 2 + (b - a);
-}
 
 // ---------------------------------------------------------------- FP32 pair quadrature (2D)
 // Inner quadrature of one outer point against triangle Q (relative to the outer point): returns

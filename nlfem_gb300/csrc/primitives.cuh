@@ -180,4 +180,10 @@ __device__ __forceinline__ double fx_to_double(unsigned long long lo, unsigned l
     return neg ? -d : d;
 }
 
+// Index of (a, b), a <= b, in the row-major upper triangle of a dV x dV symmetric matrix.
+template <int dV>
+__host__ __device__ __forceinline__ int sym_idx(int a, int b) {
+    return a * dV - (a * (a - 1)) / 2 + (b - a);
+}
+
 }  // namespace nlg

@@ -257,6 +257,51 @@ __global__ void k_close_list(QuadArgs a, int *list, unsigned long long *count) {
 
 // One warp per close pair: integrate_fractional (integration.cpp:187-288) with join()
 // (:1913-1958), FP64 throughout; lanes stride over the Duffy points, warp-reduce the blocks.
+// Sum over the Duffy points of one close pair (integration.cpp:187-288) of w pxy pxy^T, upper
+// triangle of the nL x nL matrix, nL = 6 - NEQ: the lanes take the (map, Gauss point) items in
+// turn. The kernel value |x - y|^-(d+2s) is taken as exp2(-(d+2s)/2 log2 |x - y|^2), the same
+// function as the reference's 1/pow(sqrt(r), d+2s) without the power's extra work.
+template <int NEQ>
+__device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duffy &d, int c, int nT,
+                                                 const double *EA, const double *EB, double dAB, double *M) {
+    constexpr int NL = 6 - NEQ, SH = 3 - NEQ;
+    const int lane = threadIdx.x & 31;
+    const int total = nT * d.nPg;
+    const double *al_base = d.alpha[c];
+    const double *td_base = d.tdet[c];
+    const double a0 = EA[2] - EA[0], a1 = EA[4] - EA[0], a2 = EA[3] - EA[1], a3 = EA[5] - EA[1];
+    const double b0 = EB[2] - EB[0], b1 = EB[4] - EB[0], b2 = EB[3] - EB[1], b3 = EB[5] - EB[1];
+    const double hexp = -0.5 * P.expo;
+    for (int idx = lane; idx < total; idx += 32) {
+        const int k = idx % d.nPg;
+        const double *al = &al_base[(long long)idx * 4];
+        const double tf = td_base[idx];
+        const double x0 = al[0] * a0 + al[1] * a1 + EA[0], x1 = al[0] * a2 + al[1] * a3 + EA[1];
+        const double y0 = al[2] * b0 + al[3] * b1 + EB[0], y1 = al[2] * b2 + al[3] * b3 + EB[1];
+        const double z0 = x0 - y0, z1 = x1 - y1;
+        const double ker = P.kc * exp2(hexp * log2(z0 * z0 + z1 * z1));
+        const double px[3] = {1.0 - al[0] - al[1], al[0], al[1]};
+        const double py[3] = {1.0 - al[2] - al[3], al[2], al[3]};
+        double v[NL];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (i < NEQ) {
+                v[i] = px[i] - py[i];
+            } else {
+                v[i] = px[i];
+                v[i + SH] = -py[i];
+            }
+        }
+        const double base = ker * tf * d.dg[k] * dAB;
+#pragma unroll
+        for (int aa = 0; aa < NL; aa++) {
+            const double fa = base * v[aa];
+#pragma unroll
+            for (int b = aa; b < NL; b++) M[sym_idx<6>(aa, b)] += fa * v[b];
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int lane = threadIdx.x & 31;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -311,33 +356,20 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
             tgt[aa * 6 + b] = t;
             sgn[aa * 6 + b] = s;
         }
+    // sum over the Duffy points of w pxy pxy^T (symmetric, in registers), then the four blocks
+    double M[21];
+#pragma unroll
+    for (int i = 0; i < 21; i++) M[i] = 0.0;
+    if (nEqual == 1) close_accumulate<1>(P, d, c, nT, EA, EB, dA * dB, M);
+    else if (nEqual == 2) close_accumulate<2>(P, d, c, nT, EA, EB, dA * dB, M);
+    else close_accumulate<3>(P, d, c, nT, EA, EB, dA * dB, M);
+#pragma unroll
+    for (int i = 0; i < 21; i++) M[i] = warp_sum(M[i]);
     double acc[36];
     for (int i = 0; i < 36; i++) acc[i] = 0;
-    const int total = nT * d.nPg;
-    const double *al_base = d.alpha[c];
-    const double *td_base = d.tdet[c];
-    for (int idx = lane; idx < total; idx += 32) {
-        const int k = idx % d.nPg;
-        const double *al = &al_base[(long long)idx * 4];
-        const double tf = td_base[idx];
-        double x[2], y[2];
-        x[0] = al[0] * (EA[2] - EA[0]) + al[1] * (EA[4] - EA[0]) + EA[0];
-        x[1] = al[0] * (EA[3] - EA[1]) + al[1] * (EA[5] - EA[1]) + EA[1];
-        y[0] = al[2] * (EB[2] - EB[0]) + al[3] * (EB[4] - EB[0]) + EB[0];
-        y[1] = al[2] * (EB[3] - EB[1]) + al[3] * (EB[5] - EB[1]) + EB[1];
-        const double ker = kernel_f64<2>(P, x, y);
-        const double px[3] = {1.0 - al[0] - al[1], al[0], al[1]};
-        const double py[3] = {1.0 - al[2] - al[3], al[2], al[3]};
-        double pxy[6];
-        for (int i = 0; i < nEqual; i++) pxy[i] = px[i] - py[i];
-        for (int i = nEqual; i < 3; i++) { pxy[i] = px[i]; pxy[i + shift] = -py[i]; }
-        const double base = ker * tf * d.dg[k] * dA * dB;
-        for (int aa = 0; aa < nLocal; aa++) {
-            const double fa = base * pxy[aa];
-            for (int b = 0; b < nLocal; b++) acc[tgt[aa * 6 + b]] += sgn[aa * 6 + b] * fa * pxy[b];
-        }
-    }
-    for (int i = 0; i < 36; i++) acc[i] = warp_sum(acc[i]);
+    for (int aa = 0; aa < nLocal; aa++)
+        for (int b = 0; b < nLocal; b++) acc[tgt[aa * 6 + b]] += sgn[aa * 6 + b] * M[aa <= b ? sym_idx<6>(aa, b) : sym_idx<6>(b, aa)];
+
     if (a.blocks_out) {
         if (lane == 0) {
             double *o = &a.blocks_out[p * 36];

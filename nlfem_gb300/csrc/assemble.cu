@@ -373,8 +373,14 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                     // order (and every order derived from it) does not depend on atomic timing
                     const unsigned same = __match_any_sync(FULL, cand);
                     if ((__ffs(same) - 1) != lane) cand = -1;
+                    // the visited array is private to this warp and the candidates of one step are
+                    // distinct, so a plain load and store suffice (steps are ordered by the warp
+                    // synchronisations below; the load may hit L1)
                     bool fresh = false;
-                    if (cand >= 0) fresh = atomicExch(&visited[cand - eoff], stamp) != stamp;
+                    if (cand >= 0) {
+                        fresh = visited[cand - eoff] != stamp;
+                        if (fresh) visited[cand - eoff] = stamp;
+                    }
                     const bool bridge = fresh && a.labT[cand] == 0;
                     queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
                     // candidates to test are compacted, so the test runs on full warps

@@ -352,23 +352,12 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                 long long beg = 0;
                 int deg = 0;
                 if (s >= 0) { beg = a.xadj[s]; deg = (int)(a.xadj[s + 1] - beg); }
-                const int incl = warp_incl_scan(deg, lane);
-                const int total = __shfl_sync(FULL, incl, 31);
-                const int excl = incl - deg;
-                for (int c0 = 0; c0 < total; c0 += 32) {
-                    const int c = c0 + lane;
-                    // owner lane j: largest j with excl_j <= c
-                    int lo = 0, hi = 31;
-#pragma unroll
-                    for (int it = 0; it < 5; it++) {
-                        int mid = (lo + hi + 1) >> 1;
-                        int em = __shfl_sync(FULL, excl, mid);
-                        if (em <= c) lo = mid; else hi = mid - 1;
-                    }
-                    const long long bj = __shfl_sync(FULL, beg, lo);
-                    const int ej = __shfl_sync(FULL, excl, lo);
+                // each lane walks its own frontier element's neighbours (degrees are nearly
+                // uniform, so the lanes stay busy without a scan over the warp)
+                const int maxdeg = (int)__reduce_max_sync(FULL, (unsigned)deg);
+                for (int jn = 0; jn < maxdeg; jn++) {
                     int cand = -1;
-                    if (c < total) cand = a.adj[bj + (c - ej)];
+                    if (jn < deg) cand = a.adj[beg + jn];
                     // lanes holding the same candidate: the lowest one takes it, so the queue
                     // order (and every order derived from it) does not depend on atomic timing
                     const unsigned same = __match_any_sync(FULL, cand);

@@ -10,8 +10,9 @@
 // Per batch of 32 pairs, the owner lane tests its pair's outer points (FP32 distance with a
 // certified margin, exact FP64 test inside the margin), the (pair, point) items whose ball
 // contains the barycenter are compacted and integrated 32 at a time over the full inner element,
-// and the owner lane folds them in a fixed order. Lanes sharing a partner vertex add their
-// integers; all lanes then share the slot lookups in T's rows.
+// and the owner lane folds them in a fixed order. Each pair's integer blocks are balanced so its
+// rows sum to exactly zero (balance_rows). Lanes sharing a partner vertex add their integers;
+// all lanes then share the slot lookups in T's rows.
 #pragma once
 #include "passes_mix.cuh"
 
@@ -111,9 +112,9 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             for (int j = 0; j < DIM; j++) W.xf[DIM * k + j] = (float)(W.x64[DIM * k + j] - ET64[j]);
         }
         __syncwarp();
-        DF D[NS];
+        long long D[NS];   // termLocal of T's pairs, integer sums
 #pragma unroll
-        for (int i = 0; i < NS; i++) D[i] = df_zero();
+        for (int i = 0; i < NS; i++) D[i] = 0;
         const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
@@ -219,10 +220,14 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                         for (int t = 0; t < dV; t++) N[dV * r + t] = fmaf(c, rr[1 + t], N[dV * r + t]);
                     }
                 }
+                long long lx[NS];
 #pragma unroll
-                for (int i = 0; i < NS; i++) D[i] = df_add(D[i], 2.f * L[i] * rTT);
+                for (int i = 0; i < NS; i++) lx[i] = fx64(2.f * L[i] * rTT, P.fx_mul, ovf);
 #pragma unroll
                 for (int i = 0; i < dV * dV; i++) nx[i] = fx64(2.f * N[i] * rTT, P.fx_mul, ovf);
+                balance_rows<dV>(lx, nx, nullptr, nullptr);
+#pragma unroll
+                for (int i = 0; i < NS; i++) D[i] += lx[i];
             }
             // termNonloc into A[T, b] (minus sign): group sums per partner vertex, shared lookups
             __syncwarp();
@@ -282,20 +287,22 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
         }
         // termLocal of all of T's pairs into T's diagonal block
 #pragma unroll
-        for (int i = 0; i < NS; i++) D[i] = warp_sum_df(D[i]);
+        for (int i = 0; i < NS; i++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) D[i] += (long long)__shfl_xor_sync(FULL, (unsigned long long)D[i], o);
         if (lane < dV * dV) {
             const int r = lane / dV, c = lane % dV;
             RowHash h;
             h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
             if (h.mask != 0xffffffffu) {
-                DF d = df_zero();
+                long long d = 0;
                 const int si = r <= c ? sym_idx<dV>(r, c) : sym_idx<dV>(c, r);
 #pragma unroll
                 for (int i = 0; i < NS; i++)
                     if (i == si) d = D[i];
                 const long long s = slot_find_row(sm, h, a.T32[(long long)T * dV + c]);
                 if (s < 0) atomicOr(&a.err[3], 1);
-                else red_add(vals, s, fx64(d.hi, P.fx_mul, ovf) + fx64(d.lo, P.fx_mul, ovf));
+                else red_add(vals, s, d);
             }
         }
         __syncwarp();

@@ -148,11 +148,43 @@ __device__ __forceinline__ X sel3(const X *v, int i) {
     return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
 }
 
+// Exact row balance of one pair's integer blocks. For kernels of |x - y|, sum_c termLocal[r][c]
+// = sum_c termNonloc[r][c] and sum_c' termLocalPrime[c][c'] = sum_r termNonlocPrime[r][c] hold
+// in exact arithmetic (the basis functions sum to one). The diagonal entries take the rounding,
+// so each of the pair's rows sums to exactly zero and the assembled operator annihilates
+// constants exactly, as the FP64 reference does to rounding.
+template <int dV>
+__device__ __forceinline__ void balance_rows(long long *lx, const long long *nx, long long *lpx,
+                                             const long long *mx) {
+#pragma unroll
+    for (int r = 0; r < dV; r++) {
+        long long s = 0;
+#pragma unroll
+        for (int c = 0; c < dV; c++) s += nx[dV * r + c];
+#pragma unroll
+        for (int c = 0; c < dV; c++)
+            if (c != r) s -= lx[c < r ? sym_idx<dV>(c, r) : sym_idx<dV>(r, c)];
+        lx[sym_idx<dV>(r, r)] = s;
+    }
+    if (lpx) {
+#pragma unroll
+        for (int c = 0; c < dV; c++) {
+            long long s = 0;
+#pragma unroll
+            for (int r = 0; r < dV; r++) s += mx[dV * r + c];
+#pragma unroll
+            for (int q = 0; q < dV; q++)
+                if (q != c) s -= lpx[q < c ? sym_idx<dV>(q, c) : sym_idx<dV>(c, q)];
+            lpx[sym_idx<dV>(c, c)] = s;
+        }
+    }
+}
+
 __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }
 
-__global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {
+__global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const PassArgs &a = ma.p;
     const SlotMap &sm = ma.m;
@@ -203,9 +235,9 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
             W.xf[k] = f2((float)(W.x64[2 * k] - ET64[0]), (float)(W.x64[2 * k + 1] - ET64[1]));
         }
         __syncwarp();
-        DF D[6];
+        long long D[6];   // termLocal of T's pairs, integer sums
 #pragma unroll
-        for (int i = 0; i < 6; i++) D[i] = df_zero();
+        for (int i = 0; i < 6; i++) D[i] = 0;
         const bool frac_close = P.singular && P.close == MTH_FRACTIONAL;
         const float sqf = P.sqdelta_f;
         for (long long p0 = lb; p0 < le; p0 += 32) {
@@ -270,11 +302,11 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
             }
             __syncwarp();
             // owner: fold the item sums into the pair's blocks, in fixed point from here on
-            long long nx[9], mx[9], lpx[6];
+            long long nx[9], mx[9], lpx[6], lx[6];
 #pragma unroll
             for (int i = 0; i < 9; i++) nx[i] = mx[i] = 0;
 #pragma unroll
-            for (int i = 0; i < 6; i++) lpx[i] = 0;
+            for (int i = 0; i < 6; i++) lpx[i] = lx[i] = 0;
             if (act) {
                 if (close) {
                     nclose++;
@@ -283,8 +315,10 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
                         atomicOr(&a.err[3], 1);
                     } else {
                         const double *cb = &a.closebuf[cs * 36];
+#pragma unroll
                         for (int i = 0; i < 3; i++)
-                            for (int j = i; j < 3; j++) D[sym_idx<3>(i, j)] = df_add(D[sym_idx<3>(i, j)], df_from_double(cb[3 * i + j]));
+#pragma unroll
+                            for (int j = i; j < 3; j++) lx[sym_idx<3>(i, j)] = fx64d(cb[3 * i + j], P.fx_mul, ovf);
 #pragma unroll
                         for (int i = 0; i < 9; i++) {
                             nx[i] = fx64d(cb[9 + i], P.fx_mul, ovf);    // termNonloc [T vertex][b vertex]
@@ -314,12 +348,15 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
                         for (int ab = 0; ab < 6; ab++) LP[ab] = fmaf(dk, rr[4 + ab], LP[ab]);
                     }
 #pragma unroll
-                    for (int i = 0; i < 6; i++) D[i] = df_add(D[i], L[i] * rTT);
+                    for (int i = 0; i < 6; i++) lx[i] = fx64(L[i] * rTT, P.fx_mul, ovf);
 #pragma unroll
                     for (int i = 0; i < 9; i++) mx[i] = nx[i] = fx64(N[i] * rTT, P.fx_mul, ovf);
 #pragma unroll
                     for (int i = 0; i < 6; i++) lpx[i] = fx64(LP[i] * rTT, P.fx_mul, ovf);
                 }
+                balance_rows<3>(lx, nx, lpx, mx);
+#pragma unroll
+                for (int i = 0; i < 6; i++) D[i] += lx[i];
                 // termLocalPrime into the partner's diagonal block
                 cp_async_wait_all();
                 const int *ds = W.ds[lane];
@@ -398,12 +435,18 @@ __global__ void __launch_bounds__(MIX_THREADS) k_pass_mix2d(MixArgs ma, Rule rul
         }
         // termLocal of all of T's pairs into T's diagonal block
 #pragma unroll
-        for (int i = 0; i < 6; i++) D[i] = warp_sum_df(D[i]);
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) D[i] += (long long)__shfl_xor_sync(FULL, (unsigned long long)D[i], o);
         if (lane < 9) {
             const int r = lane / 3, c = lane % 3;
             const int s = sm.dslot[(long long)T * 9 + lane];
-            const DF d = D[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)];
-            if (s >= 0) red_add(vals, s, fx64(d.hi, P.fx_mul, ovf) + fx64(d.lo, P.fx_mul, ovf));
+            const int si = r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r);
+            long long d = 0;
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+                if (i == si) d = D[i];
+            if (s >= 0) red_add(vals, s, d);
             else if (keepmask & (1u << r)) atomicOr(&a.err[3], 1);
         }
         __syncwarp();

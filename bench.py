@@ -104,6 +104,7 @@ def config_dict(args, extra, problems):
     d["nV"] = int(sum(m["vertices"].shape[0] for m, _, _ in problems))
     d["precision"] = "mixed (headline) and fp64"
     d["l2"] = "flushed between steps (256 MiB write)"
+    d["graph"] = not args.no_graph
     return d
 
 
@@ -236,14 +237,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def timed_session(problems, steps, warmup, flush, clocks_index=0, dist=None):
+def timed_session(problems, steps, warmup, flush, clocks_index=0, dist=None, graph=True):
     """W untimed + K timed assemblies from HBM-resident inputs; L2 flushed before each step.
+    With graph=True the steps replay the assembly captured as a CUDA graph during the warm-up
+    (every kernel of the step still runs; only the host-side orchestration is replaced).
     Returns (pairs, seconds, last stats, per-step stats, clocks, session)."""
     import torch
     from nlfem_gb300 import nlfem
     sess = nlfem.Session(problems)
     for _ in range(warmup):
-        sess.assemble()
+        sess.assemble(graph=graph)
     stats = []
     with Clocks(clocks_index) as clk:
         if dist is not None:
@@ -252,7 +255,7 @@ def timed_session(problems, steps, warmup, flush, clocks_index=0, dist=None):
         for _ in range(steps):
             flush.fill_(1)
             torch.cuda.synchronize()
-            stats.append(sess.assemble())   # device time of the step: CUDA events on its stream
+            stats.append(sess.assemble(graph=graph))   # device time: CUDA events on its stream
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
@@ -299,7 +302,8 @@ def run_gpu(args, rank=0, world=1, dist=None):
     problems, extra = workload(args, "mixed")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    pairs, secs, st, all_st, clocks, sess = timed_session(problems, args.steps, args.warmup, flush, dev, dist)
+    pairs, secs, st, all_st, clocks, sess = timed_session(problems, args.steps, args.warmup, flush, dev, dist,
+                                                          graph=not args.no_graph)
     launches = int(sum(s["n_launches"] for s in all_st))
     if dist is not None:
         t = torch.tensor([secs], dtype=torch.float64, device="cuda")
@@ -414,6 +418,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="time normal assemblies instead of CUDA-graph replays")
     args = ap.parse_args()
     args.fp64_steps_set = args.fp64_steps is not None
     if args.fp64_steps is None:

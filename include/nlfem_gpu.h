@@ -104,6 +104,10 @@ void nlfem_csr_free(nlfem_csr *m);
 typedef struct nlfem_session nlfem_session;
 int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out);
 int nlfem_session_assemble(nlfem_session *s);            /* inputs already in HBM */
+/* The same assembly replayed from a CUDA graph: the first call assembles and captures the
+ * sequence, later calls launch the graph (falls back to a normal assembly when a capacity check
+ * trips). Mixed-precision sessions only; other sessions assemble normally. */
+int nlfem_session_assemble_graph(nlfem_session *s);
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out);
 void nlfem_session_destroy(nlfem_session *s);
 

@@ -277,6 +277,10 @@ struct Session {
     DevBuf out64a, out64b;
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
     int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
+    // graph replay: the stages run without host reads, on the sizes of the previous assembly
+    bool replay = false;
+    long long nadj = 0, htot = 0;
+    cudaGraphExec_t gexec = nullptr;
     long long qcap = 0, pool_cap = 0;
     long long P = 0, nnz_struct = 0, nnz = 0;
     long long nlaunch = 0;   // kernels launched by the current assembly
@@ -290,6 +294,7 @@ struct Session {
                          &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                          &hcap, &hptr, &htab, &tpos, &dslot};
         for (DevBuf *b : all) b->release();
+        if (gexec) cudaGraphExecDestroy(gexec);
         if (st) {
             for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
             cudaStreamDestroy(st);
@@ -342,6 +347,7 @@ static int scan_excl(Session &S, const TIn *in, long long n, long long *out) {
 
 template <typename T>
 static int d2h(Session &S, T *host, const T *dev, size_t n) {
+    if (S.replay) return NLFEM_OK;   // captured sequence: the host values are those of the last run
     CK(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, S.st));
     CK(cudaStreamSynchronize(S.st));
     return NLFEM_OK;
@@ -514,12 +520,12 @@ static int run_dual(Session &S) {
     k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), nullptr, S.adjcnt.get<int>(), nullptr, S.err.get<int>() + 8); ++S.nlaunch;
     r = scan_excl<int>(S, S.adjcnt.get<int>(), nE, S.xadj.get<long long>());
     if (r) return r;
-    long long nadj = 0;
-    r = d2h(S, &nadj, S.xadj.get<long long>() + nE, 1);
+    r = d2h(S, &S.nadj, S.xadj.get<long long>() + nE, 1);
     if (r) return r;
-    ENS(S.adj, sizeof(int) * (nadj + 1));
+    ENS(S.adj, sizeof(int) * (S.nadj + 1));
     k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), S.xadj.get<long long>(), S.adjcnt.get<int>(), S.adj.get<int>(), S.err.get<int>() + 8); ++S.nlaunch;
     CK(cudaGetLastError());
+    if (S.replay) return NLFEM_OK;
     int e8 = 0;
     r = d2h(S, &e8, S.err.get<int>() + 8, 1);
     if (r) return r;
@@ -565,6 +571,7 @@ static int run_bfs(Session &S) {
         kfn<<<nblocks, BFS_THREADS, 0, S.st>>>(a, S.rule);
         ++S.nlaunch;
         CK(cudaGetLastError());
+        if (S.replay) return NLFEM_OK;   // overflow flags are checked after the replay
         unsigned long long hc[3];
         int he[2];
         int r = d2h(S, hc, cnt, 3);
@@ -690,11 +697,10 @@ static int run_slot_maps(Session &S) {
     k_hash_cap<<<grid_for(nV, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.hcap.get<long long>()); ++S.nlaunch;
     int r = scan_excl<long long>(S, S.hcap.get<long long>(), nV, S.hptr.get<long long>());
     if (r) return r;
-    long long htot = 0;
-    r = d2h(S, &htot, S.hptr.get<long long>() + nV, 1);
+    r = d2h(S, &S.htot, S.hptr.get<long long>() + nV, 1);
     if (r) return r;
-    ENS(S.htab, sizeof(unsigned long long) * (htot + 1));
-    CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (htot + 1), S.st));
+    ENS(S.htab, sizeof(unsigned long long) * (S.htot + 1));
+    CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (S.htot + 1), S.st));
     k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
     if (S.pmode != PM_RETRI) {   // the barycenter pass writes its own rows only: no mirror slots
         CK(cudaGetLastError());
@@ -880,10 +886,7 @@ static PassRule make_pass_rule(const Rule &r, int dim) {
 static int run_close(Session &S) {
     if (S.dim != 2 || S.duffy_nPg == 0) return NLFEM_OK;
     const long long nE = S.nE;
-    long long nadj = 0;
-    int r = d2h(S, &nadj, S.xadj.get<long long>() + nE, 1);
-    if (r) return r;
-    const long long nslot = nadj + nE;
+    const long long nslot = S.nadj + nE;
     ENS(S.closeA, sizeof(int) * (nslot + 1));
     ENS(S.closeB, sizeof(int) * (nslot + 1));
     ENS(S.closebuf, sizeof(double) * 36 * (nslot + 1));
@@ -928,6 +931,7 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 4, 0, 3 * sizeof(unsigned long long), S.st));
         kfn<<<(unsigned)(S.nSM * per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
         CK(cudaGetLastError());
+        if (S.replay) return NLFEM_OK;   // the overflow flag is checked after the replay
         int ovf = 0;
         int r = d2h(S, &ovf, S.err.get<int>() + 5, 1);
         if (r) return r;
@@ -1017,29 +1021,43 @@ static int check_errors(Session &S) {
     return NLFEM_OK;
 }
 
+// Phase event i; inside a capture it becomes an event-record node of the graph.
+static cudaError_t phase_event(Session &S, int i) {
+    return S.replay ? cudaEventRecordWithFlags(S.ev[i], S.st, cudaEventRecordExternal) : cudaEventRecord(S.ev[i], S.st);
+}
+
+// The assembly as one ordered sequence of stream work (also what a graph captures).
 template <int DIM>
-static int run_system_t(Session &S) {
+static int run_system_body(Session &S) {
     int r;
     S.nlaunch = 0;
-    CK(cudaEventRecord(S.ev[0], S.st));
+    CK(phase_event(S, 0));
     if ((r = run_prep<DIM>(S))) return r;
     if ((r = run_dual<DIM>(S))) return r;
     if ((r = run_bfs<DIM>(S))) return r;
     if ((r = run_pairs<DIM>(S))) return r;
     if (S.pmode == PM_COLORED && (r = run_color(S))) return r;   // the one-sided passes need no colors
-    CK(cudaEventRecord(S.ev[1], S.st));
+    CK(phase_event(S, 1));
     if ((r = run_pattern<DIM>(S))) return r;
-    CK(cudaEventRecord(S.ev[2], S.st));
+    CK(phase_event(S, 2));
     if ((r = run_passes<DIM>(S))) return r;
-    CK(cudaEventRecord(S.ev[3], S.st));
+    CK(phase_event(S, 3));
     if ((r = run_finish(S))) return r;
-    CK(cudaEventRecord(S.ev[4], S.st));
+    CK(phase_event(S, 4));
+    return NLFEM_OK;
+}
+
+// After the sequence: errors, timings (CUDA events on the assembly stream) and counters.
+static int run_system_post(Session &S) {
+    int r;
     CK(cudaStreamSynchronize(S.st));
     if ((r = check_errors(S))) return r;
     float t[4];
     for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]));
-    unsigned long long ncl[4] = {0, 0, 0, 0};
+    unsigned long long ncl[5] = {0, 0, 0, 0, 0};
     if ((r = d2h(S, ncl, S.counters.get<unsigned long long>() + 4, 4))) return r;
+    if ((r = d2h(S, &ncl[4], S.counters.get<unsigned long long>() + 1, 1))) return r;
+    S.stats.n_candidates = (long)ncl[4];
     S.stats.n_close = (long)ncl[0];
     S.stats.n_subtri = (long)ncl[1];
     S.stats.n_ambiguous = (long)(ncl[2] + ncl[3]);
@@ -1053,7 +1071,58 @@ static int run_system_t(Session &S) {
     return NLFEM_OK;
 }
 
+template <int DIM>
+static int run_system_t(Session &S) {
+    int r = run_system_body<DIM>(S);
+    return r ? r : run_system_post(S);
+}
+
+// Graph replay of a session. The first call assembles normally, which sizes every buffer, and
+// then captures the same sequence without host reads into a CUDA graph; later calls launch the
+// graph. Capacity flags (BFS queue or pool, fixed-point range) are checked after each replay;
+// if one tripped, the graph is dropped and the assembly reruns normally. Only the one-sided
+// passes are captured (the colored passes read the color count on the host).
+template <int DIM>
+static int run_system_graph_t(Session &S) {
+    int r;
+    if (S.gexec) {
+        const long long launches = S.nlaunch;
+        CK(cudaGraphLaunch(S.gexec, S.st));
+        CK(cudaStreamSynchronize(S.st));
+        int he[6];
+        if ((r = d2h(S, he, S.err.get<int>(), 6))) return r;
+        if (!he[0] && !he[1] && !he[5]) {
+            S.nlaunch = launches;
+            return run_system_post(S);
+        }
+        cudaGraphExecDestroy(S.gexec);
+        S.gexec = nullptr;
+    }
+    if ((r = run_system_t<DIM>(S))) return r;
+    if (S.pmode == PM_COLORED) return NLFEM_OK;
+    const nlfem_stats keep = S.stats;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal));
+    S.replay = true;
+    r = run_system_body<DIM>(S);
+    S.replay = false;
+    const long long launches = S.nlaunch;
+    const cudaError_t e = cudaStreamEndCapture(S.st, &g);
+    if (!r && e != cudaSuccess) r = fail(NLFEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    if (!r) {
+        const cudaError_t ei = cudaGraphInstantiate(&S.gexec, g, 0);
+        if (ei != cudaSuccess) { S.gexec = nullptr; r = fail(NLFEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei)); }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    S.nlaunch = launches;
+    S.stats = keep;
+    g_stats = keep;
+    return r;
+}
+
 static int run_system(Session &S) { return S.dim == 2 ? run_system_t<2>(S) : run_system_t<3>(S); }
+static int run_system_graph(Session &S) { return S.dim == 2 ? run_system_graph_t<2>(S) : run_system_graph_t<3>(S); }
 
 template <int DIM>
 static int run_forcing_t(Session &S) {
@@ -1176,6 +1245,11 @@ int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out)
 int nlfem_session_assemble(nlfem_session *s) {
     if (!s) return fail(NLFEM_ERR_INVALID, "null session");
     return run_system(s->S);
+}
+
+int nlfem_session_assemble_graph(nlfem_session *s) {
+    if (!s) return fail(NLFEM_ERR_INVALID, "null session");
+    return run_system_graph(s->S);
 }
 
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out) {

@@ -227,8 +227,10 @@ class Session:
         self.h = ctypes.c_void_p()
         _lib.check(self.lib.nlfem_session_create(self.arr, len(self.ps), ctypes.byref(self.h)))
 
-    def assemble(self):
-        _lib.check(self.lib.nlfem_session_assemble(self.h))
+    def assemble(self, graph=False):
+        """Assemble all problems; graph=True replays a captured CUDA graph after the first call."""
+        fn = self.lib.nlfem_session_assemble_graph if graph else self.lib.nlfem_session_assemble
+        _lib.check(fn(self.h))
         return _lib.stats()
 
     def download(self, i=0):

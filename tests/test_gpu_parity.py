@@ -406,3 +406,31 @@ def test_mixed_3d_deterministic_and_fp64_pattern(nl):
     assert same_pattern(A1, B)
     fro, mx = rel_errors(A1, B)
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+@pytest.mark.parametrize("case", ["retri_batch", "bary3d", "fractional"])
+def test_session_graph_replay_bitwise(nl, case):
+    if case == "retri_batch":
+        probs = [(square_mesh(20, 0.12, jitter=0.2, seed=9), {"function": "parabola", "horizon": 0.12, "outputdim": 1},
+                  conf2d(precision="mixed")),
+                 (square_mesh(14, 0.2, jitter=0.1, seed=2), {"function": "constant", "horizon": 0.2, "outputdim": 1},
+                  conf2d(precision="mixed"))]
+    elif case == "bary3d":
+        probs = [(cube_mesh(5, 0.1, jitter=0.1, seed=5), {"function": "constant3D", "horizon": 0.3, "outputdim": 1},
+                  conf3d(precision="mixed"))]
+    else:
+        probs = [(square_mesh(10, 0.2, jitter=0.1, seed=3),
+                  {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4},
+                  conf2d(rule="16", close="fractional", deg=3, precision="mixed"))]
+    s = nl.Session(probs)
+    try:
+        st0 = s.assemble()
+        ref = [s.download(i) for i in range(len(probs))]
+        for _ in range(3):
+            st = s.assemble(graph=True)
+            assert st["n_pairs"] == st0["n_pairs"] and st["nnz_structural"] == st0["nnz_structural"]
+            for i, B in enumerate(ref):
+                A = s.download(i)
+                assert same_pattern(A, B) and np.array_equal(A.data, B.data)
+    finally:
+        s.close()

@@ -34,10 +34,9 @@ import numpy as np
 
 METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel err"
 
-# DRAM traffic of one k_pass_mix2d launch (one color) of the default workload, from the ncu
-# capture summarised in profiles/ (read + write bytes; None when the workload differs from the
-# captured one).
-PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): None}
+# DRAM traffic (read + write bytes) of the one k_pass_mix2d launch of a C2 assembly, from the ncu
+# capture summarised in profiles/k_pass_mix2d_2d-constant.md; None for workloads not captured.
+PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): 11.90e9 + 4.22e9}
 
 
 def workload(args, precision):

@@ -52,28 +52,25 @@ __device__ __forceinline__ bool fin_triangle(F2 y, float ey, const F2 *P, const 
     return in;
 }
 
-// Polygon point bookkeeping: position, edge it lies on (-1: a vertex or a cap point), error of
-// its position across its edge line (rounding) and along it (root error, large near tangency).
-struct FPoly {
-    F2 R[9];
-    float eperp[9], ealong[9];
-    signed char edge[9];
-    int n;
-};
-
+// Polygon point bookkeeping: the positions go to the caller's array; the error bounds of a
+// point (across its edge line: rounding; along it: root error, large near tangency) are needed
+// only for the caps next to the last and the first point, so only those two are kept.
 struct FPt {
     F2 y;
     float eperp, ealong;
-    int edge;
 };
 
-__device__ __forceinline__ FPt fpt_of(const FPoly &Y, int i) {
-    return FPt{Y.R[i], Y.eperp[i], Y.ealong[i], (int)Y.edge[i]};
-}
+struct FPoly {
+    F2 *R;     // points, at most 9
+    int n;
+    FPt first, last;
+};
 
 __device__ __forceinline__ void fpush(FPoly &Y, const FPt &p, bool &amb) {
     if (Y.n >= 9) { amb = true; return; }
-    Y.R[Y.n] = p.y; Y.eperp[Y.n] = p.eperp; Y.ealong[Y.n] = p.ealong; Y.edge[Y.n] = (signed char)p.edge;
+    Y.R[Y.n] = p.y;
+    if (Y.n == 0) Y.first = p;
+    Y.last = p;
     Y.n++;
 }
 
@@ -97,7 +94,7 @@ __device__ __forceinline__ void fplace_cap(FPoly &Y, const FPt &a, const FPt &b,
     const F2 y = f2(m.x * s, m.y * s);
     const float em = 0.5f * (a.eperp + a.ealong + b.eperp + b.ealong);
     const float ey = delta * em * rsqrtf(mm) + em + 8.f * U32 * delta;
-    if (fin_triangle(y, ey, P, nu, amb, why)) fpush(Y, FPt{y, ey, 0.f, -1}, amb);
+    if (fin_triangle(y, ey, P, nu, amb, why)) fpush(Y, FPt{y, ey, 0.f}, amb);
 }
 
 // FP32 method_retriangulate with the triangle P given relative to the ball center. Returns the
@@ -106,6 +103,7 @@ __device__ __forceinline__ void fplace_cap(FPoly &Y, const FPt &a, const FPt &b,
 __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F2 *R, bool &amb,
                                               unsigned *why = nullptr) {
     FPoly Y;
+    Y.R = R;
     Y.n = 0;
     bool is_onEdge = false, is_firstPointLiesOnVertex = true;
     const F2 e1 = P[1] - P[0], e2 = P[2] - P[0];
@@ -126,7 +124,7 @@ __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F
         const float dp = dot(p, p);
         if (dp > sqlo && dp < sqhi) { amb = true; if (why) *why |= 2u; }
         if (dp <= sq) {
-            fpush(Y, FPt{p, 4.f * U32 * (fabsf(p.x) + fabsf(p.y)), 0.f, -1}, amb);
+            fpush(Y, FPt{p, 4.f * U32 * (fabsf(p.x) + fabsf(p.y)), 0.f}, amb);
             is_onEdge = false;
         }
         const float ab = dot(q, b), aa = dot(q, q), bb = dot(b, b);
@@ -161,23 +159,24 @@ __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F
             if (fabsf(lam2) <= MARG_L || fabsf(lam2 - 1.f) <= MARG_L) { amb = true; if (why) *why |= 16u; }
             if (lam1 >= 0.f && lam1 <= 1.f) {
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
-                const FPt y1{f2(fmaf(lam1, b.x, q.x), fmaf(lam1, b.y, q.y)), eperp, ealong, k};
-                if (is_onEdge && caps) fplace_cap(Y, fpt_of(Y, Y.n - 1), y1, sq, P, nu, orientation, amb, why);
+                const FPt y1{f2(fmaf(lam1, b.x, q.x), fmaf(lam1, b.y, q.y)), eperp, ealong};
+                if (is_onEdge && caps) fplace_cap(Y, Y.last, y1, sq, P, nu, orientation, amb, why);
                 fpush(Y, y1, amb);
                 is_onEdge = true;
             }
             if (lam2 >= 0.f && lam2 <= 1.f && v > 0.f) {
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
-                const FPt y2{f2(fmaf(lam2, b.x, q.x), fmaf(lam2, b.y, q.y)), eperp, ealong, k};
-                if (is_onEdge && caps) fplace_cap(Y, fpt_of(Y, Y.n - 1), y2, sq, P, nu, orientation, amb, why);
+                const FPt y2{f2(fmaf(lam2, b.x, q.x), fmaf(lam2, b.y, q.y)), eperp, ealong};
+                if (is_onEdge && caps) fplace_cap(Y, Y.last, y2, sq, P, nu, orientation, amb, why);
                 fpush(Y, y2, amb);
                 is_onEdge = true;
             }
         }
     }
-    if (is_onEdge && (!is_firstPointLiesOnVertex && Y.n > 1) && caps)
-        fplace_cap(Y, fpt_of(Y, Y.n - 1), fpt_of(Y, 0), sq, P, nu, orientation, amb, why);
-    for (int i = 0; i < Y.n; i++) R[i] = Y.R[i];
+    if (is_onEdge && (!is_firstPointLiesOnVertex && Y.n > 1) && caps) {
+        const FPt last = Y.last, first = Y.first;
+        fplace_cap(Y, last, first, sq, P, nu, orientation, amb, why);
+    }
     return Y.n;
 }
 

@@ -345,19 +345,34 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
             const long long lvl_end = qtail;
             const int method = (P.singular && level == 0) ? P.close : P.remote;
             int nbuf = 0;
+            // frontier groups of 32 elements; the next group's entries and adjacency ranges are
+            // loaded while the current one is expanded (entries before lvl_end are final)
+            long long beg_n = 0;
+            int deg_n = 0;
+            {
+                int sn = qhead + lane < lvl_end ? queue[qhead + lane] : -1;
+                if (sn < -1) sn = -sn - 2;   // label-0 bridge stored as -(e+2)
+                if (sn >= 0) { beg_n = a.xadj[sn]; deg_n = (int)(a.xadj[sn + 1] - beg_n); }
+            }
             for (long long g = qhead; g < lvl_end; g += 32) {
-                long long gi = g + lane;
-                int s = gi < lvl_end ? queue[gi] : -1;
-                if (s < -1) s = -s - 2;   // label-0 bridge stored as -(e+2)
-                long long beg = 0;
-                int deg = 0;
-                if (s >= 0) { beg = a.xadj[s]; deg = (int)(a.xadj[s + 1] - beg); }
+                const long long beg = beg_n;
+                const int deg = deg_n;
+                {
+                    const long long gi = g + 32 + lane;
+                    int sn = gi < lvl_end ? queue[gi] : -1;
+                    if (sn < -1) sn = -sn - 2;
+                    beg_n = 0;
+                    deg_n = 0;
+                    if (sn >= 0) { beg_n = a.xadj[sn]; deg_n = (int)(a.xadj[sn + 1] - beg_n); }
+                }
                 // each lane walks its own frontier element's neighbours (degrees are nearly
                 // uniform, so the lanes stay busy without a scan over the warp)
                 const int maxdeg = (int)__reduce_max_sync(FULL, (unsigned)deg);
+                int cand_next = deg > 0 ? a.adj[beg] : -1;   // the adjacency runs one step ahead
                 for (int jn = 0; jn < maxdeg; jn++) {
-                    int cand = -1;
-                    if (jn < deg) cand = a.adj[beg + jn];
+                    int cand = cand_next;
+                    cand_next = jn + 1 < deg ? a.adj[beg + jn + 1] : -1;
+                    const int lab = cand >= 0 ? a.labT[cand] : 1;   // before the visited store
                     // lanes holding the same candidate: the lowest one takes it, so the queue
                     // order (and every order derived from it) does not depend on atomic timing
                     const unsigned same = __match_any_sync(FULL, cand);
@@ -370,7 +385,7 @@ __global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
                         fresh = visited[cand - eoff] != stamp;
                         if (fresh) visited[cand - eoff] = stamp;
                     }
-                    const bool bridge = fresh && a.labT[cand] == 0;
+                    const bool bridge = fresh && lab == 0;
                     queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
                     // candidates to test are compacted, so the test runs on full warps
                     const bool totest = fresh && !bridge;

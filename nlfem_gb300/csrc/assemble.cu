@@ -514,6 +514,12 @@ struct RowArgs {
     const long long *rowptr;   // fill mode
     int *cols;                 // fill mode (null: count mode)
     int *rowcnt;               // count mode
+    // direct mode (bitmap kernel, pass 2): rows placed in scratch at an atomic cursor
+    int *scratch;
+    long long cap;             // scratch capacity (ints)
+    unsigned long long *cursor;
+    long long *rowoff;         // scratch offset of each row
+    int *ovf;                  // set when the scratch is too small
 };
 
 // One warp per row (vertex) u with label > 0: union of the vertices of every element that
@@ -579,7 +585,8 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long u = gw; u < a.nV; u += nw) {
         if (a.labV[u] <= 0) {
-            if (pass == 0 && lane == 0) a.rowcnt[u] = 0;
+            if (pass != 1 && lane == 0) a.rowcnt[u] = 0;
+            if (pass == 2 && lane == 0) a.rowoff[u] = 0;
             continue;
         }
         const ProbParams &P = a.probs[a.vprob[u]];
@@ -611,6 +618,38 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         __syncwarp();
         lo = __reduce_min_sync(FULL, lo);
         hi = __reduce_max_sync(FULL, hi);
+        if (pass == 2) {   // direct: count, take scratch space, write the sorted columns there
+            int cnt = 0;
+            if (hi >= 0)
+                for (int wi = (lo >> 5) + lane; wi <= (hi >> 5); wi += 32) cnt += __popc(bm[wi]);
+            cnt = warp_sum(cnt);
+            unsigned long long off = 0;
+            if (lane == 0) {
+                off = atomicAdd(a.cursor, (unsigned long long)cnt);
+                a.rowcnt[u] = cnt;
+                a.rowoff[u] = (long long)off;
+                if ((long long)off + cnt > a.cap) atomicOr(a.ovf, 1);
+            }
+            off = __shfl_sync(FULL, off, 0);
+            if (hi >= 0 && (long long)off + cnt <= a.cap) {
+                long long w = (long long)off;
+                for (int w0 = lo >> 5; w0 <= (hi >> 5); w0 += 32) {
+                    const int wi = w0 + lane;
+                    unsigned bits = wi <= (hi >> 5) ? bm[wi] : 0u;
+                    const int c = __popc(bits);
+                    const int incl = warp_incl_scan(c, lane);
+                    long long o = w + incl - c;
+                    while (bits) {
+                        const int b = __ffs(bits) - 1;
+                        a.scratch[o++] = voff + wi * 32 + b;
+                        bits &= bits - 1;
+                    }
+                    w += __shfl_sync(FULL, incl, 31);
+                }
+            }
+            __syncwarp();
+            continue;
+        }
         long long w = pass ? a.rowptr[u] : 0;
         if (hi >= 0) {
             for (int w0 = lo >> 5; w0 <= (hi >> 5); w0 += 32) {
@@ -631,6 +670,18 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         }
         if (pass == 0 && lane == 0) a.rowcnt[u] = (int)w;
         __syncwarp();
+    }
+}
+
+// Direct mode, second step: each row's columns from the scratch into CSR order (one warp per row).
+__global__ void k_row_copy(const long long *__restrict__ rowptr, const long long *__restrict__ rowoff,
+                           long long nV, const int *__restrict__ scratch, int *__restrict__ cols) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long u = gw; u < nV; u += nw) {
+        const long long b = rowptr[u], n = rowptr[u + 1] - b, o = rowoff[u];
+        for (long long i = lane; i < n; i += 32) cols[b + i] = scratch[o + i];
     }
 }
 

@@ -36,9 +36,11 @@ struct DevBuf {
     }
 };
 
-static int ensure(DevBuf &b, size_t bytes) {
+static int ensure(DevBuf &b, size_t bytes, bool no_grow) {
     if (bytes == 0) bytes = 16;
     if (bytes <= b.cap) return NLFEM_OK;
+    // a captured sequence cannot allocate; the run before the capture sizes every buffer
+    if (no_grow) return fail(NLFEM_ERR_CUDA, "internal: a buffer would grow during graph capture");
     b.release();
     size_t want = std::max(bytes, (size_t)(b.cap + b.cap / 4));
     cudaError_t e = cudaMalloc(&b.p, want);
@@ -55,7 +57,7 @@ static int ensure(DevBuf &b, size_t bytes) {
     b.cap = want;
     return NLFEM_OK;
 }
-#define ENS(buf, bytes) do { int r_ = ensure(buf, bytes); if (r_) return r_; } while (0)
+#define ENS(buf, bytes) do { int r_ = ensure(buf, bytes, S.replay); if (r_) return r_; } while (0)
 
 // ---------------------------------------------------------------- configuration parsing
 static int kernel_id(const char *s) {
@@ -276,6 +278,8 @@ struct Session {
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
     DevBuf out64a, out64b;
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
+    DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
+    long long pat_cap = 0;
     int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
     bool replay = false;
@@ -292,7 +296,7 @@ struct Session {
                          &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                          &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                          &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                         &hcap, &hptr, &htab, &tpos, &dslot};
+                         &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff};
         for (DevBuf *b : all) b->release();
         if (gexec) cudaGraphExecDestroy(gexec);
         if (st) {
@@ -730,11 +734,39 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     a.probs = S.prm.get<ProbParams>(); a.nV = nV;
     a.marks = nullptr; a.mstride = 0;
     a.rowptr = nullptr; a.cols = nullptr; a.rowcnt = S.rowcnt.get<int>();
+    a.scratch = nullptr; a.cap = 0; a.cursor = nullptr; a.rowoff = nullptr; a.ovf = nullptr;
     const size_t smem = (size_t)words * 4 * (threads / 32);
     CK(cudaFuncSetAttribute(k_row_pattern_bm<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pattern_bm<DIM>, threads, smem));
     const unsigned grid = (unsigned)(S.nSM * std::max(per_sm, 1));
+    if (S.pat_cap > 0) {
+        // single bitmap pass: rows go to a scratch of the previous assembly's size, then a copy
+        // puts them in CSR order; a scratch overflow falls back to the two passes below
+        ENS(S.rowoff, sizeof(long long) * (nV + 1));
+        ENS(S.pscratch, sizeof(int) * (S.pat_cap + 1));
+        unsigned long long *cursor = S.counters.get<unsigned long long>() + 11;
+        CK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), S.st));
+        CK(cudaMemsetAsync(S.err.get<int>() + 6, 0, sizeof(int), S.st));
+        a.scratch = S.pscratch.get<int>(); a.cap = S.pat_cap; a.cursor = cursor;
+        a.rowoff = S.rowoff.get<long long>(); a.ovf = S.err.get<int>() + 6;
+        k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 2, words); ++S.nlaunch;
+        int r = scan_excl<int>(S, S.rowcnt.get<int>(), nV, S.rowptr.get<long long>());
+        if (r) return r;
+        int ovf = 0;
+        if ((r = d2h(S, &ovf, S.err.get<int>() + 6, 1))) return r;
+        if (!ovf) {
+            if ((r = d2h(S, &S.nnz_struct, S.rowptr.get<long long>() + nV, 1))) return r;
+            ENS(S.cols, sizeof(int) * (S.nnz_struct + 1));
+            k_row_copy<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.rowoff.get<long long>(), nV,
+                                                    S.pscratch.get<int>(), S.cols.get<int>()); ++S.nlaunch;
+            CK(cudaGetLastError());
+            S.stats.nnz_structural = (long)S.nnz_struct;
+            if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
+            return NLFEM_OK;
+        }
+        a.scratch = nullptr; a.cap = 0; a.cursor = nullptr; a.rowoff = nullptr; a.ovf = nullptr;
+    }
     k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 0, words); ++S.nlaunch;
     int r = scan_excl<int>(S, S.rowcnt.get<int>(), nV, S.rowptr.get<long long>());
     if (r) return r;
@@ -745,6 +777,9 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(a, 1, words); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
+    S.pat_cap = S.nnz_struct;   // the next assembly builds the pattern in one pass
+    ENS(S.rowoff, sizeof(long long) * (nV + 1));
+    ENS(S.pscratch, sizeof(int) * (S.pat_cap + 1));
     if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
@@ -1089,9 +1124,9 @@ static int run_system_graph_t(Session &S) {
         const long long launches = S.nlaunch;
         CK(cudaGraphLaunch(S.gexec, S.st));
         CK(cudaStreamSynchronize(S.st));
-        int he[6];
-        if ((r = d2h(S, he, S.err.get<int>(), 6))) return r;
-        if (!he[0] && !he[1] && !he[5]) {
+        int he[7];
+        if ((r = d2h(S, he, S.err.get<int>(), 7))) return r;
+        if (!he[0] && !he[1] && !he[5] && !he[6]) {
             S.nlaunch = launches;
             return run_system_post(S);
         }

@@ -426,6 +426,10 @@ def test_session_graph_replay_bitwise(nl, case):
     try:
         st0 = s.assemble()
         ref = [s.download(i) for i in range(len(probs))]
+        s.assemble()   # a repeated assembly builds the pattern in one pass (scratch sized by the first)
+        for i, B in enumerate(ref):
+            A = s.download(i)
+            assert same_pattern(A, B) and np.array_equal(A.data, B.data)
         for _ in range(3):
             st = s.assemble(graph=True)
             assert st["n_pairs"] == st0["n_pairs"] and st["nnz_structural"] == st0["nnz_structural"]
@@ -434,3 +438,13 @@ def test_session_graph_replay_bitwise(nl, case):
                 assert same_pattern(A, B) and np.array_equal(A.data, B.data)
     finally:
         s.close()
+    # a session whose first call already asks for the graph (capture right after the first run)
+    s2 = nl.Session(probs)
+    try:
+        for _ in range(3):
+            s2.assemble(graph=True)
+            for i, B in enumerate(ref):
+                A = s2.download(i)
+                assert same_pattern(A, B) and np.array_equal(A.data, B.data)
+    finally:
+        s2.close()

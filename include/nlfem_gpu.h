@@ -75,6 +75,16 @@ typedef struct nlfem_csr {
     double *values; /* nnz */
 } nlfem_csr;
 
+/* The same with 32-bit row pointers and columns (matrices below 2^31 entries): the index type
+ * scipy uses for such matrices, so the Python layer wraps the arrays without copying. */
+typedef struct nlfem_csr32 {
+    long K;
+    long nnz;
+    int *indptr;    /* K+1 */
+    int *indices;   /* nnz, ascending within a row */
+    double *values; /* nnz */
+} nlfem_csr32;
+
 /* Run statistics of the last assembly on this thread. */
 typedef struct nlfem_stats {
     long n_pairs;        /* interacting ordered element pairs (contributing integrate() calls) */
@@ -99,6 +109,13 @@ int nlfem_load_vector(const nlfem_problem *prob, double *fd);
 /* Many independent problems in one pass; outs[i] receives problem i's matrix. */
 int nlfem_stiffness_batch(const nlfem_problem *probs, int n, nlfem_csr *outs);
 void nlfem_csr_free(nlfem_csr *m);
+/* 32-bit variants (NLFEM_ERR_UNSUPPORTED when a matrix has 2^31 entries or more). */
+int nlfem_stiffness_matrix32(const nlfem_problem *prob, nlfem_csr32 *out);
+int nlfem_stiffness_batch32(const nlfem_problem *probs, int n, nlfem_csr32 *outs);
+void nlfem_csr32_free(nlfem_csr32 *m);
+/* The one-shot calls keep the device buffers of their last assembly for the next call on the
+ * same device (no counterpart in the reference); this frees them. */
+void nlfem_cache_release(void);
 
 /* Device-resident sessions: upload once, assemble many times (benchmarks, repeated solves). */
 typedef struct nlfem_session nlfem_session;
@@ -109,6 +126,7 @@ int nlfem_session_assemble(nlfem_session *s);            /* inputs already in HB
  * trips). Mixed-precision sessions only; other sessions assemble normally. */
 int nlfem_session_assemble_graph(nlfem_session *s);
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out);
+int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out);
 void nlfem_session_destroy(nlfem_session *s);
 
 /* The interacting pairs (aT, bT) of the BFS, sorted by (aT, bT). Free *pairs with free(). */

@@ -41,6 +41,11 @@ class CSR(ctypes.Structure):
                 ("indices", _lp), ("values", _dp)]
 
 
+class CSR32(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_long), ("nnz", ctypes.c_long), ("indptr", _ip),
+                ("indices", _ip), ("values", _dp)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_long), ("n_candidates", ctypes.c_long),
                 ("n_close", ctypes.c_long), ("nnz_structural", ctypes.c_long),
@@ -94,6 +99,14 @@ def load():
     l.nlfem_toPhys.argtypes = [_dp, _dp, ctypes.c_int, _dp]
     l.nlfem_solve2x2.argtypes = [_dp, _dp, _dp]
     l.nlfem_measure_peaks.argtypes = [_dp, _dp]
+    C32 = ctypes.POINTER(CSR32)
+    l.nlfem_stiffness_matrix32.argtypes = [P, C32]
+    l.nlfem_stiffness_batch32.argtypes = [P, ctypes.c_int, C32]
+    l.nlfem_csr32_free.argtypes = [C32]
+    l.nlfem_csr32_free.restype = None
+    l.nlfem_session_download32.argtypes = [ctypes.c_void_p, ctypes.c_int, C32]
+    l.nlfem_cache_release.argtypes = []
+    l.nlfem_cache_release.restype = None
     vp = ctypes.c_void_p   # device pointers and the stream are passed as raw addresses
     l.nlfem_load_vector_noalloc.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, vp, vp, vp, vp,
                                             _dp, ctypes.c_int, _dp, ctypes.c_char_p, vp, vp]
@@ -120,4 +133,6 @@ EXPORTED = [
     "nlfem_pair_list", "nlfem_pair_blocks", "nlfem_method_retriangulate",
     "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
     "nlfem_par_assemble", "nlfem_load_vector_noalloc", "nlfem_measure_peaks",
+    "nlfem_stiffness_matrix32", "nlfem_stiffness_batch32", "nlfem_csr32_free", "nlfem_session_download32",
+    "nlfem_cache_release",
 ]

@@ -202,6 +202,7 @@ struct ProbParams {
     double fx_unit;   // value of one unit of the 64-bit fixed-point CSR sums: 2^fx_ue
     float fx_mul;     // 2^-fx_ue
     int fx_ue;        // scale_exp + guard bits - 62
+    double el;        // mean element measure (bounding box / nE), for capacity estimates
 };
 
 // FP64 kernel value k(x, y) (model.cpp:25-28, 52-60, 62-65, 126-138)

@@ -199,6 +199,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     double vol = 1;
     for (int j = 0; j < p.dim; j++) vol *= std::max(hi[j] - lo[j], 1e-300);
     const double el = vol / (double)p.nE;
+    P.el = el;
     double mag;
     if (system) {
         const double h = pow(el, 1.0 / p.dim);
@@ -289,15 +290,18 @@ struct Session {
     long long P = 0, nnz_struct = 0, nnz = 0;
     long long nlaunch = 0;   // kernels launched by the current assembly
     nlfem_stats stats;
+    // every device buffer of the session, in a fixed order
+    std::vector<DevBuf *> buffers() {
+        return {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
+                &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited,
+                &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
+                &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
+                &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
+                &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
+                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff};
+    }
     ~Session() {
-        DevBuf *all[] = {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
-                         &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited,
-                         &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
-                         &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
-                         &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
-                         &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                         &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff};
-        for (DevBuf *b : all) b->release();
+        for (DevBuf *b : buffers()) b->release();
         if (gexec) cudaGraphExecDestroy(gexec);
         if (st) {
             for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
@@ -549,7 +553,18 @@ static int run_bfs(Session &S) {
     const int nblocks = S.nSM * std::max(per_sm, 1);
     const int nwarps = nblocks * BFS_WARPS;
     if (S.qcap == 0) S.qcap = std::min<long long>(S.maxNE + 1, 8192);
-    if (S.pool_cap == 0) S.pool_cap = std::max<long long>(nE * 64, 1 << 20);
+    if (S.pool_cap == 0) {
+        // expected pairs: per outer element, the elements meeting a ball of radius delta + 2h
+        // (h the mean element size), with 10% headroom; a short pool only costs a retry
+        double est = 0;
+        for (const ProbParams &q : S.hprm) {
+            const double h = S.dim == 2 ? sqrt(2.0 * q.el) : cbrt(6.0 * q.el);
+            const double r = q.delta + 2.0 * h;
+            const double ball = S.dim == 2 ? M_PI * r * r : 4.0 / 3.0 * M_PI * r * r * r;
+            est += (double)q.nE * std::min((double)q.nE, ball / std::max(q.el, 1e-300) + 16.0);
+        }
+        S.pool_cap = std::max<long long>((long long)(1.1 * est), 1 << 20);
+    }
     ENS(S.visited, sizeof(unsigned) * (size_t)nwarps * S.maxNE);
     ENS(S.seg_start, sizeof(long long) * (nE + 1));
     ENS(S.seg_cnt, sizeof(int) * (nE + 1));
@@ -1186,6 +1201,48 @@ __global__ void k_export(const long long *__restrict__ fptr, const int *__restri
     for (long long j = i; j < n; j += (long long)gridDim.x * blockDim.x) indices[j] = (long long)fcols[base + j] - c0;
 }
 
+// 32-bit CSR of problem i (nnz below 2^31): row pointers rebased to the problem, columns local.
+__global__ void k_export32(const long long *__restrict__ fptr, const int *__restrict__ fcols, long long r0,
+                           long long nrows, int c0, int *__restrict__ indptr, int *__restrict__ indices) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long base = fptr[r0];
+    if (i <= nrows) indptr[i] = (int)(fptr[r0 + i] - base);
+    const long long n = fptr[r0 + nrows] - base;
+    for (long long j = i; j < n; j += (long long)gridDim.x * blockDim.x) indices[j] = fcols[base + j] - c0;
+}
+
+static int download32(Session &S, int i, nlfem_csr32 *out) {
+    const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
+    long long b[2];
+    int r = d2h(S, &b[0], S.fptr.get<long long>() + r0, 1);
+    if (r) return r;
+    r = d2h(S, &b[1], S.fptr.get<long long>() + r0 + nrows, 1);
+    if (r) return r;
+    const long long nnz = b[1] - b[0];
+    if (nnz > 0x7fffffffLL || nrows > 0x7fffffffLL)
+        return fail(NLFEM_ERR_UNSUPPORTED, "matrix too large for 32-bit indices");
+    ENS(S.out64a, sizeof(int) * (nrows + 1));
+    ENS(S.out64b, sizeof(int) * (nnz + 1));
+    k_export32<<<grid_for(std::max(nrows + 1, nnz), 256), 256, 0, S.st>>>(S.fptr.get<long long>(), S.fcols.get<int>(), r0, nrows, (int)r0, S.out64a.get<int>(), S.out64b.get<int>()); ++S.nlaunch;
+    CK(cudaGetLastError());
+    out->K = (long)nrows;
+    out->nnz = (long)nnz;
+    out->indptr = (int *)malloc(sizeof(int) * (nrows + 1));
+    out->indices = (int *)malloc(sizeof(int) * (nnz ? nnz : 1));
+    out->values = (double *)malloc(sizeof(double) * (nnz ? nnz : 1));
+    if (!out->indptr || !out->indices || !out->values) {
+        nlfem_csr32_free(out);
+        return fail(NLFEM_ERR_NOMEM, "host allocation failed");
+    }
+    CK(cudaMemcpyAsync(out->indptr, S.out64a.p, sizeof(int) * (nrows + 1), cudaMemcpyDeviceToHost, S.st));
+    if (nnz) {
+        CK(cudaMemcpyAsync(out->indices, S.out64b.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost, S.st));
+        CK(cudaMemcpyAsync(out->values, S.fvals.get<double>() + b[0], sizeof(double) * nnz, cudaMemcpyDeviceToHost, S.st));
+    }
+    CK(cudaStreamSynchronize(S.st));
+    return NLFEM_OK;
+}
+
 static int download(Session &S, int i, nlfem_csr *out) {
     const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
     long long b[2];
@@ -1241,6 +1298,37 @@ struct nlfem_session {
     std::vector<nlfem_problem> probs;
 };
 
+// Device buffers of the last one-shot assembly (nlfem_stiffness_matrix / _batch), kept for the
+// next one on the same device so repeated calls do not allocate: buffers only grow, and every
+// stage initialises what it reads. nlfem_cache_release frees them.
+namespace nlg {
+static std::mutex g_cache_mu;
+static Session *g_cache = nullptr;
+static int g_cache_dev = -1;
+
+static void cache_take(Session &S) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return; }
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    if (!g_cache || g_cache_dev != dev) return;
+    std::vector<DevBuf *> from = g_cache->buffers(), to = S.buffers();
+    for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
+    delete g_cache;
+    g_cache = nullptr;
+}
+
+static void cache_give(Session &S) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return; }
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    if (g_cache) return;   // another call's buffers are cached already: these are freed
+    g_cache = new Session();
+    g_cache_dev = dev;
+    std::vector<DevBuf *> from = S.buffers(), to = g_cache->buffers();
+    for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
+}
+}  // namespace nlg
+
 extern "C" {
 
 const char *nlfem_last_error(void) { return g_err.c_str(); }
@@ -1261,6 +1349,17 @@ void nlfem_csr_free(nlfem_csr *m) {
     if (!m) return;
     free(m->indptr); free(m->indices); free(m->values);
     m->indptr = nullptr; m->indices = nullptr; m->values = nullptr;
+}
+
+void nlfem_csr32_free(nlfem_csr32 *m) {
+    if (!m) return;
+    free(m->indptr); free(m->indices); free(m->values);
+    m->indptr = nullptr; m->indices = nullptr; m->values = nullptr;
+}
+
+int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out) {
+    if (!s || !out || i < 0 || i >= s->S.nProb) return fail(NLFEM_ERR_INVALID, "bad session download");
+    return download32(s->S, i, out);
 }
 
 int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out) {
@@ -1294,15 +1393,61 @@ int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out) {
 
 void nlfem_session_destroy(nlfem_session *s) { delete s; }
 
+// One-shot session on the cached buffers of the previous one-shot call.
+static int session_create_cached(const nlfem_problem *probs, int n, nlfem_session **out) {
+    if (!probs || n <= 0 || !out) return fail(NLFEM_ERR_INVALID, "no problems");
+    int r = device_ok();
+    if (r) return r;
+    nlfem_session *s = new nlfem_session();
+    cache_take(s->S);
+    s->probs.assign(probs, probs + n);
+    r = session_init(s->S, probs, n, true);
+    if (!r) r = session_upload(s->S, probs);
+    if (r) { cache_give(s->S); delete s; return r; }
+    *out = s;
+    return NLFEM_OK;
+}
+
+static void session_destroy_cached(nlfem_session *s) {
+    if (!s) return;
+    cudaStreamSynchronize(s->S.st);
+    cudaGetLastError();
+    cache_give(s->S);
+    delete s;
+}
+
 int nlfem_stiffness_batch(const nlfem_problem *probs, int n, nlfem_csr *outs) {
     if (!outs) return fail(NLFEM_ERR_INVALID, "null output");
     nlfem_session *s = nullptr;
-    int r = nlfem_session_create(probs, n, &s);
+    int r = session_create_cached(probs, n, &s);
     if (r) return r;
     r = run_system(s->S);
     for (int i = 0; !r && i < n; i++) r = download(s->S, i, &outs[i]);
-    nlfem_session_destroy(s);
+    session_destroy_cached(s);
     return r;
+}
+
+int nlfem_stiffness_batch32(const nlfem_problem *probs, int n, nlfem_csr32 *outs) {
+    if (!outs) return fail(NLFEM_ERR_INVALID, "null output");
+    nlfem_session *s = nullptr;
+    int r = session_create_cached(probs, n, &s);
+    if (r) return r;
+    r = run_system(s->S);
+    for (int i = 0; !r && i < n; i++) r = download32(s->S, i, &outs[i]);
+    if (r)
+        for (int i = 0; i < n; i++) nlfem_csr32_free(&outs[i]);
+    session_destroy_cached(s);
+    return r;
+}
+
+int nlfem_stiffness_matrix32(const nlfem_problem *prob, nlfem_csr32 *out) {
+    return nlfem_stiffness_batch32(prob, 1, out);
+}
+
+void nlfem_cache_release(void) {
+    std::lock_guard<std::mutex> g(g_cache_mu);
+    delete g_cache;
+    g_cache = nullptr;
 }
 
 int nlfem_stiffness_matrix(const nlfem_problem *prob, nlfem_csr *out) {

@@ -170,6 +170,37 @@ def _csr_to_scipy(m):
     return sp.csr_matrix((values, indices, indptr), shape=(K, K))
 
 
+class _CSR32Owner:
+    """Keeps the library's CSR arrays alive until the numpy views on them are collected."""
+
+    def __init__(self, lib, m):
+        self.lib, self.m = lib, m
+
+    def __del__(self):
+        try:
+            self.lib.nlfem_csr32_free(ctypes.byref(self.m))
+        except Exception:
+            pass
+
+
+def _view(ptr, n, ctype, dtype, owner):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    buf = (ctype * n).from_address(ctypes.cast(ptr, ctypes.c_void_p).value)
+    buf._owner = owner   # the array -> buffer -> owner chain frees the memory with the last view
+    return np.frombuffer(buf, dtype=dtype)
+
+
+def _csr32_to_scipy(lib, m):
+    """scipy CSR over the library's 32-bit arrays, without copying them."""
+    owner = _CSR32Owner(lib, m)
+    K, nnz = int(m.K), int(m.nnz)
+    indptr = _view(m.indptr, K + 1, ctypes.c_int, np.int32, owner)
+    indices = _view(m.indices, nnz, ctypes.c_int, np.int32, owner)
+    values = _view(m.values, nnz, ctypes.c_double, np.float64, owner)
+    return sp.csr_matrix((values, indices, indptr), shape=(K, K), copy=False)
+
+
 # ---------------------------------------------------------------- public API
 def stiffnessMatrix(mesh, kernel, configuration):
     """Stiffness matrix of the nonlocal operator on the mesh (nlfem.pyx:128-274), on the GPU."""
@@ -177,12 +208,19 @@ def stiffnessMatrix(mesh, kernel, configuration):
         raise ValueError("The output dimension of the mesh has to be equal to the output dimension of the kernel.")
     lib = _lib.load()
     p = _Problem(mesh, kernel, configuration, system=True)
-    out = _lib.CSR()
-    _lib.check(lib.nlfem_stiffness_matrix(ctypes.byref(p.c), ctypes.byref(out)))
-    try:
-        A = _csr_to_scipy(out)
-    finally:
-        lib.nlfem_csr_free(ctypes.byref(out))
+    out32 = _lib.CSR32()
+    code = lib.nlfem_stiffness_matrix32(ctypes.byref(p.c), ctypes.byref(out32))
+    if code == 0:
+        A = _csr32_to_scipy(lib, out32)
+    else:
+        if code != 4:   # NLFEM_ERR_UNSUPPORTED: 2^31 entries or more, 64-bit indices below
+            _lib.check(code)
+        out = _lib.CSR()
+        _lib.check(lib.nlfem_stiffness_matrix(ctypes.byref(p.c), ctypes.byref(out)))
+        try:
+            A = _csr_to_scipy(out)
+        finally:
+            lib.nlfem_csr_free(ctypes.byref(out))
     path = configuration.get("savePath")
     if path:
         write_arma_spMat(path, A)
@@ -206,6 +244,17 @@ def stiffnessMatrix_batch(problems):
     lib = _lib.load()
     ps = [_Problem(m, k, c, system=True) for (m, k, c) in problems]
     arr = (_lib.Problem * len(ps))(*[p.c for p in ps])
+    outs32 = (_lib.CSR32 * len(ps))()
+    code = lib.nlfem_stiffness_batch32(arr, len(ps), outs32)
+    if code == 0:
+        res = []
+        for i in range(len(ps)):
+            m = _lib.CSR32()
+            ctypes.pointer(m)[0] = outs32[i]
+            res.append(_csr32_to_scipy(lib, m))
+        return res
+    if code != 4:
+        _lib.check(code)
     outs = (_lib.CSR * len(ps))()
     _lib.check(lib.nlfem_stiffness_batch(arr, len(ps), outs))
     res = []
@@ -234,6 +283,12 @@ class Session:
         return _lib.stats()
 
     def download(self, i=0):
+        out32 = _lib.CSR32()
+        code = self.lib.nlfem_session_download32(self.h, i, ctypes.byref(out32))
+        if code == 0:
+            return _csr32_to_scipy(self.lib, out32)
+        if code != 4:
+            _lib.check(code)
         out = _lib.CSR()
         _lib.check(self.lib.nlfem_session_download(self.h, i, ctypes.byref(out)))
         try:

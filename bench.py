@@ -174,11 +174,27 @@ def algorithmic_flops(st, conf, kernel, dim=2):
       weight 2, innerLocal 2, innerNonloc 8).
     n_subtri counts each (pair, outer point, sub-triangle) unit once (for baryCenter: each
     (pair, outer point) whose ball contains the barycenter). Close pairs of the singular kernel
-    (FP64 Duffy rules) are not included."""
+    (FP64 Duffy rules) are not included.
+
+    Constant kernels ("constant", "constant3D") take closed forms on the mixed path, and the model
+    then counts those instead of the inner-point loops (the same sums, fewer operations):
+      retriangulate, per pair 12; (pair, outer point) 30 (class test) + 57 (fold); inside item 10
+      (the element's precomputed sums times kc |b|); cut item 133 (polygon) + 26 (basis at the
+      first two points, the ten results); cut sub-triangle 11 + 13 (basis at its third point) + 60
+      (moment sums);
+      baryCenter, per (pair, outer point) 64; item 5.
+    Those counts need the item classes (n_items_in / n_items_cut)."""
     nPx = len(conf["quadrature"]["outer"]["weights"])
     nPy = len(conf["quadrature"]["inner"]["weights"])
+    const = kernel["function"] in ("constant", "constant3D") and conf.get("precision") == "mixed"
     if conf["approxBalls"]["method"] == "baryCenter":
+        if const:
+            return st["n_pairs"] * nPx * 64 + st["n_items_in"] * 5
         return st["n_pairs"] * nPx * 64 + st["n_subtri"] * nPy * 30
+    if const:
+        n_in, n_cut = st["n_items_in"], st["n_items_cut"]
+        sub_cut = st["n_subtri"] - n_in
+        return st["n_pairs"] * (12 + nPx * 87) + n_in * 10 + n_cut * (133 + 26) + sub_cut * 84
     kf = {"constant": 0, "parabola": 7, "fractional": 0, "mixed": 3.5}.get(kernel["function"], 0)
     return st["n_pairs"] * (12 + nPx * 198) + st["n_subtri"] * (11 + nPy * (51 + kf))
 
@@ -363,8 +379,9 @@ def run_gpu(args, rank=0, world=1, dist=None):
         "roofline": {"bound": "fp32", "kernel": kname,
                      "achieved": achieved, "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
                      "traffic": PASS_TRAFFIC_BYTES.get((args.workload, extra.get("n"), extra.get("delta"))),
-                     "note": "achieved = algorithmic flops of the reference algorithm for the step (FLOP model in "
-                             "bench.algorithmic_flops; FP64 close pairs not counted) / device time of the "
+                     "note": "achieved = flops of the algorithm that ran for the step (FLOP model in "
+                             "bench.algorithmic_flops: the reference's inner-point loops, or their closed forms "
+                             "for constant kernels; FP64 close pairs not counted) / device time of the "
                              "quadrature phase; peak = FP32 FMA throughput measured in this run (of measured); "
                              "CUDA-core bound path with no GEMM-shaped work, so neither the tensor-core nor the "
                              "HBM peak applies"},

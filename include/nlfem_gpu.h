@@ -96,6 +96,9 @@ typedef struct nlfem_stats {
     double ms_total;     /* device time of the assembly (CUDA events) */
     double ms_bfs, ms_pattern, ms_quad, ms_finish;
     long n_launches;     /* kernels the library launched for the assembly */
+    long n_items_in;     /* one-sided mixed passes: (pair, outer point) items whose ball holds the
+                            inner element (retriangulate) or its barycenter (baryCenter) */
+    long n_items_cut;    /* one-sided mixed retriangulate pass: items whose ball cuts the element */
 } nlfem_stats;
 
 const char *nlfem_last_error(void);

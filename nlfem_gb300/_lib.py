@@ -52,7 +52,8 @@ class Stats(ctypes.Structure):
                 ("n_subtri", ctypes.c_long), ("n_ambiguous", ctypes.c_long),
                 ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double),
                 ("ms_pattern", ctypes.c_double), ("ms_quad", ctypes.c_double),
-                ("ms_finish", ctypes.c_double), ("n_launches", ctypes.c_long)]
+                ("ms_finish", ctypes.c_double), ("n_launches", ctypes.c_long),
+                ("n_items_in", ctypes.c_long), ("n_items_cut", ctypes.c_long)]
 
 
 class NlfemError(RuntimeError):

@@ -134,6 +134,7 @@ struct PassArgs {
     int *err;                   // [3] slot missing
     unsigned long long *n_subtri, *n_amb;
     unsigned long long *n_close;   // pairs integrated with the close-pair rule (from closebuf)
+    unsigned long long *n_in, *n_cut;   // one-sided passes: (pair, outer point) items by class
     unsigned char *touched;     // mixed precision: slots that received a contribution
 };
 
@@ -253,6 +254,11 @@ struct PassRule {
     float cy[MAXQ * 4];     // dy_i * psi_a (P_i)
     float dxf[MAXQ];
     float pyf[MAXQ * 3];    // inner points P_i (FP32, any dimension)
+    // Constant kernels: the inner rule's sums over a whole element, sum_i dy_i * (1, psi_a,
+    // psi_a psi_b (upper triangle)), and (2D) its moments sum_i dy_i * (1, px, py, px^2, px py,
+    // py^2) over the reference triangle.
+    float insum[1 + 4 + 10];
+    float mom[6];
 };
 
 

@@ -56,7 +56,9 @@ __device__ __forceinline__ float kernel_f32_r2(const ProbParams &P, float r2) {
     }
 }
 
-template <int DIM>
+// CK: every problem of the launch has a constant kernel; an item's sums over the full inner
+// element are then kc |b| times the rule's precomputed element sums.
+template <int DIM, bool CK>
 __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rule, PassRule pr) {
     constexpr int dV = DIM + 1, NS = dV * (dV + 1) / 2, RN = DIM + 2;
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
     BaryEntry<DIM> *slist = reinterpret_cast<BaryEntry<DIM> *>(res);
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
-    unsigned nsub = 0, namb = 0;
+    unsigned nsub = 0, namb = 0, nitin = 0;
     unsigned char mycls[MAXQ];
     for (;;) {
         int idx = 0;
@@ -138,6 +140,12 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             // owner: which outer points see the partner's barycenter inside the ball
             bool have_b64 = false;
             double b64[DIM];
+            float inv[RN];   // constant kernel: an item's sums
+            if (CK) {
+                const float kr = P.kc_f * W.prt[lane];
+#pragma unroll
+                for (int q = 0; q < RN; q++) inv[q] = kr * pr.insum[q];
+            }
             for (int k = 0; k < nPx; k++) {
                 unsigned char c = 0;
                 if (act) {
@@ -155,12 +163,19 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                     }
                 }
                 mycls[k] = c;
+                nitin += c;
                 float *rr = &res[(lane * nPx + k) * RN];
+                if (CK && c) {
+                    nsub++;
 #pragma unroll
-                for (int q = 0; q < RN; q++) rr[q] = 0.f;
+                    for (int q = 0; q < RN; q++) rr[q] = inv[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < RN; q++) rr[q] = 0.f;
+                }
             }
             __syncwarp();
-            const int nin = build_list(mycls, nPx, 1, lst);
+            const int nin = CK ? 0 : build_list(mycls, nPx, 1, lst);
             for (int c0 = 0; c0 < nin; c0 += 32) {
                 if (c0 + lane < nin) {
                     const int it = lst[c0 + lane];
@@ -309,9 +324,11 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
     }
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
+    nitin = warp_sum(nitin);
     if (lane == 0) {
         if (nsub && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)nsub);
         if (namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
+        if (nitin && a.n_in) atomicAdd(a.n_in, (unsigned long long)nitin);
     }
 }
 

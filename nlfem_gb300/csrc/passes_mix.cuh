@@ -126,6 +126,70 @@ __device__ __forceinline__ void item_cut(const ProbParams &P, const Rule &rule, 
     for (int ab = 0; ab < 6; ab++) res[4 + ab] = lp[ab];
 }
 
+// Inner sums of one "cut" item for a constant kernel. The kernel weight of every inner point is
+// kc |S| dy_i, and the basis functions of b are affine, so on a fan sub-triangle S = (A, B, C)
+// psi_a(y_i) = psi_a(A) + (psi_a(B) - psi_a(A)) px_i + (psi_a(C) - psi_a(A)) py_i, and the rule's
+// sums over S follow from its moments m = sum_i dy_i (1, px, py, px^2, px py, py^2):
+//   sum_i dy_i psi_a = al_a m0 + be_a mx + ga_a my,
+//   sum_i dy_i psi_a psi_b = al_a t0_b + be_a t1_b + ga_a t2_b  (t_b the first sums of psi_b with
+//   weights (1, px, py)).
+// This equals the quadrature sum of the general item for any rule. The basis values come from the
+// polygon's points (one evaluation per point instead of per inner point), and every sum stays in
+// the basis functions' own range, so no cancellation enters where a basis function is small.
+__device__ __forceinline__ void item_cut_const(const ProbParams &P, const PassRule &pr, const float *pc, F2 x,
+                                               const double *x64, const double *Eb64, float *res,
+                                               unsigned &nsub, unsigned &namb) {
+    const F2 Q[3] = {f2(pc[0] - x.x, pc[1] - x.y), f2(pc[2] - x.x, pc[3] - x.y), f2(pc[4] - x.x, pc[5] - x.y)};
+    const F2 e1 = Q[1] - Q[0], e2 = Q[2] - Q[0];
+    const float idet = 1.f / (e1.x * e2.y - e1.y * e2.x);
+    F2 R[9];
+    const int n = cut_polygon(Q, P.sqdelta_f, P, x64, Eb64, R, namb);
+    const float m0 = pr.mom[0], mx = pr.mom[1], my = pr.mom[2], mxx = pr.mom[3], mxy = pr.mom[4], myy = pr.mom[5];
+    auto basis = [&](F2 y, float *l) {   // psi_0..2 of b at y (as the general item evaluates them)
+        const float dxr = y.x - Q[0].x, dyr = y.y - Q[0].y;
+        l[1] = (e2.y * dxr - e2.x * dyr) * idet;
+        l[2] = (e1.x * dyr - e1.y * dxr) * idet;
+        l[0] = 1.f - l[1] - l[2];
+    };
+    float S0 = 0.f, S1[3] = {0.f, 0.f, 0.f}, S2[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float la[3], lb[3], lc[3];
+    if (n >= 3) {
+        basis(R[0], la);
+        basis(R[1], lb);
+    }
+    for (int r = 0; r + 2 < n; r++) {
+        nsub++;
+        const F2 B = R[r + 1] - R[0], C = R[r + 2] - R[0];
+        const float rT = fabsf(B.x * C.y - B.y * C.x);
+        basis(R[r + 2], lc);
+        float t0[3], t1[3], t2[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
+            t0[q] = fmaf(al, m0, fmaf(be, mx, ga * my));
+            t1[q] = fmaf(al, mx, fmaf(be, mxx, ga * mxy));
+            t2[q] = fmaf(al, my, fmaf(be, mxy, ga * myy));
+        }
+        S0 = fmaf(rT, m0, S0);
+        int t = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            S1[q] = fmaf(rT, t0[q], S1[q]);
+            const float al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
+#pragma unroll
+            for (int q2 = q; q2 < 3; q2++, t++) S2[t] = fmaf(rT, fmaf(al, t0[q2], fmaf(be, t1[q2], ga * t2[q2])), S2[t]);
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++) lb[q] = lc[q];
+    }
+    const float kc = P.kc_f;
+    res[0] = kc * S0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) res[1 + q] = kc * S1[q];
+#pragma unroll
+    for (int q = 0; q < 6; q++) res[4 + q] = kc * S2[q];
+}
+
 // Appends this lane's items of class cls (one per outer point k with that class) to list, in
 // (k, lane) order; returns the list length (uniform).
 __device__ __forceinline__ int build_list(const unsigned char *mycls, int nPx, int cls,
@@ -184,6 +248,9 @@ __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }
 
+// CK: every problem of the launch has a constant kernel; inside items then take the rule's
+// precomputed element sums and cut items the moment form (item_cut_const).
+template <bool CK>
 __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const PassArgs &a = ma.p;
@@ -197,7 +264,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
     ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
-    unsigned nsub = 0, namb = 0, nclose = 0;
+    unsigned nsub = 0, namb = 0, nclose = 0, nitin = 0, nitcut = 0;
     unsigned char mycls[MAXQ];
     for (;;) {
         int idx = 0;
@@ -269,6 +336,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 for (int q = 0; q < 9; q++) cp_async4(&W.ds[lane][q], &sm.dslot[(long long)part * 9 + q]);
             }
             cp_async_commit();
+            float inv[RES_N];   // constant kernel: an inside item's sums
+            if (CK) {
+                const float kr = P.kc_f * W.prt[lane];
+#pragma unroll
+                for (int q = 0; q < RES_N; q++) inv[q] = kr * pr.insum[q];
+            }
             for (int k = 0; k < nPx; k++) {
                 unsigned char c = CLS_OUT;
                 if (act && !close) {
@@ -277,12 +350,20 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     c = (unsigned char)fclassify(Q, sqf);
                 }
                 mycls[k] = c;
+                nitin += c == CLS_IN;
+                nitcut += c == CLS_CUT;
                 float *rr = &res[(lane * nPx + k) * RES_N];
+                if (CK && c == CLS_IN) {
+                    nsub++;
 #pragma unroll
-                for (int q = 0; q < RES_N; q++) rr[q] = 0.f;
+                    for (int q = 0; q < RES_N; q++) rr[q] = inv[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < RES_N; q++) rr[q] = 0.f;
+                }
             }
             __syncwarp();
-            const int nin = build_list(mycls, nPx, CLS_IN, lst);
+            const int nin = CK ? 0 : build_list(mycls, nPx, CLS_IN, lst);
             const int ncut = build_list(mycls, nPx, CLS_CUT, lst + 32 * nPx);
             for (int c0 = 0; c0 < nin; c0 += 32) {
                 if (c0 + lane < nin) {
@@ -296,8 +377,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 if (c0 + lane < ncut) {
                     const int it = lst[32 * nPx + c0 + lane];
                     const int k = it >> 5, j = it & 31;
-                    item_cut(P, rule, W.pc[j], W.xf[k], &W.x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
-                             &res[(j * nPx + k) * RES_N], nsub, namb);
+                    if (CK)
+                        item_cut_const(P, pr, W.pc[j], W.xf[k], &W.x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
+                                       &res[(j * nPx + k) * RES_N], nsub, namb);
+                    else
+                        item_cut(P, rule, W.pc[j], W.xf[k], &W.x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
+                                 &res[(j * nPx + k) * RES_N], nsub, namb);
                 }
             }
             __syncwarp();
@@ -454,10 +539,14 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
     nclose = warp_sum(nclose);
+    nitin = warp_sum(nitin);
+    nitcut = warp_sum(nitcut);
     if (lane == 0) {
         if (nsub && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)nsub);
         if (namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
         if (nclose && a.n_close) atomicAdd(a.n_close, (unsigned long long)nclose);
+        if (nitin && a.n_in) atomicAdd(a.n_in, (unsigned long long)nitin);
+        if (nitcut && a.n_cut) atomicAdd(a.n_cut, (unsigned long long)nitcut);
     }
 }
 

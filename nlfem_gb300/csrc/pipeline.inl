@@ -921,14 +921,27 @@ static PassRule make_pass_rule(const Rule &r, int dim) {
             for (int b = a; b < dV; b++) pr.cxx[NS * k + t++] = (float)(r.dx[k] * r.psix[dV * k + a] * r.psix[dV * k + b]);
         }
     }
+    double insum[1 + 4 + 10] = {0}, mom[6] = {0};
     for (int i = 0; i < r.nPy; i++) {
         for (int c = 0; c < dim; c++) pr.pyf[dim * i + c] = (float)r.Py[dim * i + c];
         int t = 0;
+        insum[0] += r.dy[i];
         for (int a = 0; a < dV; a++) {
             pr.cy[dV * i + a] = (float)(r.dy[i] * r.psiy[dV * i + a]);
-            for (int b = a; b < dV; b++) pr.cyy[NS * i + t++] = (float)(r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b]);
+            insum[1 + a] += r.dy[i] * r.psiy[dV * i + a];
+            for (int b = a; b < dV; b++) {
+                insum[1 + dV + t] += r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b];
+                pr.cyy[NS * i + t++] = (float)(r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b]);
+            }
+        }
+        if (dim == 2) {
+            const double px = r.Py[2 * i], py = r.Py[2 * i + 1], w = r.dy[i];
+            mom[0] += w; mom[1] += w * px; mom[2] += w * py;
+            mom[3] += w * px * px; mom[4] += w * px * py; mom[5] += w * py * py;
         }
     }
+    for (int q = 0; q < 1 + 4 + 10; q++) pr.insum[q] = (float)insum[q];
+    for (int q = 0; q < 6; q++) pr.mom[q] = (float)mom[q];
     return pr;
 }
 
@@ -979,6 +992,7 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr
         CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.err.get<int>() + 5, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 4, 0, 3 * sizeof(unsigned long long), S.st));
+        CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 12, 0, 2 * sizeof(unsigned long long), S.st));
         kfn<<<(unsigned)(S.nSM * per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
         CK(cudaGetLastError());
         if (S.replay) return NLFEM_OK;   // the overflow flag is checked after the replay
@@ -1007,6 +1021,7 @@ static int run_passes(Session &S) {
     }
     unsigned long long *cnt = S.counters.get<unsigned long long>();
     CK(cudaMemsetAsync(cnt + 4, 0, 3 * sizeof(unsigned long long), S.st));
+    CK(cudaMemsetAsync(cnt + 12, 0, 2 * sizeof(unsigned long long), S.st));
     int r = run_close(S);
     if (r) return r;
     PassArgs a;
@@ -1018,12 +1033,17 @@ static int run_passes(Session &S) {
     a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
     a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
     a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
-    a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4;
+    a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);
-    if (S.pmode == PM_RETRI) return run_pass_one_sided(S, a, pr, k_pass_mix2d, MIX_THREADS, mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
+    bool ck = true;   // every problem has a constant kernel: closed-form inner sums
+    for (const ProbParams &q : S.hprm) ck = ck && (q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D);
+    if (S.pmode == PM_RETRI)
+        return run_pass_one_sided(S, a, pr, ck ? k_pass_mix2d<true> : k_pass_mix2d<false>, MIX_THREADS,
+                                  mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
     if (S.pmode == PM_BARY)
-        return run_pass_one_sided(S, a, pr, k_pass_bary<DIM>, BARY_THREADS, bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
+        return run_pass_one_sided(S, a, pr, ck ? k_pass_bary<DIM, true> : k_pass_bary<DIM, false>, BARY_THREADS,
+                                  bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
     const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
     if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else CK(cudaFuncSetAttribute(k_pass<DIM, PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1104,9 +1124,12 @@ static int run_system_post(Session &S) {
     if ((r = check_errors(S))) return r;
     float t[4];
     for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], S.ev[i], S.ev[i + 1]));
-    unsigned long long ncl[5] = {0, 0, 0, 0, 0};
+    unsigned long long ncl[7] = {0, 0, 0, 0, 0, 0, 0};
     if ((r = d2h(S, ncl, S.counters.get<unsigned long long>() + 4, 4))) return r;
     if ((r = d2h(S, &ncl[4], S.counters.get<unsigned long long>() + 1, 1))) return r;
+    if ((r = d2h(S, &ncl[5], S.counters.get<unsigned long long>() + 12, 2))) return r;
+    S.stats.n_items_in = (long)ncl[5];
+    S.stats.n_items_cut = (long)ncl[6];
     S.stats.n_candidates = (long)ncl[4];
     S.stats.n_close = (long)ncl[0];
     S.stats.n_subtri = (long)ncl[1];

@@ -183,10 +183,13 @@ def algorithmic_flops(st, conf, kernel, dim=2):
       first two points, the ten results); cut sub-triangle 11 + 13 (basis at its third point) + 60
       (moment sums);
       baryCenter, per (pair, outer point) 64; item 5.
-    Those counts need the item classes (n_items_in / n_items_cut)."""
+    Those counts need the item classes (n_items_in / n_items_cut). A batch that mixes kernels is
+    counted with the closed forms for every problem (a lower bound)."""
     nPx = len(conf["quadrature"]["outer"]["weights"])
     nPy = len(conf["quadrature"]["inner"]["weights"])
-    const = kernel["function"] in ("constant", "constant3D") and conf.get("precision") == "mixed"
+    # a batch mixing constant and other kernels ("mixed") is counted with the closed forms
+    # throughout, a lower bound on the operations that ran
+    const = kernel["function"] in ("constant", "constant3D", "mixed") and conf.get("precision") == "mixed"
     if conf["approxBalls"]["method"] == "baryCenter":
         if const:
             return st["n_pairs"] * nPx * 64 + st["n_items_in"] * 5

@@ -56,8 +56,8 @@ __device__ __forceinline__ float kernel_f32_r2(const ProbParams &P, float r2) {
     }
 }
 
-// CK: every problem of the launch has a constant kernel; an item's sums over the full inner
-// element are then kc |b| times the rule's precomputed element sums.
+// CK: the launch covers constant-kernel problems only; an item's sums over the full inner element
+// are then kc |b| times the rule's precomputed element sums.
 template <int DIM, bool CK>
 __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rule, PassRule pr) {
     constexpr int dV = DIM + 1, NS = dV * (dV + 1) / 2, RN = DIM + 2;

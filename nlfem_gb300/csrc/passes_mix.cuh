@@ -248,7 +248,7 @@ __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }
 
-// CK: every problem of the launch has a constant kernel; inside items then take the rule's
+// CK: the launch covers constant-kernel problems only; inside items then take the rule's
 // precomputed element sums and cut items the moment form (item_cut_const).
 template <bool CK>
 __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {

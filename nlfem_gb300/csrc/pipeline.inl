@@ -280,6 +280,8 @@ struct Session {
     DevBuf out64a, out64b;
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
+    DevBuf kclist;                          // elements of constant-kernel problems, then the others
+    long long kc_nconst = -1;               // length of the first part (-1: list not built)
     long long pat_cap = 0;
     int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
@@ -298,7 +300,7 @@ struct Session {
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff};
+                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -970,31 +972,65 @@ static int run_close(Session &S) {
     return NLFEM_OK;
 }
 
-// One-sided mixed 2D pass (passes_mix.cuh): one persistent launch over all elements. A
-// contribution outside the fixed-point range sets err[5]; the pass is then redone with a unit
-// 2^16 times coarser.
+// One-sided mixed passes (passes_mix.cuh, passes_bary.cuh): one persistent launch over all
+// elements. kconst is the closed-form instance for constant kernels, kgen the general one. A batch
+// that mixes kernels runs both, each over its problems' elements (constant-kernel elements listed
+// first), so every problem goes through the same code as its single assembly and the batch matrices
+// equal the single ones bit for bit. A contribution outside the fixed-point range sets err[5]; the
+// pass is then redone with a unit 2^16 times coarser.
 typedef void (*OneSidedKernel)(MixArgs, Rule, PassRule);
-static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, OneSidedKernel kfn, int threads,
-                              size_t smem) {
+static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, OneSidedKernel kgen,
+                              OneSidedKernel kconst, int threads, size_t smem) {
     const long long nnz = S.nnz_struct;
-    CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem));
-    if (per_sm < 1) return fail(NLFEM_ERR_UNSUPPORTED, "quadrature rule too large for the pass's shared memory");
+    int nconst_p = 0;
+    for (const ProbParams &q : S.hprm) nconst_p += q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D;
+    struct Launch { OneSidedKernel k; const int *list; int count; int per_sm; };
+    Launch L[2];
+    int nl = 0;
+    if (nconst_p == 0 || nconst_p == (int)S.hprm.size()) {
+        L[nl++] = Launch{nconst_p ? kconst : kgen, nullptr, (int)S.nE, 0};
+    } else {
+        if (S.kc_nconst < 0) {
+            if (S.replay) return fail(NLFEM_ERR_UNSUPPORTED, "element list by kernel class missing in graph capture");
+            std::vector<int> h;
+            h.reserve((size_t)S.nE);
+            for (int pass = 0; pass < 2; pass++)
+                for (const ProbParams &q : S.hprm) {
+                    const bool c = q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D;
+                    if (c == (pass == 0))
+                        for (int e = 0; e < q.nE; e++) h.push_back(q.elem_off + e);
+                    if (pass == 0 && &q == &S.hprm.back()) S.kc_nconst = (long long)h.size();
+                }
+            ENS(S.kclist, sizeof(int) * (h.size() + 1));
+            CK(cudaMemcpyAsync(S.kclist.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, S.st));
+            CK(cudaStreamSynchronize(S.st));
+        }
+        const int *lst = S.kclist.get<int>();
+        L[nl++] = Launch{kconst, lst, (int)S.kc_nconst, 0};
+        L[nl++] = Launch{kgen, lst + S.kc_nconst, (int)(S.nE - S.kc_nconst), 0};
+    }
+    for (int i = 0; i < nl; i++) {
+        CK(cudaFuncSetAttribute(L[i].k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&L[i].per_sm, L[i].k, threads, smem));
+        if (L[i].per_sm < 1) return fail(NLFEM_ERR_UNSUPPORTED, "quadrature rule too large for the pass's shared memory");
+    }
     MixArgs ma;
     ma.p = pa;
-    ma.p.list = nullptr;
-    ma.p.count = (int)S.nE;
     ma.m = slot_map(S);
     ma.work = reinterpret_cast<int *>(S.counters.get<unsigned long long>() + 10);
     for (int attempt = 0; attempt < 4; attempt++) {
         CK(cudaMemsetAsync(S.vals.p, 0, sizeof(long long) * (nnz + 1), S.st));
-        CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.err.get<int>() + 5, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 4, 0, 3 * sizeof(unsigned long long), S.st));
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 12, 0, 2 * sizeof(unsigned long long), S.st));
-        kfn<<<(unsigned)(S.nSM * per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
-        CK(cudaGetLastError());
+        for (int i = 0; i < nl; i++) {
+            if (L[i].count == 0) continue;
+            ma.p.list = L[i].list;
+            ma.p.count = L[i].count;
+            CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
+            L[i].k<<<(unsigned)(S.nSM * L[i].per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
+            CK(cudaGetLastError());
+        }
         if (S.replay) return NLFEM_OK;   // the overflow flag is checked after the replay
         int ovf = 0;
         int r = d2h(S, &ovf, S.err.get<int>() + 5, 1);
@@ -1036,13 +1072,11 @@ static int run_passes(Session &S) {
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);
-    bool ck = true;   // every problem has a constant kernel: closed-form inner sums
-    for (const ProbParams &q : S.hprm) ck = ck && (q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D);
     if (S.pmode == PM_RETRI)
-        return run_pass_one_sided(S, a, pr, ck ? k_pass_mix2d<true> : k_pass_mix2d<false>, MIX_THREADS,
+        return run_pass_one_sided(S, a, pr, k_pass_mix2d<false>, k_pass_mix2d<true>, MIX_THREADS,
                                   mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
     if (S.pmode == PM_BARY)
-        return run_pass_one_sided(S, a, pr, ck ? k_pass_bary<DIM, true> : k_pass_bary<DIM, false>, BARY_THREADS,
+        return run_pass_one_sided(S, a, pr, k_pass_bary<DIM, false>, k_pass_bary<DIM, true>, BARY_THREADS,
                                   bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
     const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
     if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -338,6 +338,24 @@ def test_mixed_matches_oracle(nl, orc, n, delta, kern, jit):
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
+def test_mixed_batch_mixed_kernels(nl, orc):
+    """A batch mixing constant (closed-form inner sums) and parabola problems equals the single
+    assemblies, and each problem matches the oracle."""
+    probs = []
+    for i, (n, d, kn) in enumerate([(10, 0.1, "constant"), (14, 0.13, "parabola"), (8, 0.2, "constant")]):
+        probs.append((square_mesh(n, d, jitter=0.2, seed=i), {"function": kn, "horizon": d, "outputdim": 1},
+                      conf2d(precision="mixed")))
+    As = nl.stiffnessMatrix_batch(probs)
+    for (m, k, c), A in zip(probs, As):
+        B = nl.stiffnessMatrix(m, k, c)
+        assert same_pattern(A, B)
+        assert abs(A - B).max() <= 1e-12 * abs(B).max()
+        R = orc.assemble(m, k, conf2d())["A"]
+        assert same_pattern(A, R)
+        fro, mx = rel_errors(A, R)
+        assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
 def test_mixed_pair_list_exact(nl, orc):
     m = square_mesh(24, 0.13, jitter=0.2, seed=3)
     k = {"function": "constant", "horizon": 0.13, "outputdim": 1}
@@ -386,9 +404,10 @@ def test_mixed_pattern_equals_fp64_at_scale(nl):
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
-def test_mixed_barycenter_2d(nl, orc):
+@pytest.mark.parametrize("kern", ["parabola", "constant"])
+def test_mixed_barycenter_2d(nl, orc, kern):
     m = square_mesh(16, 0.15, jitter=0.2, seed=4)
-    k = {"function": "parabola", "horizon": 0.15, "outputdim": 1}
+    k = {"function": kern, "horizon": 0.15, "outputdim": 1}
     A = nl.stiffnessMatrix(m, k, conf2d(method="baryCenter", precision="mixed"))
     B = orc.assemble(m, k, conf2d(method="baryCenter"))["A"]
     assert same_pattern(A, B)

@@ -292,8 +292,10 @@ __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, 
     return interacts_filtered<DIM>(P, method, xs, xsf, nPx, Eb, pb, namb);
 }
 
+// 3D searches (barycenter tests, no polygon geometry) fit 64 registers and gain from the doubled
+// residency; the 2D retriangulate test needs more.
 template <int DIM, int PREC>
-__global__ void __launch_bounds__(BFS_THREADS) k_bfs(BfsArgs a, Rule rule) {
+__global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a, Rule rule) {
     constexpr int dV = DIM + 1;
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
     __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];

@@ -31,7 +31,6 @@ struct MixWarp {
     float pc[32][6];        // partner element, local coordinates
     float prt[32];          // partner |det|
     int pid[32];            // partner element
-    int ds[32][9];          // partner's diagonal-block slots (prefetched at the start of a batch)
     long long rhb[3], rrb[3];   // T's rows: hash table start, CSR row start
     unsigned rmask[3];          // T's rows: hash capacity - 1 (0xffffffff: no row)
     int tvs[3];                 // T's vertices
@@ -50,17 +49,16 @@ __host__ __device__ constexpr size_t mix_warp_bytes(int nPx) {
     return ((sizeof(MixWarp) + 15) / 16) * 16 + mix_res_bytes(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
 }
 
-__device__ __forceinline__ void cp_async4(void *dst_smem, const void *src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 struct MixArgs {
     PassArgs p;
     SlotMap m;
     int *work;   // global element counter
+    // one-sided retriangulate pass only:
+    long long *valsN;   // termNonloc of each outer element into its own rows; the transposed
+                        // contributions come from k_sym_add (the matrix is symmetric)
+    long long *elp;     // termLocalPrime per partner element, upper triangle (k_elem_blocks adds
+                        // it to the diagonal-block slots)
 };
 
 // Inner sums of one "inside" item: the ball around x contains the partner element b.
@@ -331,11 +329,6 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             for (int j = 0; j < 6; j++) W.pc[lane][j] = pc[j];
             W.prt[lane] = a.adetf[part];
             W.pid[lane] = part;
-            if (act) {
-#pragma unroll
-                for (int q = 0; q < 9; q++) cp_async4(&W.ds[lane][q], &sm.dslot[(long long)part * 9 + q]);
-            }
-            cp_async_commit();
             float inv[RES_N];   // constant kernel: an inside item's sums
             if (CK) {
                 const float kr = P.kc_f * W.prt[lane];
@@ -442,22 +435,16 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 balance_rows<3>(lx, nx, lpx, mx);
 #pragma unroll
                 for (int i = 0; i < 6; i++) D[i] += lx[i];
-                // termLocalPrime into the partner's diagonal block
-                cp_async_wait_all();
-                const int *ds = W.ds[lane];
+                // termLocalPrime into the partner's block accumulator
 #pragma unroll
-                for (int r = 0; r < 3; r++) {
-#pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        const int s = ds[3 * r + c];
-                        if (s >= 0) red_add(vals, s, lpx[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)]);
-                        else if (a.labV[pv[r]] > 0) atomicOr(&a.err[3], 1);
-                    }
-                }
+                for (int q = 0; q < 6; q++) red_add(ma.elp, (long long)part * 6 + q, lpx[q]);
             }
-            // termNonloc into A[T, b] and its mirror into A[b, T] (both with the minus sign):
-            // lanes sharing a partner vertex add their integers, the first of them lists the sums
-            // (over the item results, read by now); then all lanes share the (vertex, row) lookups
+            // termNonloc into A[T, b] (minus sign): lanes sharing a partner vertex add their
+            // integers, the first of them lists the sums (over the item results, read by now); then
+            // all lanes share the (vertex, row) lookups. The mirror A[b, T] -= N^T comes from the
+            // symmetric completion (k_sym_add), except where T's vertex has no row (written here
+            // into the partner vertex's row) and for close pairs, whose termNonlocPrime block is
+            // its own FP64 result (the difference to N^T is added here).
             __syncwarp();
             const bool anyclose = __any_sync(FULL, close);
             int nent = 0;
@@ -504,11 +491,11 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 if (h.mask != 0xffffffffu) {
                     const long long s = slot_find_row(sm, h, col);
                     if (s < 0) { atomicOr(&a.err[3], 1); continue; }
-                    red_add(vals, s, -sn);
-                    if (keepc) {
+                    red_add(ma.valsN, s, -sn);
+                    if (anyclose && keepc && sq != sn) {
                         const int tp = sm.tpos[s];
                         if (tp < 0) atomicOr(&a.err[3], 1);
-                        else red_add(vals, sm.rowptr[col] + tp, -sq);
+                        else red_add(vals, sm.rowptr[col] + tp, sn - sq);
                     }
                 } else if (keepc) {
                     const long long q = slot_find(sm, col, W.tvs[r]);
@@ -548,6 +535,51 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         if (nitin && a.n_in) atomicAdd(a.n_in, (unsigned long long)nitin);
         if (nitcut && a.n_cut) atomicAdd(a.n_cut, (unsigned long long)nitcut);
     }
+}
+
+// Symmetric completion of the one-sided retriangulate pass: every slot (t, v) adds the
+// termNonloc sums of the transposed slot (v, t) when v has a row. Integer sums, so the completed
+// matrix is exactly symmetric in these contributions, as the reference's A[b, T] -= termNonlocPrime
+// = termNonloc^T (kernels of |x - y|) makes it. One warp per row.
+__global__ void k_sym_add(const long long *__restrict__ rowptr, const int *__restrict__ cols,
+                          const int *__restrict__ tpos, const long long *__restrict__ valsN, long long nrows,
+                          long long *__restrict__ vals) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t < nrows; t += nw) {
+        const long long b = rowptr[t], e = rowptr[t + 1];
+        for (long long s = b + lane; s < e; s += 32) {
+            long long v = valsN[s];
+            const int tp = tpos[s];
+            if (tp >= 0) v += valsN[rowptr[cols[s]] + tp];
+            vals[s] += v;
+        }
+    }
+}
+
+// termLocalPrime blocks accumulated per partner element into its diagonal-block slots.
+__global__ void k_elem_blocks(const long long *__restrict__ elp, const int *__restrict__ dslot,
+                              const int *__restrict__ T32, const int *__restrict__ labV, long long nE,
+                              long long *__restrict__ vals, int *__restrict__ err) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    long long b[6];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        b[q] = elp[e * 6 + q];
+        any |= b[q] != 0;
+    }
+    if (!any) return;
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int s = dslot[e * 9 + 3 * r + c];
+            if (s >= 0) red_add(vals, s, b[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)]);
+            else if (labV[T32[e * 3 + r]] > 0) atomicOr(&err[3], 1);
+        }
 }
 
 }  // namespace nlg

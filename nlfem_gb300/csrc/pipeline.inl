@@ -280,6 +280,7 @@ struct Session {
     DevBuf out64a, out64b;
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
+    DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
     DevBuf kclist;                          // elements of constant-kernel problems, then the others
     long long kc_nconst = -1;               // length of the first part (-1: list not built)
     long long pat_cap = 0;
@@ -300,7 +301,7 @@ struct Session {
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist};
+                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -1018,8 +1019,21 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr
     ma.p = pa;
     ma.m = slot_map(S);
     ma.work = reinterpret_cast<int *>(S.counters.get<unsigned long long>() + 10);
+    ma.valsN = nullptr;
+    ma.elp = nullptr;
+    const bool retri = S.pmode == PM_RETRI;
+    if (retri) {
+        ENS(S.valsN, sizeof(long long) * (nnz + 1));
+        ENS(S.elp, sizeof(long long) * 6 * (S.nE + 1));
+        ma.valsN = S.valsN.get<long long>();
+        ma.elp = S.elp.get<long long>();
+    }
     for (int attempt = 0; attempt < 4; attempt++) {
         CK(cudaMemsetAsync(S.vals.p, 0, sizeof(long long) * (nnz + 1), S.st));
+        if (retri) {
+            CK(cudaMemsetAsync(S.valsN.p, 0, sizeof(long long) * (nnz + 1), S.st));
+            CK(cudaMemsetAsync(S.elp.p, 0, sizeof(long long) * 6 * (S.nE + 1), S.st));
+        }
         CK(cudaMemsetAsync(S.err.get<int>() + 5, 0, sizeof(int), S.st));
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 4, 0, 3 * sizeof(unsigned long long), S.st));
         CK(cudaMemsetAsync(S.counters.get<unsigned long long>() + 12, 0, 2 * sizeof(unsigned long long), S.st));
@@ -1029,6 +1043,12 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr
             ma.p.count = L[i].count;
             CK(cudaMemsetAsync(ma.work, 0, sizeof(int), S.st));
             L[i].k<<<(unsigned)(S.nSM * L[i].per_sm), threads, smem, S.st>>>(ma, S.rule, pr); ++S.nlaunch;
+            CK(cudaGetLastError());
+        }
+        if (retri) {   // termLocalPrime blocks, then the transposed termNonloc sums
+            long long *vals = reinterpret_cast<long long *>(S.vals.p);
+            k_elem_blocks<<<grid_for(S.nE, 256), 256, 0, S.st>>>(ma.elp, S.dslot.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.nE, vals, S.err.get<int>()); ++S.nlaunch;
+            k_sym_add<<<S.nSM * 16, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), S.tpos.get<int>(), ma.valsN, S.nV, vals); ++S.nlaunch;
             CK(cudaGetLastError());
         }
         if (S.replay) return NLFEM_OK;   // the overflow flag is checked after the replay

@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
                 for (int jn = 0; jn < maxdeg; jn++) {
                     int cand = cand_next;
                     cand_next = jn + 1 < deg ? a.adj[beg + jn + 1] : -1;
-                    const int lab = cand >= 0 ? a.labT[cand] : 1;   // before the visited store
+                    const int lab = (P.bridges && cand >= 0) ? a.labT[cand] : 1;   // before the visited store
                     // lanes holding the same candidate: the lowest one takes it, so the queue
                     // order (and every order derived from it) does not depend on atomic timing
                     const unsigned same = __match_any_sync(FULL, cand);

@@ -24,10 +24,10 @@ constexpr int MIX_WARPS = 4;
 constexpr int MIX_THREADS = 32 * MIX_WARPS;
 constexpr int RES_N = 10;   // per item: innerLocal, innerNonloc[3], inner termLocalPrime sums[6]
 
-// Per-warp shared scratch; nPx-dependent arrays follow the struct in dynamic shared memory.
+// Per-warp shared scratch; nPx-dependent arrays follow the struct in dynamic shared memory:
+// the outer points of T (FP64, exact; FP32 relative to T's vertex 0), the item results and the
+// item lists.
 struct MixWarp {
-    double x64[MAXQ * 2];   // outer points of T (FP64, exact)
-    F2 xf[MAXQ];            // outer points of T, local
     float pc[32][6];        // partner element, local coordinates
     float prt[32];          // partner |det|
     int pid[32];            // partner element
@@ -45,8 +45,10 @@ __host__ __device__ constexpr size_t mix_res_bytes(int nPx) {
     return (size_t)32 * nPx * RES_N * 4 > 96 * sizeof(ScatEntry) ? (size_t)32 * nPx * RES_N * 4 : 96 * sizeof(ScatEntry);
 }
 __host__ __device__ constexpr size_t mix_warp_bytes(int nPx) {
-    // MixWarp + res[32][nPx][RES_N] floats (or the scatter list) + lists[2][32 * nPx] shorts
-    return ((sizeof(MixWarp) + 15) / 16) * 16 + mix_res_bytes(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
+    // MixWarp + x64[nPx * 2] doubles + xf[nPx] F2 + res[32][nPx][RES_N] floats (or the scatter
+    // list) + lists[2][32 * nPx] shorts
+    return ((sizeof(MixWarp) + 15) / 16) * 16 + (size_t)nPx * 16 + ((size_t)nPx * 8 + 15) / 16 * 16 +
+           mix_res_bytes(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
 }
 
 
@@ -257,7 +259,9 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
     const int nPx = rule.nPx;
     unsigned char *wbase = s_raw + (size_t)wib * mix_warp_bytes(nPx);
     MixWarp &W = *reinterpret_cast<MixWarp *>(wbase);
-    float *res = reinterpret_cast<float *>(wbase + ((sizeof(MixWarp) + 15) / 16) * 16);   // [32][nPx][RES_N]
+    double *x64 = reinterpret_cast<double *>(wbase + ((sizeof(MixWarp) + 15) / 16) * 16);   // [nPx * 2]
+    F2 *xf = reinterpret_cast<F2 *>(x64 + 2 * nPx);                                          // [nPx]
+    float *res = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(xf) + ((size_t)nPx * 8 + 15) / 16 * 16);   // [32][nPx][RES_N]
     unsigned short *lst = reinterpret_cast<unsigned short *>(reinterpret_cast<unsigned char *>(res) + mix_res_bytes(nPx));   // [2][32*nPx]
     ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
@@ -296,8 +300,8 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         const float olo0 = a.EClo[(long long)T * 6], olo1 = a.EClo[(long long)T * 6 + 1];
         const float rTT = a.adetf[T];
         for (int k = lane; k < nPx; k += 32) {
-            xtoPhys<2>(ET64, &rule.Px[2 * k], &W.x64[2 * k]);
-            W.xf[k] = f2((float)(W.x64[2 * k] - ET64[0]), (float)(W.x64[2 * k + 1] - ET64[1]));
+            xtoPhys<2>(ET64, &rule.Px[2 * k], &x64[2 * k]);
+            xf[k] = f2((float)(x64[2 * k] - ET64[0]), (float)(x64[2 * k + 1] - ET64[1]));
         }
         __syncwarp();
         long long D[6];   // termLocal of T's pairs, integer sums
@@ -338,7 +342,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             for (int k = 0; k < nPx; k++) {
                 unsigned char c = CLS_OUT;
                 if (act && !close) {
-                    const F2 x = W.xf[k];
+                    const F2 x = xf[k];
                     const F2 Q[3] = {f2(pc[0] - x.x, pc[1] - x.y), f2(pc[2] - x.x, pc[3] - x.y), f2(pc[4] - x.x, pc[5] - x.y)};
                     c = (unsigned char)fclassify(Q, sqf);
                 }
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     const int it = lst[c0 + lane];
                     const int k = it >> 5, j = it & 31;
                     nsub++;
-                    item_in(P, rule, pr, W.pc[j], W.prt[j], W.xf[k], &res[(j * nPx + k) * RES_N]);
+                    item_in(P, rule, pr, W.pc[j], W.prt[j], xf[k], &res[(j * nPx + k) * RES_N]);
                 }
             }
             for (int c0 = 0; c0 < ncut; c0 += 32) {
@@ -371,10 +375,10 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     const int it = lst[32 * nPx + c0 + lane];
                     const int k = it >> 5, j = it & 31;
                     if (CK)
-                        item_cut_const(P, pr, W.pc[j], W.xf[k], &W.x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
+                        item_cut_const(P, pr, W.pc[j], xf[k], &x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
                                        &res[(j * nPx + k) * RES_N], nsub, namb);
                     else
-                        item_cut(P, rule, W.pc[j], W.xf[k], &W.x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
+                        item_cut(P, rule, W.pc[j], xf[k], &x64[2 * k], &a.EC[(long long)W.pid[j] * 6],
                                  &res[(j * nPx + k) * RES_N], nsub, namb);
                 }
             }

@@ -188,6 +188,9 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         P.load = load_id(p.forcing);
         if (P.load < 0) return fail(NLFEM_ERR_UNSUPPORTED, std::string("unknown forcing: ") + (p.forcing ? p.forcing : "(null)"));
     }
+    P.bridges = 0;
+    if (p.elementLabels)
+        for (long e = 0; e < p.nE && !P.bridges; e++) P.bridges = p.elementLabels[e] == 0;
     // fixed-point scale: typical magnitude of an entry
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (long v = 0; v < p.nV; v++)

@@ -902,7 +902,7 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
         k_iota<<<grid_for(n, 256), 256, 0, S.st>>>(S.closelist.get<int>(), n); ++S.nlaunch;
         a.list = S.closelist.get<int>();
         a.nlist = n;
-        k_quad_close<<<grid_for(n * 32, 128), 128, 0, S.st>>>(a, duffy_view(S)); ++S.nlaunch;
+        k_quad_close<false><<<grid_for(n * 32, 128), 128, 0, S.st>>>(a, duffy_view(S)); ++S.nlaunch;
     } else {
         k_quad_fp64<DIM><<<grid_for(n, 128), 128, 0, S.st>>>(a, S.rule); ++S.nlaunch;
     }
@@ -971,7 +971,10 @@ static int run_close(Session &S) {
     k_iota<<<grid_for(nslot, 256), 256, 0, S.st>>>(S.closelist.get<int>(), nslot); ++S.nlaunch;
     a.list = S.closelist.get<int>();
     a.nlist = nslot;
-    k_quad_close<<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S)); ++S.nlaunch;
+    // the mixed path takes the kernel power in FP32 after an exact binary range reduction
+    if (S.prec == PREC_MIX) k_quad_close<true><<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+    else k_quad_close<false><<<grid_for(nslot * 32, 128), 128, 0, S.st>>>(a, duffy_view(S));
+    ++S.nlaunch;
     CK(cudaGetLastError());
     return NLFEM_OK;
 }

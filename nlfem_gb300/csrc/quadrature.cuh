@@ -257,11 +257,26 @@ __global__ void k_close_list(QuadArgs a, int *list, unsigned long long *count) {
 
 // One warp per close pair: integrate_fractional (integration.cpp:187-288) with join()
 // (:1913-1958), FP64 throughout; lanes stride over the Duffy points, warp-reduce the blocks.
+// r2^h (h < 0) for the mixed path: r2 = m 2^E exactly (frexp, m in [1/2, 1)), and h E = I + f
+// with I = floor(h E) an integer, so r2^h = 2^I 2^(f + h log2 m) where only the last power, of an
+// argument in [0, 1 - h), is evaluated in FP32 (exp2f, log2f). Its relative error is a few units
+// of 2^-24 times (1 + |h|), about 3e-7, far inside the mixed path's 1e-6; the binary exponent
+// is exact. Range reduction by the exact power of two, as in any pow implementation.
+__device__ __forceinline__ double pow_split(double r2, double h) {
+    int E;
+    const double m = frexp(r2, &E);
+    const double t = h * (double)E;
+    const double I = floor(t);
+    const float g = fmaf((float)h, log2f((float)m), (float)(t - I));
+    return ldexp((double)exp2f(g), (int)I);
+}
+
 // Sum over the Duffy points of one close pair (integration.cpp:187-288) of w pxy pxy^T, upper
 // triangle of the nL x nL matrix, nL = 6 - NEQ: the lanes take the (map, Gauss point) items in
 // turn. The kernel value |x - y|^-(d+2s) is taken as exp2(-(d+2s)/2 log2 |x - y|^2), the same
-// function as the reference's 1/pow(sqrt(r), d+2s) without the power's extra work.
-template <int NEQ>
+// function as the reference's 1/pow(sqrt(r), d+2s) without the power's extra work; FAST (mixed
+// path) evaluates it with pow_split.
+template <int NEQ, bool FAST>
 __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duffy &d, int c, int nT,
                                                  const double *EA, const double *EB, double dAB, double *M) {
     constexpr int NL = 6 - NEQ, SH = 3 - NEQ;
@@ -279,7 +294,8 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
         const double x0 = al[0] * a0 + al[1] * a1 + EA[0], x1 = al[0] * a2 + al[1] * a3 + EA[1];
         const double y0 = al[2] * b0 + al[3] * b1 + EB[0], y1 = al[2] * b2 + al[3] * b3 + EB[1];
         const double z0 = x0 - y0, z1 = x1 - y1;
-        const double ker = P.kc * exp2(hexp * log2(z0 * z0 + z1 * z1));
+        const double r2 = z0 * z0 + z1 * z1;
+        const double ker = P.kc * (FAST ? pow_split(r2, hexp) : exp2(hexp * log2(r2)));
         const double px[3] = {1.0 - al[0] - al[1], al[0], al[1]};
         const double py[3] = {1.0 - al[2] - al[3], al[2], al[3]};
         double v[NL];
@@ -302,6 +318,7 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
     }
 }
 
+template <bool FAST>
 __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int lane = threadIdx.x & 31;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -360,9 +377,9 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     double M[21];
 #pragma unroll
     for (int i = 0; i < 21; i++) M[i] = 0.0;
-    if (nEqual == 1) close_accumulate<1>(P, d, c, nT, EA, EB, dA * dB, M);
-    else if (nEqual == 2) close_accumulate<2>(P, d, c, nT, EA, EB, dA * dB, M);
-    else close_accumulate<3>(P, d, c, nT, EA, EB, dA * dB, M);
+    if (nEqual == 1) close_accumulate<1, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
+    else if (nEqual == 2) close_accumulate<2, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
+    else close_accumulate<3, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
 #pragma unroll
     for (int i = 0; i < 21; i++) M[i] = warp_sum(M[i]);
     double acc[36];

@@ -131,6 +131,30 @@ def test_label_zero_bridges(nl, orc):
     assert same_pattern(A, B) and rel_errors(A, B)[0] < FP64_TOL
 
 
+@pytest.mark.parametrize("kern", ["constant", "parabola"])
+def test_label_zero_bridges_mixed(nl, orc, kern):
+    """Mixed path on a mesh with label-0 elements (searched through, never paired), with the
+    constant kernel's closed forms and the general kernel."""
+    m = square_mesh(16, 0.12, jitter=0.2, seed=7)
+    lab = m["elementLabels"].copy()
+    lab[60:90] = 0
+    from nlfem_gb300.meshes import mesh_dict
+    m2 = mesh_dict(m["vertices"], m["elements"], lab)
+    k = {"function": kern, "horizon": 0.12, "outputdim": 1}
+    A = nl.stiffnessMatrix(m2, k, conf2d(precision="mixed")); B = orc.assemble(m2, k, conf2d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+def test_mixed_no_caps(nl, orc):
+    m = square_mesh(18, 0.1, jitter=0.2, seed=11)
+    A = nl.stiffnessMatrix(m, KC, conf2d(caps=0, precision="mixed")); B = orc.assemble(m, KC, conf2d(caps=0))["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
 def test_pair_blocks_match_oracle(nl, orc):
     m = square_mesh(16, 0.1, jitter=0.2, seed=9)
     k = {"function": "parabola", "horizon": 0.1, "outputdim": 1}

@@ -172,6 +172,10 @@ struct BfsArgs {
     long long nE;
     unsigned *visited;       // nwarps * vstride
     long long vstride;
+    const long long *vptr;   // vertex -> incident elements (sorted)
+    const int *vel;
+    unsigned *vvisited;      // nwarps * vvstride: vertices whose incident elements were seen
+    long long vvstride;
     int *queue;              // nwarps * qcap
     long long qcap;
     int *pool;               // pool of bT per aT segment
@@ -300,12 +304,15 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
     __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];
     __shared__ int s_buf[BFS_WARPS][64];   // candidates waiting for the interaction test
+    __shared__ int s_vbuf[BFS_WARPS][32 * (DIM + 1)];   // fresh vertices of a frontier group
     unsigned namb = 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;   // at most BFS_WARPS
     const long long gw = (long long)blockIdx.x * wpb + wib;
     const long long nw = (long long)gridDim.x * wpb;
     unsigned *visited = a.visited + gw * a.vstride;
+    unsigned *vvis = a.vvisited + gw * a.vvstride;
+    int *vbuf = s_vbuf[wib];
     int *buf = s_buf[wib];
     int *queue = a.queue + gw * a.qcap;
     double *xs = s_x[wib];
@@ -318,6 +325,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
         }
         const ProbParams P = a.probs[a.eprob[aT]];
         const long long eoff = P.elem_off;
+        const long long voff = P.vert_off;
         const unsigned stamp = (unsigned)aT + 1u;   // unique over all problems
         const double *Ea = &a.EC[aT * DIM * dV];
         float ohi[DIM], olo[DIM];
@@ -347,65 +355,74 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
             const long long lvl_end = qtail;
             const int method = (P.singular && level == 0) ? P.close : P.remote;
             int nbuf = 0;
-            // frontier groups of 32 elements; the next group's entries and adjacency ranges are
-            // loaded while the current one is expanded (entries before lvl_end are final)
-            long long beg_n = 0;
-            int deg_n = 0;
-            {
-                int sn = qhead + lane < lvl_end ? queue[qhead + lane] : -1;
-                if (sn < -1) sn = -sn - 2;   // label-0 bridge stored as -(e+2)
-                if (sn >= 0) { beg_n = a.xadj[sn]; deg_n = (int)(a.xadj[sn + 1] - beg_n); }
-            }
+            // Frontier groups of 32 elements. The neighbours of an element are the elements
+            // incident to its vertices (vertex-sharing adjacency, as the reference's dual graph
+            // with ncommon = 1), so a vertex needs expanding only once per search: the elements
+            // incident to it are seen the first time, whichever dequeued element holds it. The
+            // set of visited elements is the same as the element-wise walk's.
             for (long long g = qhead; g < lvl_end; g += 32) {
-                const long long beg = beg_n;
-                const int deg = deg_n;
-                {
-                    const long long gi = g + 32 + lane;
-                    int sn = gi < lvl_end ? queue[gi] : -1;
-                    if (sn < -1) sn = -sn - 2;
-                    beg_n = 0;
-                    deg_n = 0;
-                    if (sn >= 0) { beg_n = a.xadj[sn]; deg_n = (int)(a.xadj[sn + 1] - beg_n); }
-                }
-                // each lane walks its own frontier element's neighbours (degrees are nearly
-                // uniform, so the lanes stay busy without a scan over the warp)
-                const int maxdeg = (int)__reduce_max_sync(FULL, (unsigned)deg);
-                int cand_next = deg > 0 ? a.adj[beg] : -1;   // the adjacency runs one step ahead
-                for (int jn = 0; jn < maxdeg; jn++) {
-                    int cand = cand_next;
-                    cand_next = jn + 1 < deg ? a.adj[beg + jn + 1] : -1;
-                    const int lab = (P.bridges && cand >= 0) ? a.labT[cand] : 1;   // before the visited store
-                    // lanes holding the same candidate: the lowest one takes it, so the queue
-                    // order (and every order derived from it) does not depend on atomic timing
-                    const unsigned same = __match_any_sync(FULL, cand);
-                    if ((__ffs(same) - 1) != lane) cand = -1;
-                    // the visited array is private to this warp and the candidates of one step are
-                    // distinct, so a plain load and store suffice (steps are ordered by the warp
-                    // synchronisations below; the load may hit L1)
+                int sn = g + lane < lvl_end ? queue[g + lane] : -1;
+                if (sn < -1) sn = -sn - 2;   // label-0 bridge stored as -(e+2)
+                int nv = 0;
+#pragma unroll
+                for (int r = 0; r < dV; r++) {
+                    int v = sn >= 0 ? a.T32[(long long)sn * dV + r] : -1;
+                    const unsigned same = __match_any_sync(FULL, v);
+                    if ((__ffs(same) - 1) != lane) v = -1;
                     bool fresh = false;
-                    if (cand >= 0) {
-                        fresh = visited[cand - eoff] != stamp;
-                        if (fresh) visited[cand - eoff] = stamp;
+                    if (v >= 0) {
+                        fresh = vvis[v - voff] != stamp;
+                        if (fresh) vvis[v - voff] = stamp;
                     }
-                    const bool bridge = fresh && lab == 0;
-                    queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
-                    // candidates to test are compacted, so the test runs on full warps
-                    const bool totest = fresh && !bridge;
-                    const unsigned m = __ballot_sync(FULL, totest);
-                    if (totest) buf[nbuf + __popc(m & lanemask_lt())] = cand;
-                    nbuf += __popc(m);
+                    const unsigned m = __ballot_sync(FULL, fresh);
+                    if (fresh) vbuf[nv + __popc(m & lanemask_lt())] = v;
+                    nv += __popc(m);
                     __syncwarp();
-                    if (nbuf >= 32) {
-                        const int b = buf[lane];
-                        const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
-                        cand_local++;
-                        queue_push(pair, b, queue, a.qcap, qtail, overflow);
-                        const int rest = nbuf - 32;
-                        const int v = lane < rest ? buf[32 + lane] : 0;
+                }
+                for (int c0 = 0; c0 < nv; c0 += 32) {
+                    const int v = c0 + lane < nv ? vbuf[c0 + lane] : -1;
+                    long long beg = 0;
+                    int deg = 0;
+                    if (v >= 0) { beg = a.vptr[v]; deg = (int)(a.vptr[v + 1] - beg); }
+                    // each lane walks its own vertex's incident elements
+                    const int maxdeg = (int)__reduce_max_sync(FULL, (unsigned)deg);
+                    int cand_next = deg > 0 ? a.vel[beg] : -1;   // the list runs one step ahead
+                    for (int jn = 0; jn < maxdeg; jn++) {
+                        int cand = cand_next;
+                        cand_next = jn + 1 < deg ? a.vel[beg + jn + 1] : -1;
+                        const int lab = (P.bridges && cand >= 0) ? a.labT[cand] : 1;   // before the visited store
+                        // lanes holding the same candidate: the lowest one takes it, so the queue
+                        // order (and every order derived from it) does not depend on atomic timing
+                        const unsigned same = __match_any_sync(FULL, cand);
+                        if ((__ffs(same) - 1) != lane) cand = -1;
+                        // the visited array is private to this warp and the candidates of one step
+                        // are distinct, so a plain load and store suffice (steps are ordered by the
+                        // warp synchronisations below; the load may hit L1)
+                        bool fresh = false;
+                        if (cand >= 0) {
+                            fresh = visited[cand - eoff] != stamp;
+                            if (fresh) visited[cand - eoff] = stamp;
+                        }
+                        const bool bridge = fresh && lab == 0;
+                        queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
+                        // candidates to test are compacted, so the test runs on full warps
+                        const bool totest = fresh && !bridge;
+                        const unsigned m = __ballot_sync(FULL, totest);
+                        if (totest) buf[nbuf + __popc(m & lanemask_lt())] = cand;
+                        nbuf += __popc(m);
                         __syncwarp();
-                        if (lane < rest) buf[lane] = v;
-                        nbuf = rest;
-                        __syncwarp();
+                        if (nbuf >= 32) {
+                            const int b = buf[lane];
+                            const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
+                            cand_local++;
+                            queue_push(pair, b, queue, a.qcap, qtail, overflow);
+                            const int rest = nbuf - 32;
+                            const int v2 = lane < rest ? buf[32 + lane] : 0;
+                            __syncwarp();
+                            if (lane < rest) buf[lane] = v2;
+                            nbuf = rest;
+                            __syncwarp();
+                        }
                     }
                 }
                 if (__any_sync(FULL, overflow)) break;

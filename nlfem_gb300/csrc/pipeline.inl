@@ -277,7 +277,7 @@ struct Session {
     std::vector<int> color_off;
     int prec = 0;
     DevBuf vcnt, vptr, vel, adjcnt, xadj, adj;
-    DevBuf visited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
+    DevBuf visited, vvisited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
     DevBuf out64a, out64b;
@@ -299,7 +299,7 @@ struct Session {
     // every device buffer of the session, in a fixed order
     std::vector<DevBuf *> buffers() {
         return {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
-                &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited,
+                &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited, &vvisited,
                 &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
@@ -572,12 +572,14 @@ static int run_bfs(Session &S) {
         S.pool_cap = std::max<long long>((long long)(1.1 * est), 1 << 20);
     }
     ENS(S.visited, sizeof(unsigned) * (size_t)nwarps * S.maxNE);
+    ENS(S.vvisited, sizeof(unsigned) * (size_t)nwarps * S.maxNV);
     ENS(S.seg_start, sizeof(long long) * (nE + 1));
     ENS(S.seg_cnt, sizeof(int) * (nE + 1));
     for (int attempt = 0; attempt < 8; attempt++) {
         ENS(S.queue, sizeof(int) * (size_t)nwarps * S.qcap);
         ENS(S.pool, sizeof(int) * (size_t)S.pool_cap);
         CK(cudaMemsetAsync(S.visited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNE, S.st));
+        CK(cudaMemsetAsync(S.vvisited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNV, S.st));
         CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 8, S.st));
         CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
         BfsArgs a;
@@ -586,6 +588,8 @@ static int run_bfs(Session &S) {
         a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
         a.probs = S.prm.get<ProbParams>(); a.nE = nE;
         a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;
+        a.vptr = S.vptr.get<long long>(); a.vel = S.vel.get<int>();
+        a.vvisited = S.vvisited.get<unsigned>(); a.vvstride = S.maxNV;
         a.queue = S.queue.get<int>(); a.qcap = S.qcap;
         a.pool = S.pool.get<int>(); a.pool_cap = S.pool_cap;
         unsigned long long *cnt = S.counters.get<unsigned long long>();

@@ -163,8 +163,7 @@ constexpr int BFS_THREADS = 256;
 constexpr int BFS_WARPS = BFS_THREADS / 32;
 
 struct BfsArgs {
-    const int *T32, *labT, *eprob, *adj;
-    const long long *xadj;
+    const int *T32, *labT, *eprob;
     const double *EC;
     const float *EChi, *EClo;
     unsigned long long *n_amb;

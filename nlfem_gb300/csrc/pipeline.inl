@@ -529,6 +529,15 @@ static int run_dual(Session &S) {
     CK(cudaMemsetAsync(S.vcnt.p, 0, sizeof(int) * (nV + 1), S.st));
     k_vinc_fill<<<grid_for(nE * dV, 256), 256, 0, S.st>>>(S.T32.get<int>(), nE * dV, dV, S.vptr.get<long long>(), S.vcnt.get<int>(), S.vel.get<int>()); ++S.nlaunch;
     k_vinc_sort<<<grid_for(nV, 256), 256, 0, S.st>>>(S.vptr.get<long long>(), nV, S.vel.get<int>()); ++S.nlaunch;
+    // The search walks the vertex incidence lists. The element dual graph is needed only by the
+    // element coloring of the colored passes and by the close-pair slots of singular kernels.
+    bool need_adj = S.pmode == PM_COLORED;
+    for (const ProbParams &q : S.hprm) need_adj = need_adj || (q.singular && q.close == MTH_FRACTIONAL);
+    if (!need_adj) {
+        S.nadj = 0;
+        CK(cudaGetLastError());
+        return NLFEM_OK;
+    }
     ENS(S.adjcnt, sizeof(int) * (nE + 1));
     ENS(S.xadj, sizeof(long long) * (nE + 1));
     k_adjacency<DIM><<<grid_for(nE, 128), 128, 0, S.st>>>(S.T32.get<int>(), nE, S.vptr.get<long long>(), S.vel.get<int>(), nullptr, S.adjcnt.get<int>(), nullptr, S.err.get<int>() + 8); ++S.nlaunch;
@@ -584,7 +593,7 @@ static int run_bfs(Session &S) {
         CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
         BfsArgs a;
         a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>();
-        a.adj = S.adj.get<int>(); a.xadj = S.xadj.get<long long>(); a.EC = S.EC.get<double>();
+        a.EC = S.EC.get<double>();
         a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
         a.probs = S.prm.get<ProbParams>(); a.nE = nE;
         a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;

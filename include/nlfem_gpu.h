@@ -76,7 +76,9 @@ typedef struct nlfem_csr {
 } nlfem_csr;
 
 /* The same with 32-bit row pointers and columns (matrices below 2^31 entries): the index type
- * scipy uses for such matrices, so the Python layer wraps the arrays without copying. */
+ * scipy uses for such matrices, so the Python layer wraps the arrays without copying. The three
+ * arrays share one pinned host block owned by the library: release it with nlfem_csr32_free
+ * only (the block is kept for the next result). */
 typedef struct nlfem_csr32 {
     long K;
     long nnz;
@@ -117,7 +119,8 @@ int nlfem_stiffness_matrix32(const nlfem_problem *prob, nlfem_csr32 *out);
 int nlfem_stiffness_batch32(const nlfem_problem *probs, int n, nlfem_csr32 *outs);
 void nlfem_csr32_free(nlfem_csr32 *m);
 /* The one-shot calls keep the device buffers of their last assembly for the next call on the
- * same device (no counterpart in the reference); this frees them. */
+ * same device, and freed 32-bit results keep their pinned host blocks (no counterpart in the
+ * reference); this frees both. */
 void nlfem_cache_release(void);
 
 /* Device-resident sessions: upload once, assemble many times (benchmarks, repeated solves). */

@@ -1,4 +1,5 @@
 // Host orchestration of the assembly pipeline and the C ABI (included by assemble.cu).
+#include <map>
 #include <mutex>
 
 namespace nlg {
@@ -287,6 +288,9 @@ struct Session {
     DevBuf kclist;                          // elements of constant-kernel problems, then the others
     long long kc_nconst = -1;               // length of the first part (-1: list not built)
     long long pat_cap = 0;
+    // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
+    // mesh has the same element and vertex counts (an overflow falls back to two passes)
+    long long hint_pat_cap = 0, hint_nE = -1, hint_nV = -1;
     int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
     bool replay = false;
@@ -774,6 +778,7 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pattern_bm<DIM>, threads, smem));
     const unsigned grid = (unsigned)(S.nSM * std::max(per_sm, 1));
+    if (S.pat_cap == 0 && S.hint_pat_cap > 0 && S.hint_nE == S.nE && S.hint_nV == S.nV) S.pat_cap = S.hint_pat_cap;
     if (S.pat_cap > 0) {
         // single bitmap pass: rows go to a scratch of the previous assembly's size, then a copy
         // puts them in CSR order; a scratch overflow falls back to the two passes below
@@ -1307,6 +1312,63 @@ __global__ void k_export32(const long long *__restrict__ fptr, const int *__rest
     for (long long j = i; j < n; j += (long long)gridDim.x * blockDim.x) indices[j] = fcols[base + j] - c0;
 }
 
+// Host blocks of the 32-bit CSR results. A result's three arrays share one block (values, then
+// indices, then row pointers). Blocks are pinned, so the device-to-host copies run at the
+// host link's rate, and a freed block is kept for the next result (pinning is slow); plain
+// malloc serves when pinning fails.
+struct HostBlock {
+    size_t bytes;
+    bool pinned;
+};
+static std::mutex g_host_mu;
+static std::map<void *, HostBlock> g_host_live;                 // handed out
+static std::vector<std::pair<void *, HostBlock>> g_host_free;   // kept for reuse
+constexpr size_t HOST_KEEP_BYTES = (size_t)16 << 30;
+
+static void *host_take(size_t bytes) {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    for (size_t k = 0; k < g_host_free.size(); k++)
+        if (g_host_free[k].second.bytes >= bytes && g_host_free[k].second.bytes <= 2 * bytes + (1 << 20)) {
+            auto e = g_host_free[k];
+            g_host_free.erase(g_host_free.begin() + k);
+            g_host_live[e.first] = e.second;
+            return e.first;
+        }
+    void *p = nullptr;
+    bool pinned = cudaMallocHost(&p, bytes) == cudaSuccess;
+    if (!pinned) {
+        cudaGetLastError();
+        p = malloc(bytes);
+        if (!p) return nullptr;
+    }
+    g_host_live[p] = HostBlock{bytes, pinned};
+    return p;
+}
+
+static void host_release(void *p, const HostBlock &b) {
+    if (b.pinned) cudaFreeHost(p);
+    else free(p);
+}
+
+static void host_give(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> g(g_host_mu);
+    auto it = g_host_live.find(p);
+    if (it == g_host_live.end()) return;
+    const HostBlock b = it->second;
+    g_host_live.erase(it);
+    size_t kept = b.bytes;
+    for (auto &e : g_host_free) kept += e.second.bytes;
+    if (kept > HOST_KEEP_BYTES) { host_release(p, b); return; }
+    g_host_free.push_back({p, b});
+}
+
+static void host_release_free() {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    for (auto &e : g_host_free) host_release(e.first, e.second);
+    g_host_free.clear();
+}
+
 static int download32(Session &S, int i, nlfem_csr32 *out) {
     const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
     long long b[2];
@@ -1323,13 +1385,15 @@ static int download32(Session &S, int i, nlfem_csr32 *out) {
     CK(cudaGetLastError());
     out->K = (long)nrows;
     out->nnz = (long)nnz;
-    out->indptr = (int *)malloc(sizeof(int) * (nrows + 1));
-    out->indices = (int *)malloc(sizeof(int) * (nnz ? nnz : 1));
-    out->values = (double *)malloc(sizeof(double) * (nnz ? nnz : 1));
-    if (!out->indptr || !out->indices || !out->values) {
-        nlfem_csr32_free(out);
+    const size_t nv = (size_t)(nnz ? nnz : 1);
+    unsigned char *blk = (unsigned char *)host_take(sizeof(double) * nv + sizeof(int) * (nv + nrows + 1));
+    if (!blk) {
+        out->indptr = nullptr; out->indices = nullptr; out->values = nullptr;
         return fail(NLFEM_ERR_NOMEM, "host allocation failed");
     }
+    out->values = (double *)blk;
+    out->indices = (int *)(blk + sizeof(double) * nv);
+    out->indptr = out->indices + nv;
     CK(cudaMemcpyAsync(out->indptr, S.out64a.p, sizeof(int) * (nrows + 1), cudaMemcpyDeviceToHost, S.st));
     if (nnz) {
         CK(cudaMemcpyAsync(out->indices, S.out64b.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost, S.st));
@@ -1409,6 +1473,9 @@ static void cache_take(Session &S) {
     if (!g_cache || g_cache_dev != dev) return;
     std::vector<DevBuf *> from = g_cache->buffers(), to = S.buffers();
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
+    S.hint_pat_cap = g_cache->hint_pat_cap;
+    S.hint_nE = g_cache->hint_nE;
+    S.hint_nV = g_cache->hint_nV;
     delete g_cache;
     g_cache = nullptr;
 }
@@ -1422,6 +1489,9 @@ static void cache_give(Session &S) {
     g_cache_dev = dev;
     std::vector<DevBuf *> from = S.buffers(), to = g_cache->buffers();
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
+    g_cache->hint_pat_cap = S.pat_cap;
+    g_cache->hint_nE = S.nE;
+    g_cache->hint_nV = S.nV;
 }
 }  // namespace nlg
 
@@ -1449,7 +1519,7 @@ void nlfem_csr_free(nlfem_csr *m) {
 
 void nlfem_csr32_free(nlfem_csr32 *m) {
     if (!m) return;
-    free(m->indptr); free(m->indices); free(m->values);
+    host_give(m->values);   // the block holding all three arrays
     m->indptr = nullptr; m->indices = nullptr; m->values = nullptr;
 }
 
@@ -1541,9 +1611,12 @@ int nlfem_stiffness_matrix32(const nlfem_problem *prob, nlfem_csr32 *out) {
 }
 
 void nlfem_cache_release(void) {
-    std::lock_guard<std::mutex> g(g_cache_mu);
-    delete g_cache;
-    g_cache = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_cache_mu);
+        delete g_cache;
+        g_cache = nullptr;
+    }
+    host_release_free();
 }
 
 int nlfem_stiffness_matrix(const nlfem_problem *prob, nlfem_csr *out) {

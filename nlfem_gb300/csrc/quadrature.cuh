@@ -275,7 +275,7 @@ __device__ __forceinline__ double pow_split(double r2, double h) {
 // triangle of the nL x nL matrix, nL = 6 - NEQ: the lanes take the (map, Gauss point) items in
 // turn. The kernel value |x - y|^-(d+2s) is taken as exp2(-(d+2s)/2 log2 |x - y|^2), the same
 // function as the reference's 1/pow(sqrt(r), d+2s) without the power's extra work; FAST (mixed
-// path) evaluates it with pow_split.
+// path) evaluates it with pow_split and sums in compensated FP32.
 template <int NEQ, bool FAST>
 __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duffy &d, int c, int nT,
                                                  const double *EA, const double *EB, double dAB, double *M) {
@@ -287,6 +287,9 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
     const double a0 = EA[2] - EA[0], a1 = EA[4] - EA[0], a2 = EA[3] - EA[1], a3 = EA[5] - EA[1];
     const double b0 = EB[2] - EB[0], b1 = EB[4] - EB[0], b2 = EB[3] - EB[1], b3 = EB[5] - EB[1];
     const double hexp = -0.5 * P.expo;
+    float Mf[FAST ? 21 : 1], Mc[FAST ? 21 : 1];   // FAST: FP32 sums and their compensation
+#pragma unroll
+    for (int q = 0; q < (FAST ? 21 : 1); q++) Mf[q] = Mc[q] = 0.f;
     for (int idx = lane; idx < total; idx += 32) {
         const int k = idx % d.nPg;
         const double *al = &al_base[(long long)idx * 4];
@@ -309,12 +312,38 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
             }
         }
         const double base = ker * tf * d.dg[k] * dAB;
+        if (FAST) {
+            // mixed path: the summands, each a product of FP64 values rounded once to FP32, are
+            // added with Kahan compensation (error about 2^-23 of the sum, independent of the
+            // point count); the lanes' sums are combined in FP64 by the caller
+            float vf[NL];
 #pragma unroll
-        for (int aa = 0; aa < NL; aa++) {
-            const double fa = base * v[aa];
+            for (int aa = 0; aa < NL; aa++) vf[aa] = (float)v[aa];
+            const float bf = (float)base;
 #pragma unroll
-            for (int b = aa; b < NL; b++) M[sym_idx<6>(aa, b)] += fa * v[b];
+            for (int aa = 0; aa < NL; aa++) {
+                const float fa = bf * vf[aa];
+#pragma unroll
+                for (int b = aa; b < NL; b++) {
+                    const int q = sym_idx<6>(aa, b);
+                    const float y = fmaf(fa, vf[b], -Mc[q]);
+                    const float t = Mf[q] + y;
+                    Mc[q] = (t - Mf[q]) - y;
+                    Mf[q] = t;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int aa = 0; aa < NL; aa++) {
+                const double fa = base * v[aa];
+#pragma unroll
+                for (int b = aa; b < NL; b++) M[sym_idx<6>(aa, b)] += fa * v[b];
+            }
         }
+    }
+    if (FAST) {
+#pragma unroll
+        for (int q = 0; q < 21; q++) M[q] = (double)Mf[q] - (double)Mc[q];
     }
 }
 

@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         long long D[6];   // termLocal of T's pairs, integer sums
 #pragma unroll
         for (int i = 0; i < 6; i++) D[i] = 0;
-        const bool frac_close = P.singular && P.close == MTH_FRACTIONAL;
+        const bool frac_close = !CK && P.singular && P.close == MTH_FRACTIONAL;   // constant kernels are regular
         const float sqf = P.sqdelta_f;
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             // into the partner vertex's row) and for close pairs, whose termNonlocPrime block is
             // its own FP64 result (the difference to N^T is added here).
             __syncwarp();
-            const bool anyclose = __any_sync(FULL, close);
+            const bool anyclose = !CK && __any_sync(FULL, close);
             int nent = 0;
 #pragma unroll 1
             for (int c = 0; c < 3; c++) {

@@ -248,10 +248,15 @@ __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }
 
-// CK: the launch covers constant-kernel problems only; inside items then take the rule's
-// precomputed element sums and cut items the moment form (item_cut_const).
-template <bool CK>
+// KIND: the kernel class of the launch's problems. MIX_CONST: constant kernels; inside items take
+// the rule's precomputed element sums and cut items the moment form (item_cut_const). MIX_REGULAR:
+// other kernels without close pairs. MIX_SINGULAR: singular kernels whose close pairs come from
+// the Duffy blocks. Each instance holds only its class's code, which keeps the kernel small (it is
+// bound by instruction fetch as much as by anything else).
+enum { MIX_CONST = 0, MIX_REGULAR = 1, MIX_SINGULAR = 2 };
+template <int KIND>
 __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {
+    constexpr bool CK = KIND == MIX_CONST;
     extern __shared__ __align__(16) unsigned char s_raw[];
     const PassArgs &a = ma.p;
     const SlotMap &sm = ma.m;
@@ -307,7 +312,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         long long D[6];   // termLocal of T's pairs, integer sums
 #pragma unroll
         for (int i = 0; i < 6; i++) D[i] = 0;
-        const bool frac_close = !CK && P.singular && P.close == MTH_FRACTIONAL;   // constant kernels are regular
+        const bool frac_close = KIND == MIX_SINGULAR && P.singular && P.close == MTH_FRACTIONAL;
         const float sqf = P.sqdelta_f;
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
@@ -450,7 +455,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             // into the partner vertex's row) and for close pairs, whose termNonlocPrime block is
             // its own FP64 result (the difference to N^T is added here).
             __syncwarp();
-            const bool anyclose = !CK && __any_sync(FULL, close);
+            const bool anyclose = KIND == MIX_SINGULAR && __any_sync(FULL, close);
             int nent = 0;
 #pragma unroll 1
             for (int c = 0; c < 3; c++) {

@@ -285,8 +285,8 @@ struct Session {
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
     DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
-    DevBuf kclist;                          // elements of constant-kernel problems, then the others
-    long long kc_nconst = -1;               // length of the first part (-1: list not built)
+    DevBuf kclist;                          // elements grouped by kernel class (pass launches)
+    long long kc_off[4] = {-1, 0, 0, 0};    // class offsets into kclist (-1: list not built)
     long long pat_cap = 0;
     // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
     // mesh has the same element and vertex counts (an overflow falls back to two passes)
@@ -438,16 +438,18 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     CK(cudaMemcpyAsync(S.eoffd.p, S.eoff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, S.st));
     CK(cudaMemcpyAsync(S.voffd.p, S.voff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, S.st));
     CK(cudaMemcpyAsync(S.prm.p, S.hprm.data(), sizeof(ProbParams) * n, cudaMemcpyHostToDevice, S.st));
-    // Duffy tables (shared by the batch: same tensor degree and s required)
+    // Duffy tables (shared by the batch's singular problems: same tensor degree and s required)
     if (system) {
-        bool need = false;
-        for (int i = 0; i < n; i++) need |= (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL);
-        if (need) {
-            const nlfem_problem &p = probs[0];
+        int first = -1;
+        for (int i = 0; i < n; i++)
+            if (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL && first < 0) first = i;
+        if (first >= 0) {
+            const nlfem_problem &p = probs[first];
             const int deg = p.tensorGaussDegree;
             const int nPg = deg * deg * deg * deg;
-            for (int i = 1; i < n; i++)
-                if (probs[i].tensorGaussDegree != deg || probs[i].fractional_s != p.fractional_s)
+            for (int i = first + 1; i < n; i++)
+                if (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL &&
+                    (probs[i].tensorGaussDegree != deg || probs[i].fractional_s != p.fractional_s))
                     return fail(NLFEM_ERR_UNSUPPORTED, "batched singular problems must share degree and s");
             S.duffy_nPg = nPg;
             const int nTr[3] = {2, 5, 6};
@@ -1004,35 +1006,43 @@ static int run_close(Session &S) {
 // equal the single ones bit for bit. A contribution outside the fixed-point range sets err[5]; the
 // pass is then redone with a unit 2^16 times coarser.
 typedef void (*OneSidedKernel)(MixArgs, Rule, PassRule);
-static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, OneSidedKernel kgen,
-                              OneSidedKernel kconst, int threads, size_t smem) {
+// Kernel class of a problem for the one-sided passes: 0 constant kernel (closed forms), 1 other
+// regular kernel, 2 singular kernel with Duffy close pairs.
+static int kernel_class(const ProbParams &q) {
+    if (q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D) return 0;
+    return (q.singular && q.close == MTH_FRACTIONAL) ? 2 : 1;
+}
+
+static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, const OneSidedKernel *kfn,
+                              int threads, size_t smem) {
     const long long nnz = S.nnz_struct;
-    int nconst_p = 0;
-    for (const ProbParams &q : S.hprm) nconst_p += q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D;
+    int ncls[3] = {0, 0, 0};
+    for (const ProbParams &q : S.hprm) ncls[kernel_class(q)]++;
     struct Launch { OneSidedKernel k; const int *list; int count; int per_sm; };
-    Launch L[2];
+    Launch L[3];
     int nl = 0;
-    if (nconst_p == 0 || nconst_p == (int)S.hprm.size()) {
-        L[nl++] = Launch{nconst_p ? kconst : kgen, nullptr, (int)S.nE, 0};
-    } else {
-        if (S.kc_nconst < 0) {
+    for (int c = 0; c < 3; c++)
+        if (ncls[c] == (int)S.hprm.size()) L[nl++] = Launch{kfn[c], nullptr, (int)S.nE, 0};
+    if (nl == 0) {   // several classes: one launch per class over its problems' elements
+        if (S.kc_off[0] < 0) {
             if (S.replay) return fail(NLFEM_ERR_UNSUPPORTED, "element list by kernel class missing in graph capture");
             std::vector<int> h;
             h.reserve((size_t)S.nE);
-            for (int pass = 0; pass < 2; pass++)
-                for (const ProbParams &q : S.hprm) {
-                    const bool c = q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D;
-                    if (c == (pass == 0))
+            for (int c = 0; c < 3; c++) {
+                S.kc_off[c] = (long long)h.size();
+                for (const ProbParams &q : S.hprm)
+                    if (kernel_class(q) == c)
                         for (int e = 0; e < q.nE; e++) h.push_back(q.elem_off + e);
-                    if (pass == 0 && &q == &S.hprm.back()) S.kc_nconst = (long long)h.size();
-                }
+            }
+            S.kc_off[3] = (long long)h.size();
             ENS(S.kclist, sizeof(int) * (h.size() + 1));
             CK(cudaMemcpyAsync(S.kclist.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, S.st));
             CK(cudaStreamSynchronize(S.st));
         }
         const int *lst = S.kclist.get<int>();
-        L[nl++] = Launch{kconst, lst, (int)S.kc_nconst, 0};
-        L[nl++] = Launch{kgen, lst + S.kc_nconst, (int)(S.nE - S.kc_nconst), 0};
+        for (int c = 0; c < 3; c++)
+            if (S.kc_off[c + 1] > S.kc_off[c])
+                L[nl++] = Launch{kfn[c], lst + S.kc_off[c], (int)(S.kc_off[c + 1] - S.kc_off[c]), 0};
     }
     for (int i = 0; i < nl; i++) {
         CK(cudaFuncSetAttribute(L[i].k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1116,12 +1126,14 @@ static int run_passes(Session &S) {
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);
-    if (S.pmode == PM_RETRI)
-        return run_pass_one_sided(S, a, pr, k_pass_mix2d<false>, k_pass_mix2d<true>, MIX_THREADS,
-                                  mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
-    if (S.pmode == PM_BARY)
-        return run_pass_one_sided(S, a, pr, k_pass_bary<DIM, false>, k_pass_bary<DIM, true>, BARY_THREADS,
-                                  bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
+    if (S.pmode == PM_RETRI) {
+        const OneSidedKernel k[3] = {k_pass_mix2d<MIX_CONST>, k_pass_mix2d<MIX_REGULAR>, k_pass_mix2d<MIX_SINGULAR>};
+        return run_pass_one_sided(S, a, pr, k, MIX_THREADS, mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
+    }
+    if (S.pmode == PM_BARY) {   // no singular kernels here
+        const OneSidedKernel k[3] = {k_pass_bary<DIM, true>, k_pass_bary<DIM, false>, k_pass_bary<DIM, false>};
+        return run_pass_one_sided(S, a, pr, k, BARY_THREADS, bary_warp_bytes<DIM>(S.rule.nPx) * BARY_WARPS);
+    }
     const size_t smem = sizeof(int) * PASS_WARPS * dV * ROWCACHE;
     if (S.prec == PREC_MIX) CK(cudaFuncSetAttribute(k_pass<DIM, PREC_MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else CK(cudaFuncSetAttribute(k_pass<DIM, PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -380,6 +380,25 @@ def test_mixed_batch_mixed_kernels(nl, orc):
         assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
+def test_mixed_batch_three_kernel_classes(nl, orc):
+    """Constant, parabola and fractional (Duffy close pairs) problems in one batch: one pass
+    launch per kernel class, each matrix equal to its single assembly."""
+    c = conf2d(rule="16", close="fractional", deg=3, precision="mixed")
+    probs = [(square_mesh(10, 0.2, jitter=0.1, seed=21), {"function": "constant", "horizon": 0.2, "outputdim": 1}, c),
+             (square_mesh(9, 0.2, jitter=0.1, seed=22), {"function": "fractional", "horizon": 0.2, "outputdim": 1,
+                                                          "fractional_s": 0.4}, c),
+             (square_mesh(8, 0.2, jitter=0.1, seed=23), {"function": "parabola", "horizon": 0.2, "outputdim": 1}, c)]
+    As = nl.stiffnessMatrix_batch(probs)
+    for (m, k, cc), A in zip(probs, As):
+        B = nl.stiffnessMatrix(m, k, cc)
+        assert same_pattern(A, B)
+        assert abs(A - B).max() <= 1e-12 * abs(B).max()
+        R = orc.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))["A"]
+        assert same_pattern(A, R)
+        fro, mx = rel_errors(A, R)
+        assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
 def test_mixed_pair_list_exact(nl, orc):
     m = square_mesh(24, 0.13, jitter=0.2, seed=3)
     k = {"function": "constant", "horizon": 0.13, "outputdim": 1}

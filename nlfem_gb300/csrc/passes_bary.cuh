@@ -73,6 +73,8 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
     BaryEntry<DIM> *slist = reinterpret_cast<BaryEntry<DIM> *>(res);
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
+    bool bad = false;   // a contribution outside the fixed-point range (reported at the end)
+    bool miss = false;  // a matrix slot not found (reported at the end)
     unsigned nsub = 0, namb = 0, nitin = 0;
     unsigned char mycls[MAXQ];
     for (;;) {
@@ -237,9 +239,9 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                 }
                 long long lx[NS];
 #pragma unroll
-                for (int i = 0; i < NS; i++) lx[i] = fx64(2.f * L[i] * rTT, P.fx_mul, ovf);
+                for (int i = 0; i < NS; i++) lx[i] = fx64(2.f * L[i] * rTT, P.fx_mul, bad);
 #pragma unroll
-                for (int i = 0; i < dV * dV; i++) nx[i] = fx64(2.f * N[i] * rTT, P.fx_mul, ovf);
+                for (int i = 0; i < dV * dV; i++) nx[i] = fx64(2.f * N[i] * rTT, P.fx_mul, bad);
                 balance_rows<dV>(lx, nx, nullptr, nullptr);
 #pragma unroll
                 for (int i = 0; i < NS; i++) D[i] += lx[i];
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                 h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
                 if (h.mask == 0xffffffffu) continue;   // T's vertex r has no row
                 const long long s = slot_find_row(sm, h, slist[e].col);
-                if (s < 0) atomicOr(&a.err[3], 1);
+                if (s < 0) miss = true;
                 else red_add(vals, s, -slist[e].v[r]);
             }
             __syncwarp();
@@ -316,12 +318,14 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                 for (int i = 0; i < NS; i++)
                     if (i == si) d = D[i];
                 const long long s = slot_find_row(sm, h, a.T32[(long long)T * dV + c]);
-                if (s < 0) atomicOr(&a.err[3], 1);
+                if (s < 0) miss = true;
                 else red_add(vals, s, d);
             }
         }
         __syncwarp();
     }
+    if (__any_sync(FULL, bad) && lane == 0) atomicOr(ovf, 1);
+    if (__any_sync(FULL, miss) && lane == 0) atomicOr(&a.err[3], 1);
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
     nitin = warp_sum(nitin);

@@ -271,6 +271,8 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
     ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
+    bool bad = false;   // a contribution outside the fixed-point range (reported at the end)
+    bool miss = false;  // a matrix slot not found (reported at the end)
     unsigned nsub = 0, namb = 0, nclose = 0, nitin = 0, nitcut = 0;
     unsigned char mycls[MAXQ];
     for (;;) {
@@ -399,22 +401,22 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     nclose++;
                     const long long cs = close_slot(a.xadj, a.adj, T, part);
                     if (cs < 0) {
-                        atomicOr(&a.err[3], 1);
+                        miss = true;
                     } else {
                         const double *cb = &a.closebuf[cs * 36];
 #pragma unroll
                         for (int i = 0; i < 3; i++)
 #pragma unroll
-                            for (int j = i; j < 3; j++) lx[sym_idx<3>(i, j)] = fx64d(cb[3 * i + j], P.fx_mul, ovf);
+                            for (int j = i; j < 3; j++) lx[sym_idx<3>(i, j)] = fx64d(cb[3 * i + j], P.fx_mul, bad);
 #pragma unroll
                         for (int i = 0; i < 9; i++) {
-                            nx[i] = fx64d(cb[9 + i], P.fx_mul, ovf);    // termNonloc [T vertex][b vertex]
-                            mx[i] = fx64d(cb[27 + i], P.fx_mul, ovf);   // termNonlocPrime [T vertex][b vertex]
+                            nx[i] = fx64d(cb[9 + i], P.fx_mul, bad);    // termNonloc [T vertex][b vertex]
+                            mx[i] = fx64d(cb[27 + i], P.fx_mul, bad);   // termNonlocPrime [T vertex][b vertex]
                         }
 #pragma unroll
                         for (int i = 0; i < 3; i++)
 #pragma unroll
-                            for (int j = i; j < 3; j++) lpx[sym_idx<3>(i, j)] = fx64d(cb[18 + 3 * i + j], P.fx_mul, ovf);
+                            for (int j = i; j < 3; j++) lpx[sym_idx<3>(i, j)] = fx64d(cb[18 + 3 * i + j], P.fx_mul, bad);
                     }
                 } else {
                     float L[6] = {0, 0, 0, 0, 0, 0}, N[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -435,11 +437,11 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                         for (int ab = 0; ab < 6; ab++) LP[ab] = fmaf(dk, rr[4 + ab], LP[ab]);
                     }
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lx[i] = fx64(L[i] * rTT, P.fx_mul, ovf);
+                    for (int i = 0; i < 6; i++) lx[i] = fx64(L[i] * rTT, P.fx_mul, bad);
 #pragma unroll
-                    for (int i = 0; i < 9; i++) mx[i] = nx[i] = fx64(N[i] * rTT, P.fx_mul, ovf);
+                    for (int i = 0; i < 9; i++) mx[i] = nx[i] = fx64(N[i] * rTT, P.fx_mul, bad);
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lpx[i] = fx64(LP[i] * rTT, P.fx_mul, ovf);
+                    for (int i = 0; i < 6; i++) lpx[i] = fx64(LP[i] * rTT, P.fx_mul, bad);
                 }
                 balance_rows<3>(lx, nx, lpx, mx);
 #pragma unroll
@@ -499,16 +501,16 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
                 if (h.mask != 0xffffffffu) {
                     const long long s = slot_find_row(sm, h, col);
-                    if (s < 0) { atomicOr(&a.err[3], 1); continue; }
+                    if (s < 0) { miss = true; continue; }
                     red_add(ma.valsN, s, -sn);
                     if (anyclose && keepc && sq != sn) {
                         const int tp = sm.tpos[s];
-                        if (tp < 0) atomicOr(&a.err[3], 1);
+                        if (tp < 0) miss = true;
                         else red_add(vals, sm.rowptr[col] + tp, sn - sq);
                     }
                 } else if (keepc) {
                     const long long q = slot_find(sm, col, W.tvs[r]);
-                    if (q < 0) atomicOr(&a.err[3], 1);
+                    if (q < 0) miss = true;
                     else red_add(vals, q, -sq);
                 }
             }
@@ -528,10 +530,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             for (int i = 0; i < 6; i++)
                 if (i == si) d = D[i];
             if (s >= 0) red_add(vals, s, d);
-            else if (keepmask & (1u << r)) atomicOr(&a.err[3], 1);
+            else if (keepmask & (1u << r)) miss = true;
         }
         __syncwarp();
     }
+    if (__any_sync(FULL, bad) && lane == 0) atomicOr(ovf, 1);
+    if (__any_sync(FULL, miss) && lane == 0) atomicOr(&a.err[3], 1);
     nsub = warp_sum(nsub);
     namb = warp_sum(namb);
     nclose = warp_sum(nclose);

@@ -79,6 +79,19 @@ __device__ __forceinline__ long long fx64(float v, float mul, int *ovf) {
     }
     return __float2ll_rn(t);
 }
+// The same with the overflow recorded in a flag of the caller (reported once, not per value).
+__device__ __forceinline__ long long fx64(float v, float mul, bool &bad) {
+    const float t = v * mul;
+    const bool ok = fabsf(t) < 4.0e18f;
+    bad |= !ok;
+    return ok ? __float2ll_rn(t) : 0;
+}
+__device__ __forceinline__ long long fx64d(double v, double mul, bool &bad) {
+    const double t = v * mul;
+    const bool ok = fabs(t) < 4.0e18;
+    bad |= !ok;
+    return ok ? __double2ll_rn(t) : 0;
+}
 __device__ __forceinline__ long long fx64d(double v, double mul, int *ovf) {
     const double t = v * mul;
     if (!(fabs(t) < 4.0e18)) {

@@ -157,18 +157,15 @@ __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F
             const float ealong = 10.f * U32 * vscale / fmaxf(sv * sqrtf(bb), 1e-30f);
             if (fabsf(lam1) <= MARG_L || fabsf(lam1 - 1.f) <= MARG_L) { amb = true; if (why) *why |= 8u; }
             if (fabsf(lam2) <= MARG_L || fabsf(lam2 - 1.f) <= MARG_L) { amb = true; if (why) *why |= 16u; }
-            if (lam1 >= 0.f && lam1 <= 1.f) {
+            // the two roots in turn (one code path for both keeps the routine small)
+#pragma unroll 1
+            for (int qi = 0; qi < 2; qi++) {
+                const float lam = qi ? lam2 : lam1;
+                if (!(lam >= 0.f && lam <= 1.f && (qi == 0 || v > 0.f))) continue;
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
-                const FPt y1{f2(fmaf(lam1, b.x, q.x), fmaf(lam1, b.y, q.y)), eperp, ealong};
-                if (is_onEdge && caps) fplace_cap(Y, Y.last, y1, sq, P, nu, orientation, amb, why);
-                fpush(Y, y1, amb);
-                is_onEdge = true;
-            }
-            if (lam2 >= 0.f && lam2 <= 1.f && v > 0.f) {
-                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Y.n != 0);
-                const FPt y2{f2(fmaf(lam2, b.x, q.x), fmaf(lam2, b.y, q.y)), eperp, ealong};
-                if (is_onEdge && caps) fplace_cap(Y, Y.last, y2, sq, P, nu, orientation, amb, why);
-                fpush(Y, y2, amb);
+                const FPt y{f2(fmaf(lam, b.x, q.x), fmaf(lam, b.y, q.y)), eperp, ealong};
+                if (is_onEdge && caps) fplace_cap(Y, Y.last, y, sq, P, nu, orientation, amb, why);
+                fpush(Y, y, amb);
                 is_onEdge = true;
             }
         }

@@ -117,21 +117,21 @@ __device__ __forceinline__ int xretriangulate(const double *xc, const double *TE
                 lam2 = xsub(term1, term2);
                 lam1 = xdiv(xmul(xdiv(1.0, lam2), aad), bb);
             }
-            const double y1[2] = {xadd(xmul(lam1, b0), q[0]), xadd(xmul(lam1, b1), q[1])};
-            const double y2[2] = {xadd(xmul(lam2, b0), q[0]), xadd(xmul(lam2, b1), q[1])};
-            if ((0 <= lam1) && (lam1 <= 1)) {
+            // the two roots in turn (one code path for both keeps the routine small)
+#pragma unroll 1
+            for (int qi = 0; qi < 2; qi++) {
+                const double lam = qi ? lam2 : lam1;
+                bool ok = (0 <= lam) && (lam <= 1);
+                if (qi) {
+                    const double dl = xsub(lam1, lam2);
+                    ok = ok && (xmul(dl, dl) > 0);
+                }
+                if (!ok) continue;
+                const double y[2] = {xadd(xmul(lam, b0), q[0]), xadd(xmul(lam, b1), q[1])};
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
                 if (is_onEdge && caps)
-                    Rdx += xplaceCap(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                if (Rdx < 9) { R[2 * Rdx] = y1[0]; R[2 * Rdx + 1] = y1[1]; Rdx += 1; }
-                is_onEdge = true;
-            }
-            const double dl = xsub(lam1, lam2);
-            if ((0 <= lam2) && (lam2 <= 1) && (xmul(dl, dl) > 0)) {
-                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (Rdx != 0);
-                if (is_onEdge && caps)
-                    Rdx += xplaceCap(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                if (Rdx < 9) { R[2 * Rdx] = y2[0]; R[2 * Rdx + 1] = y2[1]; Rdx += 1; }
+                    Rdx += xplaceCap(&R[2 * (Rdx - 1)], y, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
+                if (Rdx < 9) { R[2 * Rdx] = y[0]; R[2 * Rdx + 1] = y[1]; Rdx += 1; }
                 is_onEdge = true;
             }
         }

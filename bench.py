@@ -36,7 +36,7 @@ METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel e
 
 # DRAM traffic (read + write bytes) of the one k_pass_mix2d launch of a C2 assembly, from the ncu
 # capture summarised in profiles/k_pass_mix2d_2d-constant.md; None for workloads not captured.
-PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): 5.29e9 + 1.07e9}
+PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): 5.32e9 + 1.07e9}
 
 
 def workload(args, precision):

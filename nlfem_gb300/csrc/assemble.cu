@@ -538,6 +538,14 @@ struct RowArgs {
     unsigned long long *cursor;
     long long *rowoff;         // scratch offset of each row
     int *ovf;                  // set when the scratch is too small
+    // bitmap kernel sources: mode 0, the vertices of the pairs of the elements at the row's
+    // vertex (rows of vertices with label > 0, or of every vertex with all_rows); mode 1, the
+    // union of a given row (srcoff / srccnt / srccols) and a given transposed row (tptr / tcols)
+    int mode, all_rows;
+    const long long *srcoff;
+    const int *srccnt, *srccols;
+    const long long *tptr;
+    const int *tcols;
 };
 
 // One warp per row (vertex) u with label > 0: union of the vertices of every element that
@@ -602,7 +610,7 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long u = gw; u < a.nV; u += nw) {
-        if (a.labV[u] <= 0) {
+        if (!a.all_rows && a.labV[u] <= 0) {
             if (pass != 1 && lane == 0) a.rowcnt[u] = 0;
             if (pass == 2 && lane == 0) a.rowoff[u] = 0;
             continue;
@@ -613,7 +621,23 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         for (int i = lane; i < wu; i += 32) bm[i] = 0u;
         __syncwarp();
         int lo = 0x7fffffff, hi = -1;
-        for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
+        if (a.mode == 1) {   // union of a row and its transposed row
+            const long long o = a.srcoff[u];
+            const int n = a.srccnt[u];
+            for (int i = lane; i < n; i += 32) {
+                const int v = a.srccols[o + i] - voff;
+                atomicOr(&bm[v >> 5], 1u << (v & 31));
+                lo = min(lo, v);
+                hi = max(hi, v);
+            }
+            for (long long i = a.tptr[u] + lane; i < a.tptr[u + 1]; i += 32) {
+                const int v = a.tcols[i] - voff;
+                atomicOr(&bm[v >> 5], 1u << (v & 31));
+                lo = min(lo, v);
+                hi = max(hi, v);
+            }
+        }
+        for (long long t = a.mode == 1 ? a.vptr[u + 1] : a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
             const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
             const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
@@ -688,6 +712,40 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         }
         if (pass == 0 && lane == 0) a.rowcnt[u] = (int)w;
         __syncwarp();
+    }
+}
+
+// Transposed rows of the out-pair rows (warp per source row u, its entries in the scratch):
+// k_tcount counts, for every column v with a matrix row, the rows u holding it; k_tfill lists them
+// (in atomic order: the union pass sorts).
+__global__ void k_tcount(const long long *__restrict__ off, const int *__restrict__ cnt,
+                         const int *__restrict__ cols, const int *__restrict__ labV, long long nV,
+                         int *__restrict__ tcnt) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long u = gw; u < nV; u += nw) {
+        const long long o = off[u];
+        const int n = cnt[u];
+        for (int i = lane; i < n; i += 32) {
+            const int v = cols[o + i];
+            if (labV[v] > 0) atomicAdd(&tcnt[v], 1);
+        }
+    }
+}
+__global__ void k_tfill(const long long *__restrict__ off, const int *__restrict__ cnt,
+                        const int *__restrict__ cols, const int *__restrict__ labV, long long nV,
+                        const long long *__restrict__ tptr, int *__restrict__ tfill, int *__restrict__ tcols) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long u = gw; u < nV; u += nw) {
+        const long long o = off[u];
+        const int n = cnt[u];
+        for (int i = lane; i < n; i += 32) {
+            const int v = cols[o + i];
+            if (labV[v] > 0) tcols[tptr[v] + atomicAdd(&tfill[v], 1)] = (int)u;
+        }
     }
 }
 

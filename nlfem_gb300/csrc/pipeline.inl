@@ -285,6 +285,8 @@ struct Session {
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
     DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
+    DevBuf po_cnt, po_off, po_ptr, po_scratch, tcnt, tptr, tcols;   // transposed pattern construction
+    long long po_cap = 0, t_nnz = 0;
     DevBuf kclist;                          // elements grouped by kernel class (pass launches)
     long long kc_off[4] = {-1, 0, 0, 0};    // class offsets into kclist (-1: list not built)
     long long pat_cap = 0;
@@ -308,7 +310,8 @@ struct Session {
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp};
+                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
+                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -639,6 +642,15 @@ static int sort_segments(Session &S, const long long *ptr, long long nseg, int *
     return NLFEM_OK;
 }
 
+// Threads per block of the shared-memory bitmap pattern kernel (0: a problem's vertex bitmap is too
+// large, the global-memory marks kernel runs instead).
+static int pattern_bitmap_threads(const Session &S) {
+    const int words = (S.maxNV + 31) / 32;
+    if ((size_t)words * 4 * 8 <= 200 * 1024) return 256;
+    if ((size_t)words * 4 * 2 <= 200 * 1024) return 64;
+    return 0;
+}
+
 template <int DIM>
 static int run_pairs(Session &S) {
     const long long nE = S.nE;
@@ -652,7 +664,9 @@ static int run_pairs(Session &S) {
     ENS(S.pB, sizeof(int) * (P + 1));
     k_compact_pairs<<<grid_for(nE * 32, 256), 256, 0, S.st>>>(S.seg_start.get<long long>(), S.seg_cnt.get<int>(), S.out_ptr.get<long long>(), S.pool.get<int>(), nE, S.pA.get<int>(), S.pB.get<int>()); ++S.nlaunch;
     S.stats.n_pairs = (long)P;
-    if (S.pmode == PM_BARY) {   // barycenter pairs write the outer element's rows only: no in-lists
+    if (S.pmode == PM_BARY || (S.pmode == PM_RETRI && pattern_bitmap_threads(S))) {
+        // barycenter pairs write the outer element's rows only; the retriangulate pattern takes
+        // its in-pair columns from the transposed out-pair rows: no in-lists
         CK(cudaGetLastError());
         return NLFEM_OK;
     }
@@ -761,12 +775,75 @@ static int run_slot_maps(Session &S) {
     return NLFEM_OK;
 }
 
+// Rows of the one-sided retriangulate pass without element in-lists. Row t holds the vertices of
+// the partners of t's elements (out-pairs) and of the elements whose partners contain t
+// (in-pairs): the second set is {u : t in out-row(u)}, the transpose of the out-pair rows. So
+// the out-pair rows of every vertex go to a scratch (one bitmap pass; a first assembly counts
+// first), are transposed (count, scan, fill), and the row pass below takes the union of each
+// row and its transpose. A scratch overflow (err[10]) recounts.
+template <int DIM>
+static int run_pattern_transposed(Session &S, RowArgs &a, int words, int threads, unsigned grid, size_t smem) {
+    const long long nV = S.nV;
+    ENS(S.po_cnt, sizeof(int) * (nV + 1));
+    ENS(S.po_off, sizeof(long long) * (nV + 1));
+    ENS(S.po_ptr, sizeof(long long) * (nV + 1));
+    RowArgs o = a;
+    o.in_ptr = nullptr;
+    o.all_rows = 1;
+    o.mode = 0;
+    o.rowptr = nullptr; o.cols = nullptr;
+    o.rowcnt = S.po_cnt.get<int>();
+    o.rowoff = S.po_off.get<long long>();
+    unsigned long long *cursor = S.counters.get<unsigned long long>() + 14;
+    int *ovf = S.err.get<int>() + 10;
+    int r;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (S.po_cap == 0) {   // count the rows first
+            o.scratch = nullptr; o.cap = 0; o.cursor = nullptr; o.ovf = nullptr;
+            k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 0, words); ++S.nlaunch;
+            if ((r = scan_excl<int>(S, S.po_cnt.get<int>(), nV, S.po_ptr.get<long long>()))) return r;
+            long long tot = 0;
+            if ((r = d2h(S, &tot, S.po_ptr.get<long long>() + nV, 1))) return r;
+            S.po_cap = tot + 1;
+        }
+        ENS(S.po_scratch, sizeof(int) * (S.po_cap + 1));
+        CK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), S.st));
+        CK(cudaMemsetAsync(ovf, 0, sizeof(int), S.st));
+        o.scratch = S.po_scratch.get<int>(); o.cap = S.po_cap; o.cursor = cursor; o.ovf = ovf;
+        k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 2, words); ++S.nlaunch;
+        int of = 0;
+        if ((r = d2h(S, &of, ovf, 1))) return r;
+        if (!of) break;
+        if (attempt == 1) return fail(NLFEM_ERR_CUDA, "internal: out-pair row scratch overflow after a recount");
+        S.po_cap = 0;
+    }
+    ENS(S.tcnt, sizeof(int) * (nV + 1));
+    ENS(S.tptr, sizeof(long long) * (nV + 1));
+    CK(cudaMemsetAsync(S.tcnt.p, 0, sizeof(int) * (nV + 1), S.st));
+    k_tcount<<<S.nSM * 8, 256, 0, S.st>>>(S.po_off.get<long long>(), S.po_cnt.get<int>(), S.po_scratch.get<int>(),
+                                          S.labV.get<int>(), nV, S.tcnt.get<int>()); ++S.nlaunch;
+    if ((r = scan_excl<int>(S, S.tcnt.get<int>(), nV, S.tptr.get<long long>()))) return r;
+    if ((r = d2h(S, &S.t_nnz, S.tptr.get<long long>() + nV, 1))) return r;
+    ENS(S.tcols, sizeof(int) * (S.t_nnz + 1));
+    CK(cudaMemsetAsync(S.tcnt.p, 0, sizeof(int) * (nV + 1), S.st));
+    k_tfill<<<S.nSM * 8, 256, 0, S.st>>>(S.po_off.get<long long>(), S.po_cnt.get<int>(), S.po_scratch.get<int>(),
+                                         S.labV.get<int>(), nV, S.tptr.get<long long>(), S.tcnt.get<int>(),
+                                         S.tcols.get<int>()); ++S.nlaunch;
+    CK(cudaGetLastError());
+    a.mode = 1;
+    a.all_rows = 0;
+    a.srcoff = S.po_off.get<long long>(); a.srccnt = S.po_cnt.get<int>(); a.srccols = S.po_scratch.get<int>();
+    a.tptr = S.tptr.get<long long>(); a.tcols = S.tcols.get<int>();
+    return NLFEM_OK;
+}
+
 template <int DIM>
 static int run_pattern_bm(Session &S, int words, int threads) {
     const long long nV = S.nV;
     ENS(S.rowcnt, sizeof(int) * (nV + 1));
     ENS(S.rowptr, sizeof(long long) * (nV + 1));
     RowArgs a;
+    memset(&a, 0, sizeof(a));
     a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
     a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
     a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>();
@@ -780,6 +857,10 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pattern_bm<DIM>, threads, smem));
     const unsigned grid = (unsigned)(S.nSM * std::max(per_sm, 1));
+    if (S.pmode == PM_RETRI) {
+        int r = run_pattern_transposed<DIM>(S, a, words, threads, grid, smem);
+        if (r) return r;
+    }
     if (S.pat_cap == 0 && S.hint_pat_cap > 0 && S.hint_nE == S.nE && S.hint_nV == S.nV) S.pat_cap = S.hint_pat_cap;
     if (S.pat_cap > 0) {
         // single bitmap pass: rows go to a scratch of the previous assembly's size, then a copy
@@ -830,9 +911,7 @@ static int run_pattern(Session &S) {
     const long long nV = S.nV;
     // bitmap marks in shared memory when a problem's vertex bitmap is small enough
     const int words = (S.maxNV + 31) / 32;
-    int bm_threads = 0;
-    if ((size_t)words * 4 * 8 <= 200 * 1024) bm_threads = 256;
-    else if ((size_t)words * 4 * 2 <= 200 * 1024) bm_threads = 64;
+    const int bm_threads = pattern_bitmap_threads(S);
     if (bm_threads) return run_pattern_bm<DIM>(S, words, bm_threads);
     const int nwarps = S.nSM * 4 * 8;
     ENS(S.marks, sizeof(unsigned) * (size_t)nwarps * S.maxNV);
@@ -1252,9 +1331,9 @@ static int run_system_graph_t(Session &S) {
         const long long launches = S.nlaunch;
         CK(cudaGraphLaunch(S.gexec, S.st));
         CK(cudaStreamSynchronize(S.st));
-        int he[7];
-        if ((r = d2h(S, he, S.err.get<int>(), 7))) return r;
-        if (!he[0] && !he[1] && !he[5] && !he[6]) {
+        int he[11];
+        if ((r = d2h(S, he, S.err.get<int>(), 11))) return r;
+        if (!he[0] && !he[1] && !he[5] && !he[6] && !he[10]) {
             S.nlaunch = launches;
             return run_system_post(S);
         }

@@ -292,7 +292,7 @@ struct Session {
     long long pat_cap = 0;
     // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
     // mesh has the same element and vertex counts (an overflow falls back to two passes)
-    long long hint_pat_cap = 0, hint_nE = -1, hint_nV = -1;
+    long long hint_pat_cap = 0, hint_po_cap = 0, hint_nE = -1, hint_nV = -1;
     int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
     bool replay = false;
@@ -857,11 +857,14 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pattern_bm<DIM>, threads, smem));
     const unsigned grid = (unsigned)(S.nSM * std::max(per_sm, 1));
+    if (S.hint_nE == S.nE && S.hint_nV == S.nV) {   // one-shot calls: the previous call's sizes
+        if (S.pat_cap == 0) S.pat_cap = S.hint_pat_cap;
+        if (S.po_cap == 0) S.po_cap = S.hint_po_cap;
+    }
     if (S.pmode == PM_RETRI) {
         int r = run_pattern_transposed<DIM>(S, a, words, threads, grid, smem);
         if (r) return r;
     }
-    if (S.pat_cap == 0 && S.hint_pat_cap > 0 && S.hint_nE == S.nE && S.hint_nV == S.nV) S.pat_cap = S.hint_pat_cap;
     if (S.pat_cap > 0) {
         // single bitmap pass: rows go to a scratch of the previous assembly's size, then a copy
         // puts them in CSR order; a scratch overflow falls back to the two passes below
@@ -1565,6 +1568,7 @@ static void cache_take(Session &S) {
     std::vector<DevBuf *> from = g_cache->buffers(), to = S.buffers();
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
     S.hint_pat_cap = g_cache->hint_pat_cap;
+    S.hint_po_cap = g_cache->hint_po_cap;
     S.hint_nE = g_cache->hint_nE;
     S.hint_nV = g_cache->hint_nV;
     delete g_cache;
@@ -1581,6 +1585,7 @@ static void cache_give(Session &S) {
     std::vector<DevBuf *> from = S.buffers(), to = g_cache->buffers();
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
     g_cache->hint_pat_cap = S.pat_cap;
+    g_cache->hint_po_cap = S.po_cap;
     g_cache->hint_nE = S.nE;
     g_cache->hint_nV = S.nV;
 }

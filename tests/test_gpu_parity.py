@@ -399,6 +399,25 @@ def test_mixed_batch_three_kernel_classes(nl, orc):
         assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
+def test_one_shot_capacity_hints_overflow(nl, orc):
+    """One-shot calls reuse the previous call's pattern sizes as scratch capacities when the mesh
+    has the same counts. A second mesh with the same counts and a larger ball overflows them; the
+    recount must give the exact pattern and values."""
+    m = square_mesh(16, 0.1, jitter=0.2, seed=31)
+    k1 = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    nl.stiffnessMatrix(m, k1, conf2d(precision="mixed"))
+    m2 = square_mesh(16, 0.1, jitter=0.1, seed=32)   # same counts
+    k2 = {"function": "constant", "horizon": 0.25, "outputdim": 1}
+    A = nl.stiffnessMatrix(m2, k2, conf2d(precision="mixed"))
+    B = orc.assemble(m2, k2, conf2d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+    A1 = nl.stiffnessMatrix(m, k1, conf2d(precision="mixed"))   # and back to the smaller one
+    B1 = orc.assemble(m, k1, conf2d())["A"]
+    assert same_pattern(A1, B1)
+
+
 def test_mixed_pair_list_exact(nl, orc):
     m = square_mesh(24, 0.13, jitter=0.2, seed=3)
     k = {"function": "constant", "horizon": 0.13, "outputdim": 1}

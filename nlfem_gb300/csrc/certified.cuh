@@ -177,14 +177,16 @@ __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F
     return Y.n;
 }
 
-// Squared distance from the origin to the segment [p, q] and a bound on its FP32 error.
-__device__ __forceinline__ float fseg_dist2(F2 p, F2 q) {
+// True when the segment [p, q] stays farther than sqrt(lim) from the origin (end points given
+// farther already). The closest point is an end point unless the origin projects inside the
+// segment, where the squared distance is (p x u)^2 / |u|^2: compared multiplied by |u|^2, so no
+// division is needed (the cross product keeps its relative accuracy near the threshold).
+__device__ __forceinline__ bool fseg_far(F2 p, F2 q, float lim) {
     const F2 u = q - p;
-    const float uu = dot(u, u);
-    float t = uu > 0.f ? -dot(p, u) / uu : 0.f;
-    t = fminf(fmaxf(t, 0.f), 1.f);
-    const F2 c = f2(fmaf(t, u.x, p.x), fmaf(t, u.y, p.y));
-    return dot(c, c);
+    const float uu = dot(u, u), pu = dot(p, u);
+    if (!(pu < 0.f && -pu < uu)) return true;   // the closest point is an end point
+    const float cr = fmaf(p.x, u.y, -p.y * u.x);
+    return cr * cr > lim * uu;
 }
 
 enum { CLS_OUT = 0, CLS_IN = 1, CLS_CUT = 2 };
@@ -199,8 +201,7 @@ __device__ __forceinline__ int fclassify(const F2 *P, float sq) {
     if (d0 < sqlo && d1 < sqlo && d2 < sqlo) return CLS_IN;
     const float m = fminf(fminf(d0, d1), d2);
     if (m > sqhi) {
-        const float s0 = fseg_dist2(P[0], P[1]), s1 = fseg_dist2(P[1], P[2]), s2 = fseg_dist2(P[2], P[0]);
-        if (fminf(fminf(s0, s1), s2) > sqhi) return CLS_OUT;
+        if (fseg_far(P[0], P[1], sqhi) && fseg_far(P[1], P[2], sqhi) && fseg_far(P[2], P[0], sqhi)) return CLS_OUT;
     }
     return CLS_CUT;
 }

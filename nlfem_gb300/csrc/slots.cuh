@@ -100,8 +100,10 @@ __device__ __forceinline__ long long fx64d(double v, double mul, int *ovf) {
     }
     return __double2ll_rn(t);
 }
+// Adds v to vals[s] (a zero is added too: a branch at every call site costs more than the
+// reduction).
 __device__ __forceinline__ void red_add(long long *vals, long long s, long long v) {
-    if (v) atomicAdd(reinterpret_cast<unsigned long long *>(vals) + s, (unsigned long long)v);
+    atomicAdd(reinterpret_cast<unsigned long long *>(vals) + s, (unsigned long long)v);
 }
 
 // ------------------------------------------------------------------ construction

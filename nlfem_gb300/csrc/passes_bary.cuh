@@ -120,10 +120,12 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
 #pragma unroll
         for (int i = 0; i < NS; i++) D[i] = 0;
         const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
+        int part_next = lb + lane < le ? a.pB[lb + lane] : T;   // partners one batch ahead
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
             const bool act = p < le;
-            const int part = act ? a.pB[p] : T;
+            const int part = part_next;
+            part_next = p + 32 < le ? a.pB[p + 32] : T;
             float pc[DIM * dV];
 #pragma unroll
             for (int j = 0; j < DIM * dV; j++)

@@ -316,10 +316,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         for (int i = 0; i < 6; i++) D[i] = 0;
         const bool frac_close = KIND == MIX_SINGULAR && P.singular && P.close == MTH_FRACTIONAL;
         const float sqf = P.sqdelta_f;
+        int part_next = lb + lane < le ? a.pB[lb + lane] : T;   // partners one batch ahead
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
             const bool act = p < le;
-            const int part = act ? a.pB[p] : T;
+            const int part = part_next;
+            part_next = p + 32 < le ? a.pB[p + 32] : T;
             int pv[3];
 #pragma unroll
             for (int r = 0; r < 3; r++) pv[r] = a.T32[(long long)part * 3 + r];

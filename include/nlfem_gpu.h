@@ -123,6 +123,15 @@ void nlfem_csr32_free(nlfem_csr32 *m);
  * reference); this frees both. */
 void nlfem_cache_release(void);
 
+/* par_evaluateMass (Cassemble.h:202-204): vd = M ud with the P1 mass matrix of the first J
+ * elements whose label is positive, integrated by the rule (P, dx) of nP points. CG rows and
+ * columns are the vertices with a positive label; DG (is_dg) indices are (dim + 1) * element + a.
+ * Host arrays: elements (nE, dim + 1), elementLabels (nE), vertices (nV, dim), vertexLabels (nV),
+ * ud and vd of K * outdim entries, K = nV (CG) or (dim + 1) * nE (DG). Deterministic. */
+int nlfem_evaluate_mass(int dim, int outdim, int is_dg, long nE, long J, long nV, const long *elements,
+                        const long *elementLabels, const double *vertices, const long *vertexLabels,
+                        int nP, const double *P, const double *dx, const double *ud, double *vd);
+
 /* Device-resident sessions: upload once, assemble many times (benchmarks, repeated solves). */
 typedef struct nlfem_session nlfem_session;
 int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out);

@@ -1,4 +1,4 @@
-"""Builds libnlfem_gpu.so in-tree with nvcc for sm_103a (four translation units in parallel)."""
+"""Builds libnlfem_gpu.so in-tree with nvcc for sm_103a (five translation units in parallel)."""
 import os
 import subprocess
 import sys
@@ -40,6 +40,8 @@ def build(force=False, verbose=False):
                                   "-o", os.path.join(objdir, "noalloc.o")],
         [NVCC] + ARCH + common + ["-c", os.path.join(CSRC, "peaks.cu"),
                                   "-o", os.path.join(objdir, "peaks.o")],
+        [NVCC] + ARCH + common + ["-c", os.path.join(CSRC, "mass.cu"),
+                                  "-o", os.path.join(objdir, "mass.o")],
     ]
 
     def run(cmd):
@@ -58,7 +60,8 @@ def build(force=False, verbose=False):
                 print(l)
     tmp = LIB + ".tmp"
     run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(objdir, "assemble.o"),
-                         os.path.join(objdir, "compat.o"), os.path.join(objdir, "noalloc.o"), os.path.join(objdir, "peaks.o"), "-lcudart"])
+                         os.path.join(objdir, "compat.o"), os.path.join(objdir, "noalloc.o"), os.path.join(objdir, "peaks.o"),
+                         os.path.join(objdir, "mass.o"), "-lcudart"])
     os.replace(tmp, LIB)
     return LIB
 

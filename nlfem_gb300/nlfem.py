@@ -227,6 +227,43 @@ def stiffnessMatrix(mesh, kernel, configuration):
     return A
 
 
+def evaluateMass(mesh, ud, Px, dx):
+    """vd = M ud with the P1 mass matrix (nlfem.pyx:638-671, par_evaluateMass Cassemble.cpp:166-246),
+    on the GPU. mesh is the reference's mesh object (elements, elementLabels, vertices,
+    vertexLabels, dim, nE_Omega, is_DiscontinuousGalerkin, optional outdim: the first nE_Omega
+    elements with a positive label are summed) or a mesh dict (every element with a positive
+    label). Px, dx: the quadrature rule on the reference element."""
+    if isinstance(mesh, dict):
+        get = mesh.get
+    else:
+        def get(k, default=None):
+            return getattr(mesh, k, default)
+    elements = np.ascontiguousarray(get("elements"), dtype=np.int64)
+    elementLabels = np.ascontiguousarray(get("elementLabels"), dtype=np.int64).ravel()
+    vertices = np.ascontiguousarray(get("vertices"), dtype=np.float64)
+    vertexLabels = np.ascontiguousarray(get("vertexLabels"), dtype=np.int64).ravel()
+    nE, dV = elements.shape
+    nV, dim = vertices.shape
+    J = get("nE_Omega")
+    J = nE if J is None else int(J)
+    is_dg = int(bool(get("is_DiscontinuousGalerkin", False)))
+    outdim = int(get("outdim", 1) or 1)
+    K = dV * nE if is_dg else nV
+    u = np.ascontiguousarray(ud, dtype=np.float64).ravel()
+    if u.size != K * outdim:
+        raise ValueError(f"ud has {u.size} entries, the mesh has {K * outdim} degrees of freedom")
+    P = np.ascontiguousarray(Px, dtype=np.float64)
+    w = np.ascontiguousarray(dx, dtype=np.float64).ravel()
+    vd = np.zeros(K * outdim, dtype=np.float64)
+    lib = _lib.load()
+    lp = ctypes.POINTER(ctypes.c_long)
+    _lib.check(lib.nlfem_evaluate_mass(dim, outdim, is_dg, nE, J, nV, elements.ctypes.data_as(lp),
+                                       elementLabels.ctypes.data_as(lp), vertices.ctypes.data_as(_dp),
+                                       vertexLabels.ctypes.data_as(lp), int(w.size), P.ctypes.data_as(_dp),
+                                       w.ctypes.data_as(_dp), u.ctypes.data_as(_dp), vd.ctypes.data_as(_dp)))
+    return vd
+
+
 def loadVector(mesh, load, configuration):
     """Load vector (nlfem.pyx:276-389), on the GPU."""
     lib = _lib.load()

@@ -3,9 +3,11 @@
 The reference's rate test assembles A and f on a sequence of meshes and solves
 A_Omega u = f_Omega - A_Gamma g, with the Dirichlet data g = u_exact on the interaction layer, by
 CG. It then measures the L2 error of the discrete solution and reports log2 of successive error
-ratios. This module does the same with this package's GPU assembly (either precision). The
-linear solve (scipy CG) and the error quadrature run on the host: they check the assembled
-operator, they are not part of the assembly path.
+ratios. This module does the same with this package's GPU assembly (either precision). Two error
+measures are reported: the L2 norm of u_h - u by a 16-point rule on the host, and the reference's
+measure sqrt(d . M d), d the nodal difference, with the GPU mass product (evaluateMass). The
+linear solve (scipy CG) runs on the host: it checks the assembled operator and is not part of the
+assembly path.
 
 The default problem is the reference's "linear" load f = -2 (x_1 + 1) (model.cpp:240-242) with
 the constant kernel. That kernel reproduces -Laplace on cubic polynomials, so the nonlocal
@@ -36,6 +38,16 @@ def l2_error(mesh, uh, u_exact, rule=None):
     uhq = np.einsum("qa,ta->tq", psi, uh[E])
     d = uhq - u_exact(xq)
     return float(np.sqrt(np.sum(det[:, None] * w[None, :] * d * d)))
+
+
+def mass_error(mesh, uh, u_exact, rule=None):
+    """sqrt(d . M d) with d = u_exact - u_h at the vertices and M the P1 mass matrix on the
+    elements with label > 0 (the reference's error measure, computeRates2D.py:92-97, on the same
+    mesh), with the GPU mass product nlfem.evaluateMass."""
+    P, w = rule if rule is not None else quadrules.dunavant7()
+    d = u_exact(mesh["vertices"]) - uh
+    Md = nlfem.evaluateMass(mesh, d, P, w)
+    return float(np.sqrt(max(d @ Md, 0.0)))
 
 
 def solve(mesh, kernel, conf, load, u_exact, tol=1e-12):
@@ -74,16 +86,19 @@ def convergence(ns, delta=0.1, precision="fp64", kernel=None, load=None, u_exact
     conf = {"ansatz": "CG", "approxBalls": {"method": "retriangulate", "is_PlacePointOnCap": 1},
             "quadrature": {"outer": {"points": P, "weights": w}, "inner": {"points": P, "weights": w}},
             "precision": precision}
-    hs, errs, its = [], [], []
+    hs, errs, merrs, its = [], [], [], []
     for n in ns:
         v, e, l = meshes.regular_square(n, delta)
         mesh = meshes.mesh_dict(v, e, l)
         uh, k = solve(mesh, kernel, conf, load, u_exact)
         hs.append((1.0 + 2.0 * delta) / n)
         errs.append(l2_error(mesh, uh, u_exact))
+        merrs.append(mass_error(mesh, uh, u_exact))
         its.append(k)
     rates = [float(np.log2(errs[i - 1] / errs[i])) for i in range(1, len(errs))]
-    return {"n": list(ns), "h": hs, "l2_error": errs, "rates": rates, "cg_iterations": its}
+    mrates = [float(np.log2(merrs[i - 1] / merrs[i])) for i in range(1, len(merrs))]
+    return {"n": list(ns), "h": hs, "l2_error": errs, "rates": rates, "mass_error": merrs,
+            "mass_rates": mrates, "cg_iterations": its}
 
 
 if __name__ == "__main__":

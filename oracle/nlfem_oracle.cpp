@@ -893,4 +893,46 @@ int oracle_pair_blocks(
     return 0;
 }
 
+// par_evaluateMass (Cassemble.cpp:166-246): vd += psi_a psi_b |aT| dx_j ud over the first J
+// elements with label > 0; CG rows and columns of vertices with label > 0, DG indices
+// dV * aTdx + j; the (a, aOut, b, bOut, j) loop order of the reference, sequentially.
+int oracle_evaluate_mass(double *vd, const double *ud, const long *Elements, const long *ElementLabels,
+                         const double *Verts, const long *VertexLabels, int J, int nP, const double *P,
+                         const double *dx, int dim, int outdim, int is_dg) {
+    const int dVerts = dim + 1;
+    std::vector<double> psi((size_t)dVerts * nP);
+    double tmp[4];
+    for (int k = 0; k < nP; k++) {
+        basis(&P[dim * k], dim, tmp);
+        for (int kk = 0; kk < dVerts; kk++) psi[(size_t)nP * kk + k] = tmp[kk];
+    }
+    long aDG[4];
+    double aTE[12];
+    for (int aTdx = 0; aTdx < J; aTdx++) {
+        if (ElementLabels[aTdx] <= 0) continue;
+        const long *aAdx;
+        if (is_dg) {
+            for (int j = 0; j < dVerts; j++) aDG[j] = (long)dVerts * aTdx + j;
+            aAdx = aDG;
+        } else {
+            aAdx = &Elements[(long)dVerts * aTdx];
+        }
+        for (int jj = 0; jj < dVerts; jj++)
+            for (int j = 0; j < dim; j++) aTE[dim * jj + j] = Verts[dim * Elements[(long)dVerts * aTdx + jj] + j];
+        const double aTdet = absDetDim(aTE, dim);
+        for (int a = 0; a < dVerts; a++) {
+            if (!(is_dg || VertexLabels[aAdx[a]] > 0)) continue;
+            for (int aOut = 0; aOut < outdim; aOut++)
+                for (int b = 0; b < dVerts; b++) {
+                    if (!(is_dg || VertexLabels[aAdx[b]] > 0)) continue;
+                    for (int bOut = 0; bOut < outdim; bOut++)
+                        for (int j = 0; j < nP; j++)
+                            vd[outdim * aAdx[a] + aOut] +=
+                                psi[(size_t)nP * a + j] * psi[(size_t)nP * b + j] * aTdet * dx[j] * ud[outdim * aAdx[b] + bOut];
+                }
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -62,6 +62,9 @@ def lib():
             _lp, _lp, _dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp,
             ctypes.c_int, _dp, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
             ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_double, _lp, ctypes.c_long, _dp, _ip]
+        l.oracle_evaluate_mass.restype = ctypes.c_int
+        l.oracle_evaluate_mass.argtypes = [_dp, _dp, _lp, _lp, _dp, _lp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = l
     return _lib
 
@@ -191,3 +194,22 @@ def pair_blocks(mesh, kernel, conf, pairs, method=None):
         float(kernel.get("fractional_s", -1.0)), prp, n, out.ctypes.data_as(_dp),
         ret.ctypes.data_as(_ip))
     return out, ret
+
+
+def evaluate_mass(mesh, ud, Px, dx, J=None, outdim=1, is_dg=False):
+    """par_evaluateMass (Cassemble.cpp:166-246) on a mesh dict: vd = M ud over the first J
+    elements with label > 0 (J defaults to the number of such elements, as nE_Omega)."""
+    el, pel = _l(mesh["elements"])
+    lab, plab = _l(mesh["elementLabels"])
+    V, pV = _d(mesh["vertices"])
+    vl, pvl = _l(mesh["vertexLabels"])
+    P, pP = _d(Px)
+    w, pw = _d(dx)
+    u, pu = _d(ud)
+    dim = V.shape[1]
+    K = (dim + 1) * el.shape[0] if is_dg else V.shape[0]
+    vd = np.zeros(K * outdim)
+    J = int((lab > 0).sum()) if J is None else int(J)
+    lib().oracle_evaluate_mass(vd.ctypes.data_as(_dp), pu, pel, plab, pV, pvl, J, P.shape[0], pP, pw, dim,
+                               outdim, int(is_dg))
+    return vd

@@ -53,6 +53,20 @@ def test_no_cpu_fallback_without_device(lib):
     assert e.value.code == 2
 
 
+def test_evaluate_mass_no_cpu_fallback_and_checks(lib):
+    from nlfem_gb300 import nlfem, _lib, quadrules
+    m = square_mesh(4)
+    P, w = quadrules.dunavant7()
+    ud = np.ones(m["vertices"].shape[0])
+    with pytest.raises(ValueError):   # wrong vector length: caught before the library call
+        nlfem.evaluateMass(m, ud[:-1], P, w)
+    if lib.nlfem_device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(_lib.NlfemError) as e:
+        nlfem.evaluateMass(m, ud, P, w)
+    assert e.value.code == 2
+
+
 def test_invalid_configuration_is_reported(lib):
     from nlfem_gb300 import nlfem, _lib
     if lib.nlfem_device_count() == 0:

@@ -418,6 +418,33 @@ def test_one_shot_capacity_hints_overflow(nl, orc):
     assert same_pattern(A1, B1)
 
 
+@pytest.mark.parametrize("case", ["2d", "2d_J", "3d", "dg"])
+def test_evaluate_mass_matches_oracle(nl, orc, case):
+    """par_evaluateMass on the GPU (deterministic fixed-point sums) against the oracle's
+    sequential restatement."""
+    from types import SimpleNamespace
+    from nlfem_gb300 import quadrules
+    rng = np.random.Generator(np.random.PCG64(7))
+    if case == "3d":
+        m = cube_mesh(5, 0.1, jitter=0.1, seed=2)
+        P, w = quadrules.keast11()
+    else:
+        m = square_mesh(12, 0.1, jitter=0.2, seed=5)
+        P, w = quadrules.dunavant7()
+    nE, dV = m["elements"].shape
+    dg = case == "dg"
+    K = dV * nE if dg else m["vertices"].shape[0]
+    ud = rng.standard_normal(K)
+    J = nE // 2 if case == "2d_J" else nE
+    mesh = SimpleNamespace(elements=m["elements"], elementLabels=m["elementLabels"], vertices=m["vertices"],
+                           vertexLabels=m["vertexLabels"], dim=m["vertices"].shape[1], nE_Omega=J,
+                           is_DiscontinuousGalerkin=dg, K=K)
+    vd = nl.evaluateMass(mesh, ud, P, w)
+    ref = orc.evaluate_mass(m, ud, P, w, J=J, is_dg=dg)
+    assert np.abs(vd - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.array_equal(vd, nl.evaluateMass(mesh, ud, P, w))   # deterministic
+
+
 def test_mixed_pair_list_exact(nl, orc):
     m = square_mesh(24, 0.13, jitter=0.2, seed=3)
     k = {"function": "constant", "horizon": 0.13, "outputdim": 1}

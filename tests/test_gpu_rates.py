@@ -18,6 +18,10 @@ def test_mixed_rates_equal_fp64_rates():
     assert all(1.9 < r < 2.1 for r in a["rates"][1:]), a
     np.testing.assert_allclose(b["rates"], a["rates"], atol=0.01)
     np.testing.assert_allclose(b["l2_error"], a["l2_error"], rtol=5e-3)
+    # the reference's measure, sqrt(d . M d) with the GPU mass product: same rates for both
+    # operators (the nodal difference converges at least at second order)
+    assert all(r > 1.8 for r in a["mass_rates"][1:]), a
+    np.testing.assert_allclose(b["mass_rates"], a["mass_rates"], atol=0.02)
 
 
 def test_mixed_operator_annihilates_constants():

@@ -142,6 +142,13 @@ int nlfem_session_assemble(nlfem_session *s);            /* inputs already in HB
 int nlfem_session_assemble_graph(nlfem_session *s);
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out);
 int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out);
+/* A_Omega u = f_Omega - A_Gamma g by conjugate gradients on problem i's assembled matrix
+ * (computeRates2D.py:47-70): unknowns are the vertices with label > 0, g holds the Dirichlet
+ * values (read at label < 0). f, g and u have nV entries (host arrays); u returns the solution at
+ * label > 0 and g at label < 0. Stops when |r| <= rtol |b| (NLFEM_ERR_NUMERIC after maxit
+ * iterations); *iterations receives the count. Deterministic. */
+int nlfem_session_solve(nlfem_session *s, int i, const double *f, const double *g, double rtol, int maxit,
+                        double *u, int *iterations);
 void nlfem_session_destroy(nlfem_session *s);
 
 /* The interacting pairs (aT, bT) of the BFS, sorted by (aT, bT). Free *pairs with free(). */

@@ -108,6 +108,8 @@ def load():
     l.nlfem_session_download32.argtypes = [ctypes.c_void_p, ctypes.c_int, C32]
     l.nlfem_cache_release.argtypes = []
     l.nlfem_cache_release.restype = None
+    l.nlfem_session_solve.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp,
+                                      ctypes.POINTER(ctypes.c_int)]
     l.nlfem_evaluate_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_long,
                                       ctypes.c_long, _lp, _lp, _dp, _lp, ctypes.c_int, _dp, _dp, _dp, _dp]
     vp = ctypes.c_void_p   # device pointers and the stream are passed as raw addresses
@@ -137,5 +139,5 @@ EXPORTED = [
     "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
     "nlfem_par_assemble", "nlfem_load_vector_noalloc", "nlfem_measure_peaks",
     "nlfem_stiffness_matrix32", "nlfem_stiffness_batch32", "nlfem_csr32_free", "nlfem_session_download32",
-    "nlfem_cache_release", "nlfem_evaluate_mass",
+    "nlfem_cache_release", "nlfem_evaluate_mass", "nlfem_session_solve",
 ]

@@ -287,6 +287,7 @@ struct Session {
     DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
     DevBuf po_cnt, po_off, po_ptr, po_scratch, tcnt, tptr, tcols;   // transposed pattern construction
     long long po_cap = 0, t_nnz = 0;
+    DevBuf sv_vec, sv_part;                 // CG solve: f, g, b, x, r, p, Ap; dot partials
     DevBuf kclist;                          // elements grouped by kernel class (pass launches)
     long long kc_off[4] = {-1, 0, 0, 0};    // class offsets into kclist (-1: list not built)
     long long pat_cap = 0;
@@ -311,7 +312,7 @@ struct Session {
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                 &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
-                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols};
+                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -1589,6 +1590,139 @@ static void cache_give(Session &S) {
     g_cache->hint_nE = S.nE;
     g_cache->hint_nV = S.nV;
 }
+
+// ---------------------------------------------------------------- CG solve on the assembled matrix
+// A_Omega u = f_Omega - A_Gamma g for problem i of a session (computeRates2D.py:47-70): rows and
+// unknowns are the vertices with label > 0, g holds the Dirichlet values of the vertices with
+// label < 0 (label-0 columns are left out, as the reference's masks do). Conjugate gradients in
+// FP64 on the session's CSR: one warp per row for the products, dot products as fixed-grid block
+// partials summed on the host in a fixed order, so the iterates are deterministic.
+constexpr int SOLVE_DOT_BLOCKS = 256;
+
+__global__ void k_solve_rhs(const long long *__restrict__ fptr, const int *__restrict__ fcols,
+                            const double *__restrict__ fvals, const int *__restrict__ labV, long long r0,
+                            long long n, const double *__restrict__ f, const double *__restrict__ g,
+                            double *__restrict__ b) {
+    const int lane = threadIdx.x & 31;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;
+    const long long row = r0 + w;
+    double s = 0.0;
+    if (labV[row] > 0)
+        for (long long k = fptr[row] + lane; k < fptr[row + 1]; k += 32) {
+            const int c = fcols[k];
+            if (labV[c] < 0) s += fvals[k] * g[c - r0];
+        }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    if (lane == 0) b[w] = labV[row] > 0 ? f[w] - s : 0.0;
+}
+
+__global__ void k_solve_spmv(const long long *__restrict__ fptr, const int *__restrict__ fcols,
+                             const double *__restrict__ fvals, const int *__restrict__ labV, long long r0,
+                             long long n, const double *__restrict__ x, double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;
+    const long long row = r0 + w;
+    double s = 0.0;
+    if (labV[row] > 0)
+        for (long long k = fptr[row] + lane; k < fptr[row + 1]; k += 32) {
+            const int c = fcols[k];
+            if (labV[c] > 0) s += fvals[k] * x[c - r0];
+        }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    if (lane == 0) y[w] = s;
+}
+
+__global__ void k_solve_dot(const double *__restrict__ a, const double *__restrict__ b, long long n,
+                            double *__restrict__ part) {
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// x += alpha p, r -= alpha Ap
+__global__ void k_solve_update(double alpha, const double *__restrict__ p, const double *__restrict__ Ap,
+                               double *__restrict__ x, double *__restrict__ r, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        x[i] += alpha * p[i];
+        r[i] -= alpha * Ap[i];
+    }
+}
+// p = r + beta p
+__global__ void k_solve_dir(double beta, const double *__restrict__ r, double *__restrict__ p, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = r[i] + beta * p[i];
+}
+
+static int solve_dot(Session &S, const double *a, const double *b, long long n, double *out) {
+    k_solve_dot<<<SOLVE_DOT_BLOCKS, 256, 0, S.st>>>(a, b, n, S.sv_part.get<double>());
+    CK(cudaGetLastError());
+    double part[SOLVE_DOT_BLOCKS];
+    int r = d2h(S, part, S.sv_part.get<double>(), SOLVE_DOT_BLOCKS);
+    if (r) return r;
+    double s = 0.0;
+    for (int k = 0; k < SOLVE_DOT_BLOCKS; k++) s += part[k];
+    *out = s;
+    return NLFEM_OK;
+}
+
+static int session_solve(Session &S, int i, const double *f, const double *g, double rtol, int maxit,
+                         double *u, int *iters) {
+    if (S.nnz <= 0) return fail(NLFEM_ERR_INVALID, "solve needs an assembled session");
+    const long long r0 = S.voff[i], n = S.voff[i + 1] - S.voff[i];
+    ENS(S.sv_vec, sizeof(double) * 7 * (n + 1));
+    ENS(S.sv_part, sizeof(double) * SOLVE_DOT_BLOCKS);
+    double *vf = S.sv_vec.get<double>(), *vg = vf + (n + 1), *b = vg + (n + 1), *x = b + (n + 1);
+    double *rr = x + (n + 1), *p = rr + (n + 1), *Ap = p + (n + 1);
+    CK(cudaMemcpyAsync(vf, f, sizeof(double) * n, cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(vg, g, sizeof(double) * n, cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemsetAsync(x, 0, sizeof(double) * n, S.st));
+    const long long *fp = S.fptr.get<long long>();
+    const int *fc = S.fcols.get<int>(), *lab = S.labV.get<int>();
+    const double *fv = S.fvals.get<double>();
+    const unsigned gw = grid_for(n * 32, 256), ge = grid_for(n, 256);
+    k_solve_rhs<<<gw, 256, 0, S.st>>>(fp, fc, fv, lab, r0, n, vf, vg, b);
+    CK(cudaMemcpyAsync(rr, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, S.st));
+    CK(cudaMemcpyAsync(p, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, S.st));
+    double bb = 0.0, rs = 0.0;
+    int r = solve_dot(S, b, b, n, &bb);
+    if (r) return r;
+    rs = bb;
+    const double stop = rtol * rtol * bb;
+    int it = 0;
+    while (it < maxit && rs > stop && rs > 0.0) {
+        k_solve_spmv<<<gw, 256, 0, S.st>>>(fp, fc, fv, lab, r0, n, p, Ap);
+        double pAp = 0.0;
+        if ((r = solve_dot(S, p, Ap, n, &pAp))) return r;
+        if (!(pAp > 0.0)) return fail(NLFEM_ERR_NUMERIC, "CG breakdown: the operator is not positive definite on the search direction");
+        const double alpha = rs / pAp;
+        k_solve_update<<<ge, 256, 0, S.st>>>(alpha, p, Ap, x, rr, n);
+        double rs2 = 0.0;
+        if ((r = solve_dot(S, rr, rr, n, &rs2))) return r;
+        k_solve_dir<<<ge, 256, 0, S.st>>>(rs2 / rs, rr, p, n);
+        rs = rs2;
+        it++;
+    }
+    CK(cudaGetLastError());
+    std::vector<int> hl(n);
+    if ((r = d2h(S, u, x, n))) return r;
+    if ((r = d2h(S, hl.data(), lab + r0, n))) return r;
+    for (long long k = 0; k < n; k++)
+        if (hl[k] < 0) u[k] = g[k];
+    if (iters) *iters = it;
+    if (it >= maxit && rs > stop) return fail(NLFEM_ERR_NUMERIC, "CG did not reach the tolerance within maxit iterations");
+    return NLFEM_OK;
+}
 }  // namespace nlg
 
 extern "C" {
@@ -1646,6 +1780,13 @@ int nlfem_session_assemble(nlfem_session *s) {
 int nlfem_session_assemble_graph(nlfem_session *s) {
     if (!s) return fail(NLFEM_ERR_INVALID, "null session");
     return run_system_graph(s->S);
+}
+
+int nlfem_session_solve(nlfem_session *s, int i, const double *f, const double *g, double rtol, int maxit,
+                        double *u, int *iterations) {
+    if (!s || !f || !g || !u || i < 0 || i >= s->S.nProb || !(rtol > 0.0) || maxit < 0)
+        return fail(NLFEM_ERR_INVALID, "bad session solve");
+    return session_solve(s->S, i, f, g, rtol, maxit, u, iterations);
 }
 
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out) {

@@ -333,6 +333,21 @@ class Session:
         finally:
             self.lib.nlfem_csr_free(ctypes.byref(out))
 
+    def solve(self, i, f, g, rtol=1e-12, maxit=20000):
+        """A_Omega u = f_Omega - A_Gamma g by conjugate gradients on the GPU, on problem i's matrix
+        of the last assemble() (computeRates2D.py:47-70). f and g are vertex vectors (g read at
+        label < 0); returns (u, iterations) with u = g at label < 0."""
+        nV = int(self.ps[i].c.nV)
+        ff = np.ascontiguousarray(f, dtype=np.float64).ravel()
+        gg = np.ascontiguousarray(g, dtype=np.float64).ravel()
+        if ff.size != nV or gg.size != nV:
+            raise ValueError(f"f and g need {nV} entries")
+        u = np.zeros(nV, dtype=np.float64)
+        its = ctypes.c_int(0)
+        _lib.check(self.lib.nlfem_session_solve(self.h, i, ff.ctypes.data_as(_dp), gg.ctypes.data_as(_dp),
+                                                float(rtol), int(maxit), u.ctypes.data_as(_dp), ctypes.byref(its)))
+        return u, its.value
+
     def close(self):
         if self.h:
             self.lib.nlfem_session_destroy(self.h)

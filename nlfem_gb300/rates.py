@@ -6,8 +6,8 @@ CG. It then measures the L2 error of the discrete solution and reports log2 of s
 ratios. This module does the same with this package's GPU assembly (either precision). Two error
 measures are reported: the L2 norm of u_h - u by a 16-point rule on the host, and the reference's
 measure sqrt(d . M d), d the nodal difference, with the GPU mass product (evaluateMass). The
-linear solve (scipy CG) runs on the host: it checks the assembled operator and is not part of the
-assembly path.
+linear solve runs by CG on the host (scipy) or, with solver="gpu", on the GPU on the session's
+assembled matrix.
 
 The default problem is the reference's "linear" load f = -2 (x_1 + 1) (model.cpp:240-242) with
 the constant kernel. That kernel reproduces -Laplace on cubic polynomials, so the nonlocal
@@ -50,6 +50,19 @@ def mass_error(mesh, uh, u_exact, rule=None):
     return float(np.sqrt(max(d @ Md, 0.0)))
 
 
+def solve_gpu(mesh, kernel, conf, load, u_exact, tol=1e-12):
+    """The same with the CG iterations on the GPU, on the session's assembled matrix
+    (nlfem.Session.solve). Returns (vertex values of u_h, CG iterations)."""
+    f = nlfem.loadVector(mesh, load, conf)
+    s = nlfem.Session([(mesh, kernel, conf)])
+    try:
+        s.assemble()
+        g = np.where(mesh["vertexLabels"] < 0, u_exact(mesh["vertices"]), 0.0)
+        return s.solve(0, f, g, rtol=tol)
+    finally:
+        s.close()
+
+
 def solve(mesh, kernel, conf, load, u_exact, tol=1e-12):
     """Assemble on the GPU, impose g = u_exact on the layer vertices, solve by CG on the host.
     Returns (vertex values of u_h, CG iterations)."""
@@ -78,7 +91,8 @@ def solve(mesh, kernel, conf, load, u_exact, tol=1e-12):
     return uh, it[0]
 
 
-def convergence(ns, delta=0.1, precision="fp64", kernel=None, load=None, u_exact=u_quadratic, rule="7"):
+def convergence(ns, delta=0.1, precision="fp64", kernel=None, load=None, u_exact=u_quadratic, rule="7",
+                solver="host"):
     """L2 errors and rates over the meshes 2*n^2 (n in ns) of [-delta, 1+delta]^2."""
     kernel = kernel or {"function": "constant", "horizon": delta, "outputdim": 1}
     load = load or {"function": "linear"}
@@ -90,7 +104,7 @@ def convergence(ns, delta=0.1, precision="fp64", kernel=None, load=None, u_exact
     for n in ns:
         v, e, l = meshes.regular_square(n, delta)
         mesh = meshes.mesh_dict(v, e, l)
-        uh, k = solve(mesh, kernel, conf, load, u_exact)
+        uh, k = (solve_gpu if solver == "gpu" else solve)(mesh, kernel, conf, load, u_exact)
         hs.append((1.0 + 2.0 * delta) / n)
         errs.append(l2_error(mesh, uh, u_exact))
         merrs.append(mass_error(mesh, uh, u_exact))

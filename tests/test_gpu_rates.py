@@ -41,3 +41,25 @@ def test_mixed_operator_annihilates_constants():
     rs = np.abs(A @ np.ones(A.shape[1]))
     scale = np.abs(A).max()
     assert rs.max() <= 1e-14 * scale, rs.max() / scale
+
+
+def test_gpu_solve_matches_host_solve():
+    """CG on the GPU (Session.solve) against scipy's CG on the same assembled operator."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from nlfem_gb300 import meshes, rates, quadrules
+    v, e, l = meshes.regular_square(32, 0.1)
+    m = meshes.mesh_dict(v, e, l)
+    P, w = quadrules.dunavant7()
+    for prec in ("fp64", "mixed"):
+        conf = {"ansatz": "CG", "approxBalls": {"method": "retriangulate", "is_PlacePointOnCap": 1},
+                "quadrature": {"outer": {"points": P, "weights": w}, "inner": {"points": P, "weights": w}},
+                "precision": prec}
+        k = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+        uh, it_h = rates.solve(m, k, conf, {"function": "linear"}, rates.u_quadratic)
+        ug, it_g = rates.solve_gpu(m, k, conf, {"function": "linear"}, rates.u_quadratic)
+        assert np.abs(ug - uh).max() <= 1e-8 * np.abs(uh).max(), prec
+        assert abs(it_g - it_h) <= max(5, it_h // 10), (it_g, it_h)
+        ug2, _ = rates.solve_gpu(m, k, conf, {"function": "linear"}, rates.u_quadratic)
+        assert np.array_equal(ug, ug2)   # deterministic

@@ -64,6 +64,12 @@ typedef struct nlfem_problem {
     int is_fullConnectedComponentSearch;
     int precision;               /* NLFEM_PREC_FP64 or NLFEM_PREC_MIXED */
     int verbose;
+    /* domain decomposition (Cassemble.cpp:649-657), nZeta > 0: element -> subdomain indicator
+     * in CSR (nE + 1 row pointers, sorted column indices per row); each pair's four blocks are
+     * weighted by 1 / (the number of subdomains its two elements share) */
+    const long *zeta_indices;
+    const long *zeta_indptr;
+    long nZeta;
 } nlfem_problem;
 
 /* CSR matrix owned by the library; release with nlfem_csr_free. */

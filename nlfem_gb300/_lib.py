@@ -33,6 +33,7 @@ class Problem(ctypes.Structure):
         ("method_remote", ctypes.c_char_p), ("method_close", ctypes.c_char_p),
         ("is_PlacePointOnCap", ctypes.c_int), ("is_fullConnectedComponentSearch", ctypes.c_int),
         ("precision", ctypes.c_int), ("verbose", ctypes.c_int),
+        ("zeta_indices", _lp), ("zeta_indptr", _lp), ("nZeta", ctypes.c_long),
     ]
 
 

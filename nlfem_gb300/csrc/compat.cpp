@@ -48,8 +48,6 @@ extern "C" int nlfem_par_assemble(
     const double *Pg, int degree, const double *dg, double maxDiameter, double fractional_s,
     int is_fullConnectedComponentSearch, int verbose) {
     (void)K_Omega; (void)nV_Omega; (void)is_NeumannBoundary; (void)maxDiameter;
-    (void)ptrZetaIndicator_indices; (void)ptrZetaIndicator_indptr;
-    if (nZeta) return NLFEM_ERR_UNSUPPORTED;   // domain-decomposition weights not implemented
     std::string comp(compute ? compute : "");
     // chk_Mesh (checks.cpp:49-85)
     long chk = 0;
@@ -72,6 +70,9 @@ extern "C" int nlfem_par_assemble(
     p.is_fullConnectedComponentSearch = is_fullConnectedComponentSearch;
     p.precision = NLFEM_PREC_FP64;
     p.verbose = verbose;
+    p.zeta_indices = ptrZetaIndicator_indices;
+    p.zeta_indptr = ptrZetaIndicator_indptr;
+    p.nZeta = nZeta;
     if (comp == "system") {
         nlfem_csr A;
         memset(&A, 0, sizeof(A));

@@ -199,7 +199,8 @@ struct ProbParams {
     int kernel, remote, close, caps;
     int full_search, singular, load, scale_exp;
     int elem_off, nE, vert_off, nV;
-    int bridges, pad_i;   // bridges: the mesh has label-0 elements (searched through, never paired)
+    int bridges;          // the mesh has label-0 elements (searched through, never paired)
+    int zeta;             // domain-decomposition weights 1 / zeta on every pair
     double fx_unit;   // value of one unit of the 64-bit fixed-point CSR sums: 2^fx_ue
     float fx_mul;     // 2^-fx_ue
     int fx_ue;        // scale_exp + guard bits - 62

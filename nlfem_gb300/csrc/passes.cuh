@@ -136,6 +136,7 @@ struct PassArgs {
     unsigned long long *n_close;   // pairs integrated with the close-pair rule (from closebuf)
     unsigned long long *n_in, *n_cut;   // one-sided passes: (pair, outer point) items by class
     unsigned char *touched;     // mixed precision: slots that received a contribution
+    const long long *zptr, *zidx;   // domain decomposition: element -> subdomain indicator (CSR)
 };
 
 constexpr int PASS_THREADS = 128;
@@ -554,6 +555,22 @@ __device__ void out_bary(const ProbParams &P, const Rule &rule, const PassRule &
 }
 
 // ---------------------------------------------------------------- the pass kernel
+// Domain-decomposition weight of the pair (A, B) (Cassemble.cpp:649-657): 1 / the number of
+// subdomains both elements belong to (evaluateZeta, mathhelpers.cpp:19-38: the intersection of
+// their sorted indicator rows).
+__device__ __forceinline__ double zeta_weight(const long long *__restrict__ zptr, const long long *__restrict__ zidx,
+                                              long long A, long long B) {
+    long long i = zptr[A], ie = zptr[A + 1], j = zptr[B], je = zptr[B + 1];
+    long long n = 0;
+    while (i < ie && j < je) {
+        const long long x = zidx[i], y = zidx[j];
+        if (x < y) i++;
+        else if (y < x) j++;
+        else { n++; i++; j++; }
+    }
+    return 1.0 / (double)n;
+}
+
 template <int DIM, int PREC>
 __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, PassRule pr) {
     constexpr int dV = DIM + 1;
@@ -630,9 +647,11 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
             int bv[dV];
 #pragma unroll
             for (int r = 0; r < dV; r++) bv[r] = a.T32[(long long)bT * dV + r];
-            double Nd[dV * dV];
+            double Nd[dV * dV], Dp[NS];   // the pair's termNonloc and termLocal (upper triangle)
 #pragma unroll
             for (int i = 0; i < dV * dV; i++) Nd[i] = 0.0;
+#pragma unroll
+            for (int i = 0; i < NS; i++) Dp[i] = 0.0;
             if (act) {
                 const double *Eb64 = &a.EC[(long long)bT * DIM * dV];
                 bool done = false;
@@ -647,7 +666,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                         else {
                             const double *cb = &a.closebuf[cs * 36];
                             for (int i = 0; i < 3; i++)
-                                for (int j = i; j < 3; j++) D[sym_idx<dV>(i, j)] += cb[3 * i + j];
+                                for (int j = i; j < 3; j++) Dp[sym_idx<dV>(i, j)] += cb[3 * i + j];
                             for (int i = 0; i < 9; i++) Nd[i] = cb[9 + i];
                         }
                         done = true;
@@ -664,14 +683,14 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                         for (int i = 0; i < NS; i++) Ls[i] = 0.0;
                         out_bary<DIM, PREC>(P, rule, pr, s_xf[wib], s_x64[wib], pb, Eb64, a.adet[bT], Ls, Nd, nsub, namb);
 #pragma unroll
-                        for (int i = 0; i < NS; i++) D[i] += Ls[i] * adetT;
+                        for (int i = 0; i < NS; i++) Dp[i] += Ls[i] * adetT;
 #pragma unroll
                         for (int i = 0; i < dV * dV; i++) Nd[i] *= adetT;
                     } else if (DIM == 2) {
                         if (PREC == PREC_F64) {
                             double Ls[6] = {0, 0, 0, 0, 0, 0};
                             out_retri_f64(P, rule, s_x64[wib], Eb64, Ls, Nd, nsub, a.err);
-                            for (int i = 0; i < 6; i++) D[i] += Ls[i] * adetT;
+                            for (int i = 0; i < 6; i++) Dp[i] += Ls[i] * adetT;
                             for (int i = 0; i < 9; i++) Nd[i] *= adetT;
                         } else {
                             float pb[6];
@@ -680,11 +699,18 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                                 pb[j] = (a.EChi[(long long)bT * 6 + j] - ohi[j & 1]) + (a.EClo[(long long)bT * 6 + j] - olo[j & 1]);
                             float Lf[6] = {0, 0, 0, 0, 0, 0}, Nf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
                             out_retri_mix(P, rule, pr, (const F2 *)s_xf[wib], s_x64[wib], pb, (float)a.adet[bT], Eb64, Lf, Nf, nsub, namb);
-                            for (int i = 0; i < 6; i++) D[i] += (double)Lf[i] * adetT;
+                            for (int i = 0; i < 6; i++) Dp[i] += (double)Lf[i] * adetT;
                             for (int i = 0; i < 9; i++) Nd[i] = (double)Nf[i] * adetT;
                         }
                     }
                 }
+            }
+            {   // the pair's weight (1 without domain decomposition)
+                const double w = (act && P.zeta) ? zeta_weight(a.zptr, a.zidx, T, bT) : 1.0;
+#pragma unroll
+                for (int i = 0; i < NS; i++) D[i] += Dp[i] * w;
+#pragma unroll
+                for (int i = 0; i < dV * dV; i++) Nd[i] *= w;
             }
             // termNonloc -> A[T[a], bT[b]] with the minus sign (Cassemble.cpp:744-749)
 #pragma unroll
@@ -716,9 +742,11 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                 int av[3];
 #pragma unroll
                 for (int r = 0; r < 3; r++) av[r] = a.T32[(long long)aT * 3 + r];
-                double NPd[9];
+                double NPd[9], Dp[6];   // the pair's termNonlocPrime and termLocalPrime (upper triangle)
 #pragma unroll
                 for (int i = 0; i < 9; i++) NPd[i] = 0.0;
+#pragma unroll
+                for (int i = 0; i < 6; i++) Dp[i] = 0.0;
                 if (act) {
                     const double *Ea64 = &a.EC[(long long)aT * 6];
                     const double adetA = a.adet[aT];
@@ -734,7 +762,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                                 const double *cb = &a.closebuf[cs * 36];
                                 // LP[a][b] -> A[T[b], T[a]]: the diagonal block of T takes LP^T
                                 for (int i = 0; i < 3; i++)
-                                    for (int j = i; j < 3; j++) D[sym_idx<3>(i, j)] += cb[18 + 3 * j + i];
+                                    for (int j = i; j < 3; j++) Dp[sym_idx<3>(i, j)] += cb[18 + 3 * j + i];
                                 for (int i = 0; i < 9; i++) NPd[i] = cb[27 + i];
                             }
                             done = true;
@@ -744,7 +772,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                         if (PREC == PREC_F64) {
                             double LP[6] = {0, 0, 0, 0, 0, 0};
                             in_retri_f64(P, rule, Ea64, ET64, LP, NPd, nsub, a.err);
-                            for (int i = 0; i < 6; i++) D[i] += LP[i] * adetA;
+                            for (int i = 0; i < 6; i++) Dp[i] += LP[i] * adetA;
                             for (int i = 0; i < 9; i++) NPd[i] *= adetA;
                         } else {
                             float pa[6];
@@ -753,10 +781,17 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                                 pa[j] = (a.EChi[(long long)aT * 6 + j] - ohi[j & 1]) + (a.EClo[(long long)aT * 6 + j] - olo[j & 1]);
                             float LPf[6] = {0, 0, 0, 0, 0, 0}, NPf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
                             in_retri_mix(P, rule, pr, pa, Ea64, tlf, s_yT[wib], (float)adetT, idetT, ET64, LPf, NPf, nsub, namb);
-                            for (int i = 0; i < 6; i++) D[i] += (double)LPf[i] * adetA;
+                            for (int i = 0; i < 6; i++) Dp[i] += (double)LPf[i] * adetA;
                             for (int i = 0; i < 9; i++) NPd[i] = (double)NPf[i] * adetA;
                         }
                     }
+                }
+                {   // the pair's weight (1 without domain decomposition)
+                    const double w = (act && P.zeta) ? zeta_weight(a.zptr, a.zidx, aT, T) : 1.0;
+#pragma unroll
+                    for (int i = 0; i < 6; i++) D[i] += Dp[i] * w;
+#pragma unroll
+                    for (int i = 0; i < 9; i++) NPd[i] *= w;
                 }
                 // termNonlocPrime[a][b] -> A[T[b], aT[a]] with the minus sign (Cassemble.cpp:761-766)
 #pragma unroll

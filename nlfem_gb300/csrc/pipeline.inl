@@ -192,6 +192,14 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     P.bridges = 0;
     if (p.elementLabels)
         for (long e = 0; e < p.nE && !P.bridges; e++) P.bridges = p.elementLabels[e] == 0;
+    P.zeta = 0;
+    if (system && p.nZeta > 0) {   // the device reads the indicator rows by these pointers
+        if (!p.zeta_indices || !p.zeta_indptr) return fail(NLFEM_ERR_INVALID, "nZeta > 0 without the zeta indicator");
+        if (p.zeta_indptr[0] != 0) return fail(NLFEM_ERR_INVALID, "zeta indicator: row pointers must start at 0");
+        for (long e = 0; e < p.nE; e++)
+            if (p.zeta_indptr[e + 1] < p.zeta_indptr[e]) return fail(NLFEM_ERR_INVALID, "zeta indicator: decreasing row pointers");
+        P.zeta = 1;
+    }
     // fixed-point scale: typical magnitude of an entry
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (long v = 0; v < p.nV; v++)
@@ -288,6 +296,7 @@ struct Session {
     DevBuf po_cnt, po_off, po_ptr, po_scratch, tcnt, tptr, tcols;   // transposed pattern construction
     long long po_cap = 0, t_nnz = 0;
     DevBuf sv_vec, sv_part;                 // CG solve: f, g, b, x, r, p, Ap; dot partials
+    DevBuf zptr, zidx;                      // domain-decomposition indicator (element -> subdomains)
     DevBuf kclist;                          // elements grouped by kernel class (pass launches)
     long long kc_off[4] = {-1, 0, 0, 0};    // class offsets into kclist (-1: list not built)
     long long pat_cap = 0;
@@ -312,7 +321,7 @@ struct Session {
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                 &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
-                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part};
+                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -421,15 +430,17 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     }
     {
         // one-sided fixed-point passes for the mixed precision; colored passes otherwise
-        bool all_retri = system, all_bary = system, any_singular = false;
+        bool all_retri = system, all_bary = system, any_singular = false, any_zeta = false;
         for (const ProbParams &q : S.hprm) {
             all_retri &= (q.remote == MTH_RETRIANGULATE);
             all_bary &= (q.remote == MTH_BARYCENTER);
             any_singular |= q.singular != 0;
+            any_zeta |= q.zeta != 0;
         }
+        // domain-decomposition weights run in the colored passes (either precision)
         S.pmode = PM_COLORED;
-        if (S.prec == PREC_MIX && S.dim == 2 && all_retri) S.pmode = PM_RETRI;
-        if (S.prec == PREC_MIX && all_bary && !any_singular) S.pmode = PM_BARY;
+        if (S.prec == PREC_MIX && S.dim == 2 && all_retri && !any_zeta) S.pmode = PM_RETRI;
+        if (S.prec == PREC_MIX && all_bary && !any_singular && !any_zeta) S.pmode = PM_BARY;
     }
     const int dV = S.dV, dim = S.dim;
     ENS(S.T64, sizeof(long long) * S.nE * dV);
@@ -487,6 +498,24 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
 // Host -> device copy of the meshes (the per-step input traffic of the end-to-end path).
 static int session_upload(Session &S, const nlfem_problem *probs) {
     const int dV = S.dV, dim = S.dim;
+    bool any_zeta = false;
+    for (int i = 0; i < S.nProb; i++) any_zeta = any_zeta || S.hprm[i].zeta;
+    if (any_zeta) {   // one indicator CSR over the batch's elements (problems without: empty rows)
+        std::vector<long long> zp((size_t)S.nE + 1, 0), zi;
+        for (int i = 0; i < S.nProb; i++) {
+            const nlfem_problem &p = probs[i];
+            for (long e = 0; e < p.nE; e++) {
+                if (S.hprm[i].zeta)
+                    for (long k = p.zeta_indptr[e]; k < p.zeta_indptr[e + 1]; k++) zi.push_back(p.zeta_indices[k]);
+                zp[(size_t)S.eoff[i] + e + 1] = (long long)zi.size();
+            }
+        }
+        ENS(S.zptr, sizeof(long long) * zp.size());
+        ENS(S.zidx, sizeof(long long) * (zi.size() + 1));
+        CK(cudaMemcpyAsync(S.zptr.p, zp.data(), sizeof(long long) * zp.size(), cudaMemcpyHostToDevice, S.st));
+        if (!zi.empty()) CK(cudaMemcpyAsync(S.zidx.p, zi.data(), sizeof(long long) * zi.size(), cudaMemcpyHostToDevice, S.st));
+        CK(cudaStreamSynchronize(S.st));   // the host vectors go out of scope
+    }
     for (int i = 0; i < S.nProb; i++) {
         const nlfem_problem &p = probs[i];
         CK(cudaMemcpyAsync(S.T64.get<long long>() + (long long)S.eoff[i] * dV, p.elements, sizeof(long long) * p.nE * dV, cudaMemcpyHostToDevice, S.st));
@@ -1206,6 +1235,7 @@ static int run_passes(Session &S) {
     a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
     a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
     a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
+    a.zptr = S.zptr.get<long long>(); a.zidx = S.zidx.get<long long>();
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
     const PassRule pr = make_pass_rule(S.rule, DIM);

@@ -140,6 +140,14 @@ class _Problem:
             raise ValueError("configuration['precision'] must be 'fp64' or 'mixed'")
         c.precision = _lib.NLFEM_PREC_MIXED if prec == "mixed" else _lib.NLFEM_PREC_FP64
         c.verbose = int(conf.get("verbose", 0))
+        # domain decomposition (nlfem.pyx:204-214): mesh["nZeta"] > 0 with the element -> subdomain
+        # indicator mesh["ZetaIndicator"] (scipy CSR)
+        nZeta = int(mesh.get("nZeta", 0) or 0) if system else 0
+        if nZeta > 0:
+            Z = mesh["ZetaIndicator"]
+            c.zeta_indices = self._l(np.asarray(Z.indices)).ctypes.data_as(_lp)
+            c.zeta_indptr = self._l(np.asarray(Z.indptr)).ctypes.data_as(_lp)
+            c.nZeta = nZeta
         self.c = c
 
     def _l(self, a):

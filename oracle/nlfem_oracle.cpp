@@ -51,6 +51,9 @@ struct Mesh {
     int remote, close;   // MethodId of integrate_remote / integrate_close
     int is_singular;
     int caps, full_search;
+    // domain decomposition (Cassemble.cpp:649-657): element -> subdomain indicator, CSR
+    const long *zeta_indices = nullptr, *zeta_indptr = nullptr;
+    long nZeta = 0;
 };
 
 struct Quad {
@@ -603,12 +606,23 @@ int integrate(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m, bool
     return integrate_method(first ? m.close : m.remote, aT, bT, q, m, tL, tN, tLP, tNP);
 }
 
+// evaluateZeta (mathhelpers.cpp:19-38): the number of subdomains the two elements share, the
+// size of the intersection of their sorted indicator rows.
+double evaluateZeta(const long *ind, const long *ptr, long nColumns, long aTdx, long bTdx) {
+    const long *a0 = &ind[ptr[aTdx]], *a1 = &ind[ptr[aTdx + 1]];
+    const long *b0 = &ind[ptr[bTdx]], *b1 = &ind[ptr[bTdx + 1]];
+    std::vector<long> inter((size_t)nColumns);
+    auto ls = std::set_intersection(a0, a1, b0, b1, inter.begin());
+    return (double)(ls - inter.begin());
+}
+
 struct Counters {
     long n_pairs = 0, n_cand = 0, n_close = 0, err = 0;
 };
 
 // One outer element: BFS over the dual graph, integrate each candidate, scatter the four local
-// blocks into the map. Cassemble.cpp:555-784 (outdim = 1, weight = 1: no domain decomposition).
+// blocks, weighted by 1/zeta under domain decomposition, into the map. Cassemble.cpp:555-784
+// (outdim = 1).
 void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<long> &xadj,
                     const std::vector<long> &adj, std::vector<int> &visited,
                     std::map<unsigned long, double> &Ad, Counters &cnt, std::vector<long> *pairs) {
@@ -645,15 +659,17 @@ void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<l
                         queue.push(bTdx);                                 // :713
                         cnt.n_pairs++;
                         if (pairs) { pairs->push_back(aTdx); pairs->push_back(bTdx); }
+                        double weight = 1.;                               // :649-657
+                        if (m.nZeta) weight = 1. / evaluateZeta(m.zeta_indices, m.zeta_indptr, m.nZeta, aTdx, bTdx);
                         for (int a = 0; a < dV; a++) {                    // :721-770
                             for (int b = 0; b < dV; b++) {
                                 if (m.is_dg || m.labV[aAdx[a]] > 0) {
-                                    Ad[(unsigned long)aAdx[a] * K + aAdx[b]] += tL[dV * a + b];
-                                    Ad[(unsigned long)aAdx[a] * K + bAdx[b]] += -tN[dV * a + b];
+                                    Ad[(unsigned long)aAdx[a] * K + aAdx[b]] += tL[dV * a + b] * weight;
+                                    Ad[(unsigned long)aAdx[a] * K + bAdx[b]] += -tN[dV * a + b] * weight;
                                 }
                                 if (m.is_dg || m.labV[bAdx[b]] > 0) {
-                                    Ad[(unsigned long)bAdx[b] * K + bAdx[a]] += tLP[dV * a + b];
-                                    Ad[(unsigned long)bAdx[b] * K + aAdx[a]] += -tNP[dV * a + b];
+                                    Ad[(unsigned long)bAdx[b] * K + bAdx[a]] += tLP[dV * a + b] * weight;
+                                    Ad[(unsigned long)bAdx[b] * K + aAdx[a]] += -tNP[dV * a + b] * weight;
                                 }
                             }
                         }
@@ -722,6 +738,15 @@ int oracle_toRef(const double *E, const double *x, double *p) { return toRef(E, 
 // returning CSR and the load vector in memory. compute: "system" or "forcing".
 // subset (optional): only these outer elements are processed (CPU baseline sampling).
 // nthreads <= 1: canonical single-threaded order (one map, as the reference's 1-thread run).
+// Domain-decomposition indicator for the next oracle_par_assemble call (nZeta = 0: none).
+static const long *g_zeta_indices = nullptr, *g_zeta_indptr = nullptr;
+static long g_nZeta = 0;
+void oracle_set_zeta(const long *indices, const long *indptr, long nZeta) {
+    g_zeta_indices = indices;
+    g_zeta_indptr = indptr;
+    g_nZeta = nZeta;
+}
+
 oracle_result *oracle_par_assemble(
     const char *compute, int K, const long *ptrTriangles, const long *ptrLabelTriangles,
     const double *ptrVerts, const long *ptrLabelVerts, int nE, int nV,
@@ -735,6 +760,7 @@ oracle_result *oracle_par_assemble(
     m.dim = dim; m.dV = dim + 1; m.outdim = outdim; m.is_dg = is_DG;
     m.nE = nE; m.nV = nV; m.K = K;
     m.T = ptrTriangles; m.labT = ptrLabelTriangles; m.labV = ptrLabelVerts; m.V = ptrVerts;
+    m.zeta_indices = g_zeta_indices; m.zeta_indptr = g_zeta_indptr; m.nZeta = g_nZeta;
     m.sqdelta = sqdelta; m.delta = sqrt(sqdelta); m.frac_s = fractional_s;
     m.kernel = kernel_id(kernel); m.load = load_id(f);
     m.remote = method_id(method_remote);

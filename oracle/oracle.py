@@ -62,6 +62,8 @@ def lib():
             _lp, _lp, _dp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp,
             ctypes.c_int, _dp, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
             ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_double, _lp, ctypes.c_long, _dp, _ip]
+        l.oracle_set_zeta.restype = None
+        l.oracle_set_zeta.argtypes = [_lp, _lp, ctypes.c_long]
         l.oracle_evaluate_mass.restype = ctypes.c_int
         l.oracle_evaluate_mass.argtypes = [_dp, _dp, _lp, _lp, _dp, _lp, ctypes.c_int, ctypes.c_int, _dp, _dp,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -120,6 +122,15 @@ def assemble(mesh, kernel, conf, compute="system", load=None, nthreads=1, subset
     caps = int(conf["approxBalls"].get("is_PlacePointOnCap", 1))
     s = kernel.get("fractional_s", -1.0) if kernel else -1.0
     full = int(conf.get("is_fullConnectedComponentSearch", 0))
+    # domain decomposition (nlfem.pyx:204-214): mesh["nZeta"] > 0 with mesh["ZetaIndicator"] (CSR)
+    nZeta = int(mesh.get("nZeta", 0) or 0)
+    if nZeta > 0:
+        Z = mesh["ZetaIndicator"]
+        zi, zip_ = _l(np.asarray(Z.indices)); zp, zpp = _l(np.asarray(Z.indptr))
+        keep += [zi, zp]
+        lib().oracle_set_zeta(zip_, zpp, nZeta)
+    else:
+        lib().oracle_set_zeta(ctypes.cast(None, _lp), ctypes.cast(None, _lp), 0)
     r = lib().oracle_par_assemble(
         compute.encode(), K, elp, elabp, vep, vlabp, nE, nV,
         Pxp, Px.shape[0], dxp, Pyp, Py.shape[0], dyp, sqdelta, int(is_dg),

@@ -155,6 +155,30 @@ def test_mixed_no_caps(nl, orc):
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_domain_decomposition_weights(nl, orc, prec):
+    """Domain decomposition (Cassemble.cpp:649-657): every pair's blocks weighted by 1 / the number
+    of subdomains its elements share. Two subdomains overlap in a strip wider than the ball, so
+    every interacting pair shares one."""
+    m = square_mesh(14, 0.1, jitter=0.1, seed=8)
+    x = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
+    rows = [[0] if xi < 0.3 else ([1] if xi > 0.7 else [0, 1]) for xi in x]
+    indptr = np.cumsum([0] + [len(r) for r in rows])
+    Z = sp.csr_matrix((np.ones(indptr[-1]), np.concatenate(rows), indptr), shape=(len(rows), 2))
+    m["nZeta"] = 2
+    m["ZetaIndicator"] = Z
+    A = nl.stiffnessMatrix(m, KC, conf2d(precision=prec))
+    B = orc.assemble(m, KC, conf2d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    tol = FP64_TOL if prec == "fp64" else MIX_TOL
+    assert fro < tol and mx < tol, (fro, mx)
+    m0 = dict(m)
+    m0["nZeta"] = 0
+    B0 = orc.assemble(m0, KC, conf2d())["A"]
+    assert abs(B - B0).max() > 1e-3 * abs(B0).max()   # the weights change the matrix
+
+
 def test_pair_blocks_match_oracle(nl, orc):
     m = square_mesh(16, 0.1, jitter=0.2, seed=9)
     k = {"function": "parabola", "horizon": 0.1, "outputdim": 1}

@@ -308,6 +308,17 @@ def pinned(mesh):
     return out, nbytes
 
 
+def combine_ranks(secs, pairs, dist, device="cpu"):
+    """The job's time and work over the ranks: the slowest rank's seconds and all ranks' pairs
+    (replicas: value = all pairs / max time)."""
+    import torch
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    p = torch.tensor([pairs], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(p.item())
+
+
 def run_gpu(args, rank=0, world=1, dist=None):
     import ctypes
     import torch
@@ -324,11 +335,7 @@ def run_gpu(args, rank=0, world=1, dist=None):
                                                           graph=not args.no_graph)
     launches = int(sum(s["n_launches"] for s in all_st))
     if dist is not None:
-        t = torch.tensor([secs], dtype=torch.float64, device="cuda")
-        p = torch.tensor([pairs], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(p, op=dist.ReduceOp.SUM)
-        secs, pairs = float(t.item()), float(p.item())
+        secs, pairs = combine_ranks(secs, pairs, dist, "cuda")
     value = pairs / secs
     A_mixed = [sess.download(i) for i in range(len(problems))] if rank == 0 else []
     sess.close()

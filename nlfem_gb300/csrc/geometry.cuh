@@ -186,7 +186,12 @@ __device__ __forceinline__ bool xtoRef(const double *E, const double *y, double 
 }
 
 // ------------------------------------------------------------------- model (model.cpp)
-enum KernelId { KER_CONSTANT = 0, KER_PARABOLA = 1, KER_FRACTIONAL = 2, KER_CONSTANT3D = 3 };
+// KER_LABELED .. KER_CONSTTRUNC depend on the elements' labels or on absolute positions: FP64
+// passes only.
+enum KernelId {
+    KER_CONSTANT = 0, KER_PARABOLA = 1, KER_FRACTIONAL = 2, KER_CONSTANT3D = 3,
+    KER_LABELED = 4, KER_NOTCH = 5, KER_LABELEDNOTCH = 6, KER_LABELEDVALVE = 7, KER_CONSTTRUNC = 8
+};
 enum MethodId { MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2 };
 enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
 
@@ -194,6 +199,7 @@ enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
 struct ProbParams {
     double sqdelta, delta;
     double kc;       // kernel constant (host-computed with the reference's formula)
+    double kc2;      // labeled kernel: the constant of the label >= 21 branch
     double expo;     // fractional: dim + 2s
     float sqdelta_f, kc_f, expo_f, pad_f;
     int kernel, remote, close, caps;
@@ -207,10 +213,32 @@ struct ProbParams {
     double el;        // mean element measure (bounding box / nE), for capacity estimates
 };
 
-// FP64 kernel value k(x, y) (model.cpp:25-28, 52-60, 62-65, 126-138)
+// FP64 kernel value k(x, lx, y, ly), lx and ly the labels of the elements of x and y
+// (model.cpp:25-28, 36-42, 52-60, 62-65, 67-114, 126-138). Where the reference aborts (labeled:
+// |x - y| >= delta, or 10 lx + ly in 14..20) it sets err[7] and returns 0.
 template <int DIM>
-__device__ __forceinline__ double kernel_f64(const ProbParams &P, const double *x, const double *y) {
+__device__ __forceinline__ double kernel_f64(const ProbParams &P, const double *x, long long lx, const double *y,
+                                             long long ly, int *err) {
     switch (P.kernel) {
+    case KER_LABELED: {
+        const double z0 = xsub(x[0], y[0]), z1 = xsub(x[1], y[1]);
+        const double dist = xadd(xmul(z0, z0), xmul(z1, z1));
+        const long long label = 10 * lx + ly;
+        if (dist >= P.sqdelta || (label > 13 && label < 21)) { atomicOr(&err[7], 1); return 0.0; }
+        if (label <= 12) return P.kc;
+        if (label >= 21) return P.kc2 * (1 - dist / P.sqdelta);
+        return 0.0;
+    }
+    case KER_NOTCH: {   // zero across the notch {x1 = 0, x0 > 0}
+        const bool cross = ((x[1] > 0) != (y[1] > 0)) && x[0] > 0 && y[0] > 0;
+        return cross ? 0.0 : P.kc;
+    }
+    case KER_LABELEDNOTCH: return lx + ly == 7 ? 0.0 : P.kc;
+    case KER_LABELEDVALVE: return lx >= ly ? P.kc : 0.0;
+    case KER_CONSTTRUNC: {
+        const double z0 = xsub(x[0], y[0]), z1 = xsub(x[1], y[1]);
+        return P.sqdelta > xadd(xmul(z0, z0), xmul(z1, z1)) ? P.kc : 0.0;
+    }
     case KER_PARABOLA: {
         double z0 = x[0] - y[0], z1 = x[1] - y[1];
         return P.kc * (P.sqdelta - (z0 * z0 + z1 * z1));

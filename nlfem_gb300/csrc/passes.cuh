@@ -410,7 +410,7 @@ __device__ void in_retri_mix(const ProbParams &P, const Rule &rule, const PassRu
 // ---------------------------------------------------------------- FP64 pair quadrature (2D)
 // Reference arithmetic (integration.cpp:345-540) split by side.
 __device__ void out_retri_f64(const ProbParams &P, const Rule &rule, const double *xs64,
-                              const double *Eb, double *L, double *N, unsigned &nsub, int *err) {
+                              const double *Eb, int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
     double R[18];
     for (int k = 0; k < rule.nPx; k++) {
         const double *x = &xs64[2 * k];
@@ -424,7 +424,7 @@ __device__ void out_retri_f64(const ProbParams &P, const Rule &rule, const doubl
                 double y[2];
                 y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
                 y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
-                const double w = kernel_f64<2>(P, x, y) * rule.dy[i] * rTdet;
+                const double w = kernel_f64<2>(P, x, la, y, lb, err) * rule.dy[i] * rTdet;
                 iL += w;
                 double ref[2];
                 if (!xtoRef(Eb, y, ref)) atomicOr(&err[4], 1);
@@ -442,7 +442,7 @@ __device__ void out_retri_f64(const ProbParams &P, const Rule &rule, const doubl
 }
 
 __device__ void in_retri_f64(const ProbParams &P, const Rule &rule, const double *Ea,
-                             const double *ET, double *LP, double *NP, unsigned &nsub, int *err) {
+                             const double *ET, int la, int lT, double *LP, double *NP, unsigned &nsub, int *err) {
     double R[18];
     for (int k = 0; k < rule.nPx; k++) {
         double x[2];
@@ -456,7 +456,7 @@ __device__ void in_retri_f64(const ProbParams &P, const Rule &rule, const double
                 double y[2];
                 y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
                 y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
-                const double w = kernel_f64<2>(P, y, x) * rule.dy[i] * rTdet;
+                const double w = kernel_f64<2>(P, y, lT, x, la, err) * rule.dy[i] * rTdet;
                 double ref[2];
                 if (!xtoRef(ET, y, ref)) atomicOr(&err[4], 1);
                 const double s[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
@@ -478,7 +478,7 @@ __device__ void in_retri_f64(const ProbParams &P, const Rule &rule, const double
 template <int DIM, int PREC>
 __device__ void out_bary(const ProbParams &P, const Rule &rule, const PassRule &pr, const float *xsf,
                          const double *xs64, const float *pb, const double *Eb64, double adetb,
-                         double *L, double *N, unsigned &nsub, unsigned &namb) {
+                         int la, int lb, double *L, double *N, unsigned &nsub, unsigned &namb, int *err) {
     constexpr int dV = DIM + 1;
     constexpr int NS = dV * (dV + 1) / 2;
     double b64[DIM];
@@ -513,9 +513,9 @@ __device__ void out_bary(const ProbParams &P, const Rule &rule, const PassRule &
             for (int i = 0; i < rule.nPy; i++) {
                 double y[DIM];
                 xtoPhys<DIM>(Eb64, &rule.Py[DIM * i], y);
-                const double ker = kernel_f64<DIM>(P, &xs64[DIM * k], y);
+                const double ker = kernel_f64<DIM>(P, &xs64[DIM * k], la, y, lb, err);
                 iL += adetb * ker * rule.dy[i];
-                const double kerP = kernel_f64<DIM>(P, y, &xs64[DIM * k]);
+                const double kerP = kernel_f64<DIM>(P, y, lb, &xs64[DIM * k], la, err);
 #pragma unroll
                 for (int j = 0; j < dV; j++) iN[j] += rule.psiy[dV * i + j] * kerP * rule.dy[i] * adetb;
             }
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                         double Ls[NS];
 #pragma unroll
                         for (int i = 0; i < NS; i++) Ls[i] = 0.0;
-                        out_bary<DIM, PREC>(P, rule, pr, s_xf[wib], s_x64[wib], pb, Eb64, a.adet[bT], Ls, Nd, nsub, namb);
+                        out_bary<DIM, PREC>(P, rule, pr, s_xf[wib], s_x64[wib], pb, Eb64, a.adet[bT], a.labT[T], a.labT[bT], Ls, Nd, nsub, namb, a.err);
 #pragma unroll
                         for (int i = 0; i < NS; i++) Dp[i] += Ls[i] * adetT;
 #pragma unroll
@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                     } else if (DIM == 2) {
                         if (PREC == PREC_F64) {
                             double Ls[6] = {0, 0, 0, 0, 0, 0};
-                            out_retri_f64(P, rule, s_x64[wib], Eb64, Ls, Nd, nsub, a.err);
+                            out_retri_f64(P, rule, s_x64[wib], Eb64, a.labT[T], a.labT[bT], Ls, Nd, nsub, a.err);
                             for (int i = 0; i < 6; i++) Dp[i] += Ls[i] * adetT;
                             for (int i = 0; i < 9; i++) Nd[i] *= adetT;
                         } else {
@@ -771,7 +771,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                     if (!done && P.remote == MTH_RETRIANGULATE) {
                         if (PREC == PREC_F64) {
                             double LP[6] = {0, 0, 0, 0, 0, 0};
-                            in_retri_f64(P, rule, Ea64, ET64, LP, NPd, nsub, a.err);
+                            in_retri_f64(P, rule, Ea64, ET64, a.labT[aT], a.labT[T], LP, NPd, nsub, a.err);
                             for (int i = 0; i < 6; i++) Dp[i] += LP[i] * adetA;
                             for (int i = 0; i < 9; i++) NPd[i] *= adetA;
                         } else {

@@ -67,6 +67,11 @@ static int kernel_id(const char *s) {
     if (k == "parabola") return KER_PARABOLA;
     if (k == "fractional") return KER_FRACTIONAL;
     if (k == "constant3D") return KER_CONSTANT3D;
+    if (k == "labeled") return KER_LABELED;
+    if (k == "notch") return KER_NOTCH;
+    if (k == "labeledNotch") return KER_LABELEDNOTCH;
+    if (k == "labeledValve") return KER_LABELEDVALVE;
+    if (k == "constantTruncated") return KER_CONSTTRUNC;
     return -1;
 }
 static int method_id(const char *s) {
@@ -171,6 +176,11 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
         if (P.close == MTH_FRACTIONAL && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "fractional close pairs are 2D only");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
+        if (P.kernel >= KER_LABELED) {   // label- or position-dependent kernels of 2D meshes
+            if (p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " is implemented for 2D meshes only");
+            if (p.precision == NLFEM_PREC_MIXED)
+                return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " runs on the fp64 path only (precision \"fp64\")");
+        }
         P.caps = p.is_PlacePointOnCap ? 1 : 0;
         P.full_search = p.is_fullConnectedComponentSearch ? 1 : 0;
         const double s = p.fractional_s;
@@ -182,6 +192,14 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             P.kc = (2. - 2. * s) / (M_PI * pow(P.delta, 2. - 2. * s));
             break;
         case KER_CONSTANT3D: P.kc = 15 / (M_PI * 4 * pow(P.delta, 5)); break;              // model.cpp:62-65
+        case KER_LABELED:                                                                  // model.cpp:67-89
+            P.kc = 0.01 * 3. / (4 * pow(p.sqdelta, 2));
+            P.kc2 = 100 * 3. / (4 * pow(p.sqdelta, 2));
+            break;
+        case KER_NOTCH: case KER_LABELEDNOTCH: case KER_LABELEDVALVE:                      // model.cpp:91-114
+            P.kc = 4 / (M_PI * pow(p.sqdelta, 2));
+            break;
+        case KER_CONSTTRUNC: P.kc = 4 / (M_PI * pow(p.sqdelta, 2)); break;                 // model.cpp:30-42
         }
         P.kc_f = (float)P.kc;
         P.expo_f = (float)P.expo;
@@ -218,6 +236,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         const double ball = p.dim == 2 ? M_PI * p.sqdelta : 4.0 / 3.0 * M_PI * p.sqdelta * P.delta;
         double kmax = P.kc;
         if (P.kernel == KER_PARABOLA) kmax = P.kc * p.sqdelta;
+        if (P.kernel == KER_LABELED) kmax = std::max(P.kc, P.kc2);
         if (P.kernel == KER_FRACTIONAL) kmax = P.kc / pow(std::min(h, P.delta), P.expo);
         mag = fabs(kmax) * el * std::max(ball, el);
     } else {
@@ -1023,6 +1042,7 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
     QuadArgs a;
     memset(&a, 0, sizeof(a));
     a.pA = S.pA.get<int>(); a.pB = S.pB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    a.labT = S.labT.get<int>();
     a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
     a.probs = S.prm.get<ProbParams>(); a.P = n; a.err = S.err.get<int>();
     a.n_close = S.counters.get<unsigned long long>() + 4;
@@ -1096,6 +1116,7 @@ static int run_close(Session &S) {
     QuadArgs a;
     memset(&a, 0, sizeof(a));
     a.pA = S.closeA.get<int>(); a.pB = S.closeB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    a.labT = S.labT.get<int>();
     a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
     a.probs = S.prm.get<ProbParams>(); a.P = nslot; a.err = S.err.get<int>();
     a.n_close = S.counters.get<unsigned long long>() + 4;
@@ -1291,6 +1312,7 @@ static int check_errors(Session &S) {
     if (r) return r;
     if (he[3]) return fail(NLFEM_ERR_CUDA, "internal: CSR slot not found during scatter");
     if (he[4]) return fail(NLFEM_ERR_NUMERIC, "in solve2x2. Matrix not invertible.");
+    if (he[7]) return fail(NLFEM_ERR_NUMERIC, "kernel evaluated outside its domain (labeled: |x - y| >= delta, or 10 labelx + labely in 14..20)");
     return NLFEM_OK;
 }
 

@@ -32,6 +32,7 @@ struct Duffy {
 
 struct QuadArgs {
     const int *pA, *pB, *T32, *labV, *eprob;
+    const int *labT;          // element labels (label-dependent kernels)
     const double *EC, *adet;
     const ProbParams *probs;
     const long long *rowptr;
@@ -41,7 +42,7 @@ struct QuadArgs {
     long long P;
     const int *list;          // optional index list into the pairs
     long long nlist;
-    int *err;                 // [3] slot not found, [4] singular toRef
+    int *err;                 // [3] slot not found, [4] singular toRef, [7] kernel outside its domain
     unsigned long long *n_close;
     double *blocks_out;       // explicit-pair mode: (P, 4, dV, dV) blocks instead of scatter
     int *ret_out;             // explicit-pair mode: doesInteract
@@ -101,7 +102,7 @@ __device__ __forceinline__ bool share_vertex(const int *aV, const int *bV, int d
 
 // FP64 integrate_retriangulate (integration.cpp:345-540) of one pair.
 __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, const double *Ea,
-                                      const double *Eb, double adet_a, double *L, double *N,
+                                      const double *Eb, int la, int lb, double adet_a, double *L, double *N,
                                       double *LP, double *NP, int *err, int &nsub) {
     double R[18];
     int interacts = 0;
@@ -120,12 +121,12 @@ __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, con
                 // toPhys(E, p, out) of the sub-triangle (mathhelpers.cpp:210-215)
                 y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
                 y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
-                const double ker = kernel_f64<2>(P, x, y);
+                const double ker = kernel_f64<2>(P, x, la, y, lb, err);
                 const double w = rule.dy[i] * rTdet;
                 innerLocal += ker * w;
                 double ref[2];
                 if (!xtoRef(Eb, y, ref)) atomicOr(&err[4], 1);
-                const double kerP = kernel_f64<2>(P, y, x);
+                const double kerP = kernel_f64<2>(P, y, lb, x, la, err);
                 const double psi[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
                 const double wl = kerP * w * rule.dx[k] * adet_a;
 #pragma unroll
@@ -157,8 +158,8 @@ __device__ int quad_retriangulate_f64(const ProbParams &P, const Rule &rule, con
 // FP64 integrate_baryCenter (integration.cpp:910-1018) of one pair (2D or 3D).
 template <int DIM>
 __device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const double *Ea,
-                                   const double *Eb, double adet_a, double adet_b, double *L,
-                                   double *N, int &nsub) {
+                                   const double *Eb, int la, int lb, double adet_a, double adet_b, double *L,
+                                   double *N, int *err, int &nsub) {
     constexpr int dV = DIM + 1;
     double b[DIM];
     xbary<DIM>(Eb, b);
@@ -175,9 +176,9 @@ __device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const 
         for (int i = 0; i < rule.nPy; i++) {
             double y[DIM];
             xtoPhys<DIM>(Eb, &rule.Py[DIM * i], y);
-            const double ker = kernel_f64<DIM>(P, x, y);
+            const double ker = kernel_f64<DIM>(P, x, la, y, lb, err);
             innerLocal += adet_b * ker * rule.dy[i];
-            const double kerP = kernel_f64<DIM>(P, y, x);
+            const double kerP = kernel_f64<DIM>(P, y, lb, x, la, err);
 #pragma unroll
             for (int j = 0; j < dV; j++) iN[j] += rule.psiy[dV * i + j] * kerP * rule.dy[i] * adet_b;
         }
@@ -219,9 +220,9 @@ __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
             bool prime = false;
             int interacts = 0;
             if (method == MTH_BARYCENTER) {
-                interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.adet[aT], a.adet[bT], L, N, nsub);
+                interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.labT[aT], a.labT[bT], a.adet[aT], a.adet[bT], L, N, a.err, nsub);
             } else if (DIM == 2) {
-                interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.adet[aT], L, N, LP, NP, a.err, nsub);
+                interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.labT[aT], a.labT[bT], a.adet[aT], L, N, LP, NP, a.err, nsub);
                 prime = true;
             }
             if (a.blocks_out) {

@@ -37,7 +37,8 @@ namespace {
 const double EPSILON = 1e-15;        // mathhelpers.h:11
 const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
 
-enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_NONE = -1 };
+enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_LABELED = 4, K_NOTCH = 5,
+                K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_NONE = -1 };
 enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_NONE = -1 };
 enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_NONE = -1 };
 
@@ -181,8 +182,33 @@ void basis(const double *p, int dim, double *psi) {                        // Me
 }
 
 // ---------------------------------------------------------------- model (model.cpp)
-double kernel_value(const Mesh &m, const double *x, const double *y) {
+// k(x, labelx, y, labely). Where the reference aborts (labeled, model.cpp:74-78, 86-88) the value
+// is NaN.
+double kernel_value(const Mesh &m, const double *x, long lx, const double *y, long ly) {
     switch (m.kernel) {
+    case K_LABELED: {  // model.cpp:67-89
+        const long label = 10 * lx + ly;
+        const double dist = vec_sqL2dist(x, y, 2);
+        if (dist >= m.sqdelta) return NAN;
+        if (label <= 12) return 0.01 * 3. / (4 * pow(m.sqdelta, 2));
+        if (label >= 21) return (100 * 3. / (4 * pow(m.sqdelta, 2))) * (1 - (dist / m.sqdelta));
+        if (label == 13) return 0.0;
+        return NAN;
+    }
+    case K_NOTCH: {    // model.cpp:91-102
+        const bool xN = x[1] > 0, yN = y[1] > 0, xE = x[0] > 0, yE = y[0] > 0;
+        const bool cross = (xN != yN) && xE && yE;
+        return !cross * (4 / (M_PI * pow(m.sqdelta, 2)));
+    }
+    case K_LABELEDNOTCH:  // model.cpp:104-108
+        return !(lx + ly == 7) * (4 / (M_PI * pow(m.sqdelta, 2)));
+    case K_LABELEDVALVE:  // model.cpp:110-114
+        return lx >= ly ? 4.0 / (M_PI * pow(m.sqdelta, 2)) : 0.0;
+    case K_CONSTTRUNC: {  // model.cpp:33-42
+        double z[2] = {x[0] - y[0], x[1] - y[1]};
+        const bool interacts = m.sqdelta > vec_dot(z, z, 2);
+        return interacts * 4 / (M_PI * pow(m.sqdelta, 2));
+    }
     case K_CONSTANT:   // model.cpp:25-28
         return 4 / (M_PI * sq(m.sqdelta));
     case K_PARABOLA: { // model.cpp:52-60
@@ -250,6 +276,7 @@ int placePointOnCap(const double *ypred, const double *ycur, const double *x, do
     ynew[0] = x[0] + n[0];
     ynew[1] = x[1] + n[1];
     if (inTriangle(ynew, &TE[0], &TE[2], &TE[4], na, nb, nc)) {
+        if (Rdx >= 9) return 0;   // see method_retriangulate: R holds 9 points
         R[2 * Rdx] = ynew[0];
         R[2 * Rdx + 1] = ynew[1];
         return 1;
@@ -257,6 +284,12 @@ int placePointOnCap(const double *ypred, const double *ycur, const double *x, do
     return 0;
 }
 
+// The reference's point buffer R holds 9 points (integration.cpp:1415). Where the sphere touches
+// an edge up to rounding (on an unjittered grid with h = 0.15 and delta = 0.1, element centroids
+// lie at distance delta from grid lines), that edge yields two
+// roots about 1e-8 apart with a cap point between them; with two such edges the polygon has 10
+// or more points and the reference writes past R (undefined behaviour). Here, as in the CUDA
+// restatement, points beyond the 9th are dropped.
 int method_retriangulate(const double *xc, const double *TE, double sqdelta, double *out,
                          int caps) {                                       // integration.cpp:1393-1512
     int Rdx = 0;
@@ -274,10 +307,12 @@ int method_retriangulate(const double *xc, const double *TE, double sqdelta, dou
         double a[2] = {q[0] - xc[0], q[1] - xc[1]};
         double b[2] = {p[0] - q[0], p[1] - q[1]};
         if (vec_sqL2dist(p, xc, 2) <= sqdelta) {
-            R[2 * Rdx] = p[0];
-            R[2 * Rdx + 1] = p[1];
+            if (Rdx < 9) {
+                R[2 * Rdx] = p[0];
+                R[2 * Rdx + 1] = p[1];
+                Rdx += 1;
+            }
             is_onEdge = false;
-            Rdx += 1;
         }
         // arma::dot of two 2-vectors: a0*b0 + a1*b1
         double ab = a[0] * b[0] + a[1] * b[1];
@@ -301,19 +336,23 @@ int method_retriangulate(const double *xc, const double *TE, double sqdelta, dou
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
                 if (is_onEdge && caps)
                     Rdx += placePointOnCap(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                R[2 * Rdx] = y1[0];
-                R[2 * Rdx + 1] = y1[1];
+                if (Rdx < 9) {
+                    R[2 * Rdx] = y1[0];
+                    R[2 * Rdx + 1] = y1[1];
+                    Rdx += 1;
+                }
                 is_onEdge = true;
-                Rdx += 1;
             }
             if ((0 <= lam2) && (lam2 <= 1) && (sq(lam1 - lam2) > 0)) {
                 is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
                 if (is_onEdge && caps)
                     Rdx += placePointOnCap(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, Rdx, R);
-                R[2 * Rdx] = y2[0];
-                R[2 * Rdx + 1] = y2[1];
+                if (Rdx < 9) {
+                    R[2 * Rdx] = y2[0];
+                    R[2 * Rdx + 1] = y2[1];
+                    Rdx += 1;
+                }
                 is_onEdge = true;
-                Rdx += 1;
             }
         }
     }
@@ -356,10 +395,10 @@ int integrate_retriangulate(const Elem &aT, const Elem &bT, const Quad &q, const
             for (int i = 0; i < q.nPy; i++) {
                 toPhys3(&reTri[6 * r], &q.Py[2 * i], y);
                 double rTdet = absDet2(&reTri[6 * r]);
-                double ker = kernel_value(m, x, y);
+                double ker = kernel_value(m, x, aT.label, y, bT.label);
                 innerLocal += ker * q.dy[i] * rTdet;
                 toRef(bT.E, y, ref);
-                double kerP = kernel_value(m, y, x);
+                double kerP = kernel_value(m, y, bT.label, x, aT.label);
                 basis(ref, 2, psi);
                 for (int b = 0; b < dV; b++) {
                     innerNonloc[b] += psi[b] * ker * q.dy[i] * rTdet;
@@ -397,9 +436,9 @@ int integrate_baryCenter(const Elem &aT, const Elem &bT, const Quad &q, const Me
             for (int i = 0; i < q.nPy; i++) {
                 toPhys(bT.E, &q.Py[dim * i], dim, y);
                 double rTdet = absDetDim(bT.E, dim);
-                double ker = kernel_value(m, x, y);
+                double ker = kernel_value(m, x, aT.label, y, bT.label);
                 innerLocal += rTdet * ker * q.dy[i];
-                ker = kernel_value(m, y, x);
+                ker = kernel_value(m, y, bT.label, x, aT.label);
                 for (int b = 0; b < dV; b++) innerNonloc[b] += q.psiy[dV * i + b] * ker * q.dy[i] * rTdet;
             }
         }
@@ -465,7 +504,7 @@ int integrate_fractional(const Elem &aT, const Elem &bT, const Quad &q, const Me
             const double *al = &q.alphaC[c][(t * q.nPg + k) * 4];
             toPhys(aS.E, &al[0], 2, x);
             toPhys(bS.E, &al[2], 2, y);
-            double ker = kernel_value(m, x, y);
+            double ker = kernel_value(m, x, aT.label, y, bT.label);
             basis(&al[0], 2, psix);
             basis(&al[2], 2, psiy);
             int shift = dV - nEqual;
@@ -690,6 +729,11 @@ int kernel_id(const char *s) {
     if (k == "parabola") return K_PARABOLA;
     if (k == "fractional") return K_FRACTIONAL;
     if (k == "constant3D") return K_CONSTANT3D;
+    if (k == "labeled") return K_LABELED;
+    if (k == "notch") return K_NOTCH;
+    if (k == "labeledNotch") return K_LABELEDNOTCH;
+    if (k == "labeledValve") return K_LABELEDVALVE;
+    if (k == "constantTruncated") return K_CONSTTRUNC;
     return K_NONE;
 }
 int load_id(const char *s) {

@@ -191,6 +191,73 @@ def test_pair_blocks_match_oracle(nl, orc):
     np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
 
 
+LABEL_KERNELS = ["labeled", "notch", "labeledNotch", "labeledValve", "constantTruncated"]
+
+
+def _labeled_mesh(n=14, seed=5):
+    """Omega split into labels 3 (x0 < 0.5) and 4, the layer -1, all moved by -0.5 so that the
+    notch {x1 = 0, x0 > 0} cuts the right half. Every label pair is a case of the labeled kernel
+    (10 lx + ly in {-11, -7, -6, 9, 29, 33, 34, 39, 43, 44}); 3 + 4 = 7 closes labeledNotch."""
+    from nlfem_gb300 import meshes
+    v, e, l = meshes.regular_square(n, 0.1, jitter=0.1, seed=seed)
+    bx = v[e].mean(axis=1)[:, 0]
+    lab = np.where(l > 0, np.where(bx < 0.5, 3, 4), -1)
+    return meshes.mesh_dict(v - 0.5, e, lab)
+
+
+@pytest.mark.parametrize("name,method", [(k, "retriangulate") for k in LABEL_KERNELS] + [("labeledValve", "baryCenter"), ("notch", "baryCenter")])
+def test_label_kernels_fp64(nl, orc, name, method):
+    """Label- and position-dependent kernels (model.cpp:30-42, 67-114) on the FP64 path."""
+    m = _labeled_mesh()
+    k = {"function": name, "horizon": 0.1, "outputdim": 1}
+    A = nl.stiffnessMatrix(m, k, conf2d(method=method))
+    B = orc.assemble(m, k, conf2d(method=method))["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)
+    if name != "constantTruncated":   # the kernel matters: not the constant kernel's matrix
+        C = orc.assemble(m, KC, conf2d(method=method))["A"]
+        assert abs(B - C).max() > 1e-3 * abs(C).max()
+
+
+def test_label_kernel_pair_blocks(nl, orc):
+    m = _labeled_mesh(10, 6)
+    k = {"function": "labeled", "horizon": 0.1, "outputdim": 1}
+    pairs = orc.assemble(m, k, conf2d(), want_pairs=True)["pairs"]
+    g, gr = nl.pair_blocks(m, k, conf2d(), pairs)
+    o, orr = orc.pair_blocks(m, k, conf2d(), pairs)
+    np.testing.assert_array_equal(gr != 0, orr != 0)
+    np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
+
+
+def test_label_kernel_errors(nl):
+    from nlfem_gb300._lib import NlfemError
+    k = {"function": "labeled", "horizon": 0.1, "outputdim": 1}
+    m = square_mesh(8, 0.1, jitter=0.1, seed=1)
+    m["elementLabels"] = np.where(m["elementLabels"] > 0, 2, -1)   # 10 * 2 - 1 = 19: the reference aborts
+    with pytest.raises(NlfemError, match="outside its domain"):
+        nl.stiffnessMatrix(m, k, conf2d())
+    with pytest.raises(NlfemError, match="fp64 path only"):
+        nl.stiffnessMatrix(_labeled_mesh(8), k, conf2d(precision="mixed"))
+    # the session still works after the error
+    m = _labeled_mesh(8)
+    assert nl.stiffnessMatrix(m, k, conf2d()).nnz > 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_tangent_sphere_polygons(nl, orc, prec):
+    """Unjittered grid with h = 0.15 and delta = 0.1: element centroids lie at distance delta from
+    grid lines, the sphere touches edges up to rounding, and some polygons would need more than 9
+    points. Both sides keep the first 9."""
+    m = square_mesh(8, 0.1)
+    A = nl.stiffnessMatrix(m, KC, conf2d(precision=prec))
+    B = orc.assemble(m, KC, conf2d())["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    tol = FP64_TOL if prec == "fp64" else 1e-6
+    assert fro < tol and mx < tol, (fro, mx)
+
+
 def test_load_vector(nl, orc):
     m = square_mesh(24, 0.1, jitter=0.2, seed=8)
     f = nl.loadVector(m, {"function": "linear"}, conf2d())

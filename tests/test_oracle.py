@@ -148,3 +148,48 @@ def test_oracle_load_vector_linear():
     assert np.all(f[~keep] == 0)
     # sum of the load over all basis functions of label>0 elements = integral of f over them
     assert np.all(f[keep] < 0)
+
+
+def test_oracle_label_kernels_reduce_to_constant():
+    """The label- and position-dependent kernels (model.cpp:30-42, 67-114) equal the constant
+    kernel, or a multiple of it, where their cases say so."""
+    from oracle import oracle
+    m = square_mesh(10, 0.1, jitter=0.1, seed=2)
+    conf = conf2d()
+
+    def A(mesh, name):
+        r = oracle.assemble(mesh, {"function": name, "horizon": 0.1, "outputdim": 1}, conf)
+        assert r["n_errors"] == 0
+        return r["A"]
+
+    C = A(m, "constant")
+    # every quadrature point lies inside the ball: truncation changes nothing
+    assert abs(A(m, "constantTruncated") - C).max() == 0
+    # labels 1 and -1 never sum to 7
+    assert abs(A(m, "labeledNotch") - C).max() == 0
+    # 10 lx + ly <= 12 for labels 1 and -1: the constant 0.03 / (4 delta^4)
+    assert abs(A(m, "labeled") - C * (0.03 * np.pi / 16)).max() <= 1e-14 * abs(C).max()
+    # left of x0 = 0 nothing crosses the notch
+    ms = dict(m)
+    ms["vertices"] = m["vertices"] - np.array([2.0, 0.5])
+    assert abs(A(ms, "notch") - A(ms, "constant")).max() == 0
+    assert abs(A(dict(m, vertices=m["vertices"] - 0.5), "notch") - C).max() > 0.1 * abs(C).max()
+    # equal labels: the valve is open in both directions
+    m1 = dict(m)
+    m1["elementLabels"] = np.ones_like(m["elementLabels"])
+    m1["vertexLabels"] = np.ones_like(m["vertexLabels"])
+    assert abs(A(m1, "labeledValve") - A(m1, "constant")).max() == 0
+    # Omega split into labels 1 and 2: closed from 1 towards 2
+    m2 = dict(m)
+    bx = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
+    m2["elementLabels"] = np.where(m["elementLabels"] > 0, np.where(bx < 0.5, 1, 2), -1)
+    assert abs(A(m2, "labeledValve") - A(m2, "constant")).max() > 0.1 * abs(C).max()
+
+
+def test_oracle_labeled_kernel_outside_its_cases_is_nan():
+    """Labels 2 and -1 give 10 * 2 - 1 = 19, a case the reference aborts on (model.cpp:86-88)."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1)
+    m["elementLabels"] = np.where(m["elementLabels"] > 0, 2, -1)
+    r = oracle.assemble(m, {"function": "labeled", "horizon": 0.1, "outputdim": 1}, conf2d())
+    assert np.isnan(r["A"].data).any()

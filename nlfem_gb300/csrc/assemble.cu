@@ -189,12 +189,24 @@ struct BfsArgs {
 
 // Interaction predicate of integrate(aT, bT) for the configured method: the return value of
 // integrate_retriangulate / integrate_baryCenter / integrate_fractional (integration.cpp:539,
-// 1017, 287), OR'ed with is_fullConnectedComponentSearch.
+// 1017, 287) and of the 2D rules retriangulate_unsymm (:703), subSetBall / averageBall (:1094),
+// baryCenterRT (:1247) and noTruncation (:342), OR'ed with is_fullConnectedComponentSearch.
 template <int DIM>
 __device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method, const double *xs,
-                                                int nPx, const double *Eb) {
+                                                int nPx, const double *Ea, const double *Eb) {
     if (P.full_search) return true;
-    if (method == MTH_FRACTIONAL) return true;
+    if (method == MTH_FRACTIONAL || method == MTH_NOTRUNC) return true;
+    if (DIM == 2 && (method == MTH_SUBSET || method == MTH_AVERAGE)) {   // a vertex strictly inside
+        for (int k = 0; k < nPx; k++)
+            for (int v = 0; v <= DIM; v++)
+                if (xsqdist2(&Eb[2 * v], &xs[2 * k]) < P.sqdelta) return true;
+        return false;
+    }
+    if (DIM == 2 && method == MTH_BARY_RT) {   // aT meets the ball around bT's barycenter
+        double bc[2], R[18];
+        xbary<2>(Eb, bc);
+        return xretriangulate(bc, Ea, P.sqdelta, P.caps, R) >= 3;
+    }
     if (method == MTH_BARYCENTER) {
         double b[DIM];
         xbary<DIM>(Eb, b);
@@ -283,11 +295,11 @@ __device__ __forceinline__ void queue_push(bool push, int val, int *queue, long 
 // integrate routines, integration.cpp:539,1017).
 template <int DIM, int PREC>
 __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, int method, const double *xs,
-                                         const float *xsf, int nPx, const float *ohi, const float *olo, int b,
-                                         unsigned &namb) {
+                                         const float *xsf, int nPx, const float *ohi, const float *olo,
+                                         const double *Ea, int b, unsigned &namb) {
     constexpr int dV = DIM + 1;
     const double *Eb = &a.EC[(long long)b * DIM * dV];
-    if (PREC == PREC_F64) return interacts_exact<DIM>(P, method, xs, nPx, Eb);
+    if (PREC == PREC_F64) return interacts_exact<DIM>(P, method, xs, nPx, Ea, Eb);
     float pb[DIM * dV];
 #pragma unroll
     for (int j = 0; j < DIM * dV; j++)
@@ -341,7 +353,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
         bool self_pair = false;
         if (lane == 0) {
             visited[aT - eoff] = stamp;
-            self_pair = interacts_exact<DIM>(P, P.singular ? P.close : P.remote, xs, rule.nPx, Ea);
+            self_pair = interacts_exact<DIM>(P, P.singular ? P.close : P.remote, xs, rule.nPx, Ea, Ea);
             queue[0] = (int)aT;
         }
         self_pair = __shfl_sync(FULL, self_pair, 0);
@@ -412,7 +424,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
                         __syncwarp();
                         if (nbuf >= 32) {
                             const int b = buf[lane];
-                            const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
+                            const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
                             cand_local++;
                             queue_push(pair, b, queue, a.qcap, qtail, overflow);
                             const int rest = nbuf - 32;
@@ -430,7 +442,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
                 const int b = lane < nbuf ? buf[lane] : -1;
                 bool pair = false;
                 if (b >= 0) {
-                    pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, b, namb);
+                    pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
                     cand_local++;
                 }
                 queue_push(pair, b, queue, a.qcap, qtail, overflow);

@@ -192,7 +192,11 @@ enum KernelId {
     KER_CONSTANT = 0, KER_PARABOLA = 1, KER_FRACTIONAL = 2, KER_CONSTANT3D = 3,
     KER_LABELED = 4, KER_NOTCH = 5, KER_LABELEDNOTCH = 6, KER_LABELEDVALVE = 7, KER_CONSTTRUNC = 8
 };
-enum MethodId { MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2 };
+// MTH_RETRI_UNSYMM .. MTH_NOTRUNC: 2D, FP64 passes only.
+enum MethodId {
+    MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2, MTH_RETRI_UNSYMM = 3, MTH_SUBSET = 4,
+    MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7
+};
 enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
 
 // Per-problem parameters (one entry per independent assembly).

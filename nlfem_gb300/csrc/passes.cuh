@@ -686,6 +686,12 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                         for (int i = 0; i < NS; i++) Dp[i] += Ls[i] * adetT;
 #pragma unroll
                         for (int i = 0; i < dV * dV; i++) Nd[i] *= adetT;
+                    } else if (DIM == 2 && PREC == PREC_F64 && P.remote != MTH_RETRIANGULATE) {
+                        double Ls[6] = {0, 0, 0, 0, 0, 0};
+                        rule_out_f64(P, P.remote, rule, ET64, Eb64, a.adet[bT], a.labT[T], a.labT[bT], Ls, Nd, nsub, a.err);
+                        const double sT = P.remote == MTH_BARY_RT ? 1.0 : adetT;   // baryCenterRT carries its factor
+                        for (int i = 0; i < 6; i++) Dp[i] += Ls[i] * sT;
+                        for (int i = 0; i < 9; i++) Nd[i] *= sT;
                     } else if (DIM == 2) {
                         if (PREC == PREC_F64) {
                             double Ls[6] = {0, 0, 0, 0, 0, 0};
@@ -730,7 +736,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
             __syncwarp();
         }
         // ---------------- in side: pairs (aT, T) (prime blocks; zero for the barycenter rule)
-        const bool prime = (DIM == 2) && (P.remote == MTH_RETRIANGULATE || frac_close);
+        const bool prime = (DIM == 2) && (P.remote == MTH_RETRIANGULATE || P.remote == MTH_NOTRUNC || frac_close);
         if (prime) {
             const long long ib = a.in_ptr[T], ie = a.in_ptr[T + 1];
             const F2 tlf[3] = {f2(tl[0], tl[1]), f2(tl[2], tl[3]), f2(tl[4], tl[5])};
@@ -767,6 +773,12 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                             }
                             done = true;
                         }
+                    }
+                    if (!done && PREC == PREC_F64 && P.remote == MTH_NOTRUNC) {
+                        double LP[6] = {0, 0, 0, 0, 0, 0};
+                        rule_notrunc_prime(P, rule, Ea64, ET64, adetT, a.labT[aT], a.labT[T], LP, NPd, a.err);
+                        for (int i = 0; i < 6; i++) Dp[i] += LP[i] * adetA;
+                        for (int i = 0; i < 9; i++) NPd[i] *= adetA;
                     }
                     if (!done && P.remote == MTH_RETRIANGULATE) {
                         if (PREC == PREC_F64) {

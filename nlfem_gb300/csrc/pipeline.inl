@@ -79,6 +79,11 @@ static int method_id(const char *s) {
     if (k == "retriangulate") return MTH_RETRIANGULATE;
     if (k == "baryCenter") return MTH_BARYCENTER;
     if (k == "fractional") return MTH_FRACTIONAL;
+    if (k == "retriangulate_unsymm") return MTH_RETRI_UNSYMM;
+    if (k == "subSetBall") return MTH_SUBSET;
+    if (k == "averageBall") return MTH_AVERAGE;
+    if (k == "baryCenterRT") return MTH_BARY_RT;
+    if (k == "noTruncation") return MTH_NOTRUNC;
     return -1;
 }
 static int load_id(const char *s) {
@@ -176,6 +181,9 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
         if (P.close == MTH_FRACTIONAL && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "fractional close pairs are 2D only");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
+        if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision == NLFEM_PREC_MIXED)
+            return fail(NLFEM_ERR_UNSUPPORTED, std::string("integration method ") +
+                        (P.remote >= MTH_RETRI_UNSYMM ? p.method_remote : p.method_close) + " runs on the fp64 path only (precision \"fp64\")");
         if (P.kernel >= KER_LABELED) {   // label- or position-dependent kernels of 2D meshes
             if (p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " is implemented for 2D meshes only");
             if (p.precision == NLFEM_PREC_MIXED)

@@ -196,6 +196,178 @@ __device__ int quad_barycenter_f64(const ProbParams &P, const Rule &rule, const 
     return interacts | P.full_search;
 }
 
+// ---------------------------------------------------------------- further FP64 rules (2D)
+// Out side of the pair (aT, bT) for the rules retriangulate_unsymm, subSetBall / averageBall,
+// baryCenterRT and noTruncation. L is the upper triangle of termLocal, N[a][b] termNonloc (a: aT's
+// vertex, b: bT's vertex). Except for baryCenterRT, the blocks leave out the factor |aT|, which
+// the caller applies. Returns doesInteract without is_fullConnectedComponentSearch.
+
+// integrate_retriangulate_unysmm (integration.cpp:542-704): the retriangulated inner domain, weight
+// 2; termNonloc takes k(y, x).
+__device__ int rule_retri_unsymm(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                                 int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
+    double R[18];
+    int hit = 0;
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2];
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        const int Rdx = xretriangulate(x, Eb, P.sqdelta, P.caps, R);
+        hit |= Rdx >= 3;
+        double iL = 0, iN[3] = {0, 0, 0};
+        for (int r = 0; r + 2 < Rdx; r++) {
+            nsub++;
+            const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
+            const double rTdet = xabsDet2(tri);
+            for (int i = 0; i < rule.nPy; i++) {
+                double y[2];
+                y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
+                y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
+                const double w = rule.dy[i] * rTdet;
+                iL += kernel_f64<2>(P, x, la, y, lb, err) * w;
+                double ref[2];
+                if (!xtoRef(Eb, y, ref)) atomicOr(&err[4], 1);
+                const double kp = kernel_f64<2>(P, y, lb, x, la, err) * w;
+                iN[0] += (1.0 - ref[0] - ref[1]) * kp;
+                iN[1] += ref[0] * kp;
+                iN[2] += ref[1] * kp;
+            }
+        }
+        for (int a = 0; a < 3; a++) {
+            const double pa = 2.0 * rule.psix[3 * k + a] * rule.dx[k];
+            for (int b = a; b < 3; b++) L[sym_idx<3>(a, b)] += pa * rule.psix[3 * k + b] * iL;
+            for (int b = 0; b < 3; b++) N[3 * a + b] += pa * iN[b];
+        }
+    }
+    return hit;
+}
+
+// integrate_subSuperSetBalls (integration.cpp:1021-1095) with method_subSuperSetBalls
+// (:1251-1260): the whole inner element, weighted by the number n of its vertices strictly inside
+// the ball (subSetBall: 1 for n = 3, else 0; averageBall: 1 for n = 3, else 0.5), weight 2.
+__device__ int rule_subset(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                           double adetb, int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
+    const double wpart = P.remote == MTH_AVERAGE ? 0.5 : 0.0;
+    int hit = 0;
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2];
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        int n = 0;
+        for (int v = 0; v < 3; v++) n += xsqdist2(&Eb[2 * v], x) < P.sqdelta;
+        if (n == 0) continue;   // the reference adds zeros
+        hit = 1;
+        nsub++;
+        const double w = n == 3 ? 1.0 : wpart;
+        double iL = 0, iN[3] = {0, 0, 0};
+        for (int i = 0; i < rule.nPy; i++) {
+            double y[2];
+            xtoPhys<2>(Eb, &rule.Py[2 * i], y);
+            iL += w * adetb * kernel_f64<2>(P, x, la, y, lb, err) * rule.dy[i];
+            const double kp = kernel_f64<2>(P, y, lb, x, la, err);
+            for (int b = 0; b < 3; b++) iN[b] += w * rule.psiy[3 * i + b] * kp * rule.dy[i] * adetb;
+        }
+        for (int a = 0; a < 3; a++) {
+            const double pa = 2.0 * rule.psix[3 * k + a] * rule.dx[k];
+            for (int b = a; b < 3; b++) L[sym_idx<3>(a, b)] += pa * rule.psix[3 * k + b] * iL;
+            for (int b = 0; b < 3; b++) N[3 * a + b] += pa * iN[b];
+        }
+    }
+    return hit;
+}
+
+// integrate_baryCenterRT (integration.cpp:1155-1249): the outer domain is the part of aT inside the
+// ball around bT's barycenter (retriangulated), the inner element is whole, weight 2; the blocks
+// carry their factor 2 |sub-triangle|. The reference reads innerNonloc[outdim (a % outdim) +
+// b % outdim], which is innerNonloc[0] (the first basis function) for every b at outdim 1.
+__device__ int rule_baryrt(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                           double adetb, int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
+    double bc[2];
+    xbary<2>(Eb, bc);
+    double R[18];
+    const int Rdx = xretriangulate(bc, Ea, P.sqdelta, P.caps, R);
+    for (int r = 0; r + 2 < Rdx; r++) {
+        nsub++;
+        const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
+        const double rTdet = xabsDet2(tri);
+        for (int k = 0; k < rule.nPx; k++) {
+            double xq[2];
+            xtoPhys<2>(tri, &rule.Px[2 * k], xq);
+            double iL = 0, iN0 = 0;
+            for (int i = 0; i < rule.nPy; i++) {
+                double y[2];
+                xtoPhys<2>(Eb, &rule.Py[2 * i], y);
+                iL += kernel_f64<2>(P, xq, la, y, lb, err) * rule.dy[i] * adetb;
+                iN0 += rule.psiy[3 * i] * kernel_f64<2>(P, y, lb, xq, la, err) * rule.dy[i] * adetb;
+            }
+            double ref[2];
+            if (!xtoRef(Ea, xq, ref)) atomicOr(&err[4], 1);
+            const double ps[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
+            for (int a = 0; a < 3; a++) {
+                const double pa = 2.0 * rTdet * ps[a];
+                for (int b = a; b < 3; b++) L[sym_idx<3>(a, b)] += pa * ps[b] * rule.dx[k] * iL;
+                for (int b = 0; b < 3; b++) N[3 * a + b] += pa * rule.dx[k] * iN0;
+            }
+        }
+    }
+    return Rdx >= 3;
+}
+
+// integrate_fullyContained (integration.cpp:290-343), "noTruncation": both elements whole, every
+// pair interacts. Out side of (aT, bT): termLocal with k(x, y), termNonloc with k(y, x).
+__device__ void rule_notrunc_out(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                                 double adetb, int la, int lb, double *L, double *N, int *err) {
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2];
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        for (int i = 0; i < rule.nPy; i++) {
+            double y[2];
+            xtoPhys<2>(Eb, &rule.Py[2 * i], y);
+            const double kv = kernel_f64<2>(P, x, la, y, lb, err);
+            const double kp = kernel_f64<2>(P, y, lb, x, la, err);
+            const double f = rule.dx[k] * rule.dy[i] * adetb;
+            for (int a = 0; a < 3; a++) {
+                const double fa = f * rule.psix[3 * k + a];
+                for (int b = a; b < 3; b++) L[sym_idx<3>(a, b)] += fa * rule.psix[3 * k + b] * kv;
+                for (int b = 0; b < 3; b++) N[3 * a + b] += fa * rule.psiy[3 * i + b] * kp;
+            }
+        }
+    }
+}
+// Prime side of (aT, bT): termLocalPrime (upper triangle, bT's vertices) with k(y, x) and
+// termNonlocPrime[a][b] (a: aT's vertex, b: bT's vertex) with k(x, y), without |aT|.
+__device__ __noinline__ void rule_notrunc_prime(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                                   double adetb, int la, int lb, double *LP, double *NP, int *err) {
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2];
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        for (int i = 0; i < rule.nPy; i++) {
+            double y[2];
+            xtoPhys<2>(Eb, &rule.Py[2 * i], y);
+            const double kv = kernel_f64<2>(P, x, la, y, lb, err);
+            const double kp = kernel_f64<2>(P, y, lb, x, la, err);
+            const double f = rule.dx[k] * rule.dy[i] * adetb;
+            for (int a = 0; a < 3; a++) {
+                const double fa = f * rule.psiy[3 * i + a];
+                for (int b = a; b < 3; b++) LP[sym_idx<3>(a, b)] += fa * rule.psiy[3 * i + b] * kp;
+                const double fx = f * rule.psix[3 * k + a];
+                for (int b = 0; b < 3; b++) NP[3 * a + b] += fx * rule.psiy[3 * i + b] * kv;
+            }
+        }
+    }
+}
+
+// Out of line: the rules are rare, and inlined they would take registers from the passes' common
+// paths.
+__device__ __noinline__ int rule_out_f64(const ProbParams &P, int method, const Rule &rule, const double *Ea, const double *Eb,
+                            double adetb, int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
+    switch (method) {
+    case MTH_RETRI_UNSYMM: return rule_retri_unsymm(P, rule, Ea, Eb, la, lb, L, N, nsub, err);
+    case MTH_SUBSET: case MTH_AVERAGE: return rule_subset(P, rule, Ea, Eb, adetb, la, lb, L, N, nsub, err);
+    case MTH_BARY_RT: return rule_baryrt(P, rule, Ea, Eb, adetb, la, lb, L, N, nsub, err);
+    case MTH_NOTRUNC: nsub += rule.nPx; rule_notrunc_out(P, rule, Ea, Eb, adetb, la, lb, L, N, err); return 1;
+    }
+    return 0;
+}
+
 // One thread per (non-close) pair: FP64 quadrature and scatter.
 template <int DIM>
 __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
@@ -221,9 +393,26 @@ __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
             int interacts = 0;
             if (method == MTH_BARYCENTER) {
                 interacts = quad_barycenter_f64<DIM>(P, rule, Ea, Eb, a.labT[aT], a.labT[bT], a.adet[aT], a.adet[bT], L, N, a.err, nsub);
-            } else if (DIM == 2) {
+            } else if (DIM == 2 && method == MTH_RETRIANGULATE) {
                 interacts = quad_retriangulate_f64(P, rule, Ea, Eb, a.labT[aT], a.labT[bT], a.adet[aT], L, N, LP, NP, a.err, nsub);
                 prime = true;
+            } else if (DIM == 2) {
+                double Ls[6] = {0, 0, 0, 0, 0, 0}, LPs[6] = {0, 0, 0, 0, 0, 0};
+                unsigned ns = 0;
+                interacts = rule_out_f64(P, method, rule, Ea, Eb, a.adet[bT], a.labT[aT], a.labT[bT], Ls, N, ns, a.err) | P.full_search;
+                if (method == MTH_NOTRUNC) {
+                    rule_notrunc_prime(P, rule, Ea, Eb, a.adet[bT], a.labT[aT], a.labT[bT], LPs, NP, a.err);
+                    prime = true;
+                }
+                const double sa = method == MTH_BARY_RT ? 1.0 : a.adet[aT];
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) {
+                        const int sij = i <= j ? sym_idx<3>(i, j) : sym_idx<3>(j, i);
+                        L[3 * i + j] = Ls[sij] * sa;
+                        LP[3 * i + j] = LPs[sij] * sa;
+                    }
+                for (int i = 0; i < 9; i++) { N[i] *= sa; NP[i] *= sa; }
+                nsub += (int)ns;
             }
             if (a.blocks_out) {
                 double *o = &a.blocks_out[p * 4 * dV * dV];

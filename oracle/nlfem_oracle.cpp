@@ -40,7 +40,8 @@ const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
 enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_LABELED = 4, K_NOTCH = 5,
                 K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_NONE = -1 };
 enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_NONE = -1 };
-enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_NONE = -1 };
+enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_RETRI_UNSYMM = 3, M_SUBSET = 4,
+                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_NONE = -1 };
 
 struct Mesh {
     int dim, dV, outdim, is_dg;
@@ -452,6 +453,144 @@ int integrate_baryCenter(const Elem &aT, const Elem &bT, const Quad &q, const Me
     return (doesInteract || m.full_search);
 }
 
+// integrate_retriangulate_unysmm (integration.cpp:542-704): the retriangulated inner domain with
+// weight 2; termNonloc takes k(y, x); no prime blocks.
+int integrate_retriangulate_unsymm(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                                   double *tL, double *tN) {
+    const int dV = 3;
+    double x[2], y[2], ref[2], psi[3];
+    double reTri[9 * 3 * 2];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[2 * k], 2, x);
+        const int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        doesInteract += Rdx;
+        double innerLocal = 0, innerNonloc[3] = {0, 0, 0};
+        for (int r = 0; r < Rdx; r++) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys3(&reTri[6 * r], &q.Py[2 * i], y);
+                const double rTdet = absDet2(&reTri[6 * r]);
+                double ker = kernel_value(m, x, aT.label, y, bT.label);
+                innerLocal += ker * q.dy[i] * rTdet;
+                toRef(bT.E, y, ref);
+                ker = kernel_value(m, y, bT.label, x, aT.label);
+                basis(ref, 2, psi);
+                for (int b = 0; b < dV; b++) innerNonloc[b] += psi[b] * ker * q.dy[i] * rTdet;
+            }
+        }
+        for (int a = 0; a < dV; a++)
+            for (int b = 0; b < dV; b++) {
+                tL[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.psix[dV * k + b] * q.dx[k] * innerLocal;
+                tN[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonloc[b];
+            }
+    }
+    return (doesInteract || m.full_search);
+}
+
+// method_subSuperSetBalls (integration.cpp:1251-1260): vertices of T strictly inside the ball.
+int method_subSuperSetBalls(const double *x, const Elem &T, const Mesh &m) {
+    int n = 0;
+    for (int i = 0; i < m.dV; i++) n += (vec_sqL2dist(x, &T.E[m.dim * i], m.dim) < m.sqdelta);
+    return n;
+}
+
+// integrate_subSuperSetBalls (integration.cpp:1021-1095): the whole inner element, weighted by
+// averageWeights[#vertices inside - 1] (subSetBall: (0, 0, 1); averageBall: (0.5, 0.5, 1)).
+int integrate_subSuperSetBalls(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m, int method,
+                               double *tL, double *tN) {
+    const int dim = m.dim, dV = m.dV;
+    double W[4] = {0, 0, 0, 0};
+    if (method == M_AVERAGE) for (int i = 0; i < dV; i++) W[i] = 0.5;
+    W[2] = 1.0;
+    double x[3], y[3];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[dim * k], dim, x);
+        double innerLocal = 0, innerNonloc[4] = {0, 0, 0, 0};
+        const int nContained = method_subSuperSetBalls(x, bT, m);
+        doesInteract += nContained;
+        if (nContained >= 1) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys(bT.E, &q.Py[dim * i], dim, y);
+                const double rTdet = absDetDim(bT.E, dim);
+                double ker = kernel_value(m, x, aT.label, y, bT.label);
+                innerLocal += W[nContained - 1] * rTdet * ker * q.dy[i];
+                ker = kernel_value(m, y, bT.label, x, aT.label);
+                for (int b = 0; b < dV; b++)
+                    innerNonloc[b] += W[nContained - 1] * q.psiy[dV * i + b] * ker * q.dy[i] * rTdet;
+            }
+        }
+        for (int a = 0; a < dV; a++)
+            for (int b = 0; b < dV; b++) {
+                tL[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.psix[dV * k + b] * q.dx[k] * innerLocal;
+                tN[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonloc[b];
+            }
+    }
+    return (doesInteract || m.full_search);
+}
+
+// integrate_baryCenterRT (integration.cpp:1155-1249): the outer domain is the part of aT inside the
+// ball around bT's barycenter (retriangulated), the inner element is whole, weight 2. The
+// reference reads innerNonloc[outdim * (a % outdim) + b % outdim], which is innerNonloc[0] for
+// every (a, b) at outdim 1; kept as is.
+int integrate_baryCenterRT(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                           double *tL, double *tN) {
+    const int dV = 3;
+    double bc[2], xq[2], y[2], ref[2], psix[3];
+    double reTri[9 * 3 * 2];
+    baryCenter(2, bT.E, bc);
+    const int Rdx = method_retriangulate(bc, aT.E, m.sqdelta, reTri, m.caps);
+    if (!Rdx) return m.full_search;
+    const double bTdet = absDet2(bT.E);
+    for (int r = 0; r < Rdx; r++) {
+        const double rTdet = absDet2(&reTri[6 * r]);
+        for (int k = 0; k < q.nPx; k++) {
+            toPhys(&reTri[6 * r], &q.Px[2 * k], 2, xq);
+            double innerLocal = 0, innerNonloc[3] = {0, 0, 0};
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys(bT.E, &q.Py[2 * i], 2, y);
+                double ker = kernel_value(m, xq, aT.label, y, bT.label);
+                innerLocal += ker * q.dy[i] * bTdet;
+                ker = kernel_value(m, y, bT.label, xq, aT.label);
+                for (int b = 0; b < dV; b++) innerNonloc[b] += q.psiy[dV * i + b] * ker * q.dy[i] * bTdet;
+            }
+            toRef(aT.E, xq, ref);
+            basis(ref, 2, psix);
+            for (int a = 0; a < dV; a++)
+                for (int b = 0; b < dV; b++) {
+                    tL[dV * a + b] += 2 * rTdet * psix[a] * psix[b] * q.dx[k] * innerLocal;
+                    tN[dV * a + b] += 2 * rTdet * psix[a] * q.dx[k] * innerNonloc[0];
+                }
+        }
+    }
+    return 1;
+}
+
+// integrate_fullyContained (integration.cpp:290-343), "noTruncation": both whole elements, all
+// four blocks; every pair interacts.
+int integrate_fullyContained(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                             double *tL, double *tN, double *tLP, double *tNP) {
+    const int dim = m.dim, dV = m.dV;
+    double x[3], y[3];
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[dim * k], dim, x);
+        for (int i = 0; i < q.nPy; i++) {
+            toPhys(bT.E, &q.Py[dim * i], dim, y);
+            const double ker = kernel_value(m, x, aT.label, y, bT.label);
+            const double kerP = kernel_value(m, y, bT.label, x, aT.label);
+            for (int a = 0; a < dV; a++)
+                for (int b = 0; b < dV; b++) {
+                    const double f = q.dx[k] * q.dy[i] * aT.absDet * bT.absDet;
+                    tL[dV * a + b] += f * q.psix[dV * k + a] * q.psix[dV * k + b] * ker;
+                    tLP[dV * a + b] += f * q.psiy[dV * i + a] * q.psiy[dV * i + b] * kerP;
+                    tN[dV * a + b] += f * q.psix[dV * k + a] * q.psiy[dV * i + b] * kerP;
+                    tNP[dV * a + b] += f * q.psix[dV * k + a] * q.psiy[dV * i + b] * ker;
+                }
+        }
+    }
+    return 1;
+}
+
 // join + setupElement: integration.cpp:1897-1958
 int join(const Elem &aT, const Elem &bT, const Mesh &m, Elem &aS, Elem &bS, int *argA, int *argB) {
     int nEqual = 0;
@@ -637,6 +776,10 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
     case M_RETRIANGULATE: return integrate_retriangulate(aT, bT, q, m, tL, tN, tLP, tNP);
     case M_BARYCENTER: return integrate_baryCenter(aT, bT, q, m, tL, tN);
     case M_FRACTIONAL: return integrate_fractional(aT, bT, q, m, tL, tN, tLP, tNP);
+    case M_RETRI_UNSYMM: return integrate_retriangulate_unsymm(aT, bT, q, m, tL, tN);
+    case M_SUBSET: case M_AVERAGE: return integrate_subSuperSetBalls(aT, bT, q, m, method, tL, tN);
+    case M_BARY_RT: return integrate_baryCenterRT(aT, bT, q, m, tL, tN);
+    case M_NOTRUNC: return integrate_fullyContained(aT, bT, q, m, tL, tN, tLP, tNP);
     }
     return -1;
 }
@@ -748,6 +891,11 @@ int method_id(const char *s) {
     if (k == "retriangulate") return M_RETRIANGULATE;
     if (k == "baryCenter") return M_BARYCENTER;
     if (k == "fractional") return M_FRACTIONAL;
+    if (k == "retriangulate_unsymm") return M_RETRI_UNSYMM;
+    if (k == "subSetBall") return M_SUBSET;
+    if (k == "averageBall") return M_AVERAGE;
+    if (k == "baryCenterRT") return M_BARY_RT;
+    if (k == "noTruncation") return M_NOTRUNC;
     return M_NONE;
 }
 

@@ -258,6 +258,50 @@ def test_tangent_sphere_polygons(nl, orc, prec):
     assert fro < tol and mx < tol, (fro, mx)
 
 
+FURTHER_RULES = ["retriangulate_unsymm", "subSetBall", "averageBall", "baryCenterRT", "noTruncation"]
+
+
+@pytest.mark.parametrize("method", FURTHER_RULES)
+def test_further_rules_fp64(nl, orc, method):
+    """retriangulate_unsymm, subSetBall, averageBall, baryCenterRT and noTruncation
+    (integration.cpp:290-343, 542-704, 1021-1095, 1155-1249) on the FP64 path: assembled
+    matrices, and the blocks and interaction flags of single pairs."""
+    n = 6 if method == "noTruncation" else 14   # noTruncation pairs every element with every other
+    m = square_mesh(n, 0.1, jitter=0.15, seed=12)
+    conf = conf2d(method=method)
+    for name in ("constant", "parabola"):
+        k = {"function": name, "horizon": 0.1, "outputdim": 1}
+        A = nl.stiffnessMatrix(m, k, conf)
+        r = orc.assemble(m, k, conf, want_pairs=True)
+        B = r["A"]
+        assert same_pattern(A, B)
+        fro, mx = rel_errors(A, B)
+        assert fro < FP64_TOL and mx < FP64_TOL, (name, fro, mx)
+    rng = np.random.Generator(np.random.PCG64(5))
+    sel = r["pairs"][rng.choice(len(r["pairs"]), min(400, len(r["pairs"])), replace=False)]
+    g, gr = nl.pair_blocks(m, k, conf, sel)
+    o, orr = orc.pair_blocks(m, k, conf, sel)
+    np.testing.assert_array_equal(gr != 0, orr != 0)
+    np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
+
+
+def test_further_rules_with_label_kernel(nl, orc):
+    m = _labeled_mesh(12, 7)
+    k = {"function": "labeledValve", "horizon": 0.1, "outputdim": 1}
+    for method in ("retriangulate_unsymm", "averageBall", "baryCenterRT"):
+        A = nl.stiffnessMatrix(m, k, conf2d(method=method))
+        B = orc.assemble(m, k, conf2d(method=method))["A"]
+        assert same_pattern(A, B)
+        fro, mx = rel_errors(A, B)
+        assert fro < FP64_TOL and mx < FP64_TOL, (method, fro, mx)
+
+
+def test_further_rules_mixed_precision_refused(nl):
+    from nlfem_gb300._lib import NlfemError
+    with pytest.raises(NlfemError, match="fp64 path only"):
+        nl.stiffnessMatrix(square_mesh(6, 0.1), KC, conf2d(method="subSetBall", precision="mixed"))
+
+
 def test_load_vector(nl, orc):
     m = square_mesh(24, 0.1, jitter=0.2, seed=8)
     f = nl.loadVector(m, {"function": "linear"}, conf2d())

@@ -193,3 +193,46 @@ def test_oracle_labeled_kernel_outside_its_cases_is_nan():
     m["elementLabels"] = np.where(m["elementLabels"] > 0, 2, -1)
     r = oracle.assemble(m, {"function": "labeled", "horizon": 0.1, "outputdim": 1}, conf2d())
     assert np.isnan(r["A"].data).any()
+
+
+def test_oracle_notruncation_closed_form():
+    """noTruncation (integrate_fullyContained, integration.cpp:290-343) with the constant kernel c
+    integrates every element pair in full: A = 2 c (|D| M - m m^T) on the kept rows, M the P1 mass
+    matrix, m the integrals of the basis functions and |D| the area of the mesh."""
+    from oracle import oracle
+    m = square_mesh(4, 0.1, jitter=0.1, seed=3)
+    conf = conf2d(method="noTruncation")
+    ker = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    r = oracle.assemble(m, ker, conf, want_pairs=True)
+    nE = m["elements"].shape[0]
+    assert r["n_pairs"] == nE * nE
+    A = r["A"].toarray()
+    V, T = m["vertices"], m["elements"]
+    nV = V.shape[0]
+    M = np.zeros((nV, nV)); mv = np.zeros(nV); area = 0.0
+    for t in T:
+        e1, e2 = V[t[1]] - V[t[0]], V[t[2]] - V[t[0]]
+        at = 0.5 * abs(e1[0] * e2[1] - e1[1] * e2[0])
+        area += at
+        M[np.ix_(t, t)] += at / 12 * (np.ones((3, 3)) + np.eye(3))
+        mv[t] += at / 3
+    c = 4 / (np.pi * 0.1 ** 4)
+    B = 2 * c * (area * M - np.outer(mv, mv))
+    B[m["vertexLabels"] <= 0] = 0
+    assert np.abs(A - B).max() <= 1e-12 * np.abs(B).max()
+
+
+@pytest.mark.parametrize("method", ["retriangulate_unsymm", "subSetBall", "averageBall", "baryCenterRT"])
+def test_oracle_one_sided_rules_annihilate_constants(method):
+    """The weight-2 rules with two blocks (integration.cpp:542-704, 1021-1095, 1155-1249): with the
+    constant kernel every kept row sums to zero."""
+    from oracle import oracle
+    m = square_mesh(10, 0.1, jitter=0.15, seed=4)
+    ker = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    r = oracle.assemble(m, ker, conf2d(method=method))
+    assert r["n_errors"] == 0 and r["n_pairs"] > 0
+    A = r["A"]
+    keep = m["vertexLabels"] > 0
+    assert np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()
+    R = oracle.assemble(m, ker, conf2d())["A"]
+    assert abs(A - R).max() > 1e-3 * abs(R).max()   # not the retriangulate matrix

@@ -54,6 +54,7 @@ extern "C" int nlfem_par_assemble(
     for (long k = 0; k < nE; k++) chk += ptrLabelTriangles[k] > 0;
     if (comp == "system" && chk != nE_Omega) return NLFEM_ERR_INVALID;
     if (!is_DiscontinuousGalerkin && (long)outdim * nV != K) return NLFEM_ERR_INVALID;
+    if (is_DiscontinuousGalerkin && (long)outdim * (dim + 1) * nE != K) return NLFEM_ERR_INVALID;
     nlfem_problem p;
     memset(&p, 0, sizeof(p));
     p.dim = dim; p.outdim = outdim; p.is_dg = is_DiscontinuousGalerkin;

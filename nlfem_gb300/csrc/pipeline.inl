@@ -158,7 +158,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     memset(&P, 0, sizeof(P));
     if (p.dim != 2 && p.dim != 3) return fail(NLFEM_ERR_INVALID, "Dimension is not equal to 2 or 3.");
     if (p.outdim != 1) return fail(NLFEM_ERR_UNSUPPORTED, "only outdim = 1 is implemented");
-    if (p.is_dg) return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz is not implemented");
+    if (p.is_dg && (long long)(p.dim + 1) * p.nE >= (1LL << 31)) return fail(NLFEM_ERR_UNSUPPORTED, "mesh too large for DG");
     if (p.nE <= 0 || p.nV <= 0 || !p.elements || !p.elementLabels || !p.vertices || !p.vertexLabels)
         return fail(NLFEM_ERR_INVALID, "empty or missing mesh arrays");
     if (p.nE >= (1LL << 31) || p.nV >= (1LL << 31)) return fail(NLFEM_ERR_UNSUPPORTED, "mesh too large");
@@ -181,6 +181,10 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
         if (P.close == MTH_FRACTIONAL && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "fractional close pairs are 2D only");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
+        if (p.is_dg && P.singular)   // the close-pair rule needs vertex sharing across element DOFs
+            return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with singular kernels (close-pair rule) is not implemented");
+        if (p.is_dg && p.precision == NLFEM_PREC_MIXED)
+            return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz runs on the fp64 path only (precision \"fp64\")");
         if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision == NLFEM_PREC_MIXED)
             return fail(NLFEM_ERR_UNSUPPORTED, std::string("integration method ") +
                         (P.remote >= MTH_RETRI_UNSYMM ? p.method_remote : p.method_close) + " runs on the fp64 path only (precision \"fp64\")");
@@ -325,6 +329,14 @@ struct Session {
     DevBuf sv_vec, sv_part;                 // CG solve: f, g, b, x, r, p, Ap; dot partials
     DevBuf zptr, zidx;                      // domain-decomposition indicator (element -> subdomains)
     DevBuf kclist;                          // elements grouped by kernel class (pass launches)
+    // Discontinuous Galerkin: after the pair search, dg_swap_in swaps the row space to the element
+    // DOFs dV e + a (the identity table, every row kept, K = dV nE rows). T32, labV, vprob, vptr,
+    // vel, nV, maxNV and voff then describe DOF rows for the pattern, the passes, the finish and
+    // the download; the next run_prep swaps the mesh's vertices back (dg_restore).
+    bool dg = false, dg_rows = false;
+    long long dg_saved_nV = 0;
+    int dg_saved_maxNV = 0, dg_saved_pnV = 0;
+    DevBuf dgT32, dglabV, dgvprob, dgvptr, dgvel;
     long long kc_off[4] = {-1, 0, 0, 0};    // class offsets into kclist (-1: list not built)
     long long pat_cap = 0;
     // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
@@ -348,7 +360,8 @@ struct Session {
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                 &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
-                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx};
+                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx,
+                &dgT32, &dglabV, &dgvprob, &dgvptr, &dgvel};
     }
     ~Session() {
         for (DevBuf *b : buffers()) b->release();
@@ -442,6 +455,11 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     }
     S.nE = S.eoff[n];
     S.nV = S.voff[n];
+    S.dg = probs[0].is_dg != 0;
+    S.dg_rows = false;
+    for (int i = 1; i < n; i++)
+        if ((probs[i].is_dg != 0) != S.dg) return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the ansatz");
+    if (S.dg && n > 1) return fail(NLFEM_ERR_UNSUPPORTED, "DG problems assemble one at a time (no batches)");
     S.prec = probs[0].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64;
     for (int i = 1; i < n; i++)
         if ((probs[i].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64) != S.prec)
@@ -553,8 +571,54 @@ static int session_upload(Session &S, const nlfem_problem *probs) {
     return NLFEM_OK;
 }
 
+__global__ void k_dg_rows(long long K, int dV, int *__restrict__ T32, int *__restrict__ labV, int *__restrict__ vprob,
+                          long long *__restrict__ vptr, int *__restrict__ vel) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > K) return;
+    vptr[i] = i;
+    if (i == K) return;
+    T32[i] = (int)i;   // element e, local vertex a -> DOF dV e + a
+    labV[i] = 1;       // every DG row is kept (Cassemble.cpp:735, 751)
+    vprob[i] = 0;
+    vel[i] = (int)(i / dV);
+}
+
+// Row space of a DG assembly (one problem): the element DOFs.
+static int dg_swap_in(Session &S) {
+    const long long K = (long long)S.dV * S.nE;
+    ENS(S.dgT32, sizeof(int) * (K + 1));
+    ENS(S.dglabV, sizeof(int) * (K + 1));
+    ENS(S.dgvprob, sizeof(int) * (K + 1));
+    ENS(S.dgvptr, sizeof(long long) * (K + 1));
+    ENS(S.dgvel, sizeof(int) * (K + 1));
+    k_dg_rows<<<grid_for(K + 1, 256), 256, 0, S.st>>>(K, S.dV, S.dgT32.get<int>(), S.dglabV.get<int>(), S.dgvprob.get<int>(),
+                                                      S.dgvptr.get<long long>(), S.dgvel.get<int>()); ++S.nlaunch;
+    CK(cudaGetLastError());
+    std::swap(S.T32, S.dgT32); std::swap(S.labV, S.dglabV); std::swap(S.vprob, S.dgvprob);
+    std::swap(S.vptr, S.dgvptr); std::swap(S.vel, S.dgvel);
+    S.dg_saved_nV = S.nV; S.dg_saved_maxNV = S.maxNV; S.dg_saved_pnV = S.hprm[0].nV;
+    S.nV = K; S.maxNV = (int)K; S.voff[1] = (int)K; S.hprm[0].nV = (int)K;
+    CK(cudaMemcpyAsync(S.prm.p, S.hprm.data(), sizeof(ProbParams), cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(S.voffd.p, S.voff.data(), sizeof(int) * 2, cudaMemcpyHostToDevice, S.st));
+    S.dg_rows = true;
+    return NLFEM_OK;
+}
+
+static int dg_restore(Session &S) {
+    if (!S.dg_rows) return NLFEM_OK;
+    std::swap(S.T32, S.dgT32); std::swap(S.labV, S.dglabV); std::swap(S.vprob, S.dgvprob);
+    std::swap(S.vptr, S.dgvptr); std::swap(S.vel, S.dgvel);
+    S.nV = S.dg_saved_nV; S.maxNV = S.dg_saved_maxNV; S.voff[1] = (int)S.dg_saved_nV; S.hprm[0].nV = S.dg_saved_pnV;
+    CK(cudaMemcpyAsync(S.prm.p, S.hprm.data(), sizeof(ProbParams), cudaMemcpyHostToDevice, S.st));
+    CK(cudaMemcpyAsync(S.voffd.p, S.voff.data(), sizeof(int) * 2, cudaMemcpyHostToDevice, S.st));
+    S.dg_rows = false;
+    return NLFEM_OK;
+}
+
 template <int DIM>
 static int run_prep(Session &S) {
+    int rr = dg_restore(S);
+    if (rr) return rr;
     const long long nE = S.nE, nV = S.nV;
     constexpr int dV = DIM + 1;
     ENS(S.T32, sizeof(int) * nE * dV);
@@ -1340,6 +1404,7 @@ static int run_system_body(Session &S) {
     if ((r = run_bfs<DIM>(S))) return r;
     if ((r = run_pairs<DIM>(S))) return r;
     if (S.pmode == PM_COLORED && (r = run_color(S))) return r;   // the one-sided passes need no colors
+    if (S.dg && (r = dg_swap_in(S))) return r;   // rows: element DOFs; the search used the vertices
     CK(phase_event(S, 1));
     if ((r = run_pattern<DIM>(S))) return r;
     CK(phase_event(S, 2));
@@ -1434,6 +1499,7 @@ template <int DIM>
 static int run_forcing_t(Session &S) {
     int r;
     if ((r = run_prep<DIM>(S))) return r;
+    if (S.dg && (r = dg_swap_in(S))) return r;
     const long long nV = S.nV;
     ENS(S.facc, sizeof(unsigned long long) * 2 * (nV + 1));
     ENS(S.ftiny, sizeof(unsigned) * (nV + 1));
@@ -1846,6 +1912,7 @@ int nlfem_session_solve(nlfem_session *s, int i, const double *f, const double *
                         double *u, int *iterations) {
     if (!s || !f || !g || !u || i < 0 || i >= s->S.nProb || !(rtol > 0.0) || maxit < 0)
         return fail(NLFEM_ERR_INVALID, "bad session solve");
+    if (s->S.dg) return fail(NLFEM_ERR_UNSUPPORTED, "the solve splits rows by vertex labels: CG sessions only");
     return session_solve(s->S, i, f, g, rtol, maxit, u, iterations);
 }
 

@@ -276,7 +276,8 @@ def loadVector(mesh, load, configuration):
     """Load vector (nlfem.pyx:276-389), on the GPU."""
     lib = _lib.load()
     p = _Problem(mesh, None, configuration, system=False, load=load)
-    fd = np.zeros(int(p.c.nV) * int(p.c.outdim), dtype=np.float64)
+    K = (int(p.c.dim) + 1) * int(p.c.nE) if p.c.is_dg else int(p.c.nV)   # DG: element DOFs
+    fd = np.zeros(K * int(p.c.outdim), dtype=np.float64)
     _lib.check(lib.nlfem_load_vector(ctypes.byref(p.c), fd.ctypes.data_as(_dp)))
     path = configuration.get("savePath")
     if path:

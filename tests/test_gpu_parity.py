@@ -302,6 +302,78 @@ def test_further_rules_mixed_precision_refused(nl):
         nl.stiffnessMatrix(square_mesh(6, 0.1), KC, conf2d(method="subSetBall", precision="mixed"))
 
 
+def _conf_dg(method="retriangulate", precision="fp64"):
+    c = conf2d(method=method, precision=precision)
+    c["ansatz"] = "DG"
+    return c
+
+
+@pytest.mark.parametrize("kname,method", [("constant", "retriangulate"), ("parabola", "retriangulate"),
+                                          ("constant", "baryCenter"), ("labeledValve", "retriangulate"),
+                                          ("constant", "averageBall")])
+def test_dg_matches_oracle(nl, orc, kname, method):
+    """The DG ansatz (element DOFs dV e + a, every row kept; Cassemble.cpp:580-585, 637-642) on
+    the FP64 path, and its sum over vertex copies against the CG assembly."""
+    m = _labeled_mesh(10, 14) if kname.startswith("labeled") else square_mesh(10, 0.1, jitter=0.15, seed=14)
+    k = {"function": kname, "horizon": 0.1, "outputdim": 1}
+    A = nl.stiffnessMatrix(dict(m), k, _conf_dg(method))
+    B = orc.assemble(m, k, _conf_dg(method))["A"]
+    nE, nV = m["elements"].shape[0], m["vertices"].shape[0]
+    assert A.shape == (3 * nE, 3 * nE)
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)
+    C = nl.stiffnessMatrix(dict(m), k, conf2d(method=method))
+    P = sp.csr_matrix((np.ones(3 * nE), (np.arange(3 * nE), m["elements"].ravel())), shape=(3 * nE, nV))
+    S = (P.T @ A @ P).toarray()
+    S[m["vertexLabels"] <= 0] = 0
+    assert np.abs(S - C.toarray()).max() <= 1e-12 * abs(C).max()
+
+
+def test_dg_load_vector(nl, orc):
+    m = square_mesh(12, 0.1, jitter=0.2, seed=15)
+    f = nl.loadVector(dict(m), {"function": "linear"}, _conf_dg())
+    g = orc.assemble(m, None, _conf_dg(), compute="forcing", load={"function": "linear"})["f"]
+    assert f.shape == (3 * m["elements"].shape[0],)
+    np.testing.assert_allclose(f, g, rtol=1e-13, atol=1e-15 * np.abs(g).max())
+
+
+def test_dg_session_reassembly_and_cache(nl, orc):
+    """A DG session assembles again on its mesh (the row space goes back to the vertices for the
+    pair search), and a CG call after a DG call on the same sizes is unchanged."""
+    m = square_mesh(10, 0.1, jitter=0.1, seed=16)
+    C0 = nl.stiffnessMatrix(dict(m), KC, conf2d())
+    s = nl.Session([(dict(m), KC, _conf_dg())])
+    s.assemble()
+    A1 = s.download(0)
+    s.assemble()
+    A2 = s.download(0)
+    assert same_pattern(A1, A2) and np.array_equal(A1.data, A2.data)
+    B = orc.assemble(m, KC, _conf_dg())["A"]
+    fro, mx = rel_errors(A1, B)
+    assert fro < FP64_TOL and mx < FP64_TOL
+    nl.stiffnessMatrix(dict(m), KC, _conf_dg())
+    C1 = nl.stiffnessMatrix(dict(m), KC, conf2d())
+    assert same_pattern(C0, C1) and np.array_equal(C0.data, C1.data)
+    with pytest.raises(Exception, match="CG sessions only"):
+        s.solve(0, np.zeros(m["vertices"].shape[0]), np.zeros(m["vertices"].shape[0]))
+
+
+def test_dg_refusals(nl):
+    from nlfem_gb300._lib import NlfemError
+    m = square_mesh(6, 0.1)
+    with pytest.raises(NlfemError, match="fp64 path only"):
+        nl.stiffnessMatrix(dict(m), KC, _conf_dg(precision="mixed"))
+    kf = {"function": "fractional", "horizon": 0.1, "outputdim": 1, "fractional_s": 0.4}
+    cf = _conf_dg()
+    cf["closeElements"] = "fractional"
+    cf["quadrature"]["tensorGaussDegree"] = 3
+    with pytest.raises(NlfemError, match="singular kernels"):
+        nl.stiffnessMatrix(dict(m), kf, cf)
+    with pytest.raises(NlfemError, match="one at a time"):
+        nl.stiffnessMatrix_batch([(dict(m), KC, _conf_dg()), (dict(m), KC, _conf_dg())])
+
+
 def test_load_vector(nl, orc):
     m = square_mesh(24, 0.1, jitter=0.2, seed=8)
     f = nl.loadVector(m, {"function": "linear"}, conf2d())

@@ -236,3 +236,27 @@ def test_oracle_one_sided_rules_annihilate_constants(method):
     assert np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()
     R = oracle.assemble(m, ker, conf2d())["A"]
     assert abs(A - R).max() > 1e-3 * abs(R).max()   # not the retriangulate matrix
+
+
+def test_oracle_dg_sums_to_cg():
+    """DG scatters the same element blocks to element DOFs dV e + a (Cassemble.cpp:580-585,
+    637-642) and keeps every row: summed over the vertex copies, its rows and columns give the CG
+    matrix and load vector on the kept rows."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=6)
+    ker = {"function": "parabola", "horizon": 0.1, "outputdim": 1}
+    cdg = conf2d(); cdg["ansatz"] = "DG"
+    D = oracle.assemble(m, ker, cdg)["A"]
+    C = oracle.assemble(m, ker, conf2d())["A"]
+    T = m["elements"]; nE, nV = T.shape[0], m["vertices"].shape[0]
+    assert D.shape == (3 * nE, 3 * nE)
+    P = sp.csr_matrix((np.ones(3 * nE), (np.arange(3 * nE), T.ravel())), shape=(3 * nE, nV))
+    S = (P.T @ D @ P).toarray()
+    keep = m["vertexLabels"] > 0
+    S[~keep] = 0
+    assert np.abs(S - C.toarray()).max() <= 1e-12 * abs(C).max()
+    fd = oracle.assemble(m, None, cdg, compute="forcing", load={"function": "linear"})["f"]
+    fc = oracle.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
+    assert fd.shape == (3 * nE,)
+    g = P.T @ fd
+    assert np.abs(g[keep] - fc[keep]).max() <= 1e-13 * np.abs(fc).max()

@@ -195,7 +195,7 @@ template <int DIM>
 __device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method, const double *xs,
                                                 int nPx, const double *Ea, const double *Eb) {
     if (P.full_search) return true;
-    if (method == MTH_FRACTIONAL || method == MTH_NOTRUNC) return true;
+    if (method == MTH_FRACTIONAL || method == MTH_WEAKSING || method == MTH_NOTRUNC) return true;
     if (DIM == 2 && (method == MTH_SUBSET || method == MTH_AVERAGE)) {   // a vertex strictly inside
         for (int k = 0; k < nPx; k++)
             for (int v = 0; v <= DIM; v++)
@@ -229,7 +229,7 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
                                                    const float *xsf, int nPx, const double *Eb,
                                                    const float *pb, unsigned &namb) {
     if (P.full_search) return true;
-    if (method == MTH_FRACTIONAL) return true;
+    if (method == MTH_FRACTIONAL) return true;   // the mixed path takes no weakSingular rule
     const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
     if (method == MTH_BARYCENTER) {
         float bf[DIM];

@@ -195,7 +195,7 @@ enum KernelId {
 // MTH_RETRI_UNSYMM .. MTH_NOTRUNC: 2D, FP64 passes only.
 enum MethodId {
     MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2, MTH_RETRI_UNSYMM = 3, MTH_SUBSET = 4,
-    MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7
+    MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7, MTH_WEAKSING = 8
 };
 enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
 
@@ -216,6 +216,11 @@ struct ProbParams {
     int fx_ue;        // scale_exp + guard bits - 62
     double el;        // mean element measure (bounding box / nE), for capacity estimates
 };
+
+// Close pairs of a singular kernel take a Duffy rule: fractional or weakSingular.
+__host__ __device__ __forceinline__ bool duffy_close(const ProbParams &P) {
+    return P.singular && (P.close == MTH_FRACTIONAL || P.close == MTH_WEAKSING);
+}
 
 // FP64 kernel value k(x, lx, y, ly), lx and ly the labels of the elements of x and y
 // (model.cpp:25-28, 36-42, 52-60, 62-65, 67-114, 126-138). Where the reference aborts (labeled:

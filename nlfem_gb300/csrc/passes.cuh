@@ -90,7 +90,7 @@ __global__ void k_close_pairs(const long long *__restrict__ xadj, const int *__r
     if (a >= nE) return;
     const long long base = xadj[a] + a;
     const ProbParams &P = probs[eprob[a]];
-    const bool use = labT[a] != 0 && P.singular && P.close == MTH_FRACTIONAL;
+    const bool use = labT[a] != 0 && duffy_close(P);
     cA[base] = use ? (int)a : -1;
     cB[base] = (int)a;
     for (long long j = xadj[a]; j < xadj[a + 1]; j++) {
@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
         double D[NS];   // diagonal block A[T, T] (upper triangle): termLocal + termLocalPrime
 #pragma unroll
         for (int i = 0; i < NS; i++) D[i] = 0.0;
-        const bool frac_close = P.singular && P.close == MTH_FRACTIONAL;
+        const bool frac_close = duffy_close(P);   // fractional or weakSingular close blocks
         // ---------------- out side: pairs (T, bT)
         const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
         for (long long p0 = ob; p0 < oe; p0 += 32) {

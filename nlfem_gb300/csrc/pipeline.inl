@@ -66,6 +66,7 @@ static int kernel_id(const char *s) {
     if (k == "constant") return KER_CONSTANT;
     if (k == "parabola") return KER_PARABOLA;
     if (k == "fractional") return KER_FRACTIONAL;
+    if (k == "linearPrototypeMicroelastic") return KER_FRACTIONAL;   // c |z|^-1: exponent 1, see make_params
     if (k == "constant3D") return KER_CONSTANT3D;
     if (k == "labeled") return KER_LABELED;
     if (k == "notch") return KER_NOTCH;
@@ -79,6 +80,7 @@ static int method_id(const char *s) {
     if (k == "retriangulate") return MTH_RETRIANGULATE;
     if (k == "baryCenter") return MTH_BARYCENTER;
     if (k == "fractional") return MTH_FRACTIONAL;
+    if (k == "weakSingular") return MTH_WEAKSING;
     if (k == "retriangulate_unsymm") return MTH_RETRI_UNSYMM;
     if (k == "subSetBall") return MTH_SUBSET;
     if (k == "averageBall") return MTH_AVERAGE;
@@ -173,13 +175,18 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         if (P.remote < 0 || P.close < 0) return fail(NLFEM_ERR_UNSUPPORTED, "unknown integration method");
         if (p.dim == 3 && P.remote != MTH_BARYCENTER)
             return fail(NLFEM_ERR_INVALID, "Only Bary-Center is currently implemented as integration method for 3D and 1D.");
-        if (P.remote == MTH_FRACTIONAL)
+        if (P.remote == MTH_FRACTIONAL || P.remote == MTH_WEAKSING)
             return fail(NLFEM_ERR_INVALID, "The fractional and fractional_weakSingular integration routines are meant for close elements only.");
         std::string kn(p.kernel);
-        P.singular = (kn == "fractional");
-        if (P.singular && P.close == MTH_FRACTIONAL && (p.tensorGaussDegree <= 0 || !p.Pg || !p.dg))
+        const bool proto = kn == "linearPrototypeMicroelastic";
+        P.singular = (kn == "fractional") || proto;   // Cassemble.cpp:89-94
+        if (proto && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "kernel linearPrototypeMicroelastic is implemented for 2D meshes only");
+        if (duffy_close(P) && (p.tensorGaussDegree <= 0 || !p.Pg || !p.dg))
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
-        if (P.close == MTH_FRACTIONAL && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "fractional close pairs are 2D only");
+        if ((P.close == MTH_FRACTIONAL || P.close == MTH_WEAKSING) && p.dim != 2)
+            return fail(NLFEM_ERR_UNSUPPORTED, "fractional and weakSingular close pairs are 2D only");
+        if (P.singular && P.close == MTH_WEAKSING && p.precision == NLFEM_PREC_MIXED)
+            return fail(NLFEM_ERR_UNSUPPORTED, "the weakSingular close rule runs on the fp64 path only (precision \"fp64\")");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
         if (p.is_dg && P.singular)   // the close-pair rule needs vertex sharing across element DOFs
             return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with singular kernels (close-pair rule) is not implemented");
@@ -199,9 +206,14 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         switch (P.kernel) {
         case KER_CONSTANT: P.kc = 4 / (M_PI * (p.sqdelta * p.sqdelta)); break;             // model.cpp:25-28
         case KER_PARABOLA: P.kc = 12. / (M_PI * pow(p.sqdelta, 3)); break;                 // model.cpp:52-60
-        case KER_FRACTIONAL:                                                               // model.cpp:126-138
-            P.expo = p.dim + 2. * s;
-            P.kc = (2. - 2. * s) / (M_PI * pow(P.delta, 2. - 2. * s));
+        case KER_FRACTIONAL:
+            if (proto) {   // model.cpp:116-124: 3 / (pi delta^3) / |z|; the Duffy tables keep s
+                P.expo = 1.0;
+                P.kc = 3.0 / (M_PI * pow(P.delta, 3));
+            } else {       // model.cpp:126-138
+                P.expo = p.dim + 2. * s;
+                P.kc = (2. - 2. * s) / (M_PI * pow(P.delta, 2. - 2. * s));
+            }
             break;
         case KER_CONSTANT3D: P.kc = 15 / (M_PI * 4 * pow(P.delta, 5)); break;              // model.cpp:62-65
         case KER_LABELED:                                                                  // model.cpp:67-89
@@ -502,13 +514,13 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     if (system) {
         int first = -1;
         for (int i = 0; i < n; i++)
-            if (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL && first < 0) first = i;
+            if (duffy_close(S.hprm[i]) && first < 0) first = i;
         if (first >= 0) {
             const nlfem_problem &p = probs[first];
             const int deg = p.tensorGaussDegree;
             const int nPg = deg * deg * deg * deg;
             for (int i = first + 1; i < n; i++)
-                if (S.hprm[i].singular && S.hprm[i].close == MTH_FRACTIONAL &&
+                if (duffy_close(S.hprm[i]) &&
                     (probs[i].tensorGaussDegree != deg || probs[i].fractional_s != p.fractional_s))
                     return fail(NLFEM_ERR_UNSUPPORTED, "batched singular problems must share degree and s");
             S.duffy_nPg = nPg;
@@ -516,20 +528,30 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
             std::vector<double> h;
             for (int c = 0; c < 3; c++) {
                 std::vector<double> al((size_t)nTr[c] * nPg * 4), td((size_t)nTr[c] * nPg);
+                std::vector<double> au((size_t)nTr[c] * nPg * 4), tw((size_t)nTr[c] * nPg);
                 for (int t = 0; t < nTr[c]; t++)
                     for (int k = 0; k < nPg; k++) {
-                        double *a = &al[((size_t)t * nPg + k) * 4];
+                        double *a = &al[((size_t)t * nPg + k) * 4], *u = &au[((size_t)t * nPg + k) * 4];
                         for (int j = 0; j < 4; j++) a[j] = p.Pg[4 * k + j] * 0.5 + 0.5;
+                        for (int j = 0; j < 4; j++) u[j] = a[j];
                         double tdf = pow(a[0], 3 - 2 * p.fractional_s);
+                        double tdw = pow(a[0], 3 - 2 - 2 * p.fractional_s);   // weakSingular
                         a[0] = 1.0;
+                        duffy_traffo(c, t, u);
                         double det = duffy_traffo(c, t, a);
                         tdf *= det * 0.0625;
+                        tdw *= det * 0.0625;
                         a[0] = a[0] - a[1];
                         a[2] = a[2] - a[3];
+                        u[0] = u[0] - u[1];
+                        u[2] = u[2] - u[3];
                         td[(size_t)t * nPg + k] = tdf;
+                        tw[(size_t)t * nPg + k] = tdw;
                     }
                 h.insert(h.end(), al.begin(), al.end());
                 h.insert(h.end(), td.begin(), td.end());
+                h.insert(h.end(), au.begin(), au.end());
+                h.insert(h.end(), tw.begin(), tw.end());
             }
             h.insert(h.end(), p.dg, p.dg + nPg);
             ENS(S.duffy, sizeof(double) * h.size());
@@ -662,7 +684,7 @@ static int run_dual(Session &S) {
     // The search walks the vertex incidence lists. The element dual graph is needed only by the
     // element coloring of the colored passes and by the close-pair slots of singular kernels.
     bool need_adj = S.pmode == PM_COLORED;
-    for (const ProbParams &q : S.hprm) need_adj = need_adj || (q.singular && q.close == MTH_FRACTIONAL);
+    for (const ProbParams &q : S.hprm) need_adj = need_adj || duffy_close(q);
     if (!need_adj) {
         S.nadj = 0;
         CK(cudaGetLastError());
@@ -1079,6 +1101,8 @@ static Duffy duffy_view(const Session &S) {
     for (int c = 0; c < 3; c++) {
         d.alpha[c] = h + o; o += (size_t)nTr[c] * nPg * 4;
         d.tdet[c] = h + o; o += (size_t)nTr[c] * nPg;
+        d.alphaU[c] = h + o; o += (size_t)nTr[c] * nPg * 4;
+        d.tdetW[c] = h + o; o += (size_t)nTr[c] * nPg;
     }
     d.dg = h + o;
     d.nPg = nPg;
@@ -1121,7 +1145,7 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
     a.blocks_out = S.vals.get<double>(); a.ret_out = S.keepcnt.get<int>(); a.force_close = close;
     const ProbParams &P0 = S.hprm[0];
     const int method = close ? P0.close : P0.remote;
-    if (method == MTH_FRACTIONAL) {
+    if (method == MTH_FRACTIONAL || method == MTH_WEAKSING) {
         if (DIM != 2 || S.duffy_nPg == 0) return fail(NLFEM_ERR_INVALID, "close rule needs a 2D mesh and a tensor Gauss rule");
         k_iota<<<grid_for(n, 256), 256, 0, S.st>>>(S.closelist.get<int>(), n); ++S.nlaunch;
         a.list = S.closelist.get<int>();
@@ -1215,7 +1239,7 @@ typedef void (*OneSidedKernel)(MixArgs, Rule, PassRule);
 // regular kernel, 2 singular kernel with Duffy close pairs.
 static int kernel_class(const ProbParams &q) {
     if (q.kernel == KER_CONSTANT || q.kernel == KER_CONSTANT3D) return 0;
-    return (q.singular && q.close == MTH_FRACTIONAL) ? 2 : 1;
+    return duffy_close(q) ? 2 : 1;
 }
 
 static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, const OneSidedKernel *kfn,

@@ -25,8 +25,10 @@ struct Rule {
 // Duffy tables of the singular close-pair rule (MeshTypes.cpp:252-327), device pointers.
 struct Duffy {
     int nPg;
-    const double *alpha[3];   // [case][(t * nPg + k) * 4 + j]
-    const double *tdet[3];    // [case][t * nPg + k]
+    const double *alpha[3];   // [case][(t * nPg + k) * 4 + j], xi factored out (canceled)
+    const double *tdet[3];    // [case][t * nPg + k], xi^(3 - 2s) (fractional rule)
+    const double *alphaU[3];  // the points with xi kept (weakSingular basis functions)
+    const double *tdetW[3];   // xi^(1 - 2s) (weakSingular)
     const double *dg;         // [k]
 };
 
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
         for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
         const bool close = a.blocks_out ? (a.force_close != 0) : (P.singular && share_vertex(aV, bV, dV));
         const int method = close ? P.close : P.remote;
-        if (method != MTH_FRACTIONAL) {   // fractional close pairs: k_quad_close
+        if (method != MTH_FRACTIONAL && method != MTH_WEAKSING) {   // Duffy close pairs: k_quad_close
             double Ea[DIM * dV], Eb[DIM * dV];
 #pragma unroll
             for (int i = 0; i < DIM * dV; i++) { Ea[i] = a.EC[(long long)aT * DIM * dV + i]; Eb[i] = a.EC[(long long)bT * DIM * dV + i]; }
@@ -437,7 +439,7 @@ __global__ void k_close_list(QuadArgs a, int *list, unsigned long long *count) {
     if (p >= a.P) return;
     const int aT = a.pA[p], bT = a.pB[p];
     const ProbParams &P = a.probs[a.eprob[aT]];
-    if (!P.singular || P.close != MTH_FRACTIONAL) return;
+    if (!duffy_close(P)) return;
     int aV[dV], bV[dV];
     for (int i = 0; i < dV; i++) { aV[i] = a.T32[(long long)aT * dV + i]; bV[i] = a.T32[(long long)bT * dV + i]; }
     if (!share_vertex(aV, bV, dV)) return;
@@ -537,6 +539,42 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
     }
 }
 
+// integrate_weakSingular (integration.cpp:82-185), the lanes taking the (map, Gauss point) items
+// in turn: the kernel at the canceled points (as in the fractional rule), the basis functions at
+// the points with xi kept, the weight xi^(1 - 2s). W holds termLocal and termLocalPrime (upper
+// triangles) and termNonloc (3 x 3), all in the order of the join's sorted vertices.
+__device__ __forceinline__ void weak_accumulate(const ProbParams &P, const Duffy &d, int c, int nT,
+                                                const double *EA, const double *EB, double dAB, double *W) {
+    const int lane = threadIdx.x & 31;
+    const int total = nT * d.nPg;
+    const double a0 = EA[2] - EA[0], a1 = EA[4] - EA[0], a2 = EA[3] - EA[1], a3 = EA[5] - EA[1];
+    const double b0 = EB[2] - EB[0], b1 = EB[4] - EB[0], b2 = EB[3] - EB[1], b3 = EB[5] - EB[1];
+    const double hexp = -0.5 * P.expo;
+    for (int idx = lane; idx < total; idx += 32) {
+        const int k = idx % d.nPg;
+        const double *ac = &d.alpha[c][(long long)idx * 4];
+        const double *au = &d.alphaU[c][(long long)idx * 4];
+        const double x0 = ac[0] * a0 + ac[1] * a1 + EA[0], x1 = ac[0] * a2 + ac[1] * a3 + EA[1];
+        const double y0 = ac[2] * b0 + ac[3] * b1 + EB[0], y1 = ac[2] * b2 + ac[3] * b3 + EB[1];
+        const double z0 = x0 - y0, z1 = x1 - y1;
+        const double ker = P.kc * exp2(hexp * log2(z0 * z0 + z1 * z1));
+        const double f = ker * d.tdetW[c][idx] * d.dg[k] * dAB;
+        const double px[3] = {1.0 - au[0] - au[1], au[0], au[1]};
+        const double py[3] = {1.0 - au[2] - au[3], au[2], au[3]};
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double fx = f * px[i], fy = f * py[i];
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                W[sym_idx<3>(i, j)] += fx * px[j];
+                W[6 + sym_idx<3>(i, j)] += fy * py[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 3; j++) W[12 + 3 * i + j] += fx * py[j];
+        }
+    }
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int lane = threadIdx.x & 31;
@@ -574,6 +612,26 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int c = nEqual - 1;
     if (c < 0) return;
     const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    double acc[36];
+    for (int i = 0; i < 36; i++) acc[i] = 0;
+    if (!FAST && P.close == MTH_WEAKSING) {
+        double W[21];
+#pragma unroll
+        for (int i = 0; i < 21; i++) W[i] = 0.0;
+        weak_accumulate(P, d, c, nT, EA, EB, dA * dB, W);
+#pragma unroll
+        for (int i = 0; i < 21; i++) W[i] = warp_sum(W[i]);
+        // termLocal[argA a][argA b], termLocalPrime[argB a][argB b], termNonloc and
+        // termNonlocPrime [argA a][argB b] (integration.cpp:167-178)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                const int sij = i <= j ? sym_idx<3>(i, j) : sym_idx<3>(j, i);
+                acc[0 * 9 + 3 * argA[i] + argA[j]] = W[sij];
+                acc[2 * 9 + 3 * argB[i] + argB[j]] = W[6 + sij];
+                acc[1 * 9 + 3 * argA[i] + argB[j]] = W[12 + 3 * i + j];
+                acc[3 * 9 + 3 * argA[i] + argB[j]] = W[12 + 3 * i + j];
+            }
+    } else {
     const int nLocal = 6 - nEqual, shift = 3 - nEqual;
     // target of (a, b) in the 4 x 9 block vector and its sign
     int tgt[36];
@@ -601,10 +659,9 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     else close_accumulate<3, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
 #pragma unroll
     for (int i = 0; i < 21; i++) M[i] = warp_sum(M[i]);
-    double acc[36];
-    for (int i = 0; i < 36; i++) acc[i] = 0;
     for (int aa = 0; aa < nLocal; aa++)
         for (int b = 0; b < nLocal; b++) acc[tgt[aa * 6 + b]] += sgn[aa * 6 + b] * M[aa <= b ? sym_idx<6>(aa, b) : sym_idx<6>(b, aa)];
+    }
 
     if (a.blocks_out) {
         if (lane == 0) {

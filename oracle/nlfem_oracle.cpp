@@ -38,10 +38,10 @@ const double EPSILON = 1e-15;        // mathhelpers.h:11
 const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
 
 enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_LABELED = 4, K_NOTCH = 5,
-                K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_NONE = -1 };
+                K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_LINPROTO = 9, K_NONE = -1 };
 enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_NONE = -1 };
 enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_RETRI_UNSYMM = 3, M_SUBSET = 4,
-                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_NONE = -1 };
+                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_NONE = -1 };
 
 struct Mesh {
     int dim, dV, outdim, is_dg;
@@ -66,6 +66,8 @@ struct Quad {
     const double *dg;
     // Duffy tables of the fractional close-pair rule, index [case][ (t*nPg + k)*4 + j ]
     std::vector<double> alphaC[3], tdetFrac[3];
+    // weakSingular: the points with xi kept (alpha) and the determinant with xi^(1 - 2s)
+    std::vector<double> alphaU[3], tdetWeak[3];
 };
 
 struct Elem {
@@ -200,6 +202,12 @@ double kernel_value(const Mesh &m, const double *x, long lx, const double *y, lo
         const bool xN = x[1] > 0, yN = y[1] > 0, xE = x[0] > 0, yE = y[0] > 0;
         const bool cross = (xN != yN) && xE && yE;
         return !cross * (4 / (M_PI * pow(m.sqdelta, 2)));
+    }
+    case K_LINPROTO: {    // model.cpp:116-124
+        double z[2] = {x[0] - y[0], x[1] - y[1]};
+        const double denominator = 1.0 / sqrt(vec_dot(z, z, 2));
+        const double c = 3.0 / (M_PI * pow(m.delta, 3));
+        return c * denominator;
     }
     case K_LABELEDNOTCH:  // model.cpp:104-108
         return !(lx + ly == 7) * (4 / (M_PI * pow(m.sqdelta, 2)));
@@ -669,6 +677,42 @@ int integrate_fractional(const Elem &aT, const Elem &bT, const Quad &q, const Me
     return 1;
 }
 
+// integrate_weakSingular (integration.cpp:82-185): the Duffy maps of integrate_fractional with
+// the kernel at the canceled points, the basis functions at the points with xi kept, and the
+// determinant with xi^(1 - 2s); termNonlocPrime equals termNonloc.
+int integrate_weakSingular(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                           double *tL, double *tN, double *tLP, double *tNP) {
+    Elem aS, bS;
+    int argA[3], argB[3];
+    const int nEqual = join(aT, bT, m, aS, bS, argA, argB);
+    if (nEqual < 1 || nEqual > 3) return -1;  // reference aborts
+    const int c = nEqual - 1;
+    const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    const int dV = 3;
+    double xc[2], yc[2], psix[3], psiy[3];
+    for (int t = 0; t < nT; t++) {
+        for (int k = 0; k < q.nPg; k++) {
+            const double tw = q.tdetWeak[c][t * q.nPg + k];
+            const double *ac = &q.alphaC[c][(t * q.nPg + k) * 4];
+            const double *au = &q.alphaU[c][(t * q.nPg + k) * 4];
+            toPhys(aS.E, &ac[0], 2, xc);
+            toPhys(bS.E, &ac[2], 2, yc);
+            const double ker = kernel_value(m, xc, aT.label, yc, bT.label);
+            basis(&au[0], 2, psix);
+            basis(&au[2], 2, psiy);
+            for (int a = 0; a < dV; a++)
+                for (int b = 0; b < dV; b++) {
+                    const double f = ker * tw * q.dg[k] * aS.absDet * bS.absDet;
+                    tL[dV * argA[a] + argA[b]] += f * psix[a] * psix[b];
+                    tLP[dV * argB[a] + argB[b]] += f * psiy[a] * psiy[b];
+                    tN[dV * argA[a] + argB[b]] += f * psix[a] * psiy[b];
+                    tNP[dV * argA[a] + argB[b]] += f * psix[a] * psiy[b];
+                }
+        }
+    }
+    return 1;
+}
+
 // Duffy tables: MeshTypes.cpp:32-209 (traffo*), :252-327 (initializeQuadrule), mathhelpers.cpp:88-97
 double traffo(int c, int t, double *al) {
     const double xi = al[0], e1 = al[1], e2 = al[2], e3 = al[3];
@@ -725,18 +769,28 @@ void initializeQuadrule(Quad &q, const Mesh &m, const double *Pg) {
     for (int c = 0; c < 3; c++) {
         q.alphaC[c].assign((size_t)nTr[c] * q.nPg * 4, 0.0);
         q.tdetFrac[c].assign((size_t)nTr[c] * q.nPg, 0.0);
+        q.alphaU[c].assign((size_t)nTr[c] * q.nPg * 4, 0.0);
+        q.tdetWeak[c].assign((size_t)nTr[c] * q.nPg, 0.0);
         for (int t = 0; t < nTr[c]; t++) {
             for (int k = 0; k < q.nPg; k++) {
                 double *al = &q.alphaC[c][((size_t)t * q.nPg + k) * 4];
                 for (int j = 0; j < 4; j++) al[j] = Pg[4 * k + j];
                 for (int j = 0; j < 4; j++) al[j] = al[j] * 0.5 + 0.5;        // scale()
+                double *au = &q.alphaU[c][((size_t)t * q.nPg + k) * 4];
+                for (int j = 0; j < 4; j++) au[j] = al[j];
+                double tdw = pow(al[0], 3 - 2 - 2 * m.frac_s);
                 double tdf = pow(al[0], 3 - 2 * m.frac_s);
                 al[0] = 1.0;
+                traffo(c, t, au);
                 double det = traffo(c, t, al);
+                tdw *= det * SCALEDET;
                 tdf *= det * SCALEDET;
                 al[0] = al[0] - al[1];                                         // mirror()
                 al[2] = al[2] - al[3];
+                au[0] = au[0] - au[1];
+                au[2] = au[2] - au[3];
                 q.tdetFrac[c][(size_t)t * q.nPg + k] = tdf;
+                q.tdetWeak[c][(size_t)t * q.nPg + k] = tdw;
             }
         }
     }
@@ -780,6 +834,7 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
     case M_SUBSET: case M_AVERAGE: return integrate_subSuperSetBalls(aT, bT, q, m, method, tL, tN);
     case M_BARY_RT: return integrate_baryCenterRT(aT, bT, q, m, tL, tN);
     case M_NOTRUNC: return integrate_fullyContained(aT, bT, q, m, tL, tN, tLP, tNP);
+    case M_WEAKSING: return integrate_weakSingular(aT, bT, q, m, tL, tN, tLP, tNP);
     }
     return -1;
 }
@@ -877,6 +932,7 @@ int kernel_id(const char *s) {
     if (k == "labeledNotch") return K_LABELEDNOTCH;
     if (k == "labeledValve") return K_LABELEDVALVE;
     if (k == "constantTruncated") return K_CONSTTRUNC;
+    if (k == "linearPrototypeMicroelastic") return K_LINPROTO;
     return K_NONE;
 }
 int load_id(const char *s) {
@@ -896,6 +952,7 @@ int method_id(const char *s) {
     if (k == "averageBall") return M_AVERAGE;
     if (k == "baryCenterRT") return M_BARY_RT;
     if (k == "noTruncation") return M_NOTRUNC;
+    if (k == "weakSingular") return M_WEAKSING;
     return M_NONE;
 }
 

@@ -374,6 +374,48 @@ def test_dg_refusals(nl):
         nl.stiffnessMatrix_batch([(dict(m), KC, _conf_dg()), (dict(m), KC, _conf_dg())])
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_linear_prototype_kernel(nl, orc, prec):
+    """linearPrototypeMicroelastic (model.cpp:116-124), singular (Cassemble.cpp:89-94), with the
+    fractional close-pair rule: the oracle's values, and bit for bit the fractional kernel at
+    s = -1/2, whose formula it is."""
+    m = square_mesh(10, 0.1, jitter=0.15, seed=9)
+    kp = {"function": "linearPrototypeMicroelastic", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    kf = {"function": "fractional", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    A = nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="fractional", deg=3, precision=prec))
+    B = orc.assemble(m, kp, conf2d(rule="16", close="fractional", deg=3))["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    tol = FP64_TOL if prec == "fp64" else MIX_TOL
+    assert fro < tol and mx < tol, (fro, mx)
+    F = nl.stiffnessMatrix(dict(m), kf, conf2d(rule="16", close="fractional", deg=3, precision=prec))
+    assert same_pattern(A, F) and np.array_equal(A.data, F.data)
+
+
+def test_weak_singular_close_rule(nl, orc):
+    """The weakSingular close rule (integration.cpp:82-185) with the weakly singular kernel
+    linearPrototypeMicroelastic: the oracle's matrix and close-pair blocks, and the matrix of the
+    fractional close rule, which for this kernel is the same sum."""
+    from nlfem_gb300._lib import NlfemError
+    m = square_mesh(10, 0.1, jitter=0.15, seed=9)
+    kp = {"function": "linearPrototypeMicroelastic", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    cw = conf2d(rule="16", close="weakSingular", deg=3)
+    A = nl.stiffnessMatrix(dict(m), kp, cw)
+    B = orc.assemble(m, kp, cw)["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)
+    F = nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="fractional", deg=3))
+    assert abs(A - F).max() <= 1e-12 * abs(F).max()
+    T = m["elements"]
+    pairs = [(e, f) for e in (3, 40, 77) for f in range(T.shape[0]) if set(T[e]) & set(T[f])]
+    g, _ = nl.pair_blocks(m, kp, cw, np.array(pairs), close=True)
+    o, _ = orc.pair_blocks(m, kp, cw, np.array(pairs), method="weakSingular")
+    np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
+    with pytest.raises(NlfemError, match="fp64 path only"):
+        nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="mixed"))
+
+
 def test_load_vector(nl, orc):
     m = square_mesh(24, 0.1, jitter=0.2, seed=8)
     f = nl.loadVector(m, {"function": "linear"}, conf2d())

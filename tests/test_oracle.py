@@ -260,3 +260,40 @@ def test_oracle_dg_sums_to_cg():
     assert fd.shape == (3 * nE,)
     g = P.T @ fd
     assert np.abs(g[keep] - fc[keep]).max() <= 1e-13 * np.abs(fc).max()
+
+
+def test_oracle_linear_prototype_is_fractional_at_s_minus_half():
+    """kernel_linearPrototypeMicroelastic (model.cpp:116-124), 3 / (pi delta^3) / |x - y|, is the
+    fractional kernel's formula at s = -1/2 (model.cpp:126-138): 2 - 2s = 3, d + 2s = 1 and
+    pow(r, 1) = r, so with the same Duffy tables the two assemblies agree bit for bit."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=9)
+    conf = conf2d(rule="16", close="fractional", deg=3)
+    kp = {"function": "linearPrototypeMicroelastic", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    kf = {"function": "fractional", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    a = oracle.assemble(m, kp, conf)
+    b = oracle.assemble(m, kf, conf)
+    assert a["n_close"] > 0 and a["n_close"] == b["n_close"]
+    A, B = a["A"], b["A"]
+    assert np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices)
+    assert np.array_equal(A.data, B.data)
+
+
+def test_oracle_weak_singular_rule_matches_fractional_rule():
+    """integrate_weakSingular (integration.cpp:82-185) integrates the four terms of the bilinear
+    form one by one, with xi^(1 - 2s); integrate_fractional integrates (psi(x) - psi(y)) products
+    with xi^(3 - 2s). For a weakly singular kernel (here |z|^-1, s = -1/2) the assembled matrices
+    are the same sums up to rounding; the blocks are not."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=9)
+    kp = {"function": "linearPrototypeMicroelastic", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5}
+    for deg in (2, 4):
+        W = oracle.assemble(m, kp, conf2d(rule="16", close="weakSingular", deg=deg))
+        F = oracle.assemble(m, kp, conf2d(rule="16", close="fractional", deg=deg))
+        assert W["n_close"] == F["n_close"] > 0
+        D = (W["A"] - F["A"]).tocsr()
+        assert abs(D).max() <= 1e-13 * abs(F["A"]).max()
+    pairs = np.array([[5, 5], [5, 6], [5, 4]])
+    bw, _ = oracle.pair_blocks(m, kp, conf2d(rule="16", deg=3), pairs, method="weakSingular")
+    bf, _ = oracle.pair_blocks(m, kp, conf2d(rule="16", deg=3), pairs, method="fractional")
+    assert np.abs(bw - bf).max() > 1e-6 * np.abs(bf).max()

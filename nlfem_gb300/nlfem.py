@@ -20,6 +20,7 @@ the reference's arithmetic) or ``"mixed"`` (FP32 quadrature with FP64 cut geomet
 accumulation).
 """
 import ctypes
+import os
 import datetime
 
 import numpy as np
@@ -32,6 +33,7 @@ from .quadrules import tensorgauss
 __all__ = ["stiffnessMatrix", "loadVector", "stiffnessMatrix_fromArray", "meshFromArrays",
            "get_vertexLabel", "get_diam", "setSolutionLabels", "tensorgauss", "read_arma_mat",
            "read_arma_spMat", "timestamp", "py_retriangulate", "py_toRef", "py_toPhys",
+           "assemble", "constructAdjaciencyGraph", "remove_arma_tmp",
            "py_solve2x2", "stiffnessMatrix_batch", "pair_list", "pair_blocks", "Session",
            "write_arma_spMat", "write_arma_mat"]
 
@@ -375,6 +377,70 @@ def stiffnessMatrix_fromArray(elements, elementLabels, vertices, kernel, configu
                           kernel["outputdim"])
     setSolutionLabels(mesh, configuration.get("ansatz", "CG"), kernel["outputdim"])
     return mesh, stiffnessMatrix(mesh, kernel, configuration)
+
+
+def remove_arma_tmp(path):
+    """Deletes a temporary arma file (nlfem.pyx:103-105)."""
+    os.remove(path)
+
+
+def assemble(mesh, Px, Py, dx, dy, delta, path_spAd=None, path_fd=None, compute="systemforcing",
+             model_kernel="constant", model_f="constant", integration_method="retriangulate",
+             is_PlacePointOnCap=1, tensorGaussDegree=0):
+    """The reference's deprecated interface (nlfem.pyx:483-636). mesh is an object with the
+    attributes elements, elementLabels, vertices, vertexLabels, nE, nV, dim, K_Omega and
+    is_DiscontinuousGalerkin (optional: outdim, is_fullConnectedComponentSearch); the quadrature
+    comes as separate arrays and the horizon as delta. The same integration method serves remote
+    and close pairs, and fractional_s is -1, as in the reference. Returns (A[:K_Omega],
+    f[:K_Omega]) with None for the part `compute` ("system", "forcing" or "systemforcing") leaves
+    out; path_spAd / path_fd keep the full arma files."""
+    print("This function is deprecated. Please use stiffnessMatrix()")
+    dim = int(mesh.dim)
+    outdim = int(getattr(mesh, "outdim", 1))
+    m = {"elements": np.asarray(mesh.elements, dtype=np.int64).reshape(int(mesh.nE), dim + 1),
+         "elementLabels": np.asarray(mesh.elementLabels, dtype=np.int64).ravel(),
+         "vertices": np.asarray(mesh.vertices, dtype=np.float64).reshape(int(mesh.nV), dim),
+         "vertexLabels": np.asarray(mesh.vertexLabels, dtype=np.int64).ravel(),
+         "outdim": outdim}
+    conf = {"ansatz": "DG" if getattr(mesh, "is_DiscontinuousGalerkin", 0) else "CG",
+            "approxBalls": {"method": integration_method, "is_PlacePointOnCap": int(is_PlacePointOnCap)},
+            "closeElements": integration_method,
+            "quadrature": {"outer": {"points": np.asarray(Px, dtype=np.float64).reshape(-1, dim),
+                                     "weights": np.asarray(dx, dtype=np.float64).ravel()},
+                           "inner": {"points": np.asarray(Py, dtype=np.float64).reshape(-1, dim),
+                                     "weights": np.asarray(dy, dtype=np.float64).ravel()},
+                           "tensorGaussDegree": int(tensorGaussDegree)},
+            "is_fullConnectedComponentSearch": int(getattr(mesh, "is_fullConnectedComponentSearch", 0))}
+    K_Omega = int(mesh.K_Omega)
+    A = f = None
+    if compute in ("system", "systemforcing"):
+        kernel = {"function": model_kernel, "horizon": float(delta), "outputdim": outdim, "fractional_s": -1.0}
+        A = stiffnessMatrix(m, kernel, dict(conf, savePath=path_spAd) if path_spAd else conf)[:K_Omega]
+    if compute in ("forcing", "systemforcing"):
+        f = loadVector(m, {"function": model_f}, dict(conf, savePath=path_fd) if path_fd else conf)[:K_Omega]
+    return A, f
+
+
+def constructAdjaciencyGraph(elements, ncommon=1):
+    """Deprecated in the reference (nlfem.pyx:678-710): (nE, nCols) neighbour table of the
+    elements sharing at least ncommon vertices (each element lists itself), padded with nE. The
+    assembly does not need it. Neighbours are listed in ascending order."""
+    print("Constructing adjaciency graph...")
+    print("This function is deprecated, and its use is not required anymore.")
+    el = np.asarray(elements, dtype=np.int64)
+    nE, dV = el.shape
+    nV = int(el.max()) + 1
+    G = sp.csr_matrix((np.ones(nE * dV, dtype=np.int64), (el.ravel(), np.repeat(np.arange(nE), dV))), shape=(nV, nE))
+    N = (G.T @ G).tocsr()
+    N.data = (N.data > ncommon - 1).astype(np.int64)
+    N.eliminate_zeros()
+    N.sort_indices()
+    counts = np.diff(N.indptr)
+    neigs = np.full((nE, int(counts.max())), nE, dtype=np.int64)
+    for e in range(nE):
+        cols = N.indices[N.indptr[e]:N.indptr[e + 1]]
+        neigs[e, :cols.size] = cols
+    return neigs
 
 
 def setSolutionLabels(mesh, ansatz="CG", outputdim=1):

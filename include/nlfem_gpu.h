@@ -34,7 +34,8 @@ extern "C" {
 #define NLFEM_ERR_CUDA 2        /* no device, launch or runtime failure */
 #define NLFEM_ERR_NOMEM 3       /* device or host allocation failed */
 #define NLFEM_ERR_UNSUPPORTED 4 /* option outside the implemented set */
-#define NLFEM_ERR_NUMERIC 5     /* degenerate element (solve2x2 would abort in the reference) */
+#define NLFEM_ERR_NUMERIC 5     /* where the reference aborts: a degenerate element (solve2x2), a
+                                   labeled kernel outside its cases */
 #define NLFEM_ERR_TIMEOUT 6     /* a bounded device wait ran out */
 
 /* arithmetic of the quadrature */
@@ -45,7 +46,8 @@ extern "C" {
 typedef struct nlfem_problem {
     int dim;                     /* 2 or 3 */
     int outdim;                  /* 1 (vector-valued kernels are not implemented) */
-    int is_dg;                   /* 0: continuous P1 (K = nV), 1: discontinuous (K = nE*(dim+1)) */
+    int is_dg;                   /* 0: continuous P1 (K = nV), 1: discontinuous (K = nE*(dim+1);
+                                    FP64, one problem per call, non-singular kernels) */
     long nE, nV;
     const long *elements;        /* (nE, dim+1) vertex indices */
     const long *elementLabels;   /* (nE,) >0 domain, <0 Dirichlet layer, 0 bridge only */
@@ -56,10 +58,14 @@ typedef struct nlfem_problem {
     const double *Pg; int tensorGaussDegree; const double *dg; /* [-1,1]^4 tensor rule (singular) */
     double sqdelta;              /* squared horizon */
     double fractional_s;         /* s of the fractional kernel, -1 if unused */
-    const char *kernel;          /* "constant", "parabola", "fractional", "constant3D" */
+    const char *kernel;          /* "constant", "parabola", "fractional", "linearPrototypeMicroelastic",
+                                    "constant3D"; FP64 only, 2D: "labeled", "notch", "labeledNotch",
+                                    "labeledValve", "constantTruncated" */
     const char *forcing;         /* "linear", "linear3D", "constant" */
-    const char *method_remote;   /* "retriangulate" or "baryCenter" */
-    const char *method_close;    /* "fractional" or NULL (= method_remote) */
+    const char *method_remote;   /* "retriangulate", "baryCenter"; FP64 only, 2D: "retriangulate_unsymm",
+                                    "subSetBall", "averageBall", "baryCenterRT", "noTruncation" */
+    const char *method_close;    /* singular kernels: "fractional", "weakSingular" (FP64 only), or
+                                    NULL (= method_remote) */
     int is_PlacePointOnCap;
     int is_fullConnectedComponentSearch;
     int precision;               /* NLFEM_PREC_FP64 or NLFEM_PREC_MIXED */

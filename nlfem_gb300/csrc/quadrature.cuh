@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(128) k_quad_fp64(QuadArgs a, Rule rule) {
     if ((threadIdx.x & 31) == 0 && tot && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)tot);
 }
 
-// Flags and lists the close pairs (singular kernel, shared vertex, fractional close rule).
+// Flags and lists the close pairs (singular kernel, shared vertex, Duffy close rule).
 template <int DIM>
 __global__ void k_close_list(QuadArgs a, int *list, unsigned long long *count) {
     constexpr int dV = DIM + 1;

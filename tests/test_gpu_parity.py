@@ -416,6 +416,34 @@ def test_weak_singular_close_rule(nl, orc):
         nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="mixed"))
 
 
+@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5"])
+def test_gpu_matches_committed_fixtures(nl, name):
+    """The FP64 path against the committed oracle fixtures (tests/golden/oracle_cases.npz, made by
+    tests/golden/make_oracle_golden.py): bit-exact pattern, values within rounding."""
+    import importlib.util
+    import os
+    gdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_oracle_golden", os.path.join(gdir, "make_oracle_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    fx = np.load(os.path.join(gdir, "oracle_cases.npz"))
+    _, kernel, conf, load = mg.cases()[name]
+    # the stored mesh: the fixture's own inputs, whatever numpy this host runs
+    mesh = {k: fx[f"{name}.{k}"] for k in ("elements", "elementLabels", "vertices", "vertexLabels")}
+    indptr = fx[f"{name}.indptr"]
+    K = indptr.size - 1
+    B = sp.csr_matrix((fx[f"{name}.data"], fx[f"{name}.indices"], indptr), shape=(K, K))
+    A = nl.stiffnessMatrix(dict(mesh), kernel, conf)
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    tol = 1e-11 if name == "frac12" else FP64_TOL
+    assert fro < tol and mx < tol, (fro, mx)
+    if name == "cube5":
+        f = nl.loadVector(dict(mesh), load, conf)
+        g = fx[f"{name}.f"]
+        np.testing.assert_allclose(f, g, rtol=1e-13, atol=1e-15 * np.abs(g).max())
+
+
 def test_load_vector(nl, orc):
     m = square_mesh(24, 0.1, jitter=0.2, seed=8)
     f = nl.loadVector(m, {"function": "linear"}, conf2d())

@@ -297,3 +297,33 @@ def test_oracle_weak_singular_rule_matches_fractional_rule():
     bw, _ = oracle.pair_blocks(m, kp, conf2d(rule="16", deg=3), pairs, method="weakSingular")
     bf, _ = oracle.pair_blocks(m, kp, conf2d(rule="16", deg=3), pairs, method="fractional")
     assert np.abs(bw - bf).max() > 1e-6 * np.abs(bf).max()
+
+
+def _golden_cases_module():
+    import importlib.util
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_oracle_golden.py")
+    spec = importlib.util.spec_from_file_location("make_oracle_golden", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5"])
+def test_oracle_matches_committed_fixtures(name):
+    """The oracle against tests/golden/oracle_cases.npz: the same inputs, the same pattern and
+    pair list bit for bit, values and load vectors to 1e-13 (libm differences across hosts)."""
+    mg = _golden_cases_module()
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_cases.npz"))
+    case = mg.cases()[name]
+    assert str(fx[f"{name}.input_sha"]) == mg.input_hash(*case[:3])
+    for k in ("elements", "elementLabels", "vertices", "vertexLabels"):
+        np.testing.assert_array_equal(case[0][k], fx[f"{name}.{k}"])
+    out = mg.compute(name, case)
+    np.testing.assert_array_equal(out[f"{name}.indptr"], fx[f"{name}.indptr"])
+    np.testing.assert_array_equal(out[f"{name}.indices"], fx[f"{name}.indices"])
+    assert str(out[f"{name}.pairs_sha"]) == str(fx[f"{name}.pairs_sha"])
+    d = fx[f"{name}.data"]
+    np.testing.assert_allclose(out[f"{name}.data"], d, rtol=1e-13, atol=1e-13 * np.abs(d).max())
+    if f"{name}.f" in fx:
+        f = fx[f"{name}.f"]
+        np.testing.assert_allclose(out[f"{name}.f"], f, rtol=1e-13, atol=1e-15 * np.abs(f).max())

@@ -38,8 +38,11 @@ const double EPSILON = 1e-15;        // mathhelpers.h:11
 const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
 
 enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_LABELED = 4, K_NOTCH = 5,
-                K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_LINPROTO = 9, K_NONE = -1 };
-enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_NONE = -1 };
+                K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_LINPROTO = 9,
+                K_FIELD_CONST = 10, K_FIELD_PROTO = 11, K_FIELD_PROTO3D = 12, K_NONE = -1 };
+enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_GAUSSIAN = 3, F_JUMP = 4, F_TENSORSIN = 5,
+              F_FIELD_LINEAR = 6, F_FIELD_LINEAR3D = 7, F_FIELD_RIGHT = 8, F_FIELD_DOWN = 9, F_FIELD_BOTH = 10,
+              F_NONE = -1 };
 enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_RETRI_UNSYMM = 3, M_SUBSET = 4,
                 M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_NONE = -1 };
 
@@ -246,8 +249,68 @@ double load_value(const Mesh &m, const double *x) {
     case F_LINEAR: return -2. * (x[1] + 1.);     // model.cpp:240-242
     case F_LINEAR3D: return -2. * (x[1] + 2.);   // model.cpp:259-261
     case F_CONSTANT: return 1.0;                 // model.cpp:201-203
+    case F_GAUSSIAN: {                           // model.cpp:243-246
+        const double sqx0 = pow(x[0], 2), sqx1 = pow(x[1], 2);
+        return -4. * (sqx0 + sqx1 - 1.) * exp(-sqx0 - sqx1);
+    }
+    case F_JUMP: {                               // model.cpp:247-252
+        const bool sign = (x[0] + x[1] - 0.5 > -EPSILON);
+        return sign ? -4. : 4.;
+    }
+    case F_TENSORSIN:                            // model.cpp:253-255
+        return 32. * pow(M_PI, 2) * sin(x[0] * M_PI * 4) * sin(x[1] * M_PI * 4);
     }
     return NAN;
+}
+
+// Forcing with outdim components (model.cpp:204-239): fo[0 .. outdim-1].
+void load_vec(const Mesh &m, const double *x, double *fo) {
+    const double c = M_PI / 2.0;
+    switch (m.load) {
+    case F_FIELD_LINEAR:                         // model.cpp:204-210
+        fo[0] = -c * (1.0 + 2 * x[0]);
+        fo[1] = -c * x[1];
+        return;
+    case F_FIELD_LINEAR3D:                       // model.cpp:211-218
+        fo[0] = -c * (1.0 + 2 * x[0]) * x[1] * x[1];
+        fo[1] = -c * x[1] * x[1];
+        fo[2] = -c * x[2] * x[1] * x[1];
+        return;
+    case F_FIELD_RIGHT: fo[0] = 1.0e-1; fo[1] = 0.0; return;           // model.cpp:219-222
+    case F_FIELD_DOWN: fo[0] = 0; fo[1] = -M_PI * 2; return;          // model.cpp:223-229
+    case F_FIELD_BOTH: fo[0] = -M_PI; fo[1] = -M_PI * 2; return;      // model.cpp:230-239
+    }
+    fo[0] = load_value(m, x);
+}
+
+// Kernel with outdim x outdim components, row-major (model.cpp:140-191); scalar kernels fill kv[0].
+void kernel_vec(const Mesh &m, const double *x, long lx, const double *y, long ly, double *kv) {
+    switch (m.kernel) {
+    case K_FIELD_CONST: {                        // model.cpp:180-191
+        const double c = 4. / (M_PI * pow(m.sqdelta, 2));
+        kv[0] = c; kv[1] = 0.0; kv[2] = c; kv[3] = 0.0;
+        return;
+    }
+    case K_FIELD_PROTO: {                        // model.cpp:140-153
+        double z[2] = {x[0] - y[0], x[1] - y[1]};
+        const double denominator = 1.0 / pow(sqrt(vec_dot(z, z, 2)), 3);
+        const double c = 3.0 / pow(m.delta, 3);
+        kv[0] = c * denominator * z[0] * z[0];
+        kv[1] = c * denominator * z[0] * z[1];
+        kv[2] = c * denominator * z[1] * z[0];
+        kv[3] = c * denominator * z[1] * z[1];
+        return;
+    }
+    case K_FIELD_PROTO3D: {                      // model.cpp:155-178
+        double z[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+        const double denominator = 1.0 / pow(sqrt(vec_dot(z, z, 3)), 3);
+        const double c = 3.0 / pow(m.delta, 3);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) kv[3 * i + j] = c * denominator * z[i] * z[j];
+        return;
+    }
+    }
+    kv[0] = kernel_value(m, x, lx, y, ly);
 }
 
 // ---------------------------------------------------------------- elements (MeshTypes.cpp:216-250)
@@ -823,9 +886,141 @@ void dual_graph(const Mesh &m, std::vector<long> &xadj, std::vector<long> &adj) 
     }
 }
 
+// ---------------------------------------------------------------- outdim > 1 (vector-valued kernels)
+// The routines above with the reference's general indexing: blocks are (dV outdim) x (dV outdim),
+// row index = vertex * outdim + component, kernel values row-major outdim x outdim. Only used
+// when outdim > 1; the scalar routines are their outdim = 1 case written out.
+int integrate_retriangulate_vec(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                                double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:345-540
+    const int dV = 3, od = m.outdim, o2 = od * od, nB = dV * od;
+    double x[2], y[2], ref[2], psi[3], kv[9], kvP[9];
+    double innerLocal[9], innerNonloc[27], innerNonlocPrime[27];
+    double reTri[9 * 3 * 2];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[2 * k], 2, x);
+        const int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        doesInteract += Rdx;
+        for (int o = 0; o < o2; o++) innerLocal[o] = 0;
+        for (int b = 0; b < dV * o2; b++) { innerNonloc[b] = 0; innerNonlocPrime[b] = 0; }
+        for (int r = 0; r < Rdx; r++) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys3(&reTri[6 * r], &q.Py[2 * i], y);
+                const double rTdet = absDet2(&reTri[6 * r]);
+                kernel_vec(m, x, aT.label, y, bT.label, kv);
+                for (int o = 0; o < o2; o++) innerLocal[o] += kv[o] * q.dy[i] * rTdet;
+                toRef(bT.E, y, ref);
+                kernel_vec(m, y, bT.label, x, aT.label, kvP);
+                basis(ref, 2, psi);
+                for (int b = 0; b < dV * o2; b++) {
+                    innerNonloc[b] += psi[b / o2] * kv[b % o2] * q.dy[i] * rTdet;
+                    innerNonlocPrime[b] += psi[b / o2] * kvP[b % o2] * q.dy[i] * rTdet;
+                }
+                for (int a = 0; a < dV; a++)
+                    for (int b = 0; b < dV; b++)
+                        for (int o = 0; o < o2; o++)
+                            tLP[a * o2 * dV + (o / od) * od * dV + b * od + o % od] +=
+                                psi[a] * psi[b] * kvP[o] * q.dy[i] * q.dx[k] * rTdet * aT.absDet;
+            }
+        }
+        for (int a = 0; a < nB; a++)
+            for (int b = 0; b < nB; b++) {
+                tL[nB * a + b] += aT.absDet * q.psix[dV * k + a / od] * q.psix[dV * k + b / od] * q.dx[k] *
+                                  innerLocal[od * (a % od) + (b % od)];
+                tN[nB * a + b] += aT.absDet * q.psix[dV * k + a / od] * q.dx[k] *
+                                  innerNonloc[(a % od) * od + o2 * (b / od) + (b % od)];
+                tNP[nB * a + b] += aT.absDet * q.psix[dV * k + a / od] * q.dx[k] *
+                                   innerNonlocPrime[(a % od) * od + o2 * (b / od) + (b % od)];
+            }
+    }
+    return (doesInteract || m.full_search);
+}
+
+int integrate_baryCenter_vec(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                             double *tL, double *tN) {                       // integration.cpp:910-1018
+    const int dim = m.dim, dV = m.dV, od = m.outdim, o2 = od * od, nB = dV * od;
+    double x[3], y[3], kv[9], innerLocal[9], innerNonloc[36];
+    int doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[dim * k], dim, x);
+        for (int o = 0; o < o2; o++) innerLocal[o] = 0;
+        for (int b = 0; b < dV * o2; b++) innerNonloc[b] = 0;
+        const int Rdx = method_baryCenter(x, bT, m);
+        doesInteract += Rdx;
+        if (Rdx) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys(bT.E, &q.Py[dim * i], dim, y);
+                const double rTdet = absDetDim(bT.E, dim);
+                kernel_vec(m, x, aT.label, y, bT.label, kv);
+                for (int o = 0; o < o2; o++) innerLocal[o] += rTdet * kv[o] * q.dy[i];
+                kernel_vec(m, y, bT.label, x, aT.label, kv);
+                for (int b = 0; b < dV * o2; b++) innerNonloc[b] += q.psiy[dV * i + b / o2] * kv[b % o2] * q.dy[i] * rTdet;
+            }
+        }
+        for (int a = 0; a < nB; a++)
+            for (int b = 0; b < nB; b++) {
+                tL[nB * a + b] += 2 * aT.absDet * q.psix[dV * k + a / od] * q.psix[dV * k + b / od] * q.dx[k] *
+                                  innerLocal[od * (a % od) + (b % od)];
+                tN[nB * a + b] += 2 * aT.absDet * q.psix[dV * k + a / od] * q.dx[k] *
+                                  innerNonloc[(a % od) * od + o2 * (b / od) + (b % od)];
+            }
+    }
+    return (doesInteract || m.full_search);
+}
+
+int integrate_fractional_vec(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                             double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:187-288
+    Elem aS, bS;
+    int argA[3], argB[3];
+    const int nEqual = join(aT, bT, m, aS, bS, argA, argB);
+    if (nEqual < 1 || nEqual > 3) return -1;  // reference aborts
+    const int c = nEqual - 1;
+    const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    const int dV = 3, od = m.outdim, nLocal = 2 * dV - nEqual, shift = dV - nEqual;
+    double x[2], y[2], psix[3], psiy[3], psixy[6], kv[9];
+    for (int t = 0; t < nT; t++) {
+        for (int k = 0; k < q.nPg; k++) {
+            const double tf = q.tdetFrac[c][t * q.nPg + k];
+            const double *al = &q.alphaC[c][(t * q.nPg + k) * 4];
+            toPhys(aS.E, &al[0], 2, x);
+            toPhys(bS.E, &al[2], 2, y);
+            kernel_vec(m, x, aT.label, y, bT.label, kv);
+            basis(&al[0], 2, psix);
+            basis(&al[2], 2, psiy);
+            for (int a = 0; a < nEqual; a++) psixy[a] = psix[a] - psiy[a];
+            for (int a = nEqual; a < dV; a++) {
+                psixy[a] = psix[a];
+                psixy[a + shift] = -psiy[a];
+            }
+            for (int a = 0; a < nLocal; a++)
+                for (int aOut = 0; aOut < od; aOut++)
+                    for (int b = 0; b < nLocal; b++)
+                        for (int bOut = 0; bOut < od; bOut++) {
+                            const double f = kv[od * aOut + bOut] * tf * psixy[a] * psixy[b] * q.dg[k] * aS.absDet * bS.absDet;
+                            if (a < dV) {
+                                if (b < dV) tL[od * dV * (argA[a] * od + aOut) + argA[b] * od + bOut] += f;
+                                else tN[od * dV * (argA[a] * od + aOut) + argB[b - shift] * od + bOut] -= f;
+                            } else {
+                                if (b < dV) tNP[od * dV * (argA[b] * od + aOut) + argB[a - shift] * od + bOut] -= f;
+                                else tLP[od * dV * (argB[a - shift] * od + aOut) + argB[b - shift] * od + bOut] += f;
+                            }
+                        }
+        }
+    }
+    return 1;
+}
+
 // ---------------------------------------------------------------- integrate dispatch (integration.cpp:67-79)
 int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
                      double *tL, double *tN, double *tLP, double *tNP) {
+    if (m.outdim > 1) {
+        switch (method) {
+        case M_RETRIANGULATE: return integrate_retriangulate_vec(aT, bT, q, m, tL, tN, tLP, tNP);
+        case M_BARYCENTER: return integrate_baryCenter_vec(aT, bT, q, m, tL, tN);
+        case M_FRACTIONAL: return integrate_fractional_vec(aT, bT, q, m, tL, tN, tLP, tNP);
+        }
+        return -1;
+    }
     switch (method) {
     case M_RETRIANGULATE: return integrate_retriangulate(aT, bT, q, m, tL, tN, tLP, tNP);
     case M_BARYCENTER: return integrate_baryCenter(aT, bT, q, m, tL, tN);
@@ -868,7 +1063,8 @@ void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<l
     long aDG[4], bDG[4];
     const long *aAdx, *bAdx;
     Elem aT, bT;
-    double tL[16], tN[16], tLP[16], tNP[16];
+    double tL[144], tN[144], tLP[144], tNP[144];   // (dV outdim)^2, outdim <= 3
+    const int od = m.outdim, nB = dV * od;
     if (m.is_dg) { for (int j = 0; j < dV; j++) aDG[j] = dV * aTdx + j; aAdx = aDG; }
     else aAdx = &m.T[dV * aTdx];
     initializeElement(aTdx, m, aT);
@@ -887,7 +1083,7 @@ void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<l
                     initializeElement(bTdx, m, bT);
                     if (m.is_dg) { for (int j = 0; j < dV; j++) bDG[j] = dV * bTdx + j; bAdx = bDG; }
                     else bAdx = &m.T[dV * bTdx];
-                    for (int i = 0; i < dV * dV; i++) { tL[i] = 0; tN[i] = 0; tLP[i] = 0; tNP[i] = 0; }
+                    for (int i = 0; i < nB * nB; i++) { tL[i] = 0; tN[i] = 0; tLP[i] = 0; tNP[i] = 0; }
                     cnt.n_cand++;
                     if (first) cnt.n_close++;
                     int does = integrate(aT, bT, q, m, first, tL, tN, tLP, tNP);
@@ -898,6 +1094,21 @@ void system_element(long aTdx, const Mesh &m, const Quad &q, const std::vector<l
                         if (pairs) { pairs->push_back(aTdx); pairs->push_back(bTdx); }
                         double weight = 1.;                               // :649-657
                         if (m.nZeta) weight = 1. / evaluateZeta(m.zeta_indices, m.zeta_indptr, m.nZeta, aTdx, bTdx);
+                        if (od > 1) {                                     // :721-770, general indices
+                            for (int a = 0; a < nB; a++)
+                                for (int b = 0; b < nB; b++) {
+                                    const unsigned long ra = (unsigned long)(od * aAdx[a / od] + a % od);
+                                    const unsigned long rb = (unsigned long)(od * bAdx[b / od] + b % od);
+                                    if (m.is_dg || m.labV[aAdx[a / od]] > 0) {
+                                        Ad[ra * K + od * aAdx[b / od] + b % od] += tL[nB * a + b] * weight;
+                                        Ad[ra * K + od * bAdx[b / od] + b % od] += -tN[nB * a + b] * weight;
+                                    }
+                                    if (m.is_dg || m.labV[bAdx[b / od]] > 0) {
+                                        Ad[rb * K + od * bAdx[a / od] + a % od] += tLP[nB * a + b] * weight;
+                                        Ad[rb * K + od * aAdx[a / od] + a % od] += -tNP[nB * a + b] * weight;
+                                    }
+                                }
+                        } else
                         for (int a = 0; a < dV; a++) {                    // :721-770
                             for (int b = 0; b < dV; b++) {
                                 if (m.is_dg || m.labV[aAdx[a]] > 0) {
@@ -933,6 +1144,9 @@ int kernel_id(const char *s) {
     if (k == "labeledValve") return K_LABELEDVALVE;
     if (k == "constantTruncated") return K_CONSTTRUNC;
     if (k == "linearPrototypeMicroelastic") return K_LINPROTO;
+    if (k == "constantField") return K_FIELD_CONST;
+    if (k == "linearPrototypeMicroelasticField") return K_FIELD_PROTO;
+    if (k == "linearPrototypeMicroelasticField3D") return K_FIELD_PROTO3D;
     return K_NONE;
 }
 int load_id(const char *s) {
@@ -940,6 +1154,14 @@ int load_id(const char *s) {
     if (k == "linear") return F_LINEAR;
     if (k == "linear3D") return F_LINEAR3D;
     if (k == "constant") return F_CONSTANT;
+    if (k == "gaussian") return F_GAUSSIAN;
+    if (k == "jump") return F_JUMP;
+    if (k == "tensorsin") return F_TENSORSIN;
+    if (k == "linearField") return F_FIELD_LINEAR;
+    if (k == "linearField3D") return F_FIELD_LINEAR3D;
+    if (k == "constantRightField") return F_FIELD_RIGHT;
+    if (k == "constantDownField") return F_FIELD_DOWN;
+    if (k == "constantBothField") return F_FIELD_BOTH;
     return F_NONE;
 }
 int method_id(const char *s) {
@@ -1018,7 +1240,12 @@ oracle_result *oracle_par_assemble(
     m.is_singular = (kn == "fractional" || kn == "linearPrototypeMicroelastic" ||
                      kn == "linearPrototypeMicroelasticField");               // Cassemble.cpp:89-94
     m.caps = is_PlacePointOnCap; m.full_search = is_fullConnectedComponentSearch;
-    if (outdim != 1) return nullptr;
+    // vector-valued kernels: retriangulate, baryCenter and the fractional close rule
+    if (outdim < 1 || outdim > dim) return nullptr;
+    if (outdim > 1 && std::string(compute ? compute : "") == "system") {
+        auto ok = [](int mth) { return mth == M_RETRIANGULATE || mth == M_BARYCENTER || mth == M_FRACTIONAL; };
+        if (!ok(m.remote) || !ok(m.close)) return nullptr;
+    }
 
     Quad q;
     q.Px = Px; q.dx = dx; q.Py = Py; q.dy = dy; q.nPx = nPx; q.nPy = nPy;
@@ -1048,8 +1275,22 @@ oracle_result *oracle_par_assemble(
                 const long *aAdx;
                 if (m.is_dg) { for (int j = 0; j < m.dV; j++) aDG[j] = m.dV * aTdx + j; aAdx = aDG; }
                 else aAdx = &m.T[m.dV * aTdx];
-                double termf[4] = {0, 0, 0, 0};
+                double termf[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
                 double x[3];
+                if (outdim > 1) {                                                  // compute_f, outdim > 1
+                    for (int a = 0; a < m.dV * outdim; a++)
+                        for (int i = 0; i < nPx; i++) {
+                            // a scalar forcing sets fo[0] only: the reference reads the rest
+                            // uninitialized, here they are NaN
+                            double fo[3] = {NAN, NAN, NAN};
+                            toPhys(aT.E, &Px[dim * i], dim, x);
+                            load_vec(m, x, fo);
+                            termf[a] += q.psix[m.dV * i + a / outdim] * fo[a % outdim] * aT.absDet * dx[i];
+                        }
+                    for (int a = 0; a < m.dV * outdim; a++)
+                        if (m.is_dg || m.labV[aAdx[a / outdim]] > 0) fd[outdim * aAdx[a / outdim] + a % outdim] += termf[a] * 1.;
+                    continue;
+                }
                 for (int a = 0; a < m.dV; a++) {
                     for (int i = 0; i < nPx; i++) {
                         toPhys(aT.E, &Px[dim * i], dim, x);

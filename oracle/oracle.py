@@ -103,7 +103,9 @@ def assemble(mesh, kernel, conf, compute="system", load=None, nthreads=1, subset
         Py, Pyp = _d(q["inner"]["points"]); dy, dyp = _d(q["inner"]["weights"])
     keep += [Px, dx, Py, dy]
     is_dg = conf.get("ansatz", "CG") == "DG"
-    K = nE * (dim + 1) if is_dg else nV
+    # outdim: the kernel's outputdim for the system, the mesh's for the forcing (nlfem.pyx:220-238)
+    outdim = int(kernel.get("outputdim", 1)) if (compute == "system" and kernel) else int(mesh.get("outdim", 1))
+    K = (nE * (dim + 1) if is_dg else nV) * outdim
     deg = int(q.get("tensorGaussDegree", 0)) if compute == "system" else 0
     Pgp, dgp = _null_d(), _null_d()
     if deg:
@@ -134,7 +136,7 @@ def assemble(mesh, kernel, conf, compute="system", load=None, nthreads=1, subset
     r = lib().oracle_par_assemble(
         compute.encode(), K, elp, elabp, vep, vlabp, nE, nV,
         Pxp, Px.shape[0], dxp, Pyp, Py.shape[0], dyp, sqdelta, int(is_dg),
-        kname.encode(), fname.encode(), remote.encode(), close.encode(), caps, dim, 1,
+        kname.encode(), fname.encode(), remote.encode(), close.encode(), caps, dim, outdim,
         Pgp, deg, dgp, float(s), full, int(nthreads), subp,
         0 if sub is None else len(sub), int(want_pairs))
     if not r:

@@ -327,3 +327,112 @@ def test_oracle_matches_committed_fixtures(name):
     if f"{name}.f" in fx:
         f = fx[f"{name}.f"]
         np.testing.assert_allclose(out[f"{name}.f"], f, rtol=1e-13, atol=1e-15 * np.abs(f).max())
+
+
+def test_oracle_constant_field_components():
+    """kernelField_constant (model.cpp:180-191) is K = c [[1, 0], [1, 0]]. The blocks of a pair
+    carry K (termLocal, termNonloc) and the prime blocks, scattered transposed
+    (Cassemble.cpp:755-766), carry K^T. With A_s = M + P the scalar constant-kernel matrix split
+    into those two parts, the outdim-2 matrix (rows 2v + i, columns 2w + j) has the components
+    (0, 0) = A_s, (1, 1) = 0, (1, 0) = M and (0, 1) = P: so (0, 1) + (1, 0) = A_s."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=3)
+    A = oracle.assemble(m, {"function": "constant", "horizon": 0.1, "outputdim": 1}, conf2d())["A"].toarray()
+    V = oracle.assemble(m, {"function": "constantField", "horizon": 0.1, "outputdim": 2}, conf2d())["A"].toarray()
+    assert V.shape == (2 * A.shape[0], 2 * A.shape[0])
+    tol = 1e-14 * np.abs(A).max()
+    assert np.abs(V[0::2, 0::2] - A).max() <= tol
+    assert np.abs(V[1::2, 1::2]).max() == 0
+    assert np.abs(V[0::2, 1::2] + V[1::2, 0::2] - A).max() <= tol
+    assert np.abs(V[0::2, 1::2]).max() > 0.1 * np.abs(A).max()   # both parts are present
+    assert np.abs(V[1::2, 0::2]).max() > 0.1 * np.abs(A).max()
+
+
+def _kept_rows(m, od):
+    return np.repeat(m["vertexLabels"] > 0, od)
+
+
+def test_oracle_microelastic_field_annihilates_rigid_motions():
+    """kernelField_linearPrototypeMicroelastic (model.cpp:140-153), c z z^T / |z|^3, singular with
+    the fractional close rule: translations and the rotation (-x1, x0) make the integrand
+    K(x - y)(u(x) - u(y)) vanish pointwise, so every kept row of A u is zero to rounding. A swap
+    of component indices anywhere in the blocks or the scatter breaks this."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=3)
+    k = {"function": "linearPrototypeMicroelasticField", "horizon": 0.1, "outputdim": 2, "fractional_s": -0.5}
+    r = oracle.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))
+    A = r["A"]
+    assert r["n_close"] > 0 and not np.isnan(A.data).any()
+    V = m["vertices"]
+    keep = _kept_rows(m, 2)
+    for u in (np.tile([1.0, 0.0], V.shape[0]), np.tile([0.0, 1.0], V.shape[0]),
+              np.stack([-V[:, 1], V[:, 0]], axis=1).ravel()):
+        assert np.abs(A @ u)[keep].max() <= 1e-12 * abs(A).max() * np.abs(u).max()
+    stretch = np.stack([V[:, 0], np.zeros(V.shape[0])], axis=1).ravel()   # not a rigid motion
+    assert np.abs(A @ stretch)[keep].max() > 1e-3 * abs(A).max() * 0.01
+
+
+def test_oracle_microelastic_field_3d_annihilates_rigid_motions():
+    """kernelField_linearPrototypeMicroelastic3D (model.cpp:155-178) with the barycenter rule in
+    3D: the three translations and three rotations are annihilated on the kept rows."""
+    from oracle import oracle
+    m = cube_mesh(3, 0.1, jitter=0.1, seed=4)
+    k = {"function": "linearPrototypeMicroelasticField3D", "horizon": 0.35, "outputdim": 3}
+    # the kernel is singular at x = y and has no close rule: with the same rule inside and out the
+    # self pairs meet x = y (NaN, in the reference too), so the inner rule is the 4-point one
+    pa, pb = 0.5854101966249685, 0.1381966011250105
+    conf = conf3d()
+    conf["quadrature"]["inner"] = {"points": np.array([[pb, pb, pb], [pa, pb, pb], [pb, pa, pb], [pb, pb, pa]]),
+                                   "weights": np.full(4, 1.0 / 24)}
+    A = oracle.assemble(m, k, conf)["A"]
+    assert not np.isnan(A.data).any()
+    V = m["vertices"]
+    n = V.shape[0]
+    keep = _kept_rows(m, 3)
+    motions = [np.tile(e, n) for e in np.eye(3)]
+    for w in np.eye(3):
+        motions.append(np.cross(w, V).ravel())
+    for u in motions:
+        assert np.abs(A @ u)[keep].max() <= 1e-12 * abs(A).max() * np.abs(u).max()
+
+
+def _forcing_numpy(m, conf, fun, od):
+    """compute_f (Cassemble.cpp:149-164) written in numpy: sum_k psi_a(P_k) f(x_k) |det| dx_k."""
+    q = conf["quadrature"]["outer"]
+    P, w = np.asarray(q["points"]), np.asarray(q["weights"])
+    psi = np.column_stack([1 - P.sum(axis=1), P])
+    V, T = m["vertices"], m["elements"]
+    f = np.zeros(V.shape[0] * od)
+    for e, t in enumerate(T):
+        if m["elementLabels"][e] <= 0:
+            continue
+        E = V[t]
+        det = abs(np.linalg.det(np.column_stack([E[1] - E[0], E[2] - E[0]])))
+        x = E[0] + P @ np.vstack([E[1] - E[0], E[2] - E[0]])
+        fx = np.atleast_2d(fun(x.T)).reshape(od, -1)
+        for a in range(3):
+            if m["vertexLabels"][t[a]] > 0:
+                for c in range(od):
+                    f[od * t[a] + c] += np.sum(psi[:, a] * fx[c] * w) * det
+    return f
+
+
+@pytest.mark.parametrize("name,od,fun", [
+    ("gaussian", 1, lambda x: -4. * (x[0] ** 2 + x[1] ** 2 - 1.) * np.exp(-x[0] ** 2 - x[1] ** 2)),
+    ("jump", 1, lambda x: np.where(x[0] + x[1] - 0.5 > -1e-15, -4., 4.)),
+    ("tensorsin", 1, lambda x: 32. * np.pi ** 2 * np.sin(x[0] * np.pi * 4) * np.sin(x[1] * np.pi * 4)),
+    ("linearField", 2, lambda x: np.array([-np.pi / 2 * (1.0 + 2 * x[0]), -np.pi / 2 * x[1]])),
+    ("constantRightField", 2, lambda x: np.array([np.full_like(x[0], 0.1), np.zeros_like(x[0])])),
+    ("constantDownField", 2, lambda x: np.array([np.zeros_like(x[0]), np.full_like(x[0], -2 * np.pi)])),
+    ("constantBothField", 2, lambda x: np.array([np.full_like(x[0], -np.pi), np.full_like(x[0], -2 * np.pi)])),
+])
+def test_oracle_forcings(name, od, fun):
+    """The forcing terms of model.cpp:201-255 in the oracle's par_forcing against compute_f in
+    numpy."""
+    from oracle import oracle
+    m = square_mesh(10, 0.1, jitter=0.2, seed=8)
+    m["outdim"] = od
+    f = oracle.assemble(m, None, conf2d(), compute="forcing", load={"function": name})["f"]
+    g = _forcing_numpy(m, conf2d(), fun, od)
+    assert f.shape == g.shape
+    np.testing.assert_allclose(f, g, rtol=1e-12, atol=1e-13 * np.abs(g).max())

@@ -44,7 +44,7 @@ enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_GAUSSIAN = 3, F_JU
               F_FIELD_LINEAR = 6, F_FIELD_LINEAR3D = 7, F_FIELD_RIGHT = 8, F_FIELD_DOWN = 9, F_FIELD_BOTH = 10,
               F_NONE = -1 };
 enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_RETRI_UNSYMM = 3, M_SUBSET = 4,
-                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_NONE = -1 };
+                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_EXACT = 9, M_NONE = -1 };
 
 struct Mesh {
     int dim, dV, outdim, is_dg;
@@ -441,6 +441,105 @@ int method_retriangulate(const double *xc, const double *TE, double sqdelta, dou
     return Rdx - 2;
 }
 
+// placePointCapCenter (integration.cpp:1300-1351): the circular segment of B_delta(x) cut off by
+// the chord y_pred - y_cur. Its centroid lies on the chord's outward normal at distance
+// 4 delta sin^3(alpha) / (3 (2 alpha - sin 2 alpha)) from x (alpha: half the opening angle); if
+// it lies in the triangle it is written to cap and the segment's area (delta^2 / 2)
+// (2 alpha - sin 2 alpha) is returned, else 0.
+double placePointCapCenter(const double *ypred, const double *ycur, const double *xc, double sqdelta,
+                           const double *TE, const double *na, const double *nb, const double *nc,
+                           double orientation, double *cap) {
+    double p1[2] = {xc[0] + ypred[0] * -1, xc[1] + ypred[1] * -1};
+    double p2[2] = {xc[0] + ycur[0] * -1, xc[1] + ycur[1] * -1};
+    const double alpha = 0.5 * acos(vec_dot(p1, p2, 2) / sqdelta);
+    double s[2];
+    rightNormal(ycur, ypred, orientation, s);
+    const double scalingFactor = (4 * sqrt(sqdelta) * pow(sin(alpha), 3)) / (3 * (2 * alpha - sin(2 * alpha))) *
+                                 sqrt(1. / vec_dot(s, s, 2));
+    double centroid[2] = {xc[0] + s[0] * scalingFactor, xc[1] + s[1] * scalingFactor};
+    if (inTriangle(centroid, &TE[0], &TE[2], &TE[4], na, nb, nc)) {
+        cap[0] = centroid[0];
+        cap[1] = centroid[1];
+        return (sqdelta / 2) * (2 * alpha - sin(2 * alpha));
+    }
+    return 0.0;
+}
+
+// method_exact (integration.cpp:1632-1761): the polygon of B_delta(x) and T without cap points
+// (fan sub-triangles in out, their number returned), and up to three circular segments (caps,
+// weights, *nCaps). Points beyond R's 9 are dropped, as in method_retriangulate.
+int method_exact(const double *xc, const double *TE, double sqdelta, double *out, double *caps,
+                 double *capw, int *nCaps) {
+    *nCaps = 0;
+    int Rdx = 0;
+    double na[2], nb[2], nc[2];
+    bool is_onEdge = false, is_firstPointLiesOnVertex = true;
+    double R[9 * 2];
+    for (int i = 0; i < 18; i++) R[i] = 0;
+    const double orientation = -signDet2(TE);
+    rightNormal(&TE[0], &TE[2], orientation, na);
+    rightNormal(&TE[2], &TE[4], orientation, nb);
+    rightNormal(&TE[4], &TE[0], orientation, nc);
+    for (int k = 0; k < 3; k++) {
+        const double *p = &TE[2 * k];
+        const double *q = &TE[2 * ((k + 1) % 3)];
+        double a[2] = {q[0] - xc[0], q[1] - xc[1]};
+        double b[2] = {p[0] - q[0], p[1] - q[1]};
+        if (vec_sqL2dist(p, xc, 2) <= sqdelta) {
+            if (Rdx < 9) { R[2 * Rdx] = p[0]; R[2 * Rdx + 1] = p[1]; Rdx += 1; }
+            is_onEdge = false;
+        }
+        const double ab = a[0] * b[0] + a[1] * b[1];
+        const double aa = a[0] * a[0] + a[1] * a[1];
+        const double bb = b[0] * b[0] + b[1] * b[1];
+        const double v = sq(ab) - (aa - sqdelta) * bb;
+        if (v >= 0) {
+            const double term1 = -ab / bb;
+            const double term2 = sqrt(v) / bb;
+            double lam1, lam2;
+            if (term1 > 0) {
+                lam1 = term1 + term2;
+                lam2 = 1 / lam1 * (aa - sqdelta) / bb;
+            } else {
+                lam2 = term1 - term2;
+                lam1 = 1 / lam2 * (aa - sqdelta) / bb;
+            }
+            const double y1[2] = {lam1 * b[0] + q[0], lam1 * b[1] + q[1]};
+            const double y2[2] = {lam2 * b[0] + q[0], lam2 * b[1] + q[1]};
+            if ((0 <= lam1) && (lam1 <= 1)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
+                if (is_onEdge && *nCaps < 3) {
+                    capw[*nCaps] = placePointCapCenter(&R[2 * (Rdx - 1)], y1, xc, sqdelta, TE, na, nb, nc, orientation, &caps[2 * *nCaps]);
+                    *nCaps += !double_eq(capw[*nCaps], 0.);
+                }
+                if (Rdx < 9) { R[2 * Rdx] = y1[0]; R[2 * Rdx + 1] = y1[1]; Rdx += 1; }
+                is_onEdge = true;
+            }
+            if ((0 <= lam2) && (lam2 <= 1) && (sq(lam1 - lam2) > 0)) {
+                is_firstPointLiesOnVertex = is_firstPointLiesOnVertex && (bool)Rdx;
+                if (is_onEdge && *nCaps < 3) {
+                    capw[*nCaps] = placePointCapCenter(&R[2 * (Rdx - 1)], y2, xc, sqdelta, TE, na, nb, nc, orientation, &caps[2 * *nCaps]);
+                    *nCaps += !double_eq(capw[*nCaps], 0.);
+                }
+                if (Rdx < 9) { R[2 * Rdx] = y2[0]; R[2 * Rdx + 1] = y2[1]; Rdx += 1; }
+                is_onEdge = true;
+            }
+        }
+    }
+    if (is_onEdge && *nCaps < 3) {
+        capw[*nCaps] = placePointCapCenter(&R[2 * (Rdx - 1)], &R[0], xc, sqdelta, TE, na, nb, nc, orientation, &caps[2 * *nCaps]);
+        *nCaps += !double_eq(capw[*nCaps], 0.);
+    }
+    if (Rdx < 3) return 0;
+    for (int k = 0; k < Rdx - 2; k++)
+        for (int i = 0; i < 2; i++) {
+            out[2 * (3 * k + 0) + i] = R[i];
+            out[2 * (3 * k + 1) + i] = R[2 * (k + 1) + i];
+            out[2 * (3 * k + 2) + i] = R[2 * (k + 2) + i];
+        }
+    return Rdx - 2;
+}
+
 int method_baryCenter(const double *x, const Elem &T, const Mesh &m) {    // integration.cpp:1262-1280
     double b[3];
     baryCenter(m.dim, T.E, b);
@@ -488,6 +587,48 @@ int integrate_retriangulate(const Elem &aT, const Elem &bT, const Quad &q, const
                 tNP[dV * a + b] += aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonlocPrime[b];
             }
         }
+    }
+    return (doesInteract || m.full_search);
+}
+
+// integrate_exact, "exactBall" (integration.cpp:706-907): the polygon of method_exact with the
+// inner rule and each circular segment with one point at its centroid weighted by its exact
+// area; weight 2, termNonloc with k(y, x).
+int integrate_exact(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m, double *tL, double *tN) {
+    const int dV = 3;
+    double x[2], y[2], ref[2], psi[3];
+    double reTri[9 * 3 * 2], caps[6] = {0, 0, 0, 0, 0, 0}, capw[3] = {0, 0, 0};
+    int nCaps = 0, doesInteract = 0;
+    for (int k = 0; k < q.nPx; k++) {
+        toPhys(aT.E, &q.Px[2 * k], 2, x);
+        const int Rdx = method_exact(x, bT.E, m.sqdelta, reTri, caps, capw, &nCaps);
+        doesInteract += Rdx;
+        double innerLocal = 0, innerNonloc[3] = {0, 0, 0};
+        for (int r = 0; r < Rdx; r++) {
+            for (int i = 0; i < q.nPy; i++) {
+                toPhys3(&reTri[6 * r], &q.Py[2 * i], y);
+                const double rTdet = absDet2(&reTri[6 * r]);
+                double ker = kernel_value(m, x, aT.label, y, bT.label);
+                innerLocal += ker * q.dy[i] * rTdet;
+                toRef(bT.E, y, ref);
+                ker = kernel_value(m, y, bT.label, x, aT.label);
+                basis(ref, 2, psi);
+                for (int b = 0; b < dV; b++) innerNonloc[b] += psi[b] * ker * q.dy[i] * rTdet;
+            }
+        }
+        for (int i = 0; i < nCaps; i++) {
+            double ker = kernel_value(m, x, aT.label, &caps[2 * i], bT.label);
+            innerLocal += ker * capw[i];
+            toRef(bT.E, &caps[2 * i], ref);
+            ker = kernel_value(m, &caps[2 * i], bT.label, x, aT.label);
+            basis(ref, 2, psi);
+            for (int b = 0; b < dV; b++) innerNonloc[b] += psi[b] * ker * capw[i];
+        }
+        for (int a = 0; a < dV; a++)
+            for (int b = 0; b < dV; b++) {
+                tL[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.psix[dV * k + b] * q.dx[k] * innerLocal;
+                tN[dV * a + b] += 2 * aT.absDet * q.psix[dV * k + a] * q.dx[k] * innerNonloc[b];
+            }
     }
     return (doesInteract || m.full_search);
 }
@@ -1030,6 +1171,7 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
     case M_BARY_RT: return integrate_baryCenterRT(aT, bT, q, m, tL, tN);
     case M_NOTRUNC: return integrate_fullyContained(aT, bT, q, m, tL, tN, tLP, tNP);
     case M_WEAKSING: return integrate_weakSingular(aT, bT, q, m, tL, tN, tLP, tNP);
+    case M_EXACT: return integrate_exact(aT, bT, q, m, tL, tN);
     }
     return -1;
 }
@@ -1175,6 +1317,7 @@ int method_id(const char *s) {
     if (k == "baryCenterRT") return M_BARY_RT;
     if (k == "noTruncation") return M_NOTRUNC;
     if (k == "weakSingular") return M_WEAKSING;
+    if (k == "exactBall") return M_EXACT;
     return M_NONE;
 }
 

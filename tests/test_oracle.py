@@ -436,3 +436,34 @@ def test_oracle_forcings(name, od, fun):
     g = _forcing_numpy(m, conf2d(), fun, od)
     assert f.shape == g.shape
     np.testing.assert_allclose(f, g, rtol=1e-12, atol=1e-13 * np.abs(g).max())
+
+
+def test_oracle_exact_ball_integrates_the_ball_exactly():
+    """exactBall (integrate_exact / method_exact / placePointCapCenter, integration.cpp:706-907,
+    1300-1351, 1632-1761): the caps-free polygons plus each circular segment at its exact area.
+    With the constant kernel c, an outer point whose ball lies inside the mesh sees
+    sum over bT of the inner integral = c pi delta^2, so the termLocal blocks of an interior
+    element summed over all partners are 2 c pi delta^2 |aT| sum_k dx_k psi_a psi_b. The
+    retriangulate rule's cap points only approximate the arcs."""
+    from oracle import oracle
+    m = square_mesh(16, 0.1, jitter=0.15, seed=7)
+    V, T = m["vertices"], m["elements"]
+    aT = int(np.argmin(np.linalg.norm(V[T].mean(axis=1) - 0.5, axis=1)))
+    pairs = np.array([(aT, b) for b in range(T.shape[0])])
+    k = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    conf = conf2d()
+    P = np.asarray(conf["quadrature"]["outer"]["points"]); w = np.asarray(conf["quadrature"]["outer"]["weights"])
+    psi = np.column_stack([1 - P.sum(axis=1), P])
+    E = V[T[aT]]
+    det = abs(np.linalg.det(np.column_stack([E[1] - E[0], E[2] - E[0]])))
+    c = 4 / (np.pi * 0.1 ** 4)
+    want = 2 * c * np.pi * 0.1 ** 2 * det * (psi.T * w) @ psi
+    got = oracle.pair_blocks(m, k, conf, pairs, method="exactBall")[0][:, 0].sum(axis=0)
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    retri = oracle.pair_blocks(m, k, conf, pairs, method="retriangulate")[0][:, 0].sum(axis=0)
+    assert np.abs(retri - want / 2).max() > 1e-6 * np.abs(want).max()   # weight 1 there
+    # assembled: the one-sided rule's rows still sum to zero
+    r = oracle.assemble(m, k, conf2d(method="exactBall"))
+    A = r["A"]
+    keep = m["vertexLabels"] > 0
+    assert r["n_errors"] == 0 and np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()

@@ -39,12 +39,13 @@ const double SCALEDET = 0.0625;      // integration.cpp:44, MeshTypes.cpp:257
 
 enum KernelId { K_CONSTANT = 0, K_PARABOLA = 1, K_FRACTIONAL = 2, K_CONSTANT3D = 3, K_LABELED = 4, K_NOTCH = 5,
                 K_LABELEDNOTCH = 6, K_LABELEDVALVE = 7, K_CONSTTRUNC = 8, K_LINPROTO = 9,
-                K_FIELD_CONST = 10, K_FIELD_PROTO = 11, K_FIELD_PROTO3D = 12, K_NONE = -1 };
+                K_FIELD_CONST = 10, K_FIELD_PROTO = 11, K_FIELD_PROTO3D = 12, K_CONSTLINF = 13, K_NONE = -1 };
 enum LoadId { F_LINEAR = 0, F_LINEAR3D = 1, F_CONSTANT = 2, F_GAUSSIAN = 3, F_JUMP = 4, F_TENSORSIN = 5,
               F_FIELD_LINEAR = 6, F_FIELD_LINEAR3D = 7, F_FIELD_RIGHT = 8, F_FIELD_DOWN = 9, F_FIELD_BOTH = 10,
               F_NONE = -1 };
 enum MethodId { M_RETRIANGULATE = 0, M_BARYCENTER = 1, M_FRACTIONAL = 2, M_RETRI_UNSYMM = 3, M_SUBSET = 4,
-                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_EXACT = 9, M_NONE = -1 };
+                M_AVERAGE = 5, M_BARY_RT = 6, M_NOTRUNC = 7, M_WEAKSING = 8, M_EXACT = 9, M_RETRI_LINF = 10,
+                M_UNSYMM_LINF = 11, M_NONE = -1 };
 
 struct Mesh {
     int dim, dV, outdim, is_dg;
@@ -56,6 +57,7 @@ struct Mesh {
     int remote, close;   // MethodId of integrate_remote / integrate_close
     int is_singular;
     int caps, full_search;
+    int linf = 0;        // the retriangulate rules use the L-infinity ball (Cassemble.cpp:134-141)
     // domain decomposition (Cassemble.cpp:649-657): element -> subdomain indicator, CSR
     const long *zeta_indices = nullptr, *zeta_indptr = nullptr;
     long nZeta = 0;
@@ -214,6 +216,8 @@ double kernel_value(const Mesh &m, const double *x, long lx, const double *y, lo
     }
     case K_LABELEDNOTCH:  // model.cpp:104-108
         return !(lx + ly == 7) * (4 / (M_PI * pow(m.sqdelta, 2)));
+    case K_CONSTLINF:     // model.cpp:30-33
+        return 3 / (4 * pow(m.sqdelta, 2));
     case K_LABELEDVALVE:  // model.cpp:110-114
         return lx >= ly ? 4.0 / (M_PI * pow(m.sqdelta, 2)) : 0.0;
     case K_CONSTTRUNC: {  // model.cpp:33-42
@@ -548,6 +552,87 @@ int method_baryCenter(const double *x, const Elem &T, const Mesh &m) {    // int
 }
 
 // ---------------------------------------------------------------- integration routines
+// method_retriangulateInfty (integration.cpp:1521-1623): B_inf(x) (the square of half side delta)
+// intersected with T. Its points are T's vertices inside the square, the edges' crossings of the
+// square's sides, and the square's corners inside T. The reference inserts them into a
+// CGAL::Triangulation_2 (CGAL, not in this tree), which triangulates their convex hull. Here the
+// hull (Andrew's monotone chain, exact duplicates and collinear points dropped) is fanned from its
+// first point. Both cover the same convex polygon, so the rules integrate polynomial integrands
+// (the constantLinf2D kernel times the P1 basis) alike up to rounding; the sub-triangles differ.
+static double vec_LInfdist(const double *x, const double *y, int len) {   // mathhelpers.cpp:281-288
+    double r = 0;
+    for (int i = 0; i < len; i++) r = std::max(absolute(x[i] - y[i]), r);
+    return r;
+}
+
+int method_retriangulateInfty(const double *xc, const double *TE, double sqdelta, double *out) {
+    const double delta = sqrt(sqdelta);
+    std::vector<std::pair<double, double>> pts;
+    for (int k = 0; k < 3; k++) {
+        const double *p = &TE[2 * k];
+        const double *q = &TE[2 * ((k + 1) % 3)];
+        if (vec_LInfdist(p, xc, 2) <= delta) pts.emplace_back(p[0], p[1]);
+        const double b[2] = {p[0] - q[0], p[1] - q[1]};
+        double lambda[4] = {0, 0, 0, 0};
+        if (absolute(b[0]) > 0.) {
+            lambda[0] = (xc[0] + delta - q[0]) / b[0];
+            lambda[1] = (xc[0] - delta - q[0]) / b[0];
+        }
+        if (absolute(b[1]) > 0.) {
+            lambda[2] = (xc[1] + delta - q[1]) / b[1];
+            lambda[3] = (xc[1] - delta - q[1]) / b[1];
+        }
+        for (double l : lambda) {
+            if ((l > 0.) && (l < 1.)) {
+                const double xp[2] = {q[0] + b[0] * l, q[1] + b[1] * l};
+                if (vec_LInfdist(xp, xc, 2) <= delta * (1 + EPSILON)) pts.emplace_back(xp[0], xp[1]);
+            }
+        }
+    }
+    double na[2], nb[2], nc[2];
+    const double orientation = -signDet2(TE);
+    rightNormal(&TE[0], &TE[2], orientation, na);
+    rightNormal(&TE[2], &TE[4], orientation, nb);
+    rightNormal(&TE[4], &TE[0], orientation, nc);
+    const double sx[4] = {1, 1, -1, -1}, sy[4] = {1, -1, -1, 1};
+    for (int c = 0; c < 4; c++) {
+        const double v[2] = {xc[0] + sx[c] * delta, xc[1] + sy[c] * delta};
+        if (inTriangle(v, &TE[0], &TE[2], &TE[4], na, nb, nc)) pts.emplace_back(v[0], v[1]);
+    }
+    std::sort(pts.begin(), pts.end());
+    pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
+    if (pts.size() < 3) return 0;
+    auto cross = [](const std::pair<double, double> &o, const std::pair<double, double> &a,
+                    const std::pair<double, double> &b) {
+        return (a.first - o.first) * (b.second - o.second) - (a.second - o.second) * (b.first - o.first);
+    };
+    std::vector<std::pair<double, double>> h(2 * pts.size());
+    size_t n = 0;
+    for (size_t i = 0; i < pts.size(); i++) {   // lower hull
+        while (n >= 2 && cross(h[n - 2], h[n - 1], pts[i]) <= 0) n--;
+        h[n++] = pts[i];
+    }
+    for (size_t i = pts.size() - 1, t = n + 1; i-- > 0;) {   // upper hull
+        while (n >= t && cross(h[n - 2], h[n - 1], pts[i]) <= 0) n--;
+        h[n++] = pts[i];
+    }
+    n--;   // the last point repeats the first
+    if (n < 3) return 0;
+    for (size_t k = 0; k + 2 < n; k++) {
+        const std::pair<double, double> t3[3] = {h[0], h[k + 1], h[k + 2]};
+        for (int j = 0; j < 3; j++) {
+            out[2 * (3 * k + j) + 0] = t3[j].first;
+            out[2 * (3 * k + j) + 1] = t3[j].second;
+        }
+    }
+    return (int)n - 2;
+}
+
+// The retriangulation of the configured ball (Cassemble.cpp:134-141): L2 or L-infinity.
+int retri_method(const Mesh &m, const double *x, const double *TE, double *out) {
+    return m.linf ? method_retriangulateInfty(x, TE, m.sqdelta, out) : method_retriangulate(x, TE, m.sqdelta, out, m.caps);
+}
+
 // All four local blocks are (dV x dV) row-major, outdim = 1.
 int integrate_retriangulate(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
                             double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:345-540
@@ -558,7 +643,7 @@ int integrate_retriangulate(const Elem &aT, const Elem &bT, const Quad &q, const
     int doesInteract = 0;
     for (int k = 0; k < q.nPx; k++) {
         toPhys(aT.E, &q.Px[2 * k], 2, x);
-        int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        int Rdx = retri_method(m, x, bT.E, reTri);
         doesInteract += Rdx;
         innerLocal = 0;
         for (int b = 0; b < dV; b++) { innerNonloc[b] = 0; innerNonlocPrime[b] = 0; }
@@ -675,7 +760,7 @@ int integrate_retriangulate_unsymm(const Elem &aT, const Elem &bT, const Quad &q
     int doesInteract = 0;
     for (int k = 0; k < q.nPx; k++) {
         toPhys(aT.E, &q.Px[2 * k], 2, x);
-        const int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        const int Rdx = retri_method(m, x, bT.E, reTri);
         doesInteract += Rdx;
         double innerLocal = 0, innerNonloc[3] = {0, 0, 0};
         for (int r = 0; r < Rdx; r++) {
@@ -1040,7 +1125,7 @@ int integrate_retriangulate_vec(const Elem &aT, const Elem &bT, const Quad &q, c
     int doesInteract = 0;
     for (int k = 0; k < q.nPx; k++) {
         toPhys(aT.E, &q.Px[2 * k], 2, x);
-        const int Rdx = method_retriangulate(x, bT.E, m.sqdelta, reTri, m.caps);
+        const int Rdx = retri_method(m, x, bT.E, reTri);
         doesInteract += Rdx;
         for (int o = 0; o < o2; o++) innerLocal[o] = 0;
         for (int b = 0; b < dV * o2; b++) { innerNonloc[b] = 0; innerNonlocPrime[b] = 0; }
@@ -1156,7 +1241,7 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
                      double *tL, double *tN, double *tLP, double *tNP) {
     if (m.outdim > 1) {
         switch (method) {
-        case M_RETRIANGULATE: return integrate_retriangulate_vec(aT, bT, q, m, tL, tN, tLP, tNP);
+        case M_RETRIANGULATE: case M_RETRI_LINF: return integrate_retriangulate_vec(aT, bT, q, m, tL, tN, tLP, tNP);
         case M_BARYCENTER: return integrate_baryCenter_vec(aT, bT, q, m, tL, tN);
         case M_FRACTIONAL: return integrate_fractional_vec(aT, bT, q, m, tL, tN, tLP, tNP);
         }
@@ -1172,6 +1257,8 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
     case M_NOTRUNC: return integrate_fullyContained(aT, bT, q, m, tL, tN, tLP, tNP);
     case M_WEAKSING: return integrate_weakSingular(aT, bT, q, m, tL, tN, tLP, tNP);
     case M_EXACT: return integrate_exact(aT, bT, q, m, tL, tN);
+    case M_RETRI_LINF: return integrate_retriangulate(aT, bT, q, m, tL, tN, tLP, tNP);
+    case M_UNSYMM_LINF: return integrate_retriangulate_unsymm(aT, bT, q, m, tL, tN);
     }
     return -1;
 }
@@ -1289,6 +1376,7 @@ int kernel_id(const char *s) {
     if (k == "constantField") return K_FIELD_CONST;
     if (k == "linearPrototypeMicroelasticField") return K_FIELD_PROTO;
     if (k == "linearPrototypeMicroelasticField3D") return K_FIELD_PROTO3D;
+    if (k == "constantLinf2D") return K_CONSTLINF;
     return K_NONE;
 }
 int load_id(const char *s) {
@@ -1318,6 +1406,8 @@ int method_id(const char *s) {
     if (k == "noTruncation") return M_NOTRUNC;
     if (k == "weakSingular") return M_WEAKSING;
     if (k == "exactBall") return M_EXACT;
+    if (k == "retriangulateLinfty") return M_RETRI_LINF;
+    if (k == "retriangulate_unsymmLinfty") return M_UNSYMM_LINF;
     return M_NONE;
 }
 
@@ -1383,6 +1473,7 @@ oracle_result *oracle_par_assemble(
     m.is_singular = (kn == "fractional" || kn == "linearPrototypeMicroelastic" ||
                      kn == "linearPrototypeMicroelasticField");               // Cassemble.cpp:89-94
     m.caps = is_PlacePointOnCap; m.full_search = is_fullConnectedComponentSearch;
+    m.linf = (m.remote == M_RETRI_LINF || m.remote == M_UNSYMM_LINF || m.close == M_RETRI_LINF || m.close == M_UNSYMM_LINF);
     // vector-valued kernels: retriangulate, baryCenter and the fractional close rule
     if (outdim < 1 || outdim > dim) return nullptr;
     if (outdim > 1 && std::string(compute ? compute : "") == "system") {
@@ -1531,6 +1622,7 @@ int oracle_pair_blocks(
     m.sqdelta = sqdelta; m.delta = sqrt(sqdelta); m.frac_s = fractional_s;
     m.kernel = kernel_id(kernel); m.caps = is_PlacePointOnCap;
     int meth = method_id(method);
+    m.linf = (meth == M_RETRI_LINF || meth == M_UNSYMM_LINF);
     Quad q;
     q.Px = Px; q.dx = dx; q.Py = Py; q.dy = dy; q.nPx = nPx; q.nPy = nPy;
     q.nPg = degree > 0 ? (int)pow(degree, dim * 2) : 0;

@@ -467,3 +467,30 @@ def test_oracle_exact_ball_integrates_the_ball_exactly():
     A = r["A"]
     keep = m["vertexLabels"] > 0
     assert r["n_errors"] == 0 and np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()
+
+
+@pytest.mark.parametrize("method,weight", [("retriangulateLinfty", 1.0), ("retriangulate_unsymmLinfty", 2.0)])
+def test_oracle_linf_ball_area(method, weight):
+    """The L-infinity ball (method_retriangulateInfty, integration.cpp:1521-1623; the reference
+    triangulates the points with CGAL, here the convex hull is fanned) and kernel_constantLinf2D
+    (model.cpp:30-33): for an interior element the square of half side delta is covered exactly,
+    so the termLocal blocks summed over all partners are weight c 4 delta^2 |aT| sum_k dx psi psi."""
+    from oracle import oracle
+    m = square_mesh(16, 0.1, jitter=0.15, seed=7)
+    V, T = m["vertices"], m["elements"]
+    aT = int(np.argmin(np.linalg.norm(V[T].mean(axis=1) - 0.5, axis=1)))
+    pairs = np.array([(aT, b) for b in range(T.shape[0])])
+    k = {"function": "constantLinf2D", "horizon": 0.1, "outputdim": 1}
+    conf = conf2d()
+    P = np.asarray(conf["quadrature"]["outer"]["points"]); w = np.asarray(conf["quadrature"]["outer"]["weights"])
+    psi = np.column_stack([1 - P.sum(axis=1), P])
+    E = V[T[aT]]
+    det = abs(np.linalg.det(np.column_stack([E[1] - E[0], E[2] - E[0]])))
+    c = 3 / (4 * 0.1 ** 4)
+    want = weight * c * 4 * 0.1 ** 2 * det * (psi.T * w) @ psi
+    got = oracle.pair_blocks(m, k, conf, pairs, method=method)[0][:, 0].sum(axis=0)
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    r = oracle.assemble(m, k, conf2d(method=method))
+    A = r["A"]
+    keep = m["vertexLabels"] > 0
+    assert r["n_errors"] == 0 and np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()

@@ -3,13 +3,15 @@
  * include/Cassemble.h (and include/Cassemble.pxd) links unchanged.
  *
  *   par_assemble          <- include/Cassemble.h:125-140 (bound at include/Cassemble.pxd:12-25)
+ *   par_evaluateMass      <- include/Cassemble.h:202-204 (include/Cassemble.pxd:27-29)
  *   method_retriangulate  <- include/Cassemble.h:62-64   (include/Cassemble.pxd:32-34)
  *   toRef                 <- include/Cassemble.h:68      (include/Cassemble.pxd:38)
  *   toPhys                <- include/Cassemble.h:70      (include/Cassemble.pxd:39)
  *   solve2x2              <- include/Cassemble.h:71      (include/Cassemble.pxd:40)
  *
  * Like the reference they abort() on invalid input; the C ABI in nlfem_gpu.h returns status
- * codes instead. The computation runs on the GPU.
+ * codes instead. The computation runs on the GPU. method_retriangulateInfty (Cassemble.pxd:35-37)
+ * is not exported: the L-infinity ball has no GPU implementation yet.
  */
 #ifndef NLFEM_CASSEMBLE_COMPAT_H
 #define NLFEM_CASSEMBLE_COMPAT_H
@@ -28,6 +30,10 @@ void par_assemble(std::string compute, std::string path_spAd, std::string path_f
                   int degree = 0, const double *dg = nullptr, double maxDiameter = 0.0,
                   double fractional_s = -1.0, int is_fullConnectedComponentSearch = 0,
                   int verbose = 0);
+
+void par_evaluateMass(double *vd, const double *ud, long *Elements, const long *ElementLabels,
+                      const double *Verts, const long *VertexLabels, int K_Omega, int J, int nP,
+                      double *P, const double *dx, int dim, int outdim, int is_DiscontinuousGalerkin);
 
 int method_retriangulate(const double *xCenter, const double *TE, double sqdelta,
                          double *reTriangleList, int isPlacePointOnCap);

@@ -7,6 +7,7 @@
 #include "../../include/nlfem_gpu.h"
 #include "../../include/Cassemble_compat.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -129,6 +130,26 @@ int method_retriangulate(const double *xCenter, const double *TE, double sqdelta
     int r = nlfem_method_retriangulate(xCenter, TE, sqdelta, reTriangleList, isPlacePointOnCap);
     if (r < 0) die_on(-r, "method_retriangulate");
     return r;
+}
+
+// par_evaluateMass (Cassemble.cpp:166-246) through nlfem_evaluate_mass. The signature carries no
+// element or vertex count: the first J elements are the ones read (K_Omega is unused, as in the
+// reference), and for CG the vertex count is one past the largest vertex index they use. Like the
+// reference it adds M ud to vd.
+void par_evaluateMass(double *vd, const double *ud, long *Elements, const long *ElementLabels,
+                      const double *Verts, const long *VertexLabels, int K_Omega, int J, int nP,
+                      double *P, const double *dx, int dim, int outdim, int is_DiscontinuousGalerkin) {
+    (void)K_Omega;
+    if (J <= 0) return;
+    const long dV = dim + 1;
+    long nV = 0;
+    for (long i = 0; i < (long)J * dV; i++) nV = std::max(nV, Elements[i] + 1);
+    const long K = is_DiscontinuousGalerkin ? dV * J : nV;
+    std::vector<double> Md((size_t)K * outdim, 0.0);
+    die_on(nlfem_evaluate_mass(dim, outdim, is_DiscontinuousGalerkin, J, J, nV, Elements, ElementLabels, Verts,
+                               VertexLabels, nP, P, dx, ud, Md.data()),
+           "par_evaluateMass");
+    for (size_t i = 0; i < Md.size(); i++) vd[i] += Md[i];
 }
 
 void toRef(const double *E, const double *phys_x, double *ref_p) {

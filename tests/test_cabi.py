@@ -38,6 +38,7 @@ def test_cpp_compat_symbols_exported(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", "-C", _lib.LIB_PATH], capture_output=True,
                          text=True, check=True).stdout
     for sym in ["par_assemble(std::__cxx11::basic_string", "method_retriangulate(double const*",
+                "par_evaluateMass(double*, double const*, long*, long const*, double const*, long const*, int, int, int, double*, double const*, int, int, int)",
                 "toRef(double const*", "toPhys(double const*", "solve2x2(double const*"]:
         assert sym in out, sym
 

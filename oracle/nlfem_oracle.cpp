@@ -1194,6 +1194,41 @@ int integrate_baryCenter_vec(const Elem &aT, const Elem &bT, const Quad &q, cons
     return (doesInteract || m.full_search);
 }
 
+int integrate_weakSingular_vec(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
+                               double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:82-185
+    Elem aS, bS;
+    int argA[3], argB[3];
+    const int nEqual = join(aT, bT, m, aS, bS, argA, argB);
+    if (nEqual < 1 || nEqual > 3) return -1;  // reference aborts
+    const int c = nEqual - 1;
+    const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
+    const int dV = 3, od = m.outdim;
+    double xc[2], yc[2], psix[3], psiy[3], kv[9];
+    for (int t = 0; t < nT; t++) {
+        for (int k = 0; k < q.nPg; k++) {
+            const double tw = q.tdetWeak[c][t * q.nPg + k];
+            const double *ac = &q.alphaC[c][(t * q.nPg + k) * 4];
+            const double *au = &q.alphaU[c][(t * q.nPg + k) * 4];
+            toPhys(aS.E, &ac[0], 2, xc);
+            toPhys(bS.E, &ac[2], 2, yc);
+            kernel_vec(m, xc, aT.label, yc, bT.label, kv);
+            basis(&au[0], 2, psix);
+            basis(&au[2], 2, psiy);
+            for (int a = 0; a < dV; a++)
+                for (int aOut = 0; aOut < od; aOut++)
+                    for (int b = 0; b < dV; b++)
+                        for (int bOut = 0; bOut < od; bOut++) {
+                            const double f = kv[od * aOut + bOut] * tw * q.dg[k] * aS.absDet * bS.absDet;
+                            tL[od * dV * (argA[a] * od + aOut) + argA[b] * od + bOut] += f * psix[a] * psix[b];
+                            tLP[od * dV * (argB[a] * od + aOut) + argB[b] * od + bOut] += f * psiy[a] * psiy[b];
+                            tN[od * dV * (argA[a] * od + aOut) + argB[b] * od + bOut] += f * psix[a] * psiy[b];
+                            tNP[od * dV * (argA[a] * od + aOut) + argB[b] * od + bOut] += f * psix[a] * psiy[b];
+                        }
+        }
+    }
+    return 1;
+}
+
 int integrate_fractional_vec(const Elem &aT, const Elem &bT, const Quad &q, const Mesh &m,
                              double *tL, double *tN, double *tLP, double *tNP) {  // integration.cpp:187-288
     Elem aS, bS;
@@ -1244,6 +1279,7 @@ int integrate_method(int method, const Elem &aT, const Elem &bT, const Quad &q, 
         case M_RETRIANGULATE: case M_RETRI_LINF: return integrate_retriangulate_vec(aT, bT, q, m, tL, tN, tLP, tNP);
         case M_BARYCENTER: return integrate_baryCenter_vec(aT, bT, q, m, tL, tN);
         case M_FRACTIONAL: return integrate_fractional_vec(aT, bT, q, m, tL, tN, tLP, tNP);
+        case M_WEAKSING: return integrate_weakSingular_vec(aT, bT, q, m, tL, tN, tLP, tNP);
         }
         return -1;
     }
@@ -1477,7 +1513,7 @@ oracle_result *oracle_par_assemble(
     // vector-valued kernels: retriangulate, baryCenter and the fractional close rule
     if (outdim < 1 || outdim > dim) return nullptr;
     if (outdim > 1 && std::string(compute ? compute : "") == "system") {
-        auto ok = [](int mth) { return mth == M_RETRIANGULATE || mth == M_BARYCENTER || mth == M_FRACTIONAL; };
+        auto ok = [](int mth) { return mth == M_RETRIANGULATE || mth == M_BARYCENTER || mth == M_FRACTIONAL || mth == M_WEAKSING; };
         if (!ok(m.remote) || !ok(m.close)) return nullptr;
     }
 

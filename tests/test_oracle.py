@@ -494,3 +494,16 @@ def test_oracle_linf_ball_area(method, weight):
     A = r["A"]
     keep = m["vertexLabels"] > 0
     assert r["n_errors"] == 0 and np.abs(A @ np.ones(A.shape[0]))[keep].max() < 1e-12 * abs(A).max()
+
+
+def test_oracle_weak_and_fractional_rules_agree_for_the_field_kernel():
+    """outdim 2: the weakSingular close rule (integration.cpp:82-185, component loops) and the
+    fractional one assemble the same matrix for the weakly singular microelastic field kernel
+    (|z|^-1 homogeneous, s = -1/2), as in the scalar case."""
+    from oracle import oracle
+    m = square_mesh(8, 0.1, jitter=0.15, seed=3)
+    k = {"function": "linearPrototypeMicroelasticField", "horizon": 0.1, "outputdim": 2, "fractional_s": -0.5}
+    W = oracle.assemble(m, k, conf2d(rule="16", close="weakSingular", deg=3))
+    F = oracle.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))
+    assert W["n_close"] == F["n_close"] > 0 and W["n_errors"] == 0
+    assert abs(W["A"] - F["A"]).max() <= 1e-13 * abs(F["A"]).max()

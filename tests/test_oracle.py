@@ -507,3 +507,22 @@ def test_oracle_weak_and_fractional_rules_agree_for_the_field_kernel():
     F = oracle.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))
     assert W["n_close"] == F["n_close"] > 0 and W["n_errors"] == 0
     assert abs(W["A"] - F["A"]).max() <= 1e-13 * abs(F["A"]).max()
+
+
+def test_oracle_dg_sums_to_cg_with_close_pairs():
+    """DG with a singular kernel and the fractional close rule: summed over the vertex copies,
+    the DG matrix is the CG matrix on the kept rows (the close-pair blocks scatter to element
+    DOFs like the others)."""
+    from oracle import oracle
+    m = square_mesh(8, 0.2, jitter=0.1, seed=5)
+    k = {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4}
+    cdg = conf2d(rule="16", close="fractional", deg=3)
+    cdg["ansatz"] = "DG"
+    D = oracle.assemble(m, k, cdg)
+    C = oracle.assemble(m, k, conf2d(rule="16", close="fractional", deg=3))
+    assert D["n_close"] == C["n_close"] > 0
+    T = m["elements"]; nE, nV = T.shape[0], m["vertices"].shape[0]
+    P = sp.csr_matrix((np.ones(3 * nE), (np.arange(3 * nE), T.ravel())), shape=(3 * nE, nV))
+    S = (P.T @ D["A"] @ P).toarray()
+    S[m["vertexLabels"] <= 0] = 0
+    assert np.abs(S - C["A"].toarray()).max() <= 1e-11 * abs(C["A"]).max()

@@ -45,7 +45,31 @@ def cases():
                    conf2d(rule="16", close="fractional", deg=3), None),
         "cube5": (cube_mesh(5, 0.1, jitter=0.15, seed=2),
                   {"function": "constant3D", "horizon": 0.3, "outputdim": 1}, conf3d(), {"function": "linear3D"}),
+        # the rows beyond the reference's default configuration (the CPU pin covers these; the
+        # GPU compares against the first five)
+        "labeled10": (_labeled_mesh(10, 14), {"function": "labeled", "horizon": 0.1, "outputdim": 1}, conf2d(), None),
+        "average10": (square_mesh(10, 0.1, jitter=0.15, seed=12), kc, conf2d(method="averageBall"), None),
+        "exact8": (square_mesh(8, 0.1, jitter=0.15, seed=12), kc, conf2d(method="exactBall"), None),
+        "dg10": (square_mesh(10, 0.1, jitter=0.15, seed=14),
+                 {"function": "parabola", "horizon": 0.1, "outputdim": 1}, dict(conf2d(), ansatz="DG"),
+                 {"function": "linear"}),
+        "weak10": (square_mesh(10, 0.1, jitter=0.15, seed=9),
+                   {"function": "linearPrototypeMicroelastic", "horizon": 0.1, "outputdim": 1, "fractional_s": -0.5},
+                   conf2d(rule="16", close="weakSingular", deg=3), None),
+        "field8": (dict(square_mesh(8, 0.1, jitter=0.15, seed=3), outdim=2),
+                   {"function": "constantField", "horizon": 0.1, "outputdim": 2}, conf2d(), {"function": "constantBothField"}),
+        "linf8": (square_mesh(8, 0.1, jitter=0.15, seed=3), {"function": "constantLinf2D", "horizon": 0.1, "outputdim": 1},
+                  conf2d(method="retriangulateLinfty"), None),
     }
+
+
+def _labeled_mesh(n, seed):
+    """Labels 3 (x0 < 0.5) and 4 in Omega, -1 in the layer, everything moved by -0.5."""
+    from nlfem_gb300 import meshes
+    v, e, l = meshes.regular_square(n, 0.1, jitter=0.1, seed=seed)
+    bx = v[e].mean(axis=1)[:, 0]
+    lab = np.where(l > 0, np.where(bx < 0.5, 3, 4), -1)
+    return meshes.mesh_dict(v - 0.5, e, lab)
 
 
 def input_hash(mesh, kernel, conf):

@@ -308,7 +308,8 @@ def _golden_cases_module():
     return mod
 
 
-@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5"])
+@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5", "labeled10", "average10",
+                                  "exact8", "dg10", "weak10", "field8", "linf8"])
 def test_oracle_matches_committed_fixtures(name):
     """The oracle against tests/golden/oracle_cases.npz: the same inputs, the same pattern and
     pair list bit for bit, values and load vectors to 1e-13 (libm differences across hosts)."""

@@ -137,7 +137,7 @@ extern "C" int nlfem_evaluate_mass(int dim, int outdim, int is_dg, long nE, long
     }
     const double bound = 2.0 * vol * fmax(umax, 1e-300) * outdim;
     if (!std::isfinite(bound)) return nlfem_fail_internal(NLFEM_ERR_NUMERIC, "non-finite input to evaluate_mass");
-    const int scale_exp = (int)ceil(log2(bound));
+    const int scale_exp = exact_ceil_log2(bound);
     DevMem m;
     long long *dT = m.get<long long>((size_t)nE * dV), *dLT = m.get<long long>(nE), *dLV = m.get<long long>(nV);
     double *dVx = m.get<double>((size_t)nV * dim), *dpsi = m.get<double>(psi.size()), *ddx = m.get<double>(nP);

@@ -13,9 +13,12 @@
 // Limits: at most NOALLOC_MAX_VERTICES (1,048,576) vertices, continuous P1 only; larger meshes are
 // rejected with NLFEM_ERR_INVALID. All calls share the one array: each call clears the part it
 // uses before it starts, and calls that overlap on the GPU (two streams, or two host threads)
-// race on it, so the caller must serialize them. The first call on a device looks up the array's
-// device address with cudaGetSymbolAddress while that device is current; that set-up call should
-// come before any stream capture. The call returns after the result is in d_fd.
+// race on it, so the caller must serialize them. The first call on a device does a one-time set-up
+// with that device current: it loads every kernel of this entry point (under lazy module loading a
+// kernel's first launch can allocate) and looks up the array's device address with
+// cudaGetSymbolAddress. That first call should come before any stream capture. A device whose
+// context was torn down and made anew (cudaDeviceReset) gets the set-up again on its next call.
+// The call returns after the result is in d_fd.
 //
 // Result: bit-identical to nlfem_load_vector. compute_f (Cassemble.cpp:149-164) per element, the
 // same exact FP64 geometry, and the same 128-bit fixed-point sum whose scale follows the same rule
@@ -109,10 +112,7 @@ __global__ void k_noalloc_scale(long long nE, unsigned long long *__restrict__ s
     const double el = __ddiv_rn(vol, (double)nE);
     double mag = __dmul_rn(__dmul_rn(2.0, __dadd_rn(fm, 2.0)), el);
     if (!(mag > 0) || !isfinite(mag)) mag = 1.0;
-    int e;
-    const double m = frexp(mag, &e);
-    const int scale = (m == 0.5) ? e - 1 : e;
-    s[HDR + 6] = (unsigned long long)(long long)(scale + 4096);
+    s[HDR + 6] = (unsigned long long)(long long)(exact_ceil_log2(mag) + 4096);
 }
 
 // termf[a] of compute_f (Cassemble.cpp:149-164), summed over the elements with label > 0 into the
@@ -177,9 +177,48 @@ __global__ void k_noalloc_finish(const unsigned long long *__restrict__ s, long 
 }
 
 std::mutex g_lock;
-unsigned long long *g_addr[1024];   // device address of g_noalloc_scratch, per device ordinal
+void *g_addr[1024];                 // device address of g_noalloc_scratch, per device ordinal
+unsigned long long g_ctx[1024];     // the context it belongs to (driver context ID, never reused)
 
 unsigned grid_of(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// The ID of the current context, from the driver's cuCtxGetCurrent and cuCtxGetId (looked up once
+// through the runtime, so the library needs no link to the driver library).
+cudaError_t context_id(int dev, unsigned long long *id) {
+    typedef int (*get_current_t)(void **);
+    typedef int (*get_id_t)(void *, unsigned long long *);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return cudaErrorNotSupported;
+        get_current = (get_current_t)f1;
+        get_id = (get_id_t)f2;
+    }
+    void *c = nullptr;
+    // the current device again: since CUDA 12 this makes its primary context current
+    if (cudaSetDevice(dev) != cudaSuccess) return cudaErrorNoDevice;
+    if (get_current(&c) != 0 || !c || get_id(c, id) != 0) return cudaErrorDeviceUninitialized;
+    return cudaSuccess;
+}
+
+// Forces every kernel of this entry point to be loaded in the current context.
+cudaError_t load_kernels() {
+    const void *fns[] = {(const void *)k_noalloc_clear,      (const void *)k_noalloc_bbox<2>,
+                         (const void *)k_noalloc_bbox<3>,     (const void *)k_noalloc_scale<2>,
+                         (const void *)k_noalloc_scale<3>,    (const void *)k_noalloc_forcing<2>,
+                         (const void *)k_noalloc_forcing<3>,  (const void *)k_noalloc_finish};
+    for (const void *f : fns) {
+        cudaFuncAttributes a;
+        const cudaError_t e = cudaFuncGetAttributes(&a, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -231,17 +270,30 @@ extern "C" int nlfem_load_vector_noalloc(int dim, long nE, long nV, const long *
     unsigned long long *s;
     {
         std::lock_guard<std::mutex> g(g_lock);
-        if (!g_addr[dev]) {   // set-up, once per device, with that device current
+        unsigned long long ctx = 0;
+        if (context_id(dev, &ctx) != cudaSuccess) {
+            cudaGetLastError();
+            return nlfem_fail_internal(NLFEM_ERR_CUDA, "no current CUDA context");
+        }
+        if (!g_addr[dev] || g_ctx[dev] != ctx) {
+            // Set-up, once per device (and again if the device's context was torn down and made
+            // anew, e.g. by cudaDeviceReset), with that device current: the array's device
+            // address, and every kernel this entry point launches loaded now, because under lazy
+            // module loading a kernel's code is loaded, and device memory possibly allocated for
+            // it, at its first launch. Later calls allocate nothing.
             void *p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e == cudaSuccess && !p) e = cudaErrorInvalidSymbol;
+            if (e == cudaSuccess) e = load_kernels();
+            if (e != cudaSuccess) {
                 cudaGetLastError();
-                return nlfem_fail_internal(NLFEM_ERR_CUDA, (std::string("cudaGetSymbolAddress of the scratch array: ") +
+                return nlfem_fail_internal(NLFEM_ERR_CUDA, (std::string("set-up of the no-alloc load vector: ") +
                                                             cudaGetErrorString(e)).c_str());
             }
-            g_addr[dev] = (unsigned long long *)p;
+            g_addr[dev] = p;
+            g_ctx[dev] = ctx;
         }
-        s = g_addr[dev];
+        s = (unsigned long long *)g_addr[dev];
     }
 
     cudaStream_t st = (cudaStream_t)stream;

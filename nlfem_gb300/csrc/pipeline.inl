@@ -269,7 +269,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         mag = 2.0 * (fm + 2.0) * el;
     }
     if (!(mag > 0) || !std::isfinite(mag)) mag = 1.0;
-    P.scale_exp = (int)std::ceil(std::log2(mag));
+    P.scale_exp = exact_ceil_log2(mag);
     return set_fx_unit(P, 0);
 }
 

@@ -8,6 +8,15 @@ namespace nlg {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// ceil(log2(x)) for x > 0, exact: frexp splits x = m 2^e with m in [1/2, 1), and only m = 1/2
+// (x a power of two) gives e - 1. A rounded log2 can land on the integer below when x is a few
+// ulp above a power of two, so the fixed-point scales of the host and the device use this rule.
+__host__ __device__ inline int exact_ceil_log2(double x) {
+    int e;
+    const double m = frexp(x, &e);
+    return m == 0.5 ? e - 1 : e;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -34,67 +34,39 @@ import numpy as np
 
 METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel err"
 
-# DRAM traffic (read + write bytes) of the one k_pass_mix2d launch of a C2 assembly, from the ncu
-# capture summarised in profiles/k_pass_mix2d_2d-constant.md; None for workloads not captured.
+# DRAM traffic (read + write bytes) of the one k_pass_mix2d launch of a C2 assembly (n = 256,
+# delta = 0.1), from an ncu capture of that launch (dram__bytes_read.sum + dram__bytes_write.sum);
+# None for workloads not captured. Reported as roofline.traffic with its source.
 PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): 5.32e9 + 1.07e9}
 
 
 def workload(args, precision):
     """Problems [(mesh, kernel, configuration)] and the config record of the chosen workload."""
-    from nlfem_gb300 import meshes, quadrules
-    w = args.workload
+    from nlfem_gb300 import workloads
+    return workloads.problems(args.workload, precision, n=args.n, delta=args.delta)
 
-    def conf2d(rule, close=None, deg=0):
-        P, wts = rule
-        c = {"ansatz": "CG", "approxBalls": {"method": "retriangulate", "is_PlacePointOnCap": 1},
-             "quadrature": {"outer": {"points": P, "weights": wts}, "inner": {"points": P, "weights": wts}},
-             "precision": precision}
-        if close:
-            c["closeElements"] = close
-        if deg:
-            c["quadrature"]["tensorGaussDegree"] = deg
-        return c
 
-    if w in ("c1", "c2"):
-        n = args.n or (32 if w == "c1" else 256)
-        jit = 0.0 if w == "c1" else 0.2
-        v, e, l = meshes.regular_square(n, args.delta, jitter=jit, seed=1)
-        mesh = meshes.mesh_dict(v, e, l)
-        kernel = {"function": "constant", "horizon": args.delta, "outputdim": 1}
-        desc = (f"2D constant kernel, 2*{n}^2 triangles" + (f" jittered +-0.2h (seed 1)" if jit else "") +
-                f", delta={args.delta}, retriangulate+caps, 7-pt Dunavant outer/inner, P1 CG")
-        return [(mesh, kernel, conf2d(quadrules.dunavant7()))], {"workload": desc, "n": n, "delta": args.delta}
-    if w == "c3":
-        n = args.n or 128
-        v, e, l = meshes.regular_square(n, args.delta)
-        mesh = meshes.mesh_dict(v, e, l)
-        kernel = {"function": "fractional", "horizon": args.delta, "outputdim": 1, "fractional_s": 0.4}
-        desc = (f"2D fractional kernel s=0.4, 2*{n}^2 triangles, delta={args.delta}; regular pairs "
-                f"retriangulate+caps with the 16-pt rule, close pairs Duffy tensor Gauss degree 5 (FP64)")
-        return ([(mesh, kernel, conf2d(quadrules.dunavant16(), close="fractional", deg=5))],
-                {"workload": desc, "n": n, "delta": args.delta})
-    if w == "c4":
-        n = args.n or 32
-        v, e, l = meshes.regular_cube(n, args.delta)
-        mesh = meshes.mesh_dict(v, e, l)
-        kernel = {"function": "constant3D", "horizon": args.delta, "outputdim": 1}
-        P, wts = quadrules.keast11()
-        conf = {"ansatz": "CG", "approxBalls": {"method": "baryCenter"},
-                "quadrature": {"outer": {"points": P, "weights": wts}, "inner": {"points": P, "weights": wts}},
-                "precision": precision}
-        desc = (f"3D constant kernel, 6*{n}^3 tetrahedra (Kuhn split) of [-delta,1+delta]^3, delta={args.delta}, "
-                f"barycenter ball, 11-pt Keast outer/inner, P1 CG")
-        return [(mesh, kernel, conf)], {"workload": desc, "n": n, "delta": args.delta}
-    if w == "c5":
-        probs = []
-        for b in meshes.batch_meshes(64, seed=2024):
-            k = {"function": b["kernel"], "horizon": b["delta"], "outputdim": 1}
-            probs.append((b["mesh"], k, conf2d(quadrules.dunavant7())))
-        desc = ("64 independent 2D problems in one batch: n from {32,48,...,192} (2*n^2 triangles, jittered "
-                "+-0.2h), delta ~ U[0.05,0.2], half constant / half parabola kernel, retriangulate+caps, 7-pt rules "
-                "(PCG64 seed 2024)")
-        return probs, {"workload": desc, "problems": 64}
-    raise SystemExit(f"unknown workload {w}")
+def reference_digest(args):
+    """The digest of the reference's own FP64 assembly of this workload (tests/golden/digest_*.npz,
+    made by tests/golden/make_ref_digests.py), or None for sizes that have none."""
+    from nlfem_gb300 import digest
+    key = {("c2", 0.1): "c2", ("c2", 0.05): "c2d05", ("c3", 0.1): "c3", ("c4", 0.1): "c4",
+           ("c5", 0.1): "c5"}.get((args.workload, args.delta))
+    if key is None or args.n is not None:
+        return None
+    path = os.path.join(ROOT, "tests", "golden", f"digest_{key}.npz")
+    return digest.load(path) if os.path.exists(path) else None
+
+
+def vs_reference(mats, dg):
+    """Errors of the assembled matrices against the reference digest: the pattern (bit-exact, by
+    hash), the relative Frobenius error estimated from A u, and the max-entry error over the
+    sampled rows; the worst over the problems of a batch."""
+    from nlfem_gb300 import digest
+    digests, meta = dg
+    res = [digest.compare(A, digests[f"p{i}"]) for i, A in enumerate(mats)]
+    return {"pattern_identical": all(r["pattern_identical"] for r in res),
+            "fro_est": max(r["fro_est"] for r in res), "max_rows": max(r["max_rows"] for r in res)}
 
 
 def config_dict(args, extra, problems):
@@ -389,6 +361,8 @@ def run_gpu(args, rank=0, world=1, dist=None):
         "roofline": {"bound": "fp32", "kernel": kname,
                      "achieved": achieved, "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
                      "traffic": PASS_TRAFFIC_BYTES.get((args.workload, extra.get("n"), extra.get("delta"))),
+                     "traffic_source": "ncu DRAM bytes of this kernel's launch at n=256, delta=0.1 (not measured "
+                                       "in this run)",
                      "note": "achieved = flops of the algorithm that ran for the step (FLOP model in "
                              "bench.algorithmic_flops: the reference's inner-point loops, or their closed forms "
                              "for constant kernels; FP64 close pairs not counted) / device time of the "
@@ -403,12 +377,12 @@ def run_gpu(args, rank=0, world=1, dist=None):
     }
 
     run64 = world == 1 and not args.no_fp64 and (args.workload != "c5" or args.fp64_steps_set)
+    A64 = None
     if run64:
         problems64, _ = workload(args, "fp64")
         p64, s64, st64, _, clk64, sess64 = timed_session(problems64, args.fp64_steps, 1, flush, dev)
-        errs = []
-        for i in range(len(problems)):
-            errs.append(rel_err(A_mixed[i], sess64.download(i)))
+        A64 = [sess64.download(i) for i in range(len(problems))]
+        errs = [rel_err(A_mixed[i], A64[i]) for i in range(len(problems))]
         sess64.close()
         a64 = algorithmic_flops(st64, problems64[0][2], kernel0) / (st64["ms_quad"] / 1000.0) / 1e12
         line["fp64"] = {"value": p64 / s64, "unit": "pairs/s", "steps": args.fp64_steps,
@@ -421,6 +395,17 @@ def run_gpu(args, rank=0, world=1, dist=None):
                                    "per_problem": len(errs) > 1, "bound": 1e-6}
     elif world == 1:
         line["fp64"] = {"skipped": "pass --fp64-steps K to time the all-FP64 path on this workload"}
+    dg = reference_digest(args)
+    if dg is not None:
+        ref = {"oracle": "the reference's own src/*.cpp, FP64, compiled against project-written Armadillo/METIS "
+                         "stand-ins (oracle/ref.mk); digest of its assembly of this workload "
+                         "(tests/golden/digest_*.npz: pattern hash, A u for a seeded Gaussian u or bilinear probes, "
+                         "sampled rows)",
+               "ref_cpu_seconds": float(dg[1].get("ref_seconds", 0.0)), "ref_threads": int(dg[1].get("ref_threads", 0)),
+               "mixed": vs_reference(A_mixed, dg), "bound_mixed": 1e-6}
+        if A64 is not None:
+            ref["fp64"] = vs_reference(A64, dg)
+        line["rel_err_vs_oracle"] = ref
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         p, s, ns = cpu_sample(problems, args.cpu_seconds, threads)

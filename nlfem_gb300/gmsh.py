@@ -139,41 +139,43 @@ def read_msh(filename):
 
 
 def add_artificial_vertex(lines, vertices, elements, elementlabels):
-    """Appends a vertex at (0, 0) and one label-0 element per line cell (mesh.py:23-33)."""
-    n_vertex = vertices.shape[0]
-    vertices = np.concatenate([vertices, [[0.0, 0.0]]])
-    new_elements = np.array([[*line, n_vertex] for line in lines], dtype=np.int64).reshape(-1, 3)
-    elements = np.concatenate([elements, new_elements])
-    elementlabels = np.concatenate([elementlabels, np.zeros(new_elements.shape[0], dtype=np.int64)])
-    return vertices, elements, elementlabels
+    """Search bridges across a boundary: one extra vertex at the origin and, per line cell (a, b),
+    a degenerate element (a, b, extra) labelled 0. Label-0 elements carry no quadrature; they
+    only connect the breadth-first pair search (the convention of the reference's gmsh tutorial,
+    examples/tutorial/mesh.py:23-33)."""
+    lines = np.asarray(lines, dtype=np.int64).reshape(-1, 2)
+    extra = vertices.shape[0]
+    bridges = np.column_stack([lines, np.full(lines.shape[0], extra, dtype=np.int64)])
+    origin = np.zeros((1, vertices.shape[1]))
+    return (np.vstack([vertices, origin]), np.vstack([elements, bridges]),
+            np.concatenate([elementlabels, np.zeros(lines.shape[0], dtype=np.int64)]))
 
 
 def trim_artificial_vertex(nlfem_mesh, u=None, f_base=None):
-    """Removes the label-0 elements and vertices again (mesh.py:36-46)."""
-    nlfem_mesh["elements"] = nlfem_mesh["elements"][nlfem_mesh["elementLabels"] != 0]
-    nlfem_mesh["vertices"] = nlfem_mesh["vertices"][nlfem_mesh["vertexLabels"] != 0]
-    nlfem_mesh["vertexLabels"] = nlfem_mesh["vertexLabels"][nlfem_mesh["vertexLabels"] != 0]
-    nlfem_mesh["elementLabels"] = nlfem_mesh["elementLabels"][nlfem_mesh["elementLabels"] != 0]
-    if u is not None:
-        u = u[nlfem_mesh["solutionLabels"] != 0]
-    if f_base is not None:
-        f_base = f_base[nlfem_mesh["solutionLabels"] != 0]
-    nlfem_mesh["solutionLabels"] = nlfem_mesh["solutionLabels"][nlfem_mesh["solutionLabels"] != 0]
+    """Undoes add_artificial_vertex after a solve: the label-0 elements and vertices leave the
+    mesh dict (changed in place and returned), and u / f_base keep the entries whose solution
+    label is nonzero (examples/tutorial/mesh.py:36-46)."""
+    masks = {"element": nlfem_mesh["elementLabels"] != 0, "vertex": nlfem_mesh["vertexLabels"] != 0,
+             "solution": nlfem_mesh["solutionLabels"] != 0}
+    for key, kind in (("elements", "element"), ("elementLabels", "element"),
+                      ("vertices", "vertex"), ("vertexLabels", "vertex"), ("solutionLabels", "solution")):
+        nlfem_mesh[key] = nlfem_mesh[key][masks[kind]]
+    u, f_base = (None if a is None else a[masks["solution"]] for a in (u, f_base))
     return nlfem_mesh, u, f_base
 
 
 def read_gmsh(filename, set_art_vertex=True):
-    """(vertices (n, 2), elements (m, 3), element labels (m,)) of a 2D gmsh file
-    (mesh.py:49-58): the largest physical tag is negated; with set_art_vertex the line cells
-    become label-0 elements through an artificial vertex at (0, 0)."""
+    """(vertices (n, 2), elements (m, 3), element labels (m,)) of a 2D gmsh file: the triangles
+    with their physical tags as labels, where the largest tag names the interaction layer and
+    becomes negative; with set_art_vertex the line cells become label-0 bridges
+    (examples/tutorial/mesh.py:49-58)."""
     pts, cells = read_msh(filename)
     if 2 not in cells:
         raise ValueError("the gmsh file holds no triangles")
+    elements, tags = cells[2]
+    labels = np.where(tags == tags.max(), -tags, tags)
     vertices = np.array(pts[:, :2])
-    elements, elementlabels = cells[2]
-    elementlabels = elementlabels.copy()
-    elementlabels[elementlabels == np.max(elementlabels)] *= -1
-    if set_art_vertex:
-        lines = cells[1][0] if 1 in cells else np.zeros((0, 2), dtype=np.int64)
-        vertices, elements, elementlabels = add_artificial_vertex(lines, vertices, elements, elementlabels)
-    return vertices, elements, elementlabels
+    if not set_art_vertex:
+        return vertices, elements, labels
+    lines = cells[1][0] if 1 in cells else np.zeros((0, 2), dtype=np.int64)
+    return add_artificial_vertex(lines, vertices, elements, labels)

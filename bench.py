@@ -395,6 +395,26 @@ def run_gpu(args, rank=0, world=1, dist=None):
                                    "per_problem": len(errs) > 1, "bound": 1e-6}
     elif world == 1:
         line["fp64"] = {"skipped": "pass --fp64-steps K to time the all-FP64 path on this workload"}
+    # the same one-sided algorithm (classes, closed forms, fixed-point scatter) in FP64 arithmetic:
+    # the ratio to it is what the precision alone buys
+    A1 = None
+    if world == 1 and not args.no_fp64 and args.workload in ("c1", "c2", "c3", "c5"):
+        problems1, _ = workload(args, "fp64-onesided")
+        p1, s1, st1, _, clk1, sess1 = timed_session(problems1, args.fp64_steps, 1, flush, dev)
+        A1 = [sess1.download(i) for i in range(len(problems1))]
+        sess1.close()
+        a1 = algorithmic_flops(st1, dict(problems1[0][2], precision="mixed"), kernel0) / (st1["ms_quad"] / 1000.0) / 1e12
+        line["fp64_same_algorithm"] = {
+            "value": p1 / s1, "unit": "pairs/s", "steps": args.fp64_steps, "ms_per_step": 1000.0 * s1 / args.fp64_steps,
+            "mixed_over_fp64_same_algorithm": value / (p1 / s1),
+            "phase_ms": {"dual+bfs+pairs+color": st1["ms_bfs"], "pattern": st1["ms_pattern"],
+                         "quadrature+scatter": st1["ms_quad"], "finish": st1["ms_finish"]},
+            "roofline": {"bound": "fp64", "achieved": a1, "peak": peak64, "unit": "TFLOP/s", "frac": a1 / peak64,
+                         "note": "the mixed path's FLOP model over the FP64 instance's quadrature phase"},
+            "note": "precision \"fp64-onesided\": the headline's one-sided pass, closed forms and fixed-point sums "
+                    "in FP64 arithmetic (FP64 class tests, the exact FP64 polygon routine); the plain FP64 arm "
+                    "beside it is the reference's two-sided algorithm on the GPU",
+            "clocks": clk1}
     dg = reference_digest(args)
     if dg is not None:
         ref = {"oracle": "the reference's own src/*.cpp, FP64, compiled against project-written Armadillo/METIS "
@@ -405,6 +425,8 @@ def run_gpu(args, rank=0, world=1, dist=None):
                "mixed": vs_reference(A_mixed, dg), "bound_mixed": 1e-6}
         if A64 is not None:
             ref["fp64"] = vs_reference(A64, dg)
+        if A1 is not None:
+            ref["fp64_same_algorithm"] = vs_reference(A1, dg)
         line["rel_err_vs_oracle"] = ref
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1

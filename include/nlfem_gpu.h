@@ -41,6 +41,9 @@ extern "C" {
 /* arithmetic of the quadrature */
 #define NLFEM_PREC_FP64 0       /* all FP64, the reference's arithmetic */
 #define NLFEM_PREC_MIXED 1      /* FP32 quadrature, FP64 cut geometry and accumulation */
+#define NLFEM_PREC_FP64_ONESIDED 2 /* FP64 arithmetic in the mixed path's algorithm (one-sided pass,
+                                      closed forms, fixed-point sums): 2D retriangulate only; it
+                                      measures what the precision alone costs */
 
 /* One assembly problem. Arrays are borrowed host pointers, row-major. */
 typedef struct nlfem_problem {
@@ -68,7 +71,7 @@ typedef struct nlfem_problem {
                                     NULL (= method_remote) */
     int is_PlacePointOnCap;
     int is_fullConnectedComponentSearch;
-    int precision;               /* NLFEM_PREC_FP64 or NLFEM_PREC_MIXED */
+    int precision;               /* NLFEM_PREC_FP64, NLFEM_PREC_MIXED or NLFEM_PREC_FP64_ONESIDED */
     int verbose;
     /* domain decomposition (Cassemble.cpp:649-657), nZeta > 0: element -> subdomain indicator
      * in CSR (nE + 1 row pointers, sorted column indices per row); each pair's four blocks are

@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(HERE, "libnlfem_gpu.so")
 NLFEM_OK = 0
 NLFEM_PREC_FP64 = 0
 NLFEM_PREC_MIXED = 1
+NLFEM_PREC_FP64_ONESIDED = 2
 ERRORS = {1: "invalid input", 2: "CUDA error", 3: "out of memory", 4: "unsupported option",
           5: "degenerate element", 6: "device wait timed out"}
 

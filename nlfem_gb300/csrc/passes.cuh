@@ -248,19 +248,21 @@ __device__ __forceinline__ DF warp_sum_df(DF v) {
 }
 
 // ---------------------------------------------------------------- rule-derived constants
-struct PassRule {
-    float cx[MAXQ * 4];     // dx_k * psi_a(P_k)
-    float cxx[MAXQ * 10];   // dx_k * psi_a psi_b (P_k), upper triangle
-    float cyy[MAXQ * 10];   // dy_i * psi_a psi_b (P_i), upper triangle
-    float cy[MAXQ * 4];     // dy_i * psi_a (P_i)
-    float dxf[MAXQ];
-    float pyf[MAXQ * 3];    // inner points P_i (FP32, any dimension)
+template <typename R>
+struct PassRuleT {
+    R cx[MAXQ * 4];     // dx_k * psi_a(P_k)
+    R cxx[MAXQ * 10];   // dx_k * psi_a psi_b (P_k), upper triangle
+    R cyy[MAXQ * 10];   // dy_i * psi_a psi_b (P_i), upper triangle
+    R cy[MAXQ * 4];     // dy_i * psi_a (P_i)
+    R dxf[MAXQ];
+    R pyf[MAXQ * 3];    // inner points P_i (FP32, any dimension)
     // Constant kernels: the inner rule's sums over a whole element, sum_i dy_i * (1, psi_a,
     // psi_a psi_b (upper triangle)), and (2D) its moments sum_i dy_i * (1, px, py, px^2, px py,
     // py^2) over the reference triangle.
-    float insum[1 + 4 + 10];
-    float mom[6];
+    R insum[1 + 4 + 10];
+    R mom[6];
 };
+typedef PassRuleT<float> PassRule;
 
 
 // ---------------------------------------------------------------- FP32 pair quadrature (2D)

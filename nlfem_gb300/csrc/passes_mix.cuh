@@ -14,11 +14,94 @@
 // Close pairs of the singular kernel take their four FP64 blocks from closebuf instead.
 // Contributions are added to the CSR values as 64-bit fixed-point integers (slots.cuh), so the
 // matrix does not depend on the order in which warps finish.
+//
+// The pass is written once for its arithmetic type R. R = float is the mixed path: certified FP32
+// geometry with the exact FP64 routine as fallback, FP32 quadrature and folds. R = double runs the
+// same algorithm (same work split, classes, closed forms and fixed-point scatter) in FP64: classes
+// by FP64 tests with a 2^-40 margin, every cut polygon from the exact FP64 routine (the reference's
+// own), FP64 sums. Comparing the two isolates what the precision alone costs.
 #pragma once
 #include "passes.cuh"
 #include "slots.cuh"
 
 namespace nlg {
+
+struct D2 {
+    double x, y;
+};
+__device__ __forceinline__ D2 operator-(D2 a, D2 b) { return D2{a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ D2 operator+(D2 a, D2 b) { return D2{a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ double dot(D2 a, D2 b) { return fma(a.x, b.x, a.y * b.y); }
+
+// Arithmetic of the pass in type R: the 2-vector type, fused multiply-add, and the FP32 or FP64
+// forms of the kernel, the class test, the cut polygon and the fixed-point conversion.
+template <typename R> struct Ar;
+template <> struct Ar<float> {
+    typedef F2 V;
+    static __device__ __forceinline__ V v(float x, float y) { return F2{x, y}; }
+    static __device__ __forceinline__ float fm(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float ab(float a) { return fabsf(a); }
+    static __device__ __forceinline__ float ker(const ProbParams &P, float z0, float z1) { return kernel_f32(P, z0, z1); }
+    static __device__ __forceinline__ float kc(const ProbParams &P) { return P.kc_f; }
+    static __device__ __forceinline__ float sqd(const ProbParams &P) { return P.sqdelta_f; }
+    static __device__ __forceinline__ int cls(const F2 *Q, float sq) { return fclassify(Q, sq); }
+    static __device__ __forceinline__ int poly(const F2 *Q, const ProbParams &P, const double *x64, const double *E64,
+                                               F2 *Rp, unsigned &namb) {
+        return cut_polygon(Q, P.sqdelta_f, P, x64, E64, Rp, namb);
+    }
+    static __device__ __forceinline__ long long fx(float v, const ProbParams &P, bool &bad) { return fx64(v, P.fx_mul, bad); }
+    static __device__ __forceinline__ const float *py(const Rule &r) { return r.Pyf; }
+    static __device__ __forceinline__ const float *dy(const Rule &r) { return r.dyf; }
+};
+
+constexpr double MARG_D64 = 1.0 / 1099511627776.0;   // 2^-40, far above FP64 rounding of the tests
+
+__device__ __forceinline__ bool dseg_far(D2 p, D2 q, double lim) {
+    const D2 u = q - p;
+    const double uu = dot(u, u), pu = dot(p, u);
+    if (!(pu < 0.0 && -pu < uu)) return true;   // the closest point is an end point
+    const double cr = fma(p.x, u.y, -p.y * u.x);
+    return cr * cr > lim * uu;
+}
+
+template <> struct Ar<double> {
+    typedef D2 V;
+    static __device__ __forceinline__ V v(double x, double y) { return D2{x, y}; }
+    static __device__ __forceinline__ double fm(double a, double b, double c) { return fma(a, b, c); }
+    static __device__ __forceinline__ double ab(double a) { return fabs(a); }
+    static __device__ __forceinline__ double ker(const ProbParams &P, double z0, double z1) {
+        switch (P.kernel) {
+        case KER_PARABOLA: return P.kc * (P.sqdelta - (z0 * z0 + z1 * z1));
+        case KER_FRACTIONAL: return P.kc * exp2(-0.5 * P.expo * log2(z0 * z0 + z1 * z1));
+        default: return P.kc;
+        }
+    }
+    static __device__ __forceinline__ double kc(const ProbParams &P) { return P.kc; }
+    static __device__ __forceinline__ double sqd(const ProbParams &P) { return P.sqdelta; }
+    // IN and OUT only with a margin of 2^-40; everything else goes to the exact polygon
+    static __device__ __forceinline__ int cls(const D2 *Q, double sq) {
+        const double sqlo = sq * (1.0 - MARG_D64), sqhi = sq * (1.0 + MARG_D64);
+        const double d0 = dot(Q[0], Q[0]), d1 = dot(Q[1], Q[1]), d2 = dot(Q[2], Q[2]);
+        if (d0 < sqlo && d1 < sqlo && d2 < sqlo) return CLS_IN;
+        if (fmin(fmin(d0, d1), d2) > sqhi && dseg_far(Q[0], Q[1], sqhi) && dseg_far(Q[1], Q[2], sqhi) &&
+            dseg_far(Q[2], Q[0], sqhi))
+            return CLS_OUT;
+        return CLS_CUT;
+    }
+    // the reference's polygon (exact FP64 routine), relative to the ball center
+    static __device__ __forceinline__ int poly(const D2 *, const ProbParams &P, const double *x64, const double *E64,
+                                               D2 *Rp, unsigned &) {
+        double R64[18];
+        const int n = xretriangulate(x64, E64, P.sqdelta, P.caps, R64);
+        for (int j = 0; j < n; j++) Rp[j] = D2{R64[2 * j] - x64[0], R64[2 * j + 1] - x64[1]};
+        return n;
+    }
+    static __device__ __forceinline__ long long fx(double v, const ProbParams &P, bool &bad) {
+        return fx64d(v, (double)P.fx_mul, bad);
+    }
+    static __device__ __forceinline__ const double *py(const Rule &r) { return r.Py; }
+    static __device__ __forceinline__ const double *dy(const Rule &r) { return r.dy; }
+};
 
 constexpr int MIX_WARPS = 4;
 constexpr int MIX_THREADS = 32 * MIX_WARPS;
@@ -27,9 +110,10 @@ constexpr int RES_N = 10;   // per item: innerLocal, innerNonloc[3], inner termL
 // Per-warp shared scratch; nPx-dependent arrays follow the struct in dynamic shared memory:
 // the outer points of T (FP64, exact; FP32 relative to T's vertex 0), the item results and the
 // item lists.
+template <typename R>
 struct MixWarp {
-    float pc[32][6];        // partner element, local coordinates
-    float prt[32];          // partner |det|
+    R pc[32][6];            // partner element, local coordinates
+    R prt[32];              // partner |det|
     int pid[32];            // partner element
     long long rhb[3], rrb[3];   // T's rows: hash table start, CSR row start
     unsigned rmask[3];          // T's rows: hash capacity - 1 (0xffffffff: no row)
@@ -41,14 +125,17 @@ struct ScatEntry {
     int col, pad;
     long long v[6];
 };
+template <typename R>
 __host__ __device__ constexpr size_t mix_res_bytes(int nPx) {
-    return (size_t)32 * nPx * RES_N * 4 > 96 * sizeof(ScatEntry) ? (size_t)32 * nPx * RES_N * 4 : 96 * sizeof(ScatEntry);
+    return (size_t)32 * nPx * RES_N * sizeof(R) > 96 * sizeof(ScatEntry) ? (size_t)32 * nPx * RES_N * sizeof(R)
+                                                                          : 96 * sizeof(ScatEntry);
 }
+template <typename R>
 __host__ __device__ constexpr size_t mix_warp_bytes(int nPx) {
-    // MixWarp + x64[nPx * 2] doubles + xf[nPx] F2 + res[32][nPx][RES_N] floats (or the scatter
+    // MixWarp + x64[nPx * 2] doubles + xf[nPx] 2-vectors + res[32][nPx][RES_N] (or the scatter
     // list) + lists[2][32 * nPx] shorts
-    return ((sizeof(MixWarp) + 15) / 16) * 16 + (size_t)nPx * 16 + ((size_t)nPx * 8 + 15) / 16 * 16 +
-           mix_res_bytes(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
+    return ((sizeof(MixWarp<R>) + 15) / 16) * 16 + (size_t)nPx * 16 + ((size_t)nPx * 2 * sizeof(R) + 15) / 16 * 16 +
+           mix_res_bytes<R>(nPx) + (size_t)2 * 32 * nPx * 2 + 16;
 }
 
 
@@ -64,61 +151,68 @@ struct MixArgs {
 };
 
 // Inner sums of one "inside" item: the ball around x contains the partner element b.
-__device__ __forceinline__ void item_in(const ProbParams &P, const Rule &rule, const PassRule &pr,
-                                        const float *pc, float rT, F2 x, float *res) {
-    const F2 p0 = f2(pc[0] - x.x, pc[1] - x.y);
-    const F2 e1 = f2(pc[2] - pc[0], pc[3] - pc[1]), e2 = f2(pc[4] - pc[0], pc[5] - pc[1]);
-    float iL = 0.f, i0 = 0.f, i1 = 0.f, i2 = 0.f;
-    float lp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+template <typename R>
+__device__ __forceinline__ void item_in(const ProbParams &P, const Rule &rule, const PassRuleT<R> &pr,
+                                        const R *pc, R rT, typename Ar<R>::V x, R *res) {
+    typedef Ar<R> A;
+    const R *Py = A::py(rule), *dy = A::dy(rule);
+    const typename A::V p0 = A::v(pc[0] - x.x, pc[1] - x.y);
+    const typename A::V e1 = A::v(pc[2] - pc[0], pc[3] - pc[1]), e2 = A::v(pc[4] - pc[0], pc[5] - pc[1]);
+    R iL = 0, i0 = 0, i1 = 0, i2 = 0;
+    R lp[6] = {0, 0, 0, 0, 0, 0};
     for (int i = 0; i < rule.nPy; i++) {
-        const float px = rule.Pyf[2 * i], py = rule.Pyf[2 * i + 1];
-        const float yx = p0.x + e1.x * px + e2.x * py;
-        const float yy = p0.y + e1.y * px + e2.y * py;
-        const float kw = kernel_f32(P, -yx, -yy) * rT;
-        iL = fmaf(kw, rule.dyf[i], iL);
-        i0 = fmaf(kw, pr.cy[3 * i + 0], i0);
-        i1 = fmaf(kw, pr.cy[3 * i + 1], i1);
-        i2 = fmaf(kw, pr.cy[3 * i + 2], i2);
+        const R px = Py[2 * i], py = Py[2 * i + 1];
+        const R yx = p0.x + e1.x * px + e2.x * py;
+        const R yy = p0.y + e1.y * px + e2.y * py;
+        const R kw = A::ker(P, -yx, -yy) * rT;
+        iL = A::fm(kw, dy[i], iL);
+        i0 = A::fm(kw, pr.cy[3 * i + 0], i0);
+        i1 = A::fm(kw, pr.cy[3 * i + 1], i1);
+        i2 = A::fm(kw, pr.cy[3 * i + 2], i2);
 #pragma unroll
-        for (int ab = 0; ab < 6; ab++) lp[ab] = fmaf(kw, pr.cyy[6 * i + ab], lp[ab]);
+        for (int ab = 0; ab < 6; ab++) lp[ab] = A::fm(kw, pr.cyy[6 * i + ab], lp[ab]);
     }
     res[0] = iL; res[1] = i0; res[2] = i1; res[3] = i2;
 #pragma unroll
     for (int ab = 0; ab < 6; ab++) res[4 + ab] = lp[ab];
 }
 
-// Inner sums of one "cut" item: polygon of B(x) and b (certified FP32, exact FP64 fallback), fan
-// sub-triangles, basis of b by the inverse affine map.
-__device__ __forceinline__ void item_cut(const ProbParams &P, const Rule &rule, const float *pc, F2 x,
-                                         const double *x64, const double *Eb64, float *res,
+// Inner sums of one "cut" item: polygon of B(x) and b (certified FP32 with the exact FP64
+// fallback, or the exact FP64 routine), fan sub-triangles, basis of b by the inverse affine map.
+template <typename R>
+__device__ __forceinline__ void item_cut(const ProbParams &P, const Rule &rule, const R *pc, typename Ar<R>::V x,
+                                         const double *x64, const double *Eb64, R *res,
                                          unsigned &nsub, unsigned &namb) {
-    const F2 Q[3] = {f2(pc[0] - x.x, pc[1] - x.y), f2(pc[2] - x.x, pc[3] - x.y), f2(pc[4] - x.x, pc[5] - x.y)};
-    const F2 e1 = Q[1] - Q[0], e2 = Q[2] - Q[0];
-    const float idet = 1.f / (e1.x * e2.y - e1.y * e2.x);
-    F2 R[9];
-    const int n = cut_polygon(Q, P.sqdelta_f, P, x64, Eb64, R, namb);
-    float iL = 0.f, i0 = 0.f, i1 = 0.f, i2 = 0.f;
-    float lp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    typedef Ar<R> A;
+    typedef typename A::V V;
+    const R *Py = A::py(rule), *dy = A::dy(rule);
+    const V Q[3] = {A::v(pc[0] - x.x, pc[1] - x.y), A::v(pc[2] - x.x, pc[3] - x.y), A::v(pc[4] - x.x, pc[5] - x.y)};
+    const V e1 = Q[1] - Q[0], e2 = Q[2] - Q[0];
+    const R idet = R(1) / (e1.x * e2.y - e1.y * e2.x);
+    V Rp[9];
+    const int n = A::poly(Q, P, x64, Eb64, Rp, namb);
+    R iL = 0, i0 = 0, i1 = 0, i2 = 0;
+    R lp[6] = {0, 0, 0, 0, 0, 0};
     for (int r = 0; r + 2 < n; r++) {
         nsub++;
-        const F2 A = R[0], B = R[r + 1] - R[0], C = R[r + 2] - R[0];
-        const float rT = fabsf(B.x * C.y - B.y * C.x);
+        const V Av = Rp[0], B = Rp[r + 1] - Rp[0], C = Rp[r + 2] - Rp[0];
+        const R rT = A::ab(B.x * C.y - B.y * C.x);
         for (int i = 0; i < rule.nPy; i++) {
-            const float px = rule.Pyf[2 * i], py = rule.Pyf[2 * i + 1];
-            const float yx = A.x + B.x * px + C.x * py;
-            const float yy = A.y + B.y * px + C.y * py;
-            const float kw = kernel_f32(P, -yx, -yy) * rT * rule.dyf[i];
-            const float dxr = yx - Q[0].x, dyr = yy - Q[0].y;
-            const float r0 = (e2.y * dxr - e2.x * dyr) * idet;
-            const float r1 = (e1.x * dyr - e1.y * dxr) * idet;
-            const float s0 = 1.f - r0 - r1;
+            const R px = Py[2 * i], py = Py[2 * i + 1];
+            const R yx = Av.x + B.x * px + C.x * py;
+            const R yy = Av.y + B.y * px + C.y * py;
+            const R kw = A::ker(P, -yx, -yy) * rT * dy[i];
+            const R dxr = yx - Q[0].x, dyr = yy - Q[0].y;
+            const R r0 = (e2.y * dxr - e2.x * dyr) * idet;
+            const R r1 = (e1.x * dyr - e1.y * dxr) * idet;
+            const R s0 = R(1) - r0 - r1;
             iL += kw;
-            i0 = fmaf(kw, s0, i0);
-            i1 = fmaf(kw, r0, i1);
-            i2 = fmaf(kw, r1, i2);
-            lp[0] = fmaf(kw, s0 * s0, lp[0]); lp[1] = fmaf(kw, s0 * r0, lp[1]);
-            lp[2] = fmaf(kw, s0 * r1, lp[2]); lp[3] = fmaf(kw, r0 * r0, lp[3]);
-            lp[4] = fmaf(kw, r0 * r1, lp[4]); lp[5] = fmaf(kw, r1 * r1, lp[5]);
+            i0 = A::fm(kw, s0, i0);
+            i1 = A::fm(kw, r0, i1);
+            i2 = A::fm(kw, r1, i2);
+            lp[0] = A::fm(kw, s0 * s0, lp[0]); lp[1] = A::fm(kw, s0 * r0, lp[1]);
+            lp[2] = A::fm(kw, s0 * r1, lp[2]); lp[3] = A::fm(kw, r0 * r0, lp[3]);
+            lp[4] = A::fm(kw, r0 * r1, lp[4]); lp[5] = A::fm(kw, r1 * r1, lp[5]);
         }
     }
     res[0] = iL; res[1] = i0; res[2] = i1; res[3] = i2;
@@ -136,53 +230,56 @@ __device__ __forceinline__ void item_cut(const ProbParams &P, const Rule &rule, 
 // This equals the quadrature sum of the general item for any rule. The basis values come from the
 // polygon's points (one evaluation per point instead of per inner point), and every sum stays in
 // the basis functions' own range, so no cancellation enters where a basis function is small.
-__device__ __forceinline__ void item_cut_const(const ProbParams &P, const PassRule &pr, const float *pc, F2 x,
-                                               const double *x64, const double *Eb64, float *res,
+template <typename R>
+__device__ __forceinline__ void item_cut_const(const ProbParams &P, const PassRuleT<R> &pr, const R *pc,
+                                               typename Ar<R>::V x, const double *x64, const double *Eb64, R *res,
                                                unsigned &nsub, unsigned &namb) {
-    const F2 Q[3] = {f2(pc[0] - x.x, pc[1] - x.y), f2(pc[2] - x.x, pc[3] - x.y), f2(pc[4] - x.x, pc[5] - x.y)};
-    const F2 e1 = Q[1] - Q[0], e2 = Q[2] - Q[0];
-    const float idet = 1.f / (e1.x * e2.y - e1.y * e2.x);
-    F2 R[9];
-    const int n = cut_polygon(Q, P.sqdelta_f, P, x64, Eb64, R, namb);
-    const float m0 = pr.mom[0], mx = pr.mom[1], my = pr.mom[2], mxx = pr.mom[3], mxy = pr.mom[4], myy = pr.mom[5];
-    auto basis = [&](F2 y, float *l) {   // psi_0..2 of b at y (as the general item evaluates them)
-        const float dxr = y.x - Q[0].x, dyr = y.y - Q[0].y;
+    typedef Ar<R> A;
+    typedef typename A::V V;
+    const V Q[3] = {A::v(pc[0] - x.x, pc[1] - x.y), A::v(pc[2] - x.x, pc[3] - x.y), A::v(pc[4] - x.x, pc[5] - x.y)};
+    const V e1 = Q[1] - Q[0], e2 = Q[2] - Q[0];
+    const R idet = R(1) / (e1.x * e2.y - e1.y * e2.x);
+    V Rp[9];
+    const int n = A::poly(Q, P, x64, Eb64, Rp, namb);
+    const R m0 = pr.mom[0], mx = pr.mom[1], my = pr.mom[2], mxx = pr.mom[3], mxy = pr.mom[4], myy = pr.mom[5];
+    auto basis = [&](V y, R *l) {   // psi_0..2 of b at y (as the general item evaluates them)
+        const R dxr = y.x - Q[0].x, dyr = y.y - Q[0].y;
         l[1] = (e2.y * dxr - e2.x * dyr) * idet;
         l[2] = (e1.x * dyr - e1.y * dxr) * idet;
-        l[0] = 1.f - l[1] - l[2];
+        l[0] = R(1) - l[1] - l[2];
     };
-    float S0 = 0.f, S1[3] = {0.f, 0.f, 0.f}, S2[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    float la[3], lb[3], lc[3];
+    R S0 = 0, S1[3] = {0, 0, 0}, S2[6] = {0, 0, 0, 0, 0, 0};
+    R la[3], lb[3], lc[3];
     if (n >= 3) {
-        basis(R[0], la);
-        basis(R[1], lb);
+        basis(Rp[0], la);
+        basis(Rp[1], lb);
     }
     for (int r = 0; r + 2 < n; r++) {
         nsub++;
-        const F2 B = R[r + 1] - R[0], C = R[r + 2] - R[0];
-        const float rT = fabsf(B.x * C.y - B.y * C.x);
-        basis(R[r + 2], lc);
-        float t0[3], t1[3], t2[3];
+        const V B = Rp[r + 1] - Rp[0], C = Rp[r + 2] - Rp[0];
+        const R rT = A::ab(B.x * C.y - B.y * C.x);
+        basis(Rp[r + 2], lc);
+        R t0[3], t1[3], t2[3];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const float al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
-            t0[q] = fmaf(al, m0, fmaf(be, mx, ga * my));
-            t1[q] = fmaf(al, mx, fmaf(be, mxx, ga * mxy));
-            t2[q] = fmaf(al, my, fmaf(be, mxy, ga * myy));
+            const R al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
+            t0[q] = A::fm(al, m0, A::fm(be, mx, ga * my));
+            t1[q] = A::fm(al, mx, A::fm(be, mxx, ga * mxy));
+            t2[q] = A::fm(al, my, A::fm(be, mxy, ga * myy));
         }
-        S0 = fmaf(rT, m0, S0);
+        S0 = A::fm(rT, m0, S0);
         int t = 0;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            S1[q] = fmaf(rT, t0[q], S1[q]);
-            const float al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
+            S1[q] = A::fm(rT, t0[q], S1[q]);
+            const R al = la[q], be = lb[q] - la[q], ga = lc[q] - la[q];
 #pragma unroll
-            for (int q2 = q; q2 < 3; q2++, t++) S2[t] = fmaf(rT, fmaf(al, t0[q2], fmaf(be, t1[q2], ga * t2[q2])), S2[t]);
+            for (int q2 = q; q2 < 3; q2++, t++) S2[t] = A::fm(rT, A::fm(al, t0[q2], A::fm(be, t1[q2], ga * t2[q2])), S2[t]);
         }
 #pragma unroll
         for (int q = 0; q < 3; q++) lb[q] = lc[q];
     }
-    const float kc = P.kc_f;
+    const R kc = A::kc(P);
     res[0] = kc * S0;
 #pragma unroll
     for (int q = 0; q < 3; q++) res[1 + q] = kc * S1[q];
@@ -254,20 +351,23 @@ __device__ __forceinline__ long long shfl64(long long v, int src) {
 // the Duffy blocks. Each instance holds only its class's code, which keeps the kernel small (it is
 // bound by instruction fetch as much as by anything else).
 enum { MIX_CONST = 0, MIX_REGULAR = 1, MIX_SINGULAR = 2 };
-template <int KIND>
-__global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRule pr) {
+template <int KIND, typename R>
+__global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule rule, PassRuleT<R> pr) {
+    typedef Ar<R> A;
+    typedef typename A::V V;
+    constexpr bool F32 = sizeof(R) == 4;
     constexpr bool CK = KIND == MIX_CONST;
     extern __shared__ __align__(16) unsigned char s_raw[];
     const PassArgs &a = ma.p;
     const SlotMap &sm = ma.m;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nPx = rule.nPx;
-    unsigned char *wbase = s_raw + (size_t)wib * mix_warp_bytes(nPx);
-    MixWarp &W = *reinterpret_cast<MixWarp *>(wbase);
-    double *x64 = reinterpret_cast<double *>(wbase + ((sizeof(MixWarp) + 15) / 16) * 16);   // [nPx * 2]
-    F2 *xf = reinterpret_cast<F2 *>(x64 + 2 * nPx);                                          // [nPx]
-    float *res = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(xf) + ((size_t)nPx * 8 + 15) / 16 * 16);   // [32][nPx][RES_N]
-    unsigned short *lst = reinterpret_cast<unsigned short *>(reinterpret_cast<unsigned char *>(res) + mix_res_bytes(nPx));   // [2][32*nPx]
+    unsigned char *wbase = s_raw + (size_t)wib * mix_warp_bytes<R>(nPx);
+    MixWarp<R> &W = *reinterpret_cast<MixWarp<R> *>(wbase);
+    double *x64 = reinterpret_cast<double *>(wbase + ((sizeof(MixWarp<R>) + 15) / 16) * 16);   // [nPx * 2]
+    V *xf = reinterpret_cast<V *>(x64 + 2 * nPx);                                              // [nPx]
+    R *res = reinterpret_cast<R *>(reinterpret_cast<unsigned char *>(xf) + ((size_t)nPx * 2 * sizeof(R) + 15) / 16 * 16);   // [32][nPx][RES_N]
+    unsigned short *lst = reinterpret_cast<unsigned short *>(reinterpret_cast<unsigned char *>(res) + mix_res_bytes<R>(nPx));   // [2][32*nPx]
     ScatEntry *slist = reinterpret_cast<ScatEntry *>(res);   // scatter list, after the fold
     long long *vals = reinterpret_cast<long long *>(a.vals);
     int *ovf = &a.err[5];
@@ -305,17 +405,17 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         const double *ET64 = &a.EC[(long long)T * 6];
         const float ohi0 = a.EChi[(long long)T * 6], ohi1 = a.EChi[(long long)T * 6 + 1];
         const float olo0 = a.EClo[(long long)T * 6], olo1 = a.EClo[(long long)T * 6 + 1];
-        const float rTT = a.adetf[T];
+        const R rTT = F32 ? (R)a.adetf[T] : (R)a.adet[T];
         for (int k = lane; k < nPx; k += 32) {
             xtoPhys<2>(ET64, &rule.Px[2 * k], &x64[2 * k]);
-            xf[k] = f2((float)(x64[2 * k] - ET64[0]), (float)(x64[2 * k + 1] - ET64[1]));
+            xf[k] = A::v((R)(x64[2 * k] - ET64[0]), (R)(x64[2 * k + 1] - ET64[1]));
         }
         __syncwarp();
         long long D[6];   // termLocal of T's pairs, integer sums
 #pragma unroll
         for (int i = 0; i < 6; i++) D[i] = 0;
         const bool frac_close = KIND == MIX_SINGULAR && P.singular && P.close == MTH_FRACTIONAL;
-        const float sqf = P.sqdelta_f;
+        const R sqf = A::sqd(P);
         int part_next = lb + lane < le ? a.pB[lb + lane] : T;   // partners one batch ahead
         for (long long p0 = lb; p0 < le; p0 += 32) {
             const long long p = p0 + lane;
@@ -334,38 +434,42 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     for (int j = 0; j < 3; j++) close |= (tv[i] == pv[j]);
             }
             // owner: partner data and classes
-            float pc[6];
+            R pc[6];
 #pragma unroll
-            for (int j = 0; j < 6; j++)
-                pc[j] = (a.EChi[(long long)part * 6 + j] - ((j & 1) ? ohi1 : ohi0)) + (a.EClo[(long long)part * 6 + j] - ((j & 1) ? olo1 : olo0));
+            for (int j = 0; j < 6; j++) {
+                if (F32)
+                    pc[j] = (a.EChi[(long long)part * 6 + j] - ((j & 1) ? ohi1 : ohi0)) + (a.EClo[(long long)part * 6 + j] - ((j & 1) ? olo1 : olo0));
+                else
+                    pc[j] = (R)(a.EC[(long long)part * 6 + j] - ET64[j & 1]);
+            }
 #pragma unroll
             for (int j = 0; j < 6; j++) W.pc[lane][j] = pc[j];
-            W.prt[lane] = a.adetf[part];
+            W.prt[lane] = F32 ? (R)a.adetf[part] : (R)a.adet[part];
             W.pid[lane] = part;
-            float inv[RES_N];   // constant kernel: an inside item's sums
+            R inv[RES_N];   // constant kernel: an inside item's sums
             if (CK) {
-                const float kr = P.kc_f * W.prt[lane];
+                const R kr = A::kc(P) * W.prt[lane];
 #pragma unroll
                 for (int q = 0; q < RES_N; q++) inv[q] = kr * pr.insum[q];
             }
             for (int k = 0; k < nPx; k++) {
                 unsigned char c = CLS_OUT;
                 if (act && !close) {
-                    const F2 x = xf[k];
-                    const F2 Q[3] = {f2(pc[0] - x.x, pc[1] - x.y), f2(pc[2] - x.x, pc[3] - x.y), f2(pc[4] - x.x, pc[5] - x.y)};
-                    c = (unsigned char)fclassify(Q, sqf);
+                    const V x = xf[k];
+                    const V Q[3] = {A::v(pc[0] - x.x, pc[1] - x.y), A::v(pc[2] - x.x, pc[3] - x.y), A::v(pc[4] - x.x, pc[5] - x.y)};
+                    c = (unsigned char)A::cls(Q, sqf);
                 }
                 mycls[k] = c;
                 nitin += c == CLS_IN;
                 nitcut += c == CLS_CUT;
-                float *rr = &res[(lane * nPx + k) * RES_N];
+                R *rr = &res[(lane * nPx + k) * RES_N];
                 if (CK && c == CLS_IN) {
                     nsub++;
 #pragma unroll
                     for (int q = 0; q < RES_N; q++) rr[q] = inv[q];
                 } else {
 #pragma unroll
-                    for (int q = 0; q < RES_N; q++) rr[q] = 0.f;
+                    for (int q = 0; q < RES_N; q++) rr[q] = R(0);
                 }
             }
             __syncwarp();
@@ -421,29 +525,29 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                             for (int j = i; j < 3; j++) lpx[sym_idx<3>(i, j)] = fx64d(cb[18 + 3 * i + j], P.fx_mul, bad);
                     }
                 } else {
-                    float L[6] = {0, 0, 0, 0, 0, 0}, N[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-                    float LP[6] = {0, 0, 0, 0, 0, 0};
+                    R L[6] = {0, 0, 0, 0, 0, 0}, N[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    R LP[6] = {0, 0, 0, 0, 0, 0};
                     for (int k = 0; k < nPx; k++) {
-                        const float *rr = &res[(lane * nPx + k) * RES_N];
-                        const float dk = pr.dxf[k];
+                        const R *rr = &res[(lane * nPx + k) * RES_N];
+                        const R dk = pr.dxf[k];
 #pragma unroll
-                        for (int ab = 0; ab < 6; ab++) L[ab] = fmaf(pr.cxx[6 * k + ab], rr[0], L[ab]);
+                        for (int ab = 0; ab < 6; ab++) L[ab] = A::fm(pr.cxx[6 * k + ab], rr[0], L[ab]);
 #pragma unroll
                         for (int r = 0; r < 3; r++) {
-                            const float c = pr.cx[3 * k + r];
-                            N[3 * r + 0] = fmaf(c, rr[1], N[3 * r + 0]);
-                            N[3 * r + 1] = fmaf(c, rr[2], N[3 * r + 1]);
-                            N[3 * r + 2] = fmaf(c, rr[3], N[3 * r + 2]);
+                            const R c = pr.cx[3 * k + r];
+                            N[3 * r + 0] = A::fm(c, rr[1], N[3 * r + 0]);
+                            N[3 * r + 1] = A::fm(c, rr[2], N[3 * r + 1]);
+                            N[3 * r + 2] = A::fm(c, rr[3], N[3 * r + 2]);
                         }
 #pragma unroll
-                        for (int ab = 0; ab < 6; ab++) LP[ab] = fmaf(dk, rr[4 + ab], LP[ab]);
+                        for (int ab = 0; ab < 6; ab++) LP[ab] = A::fm(dk, rr[4 + ab], LP[ab]);
                     }
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lx[i] = fx64(L[i] * rTT, P.fx_mul, bad);
+                    for (int i = 0; i < 6; i++) lx[i] = A::fx(L[i] * rTT, P, bad);
 #pragma unroll
-                    for (int i = 0; i < 9; i++) mx[i] = nx[i] = fx64(N[i] * rTT, P.fx_mul, bad);
+                    for (int i = 0; i < 9; i++) mx[i] = nx[i] = A::fx(N[i] * rTT, P, bad);
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lpx[i] = fx64(LP[i] * rTT, P.fx_mul, bad);
+                    for (int i = 0; i < 6; i++) lpx[i] = A::fx(LP[i] * rTT, P, bad);
                 }
                 balance_rows<3>(lx, nx, lpx, mx);
 #pragma unroll

@@ -185,19 +185,19 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
         if ((P.close == MTH_FRACTIONAL || P.close == MTH_WEAKSING) && p.dim != 2)
             return fail(NLFEM_ERR_UNSUPPORTED, "fractional and weakSingular close pairs are 2D only");
-        if (P.singular && P.close == MTH_WEAKSING && p.precision == NLFEM_PREC_MIXED)
+        if (P.singular && P.close == MTH_WEAKSING && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, "the weakSingular close rule runs on the fp64 path only (precision \"fp64\")");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
         if (p.is_dg && P.singular)   // the close-pair rule needs vertex sharing across element DOFs
             return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with singular kernels (close-pair rule) is not implemented");
-        if (p.is_dg && p.precision == NLFEM_PREC_MIXED)
+        if (p.is_dg && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz runs on the fp64 path only (precision \"fp64\")");
-        if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision == NLFEM_PREC_MIXED)
+        if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, std::string("integration method ") +
                         (P.remote >= MTH_RETRI_UNSYMM ? p.method_remote : p.method_close) + " runs on the fp64 path only (precision \"fp64\")");
         if (P.kernel >= KER_LABELED) {   // label- or position-dependent kernels of 2D meshes
             if (p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " is implemented for 2D meshes only");
-            if (p.precision == NLFEM_PREC_MIXED)
+            if (p.precision != NLFEM_PREC_FP64)
                 return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " runs on the fp64 path only (precision \"fp64\")");
         }
         P.caps = p.is_PlacePointOnCap ? 1 : 0;
@@ -328,6 +328,7 @@ struct Session {
     DevBuf color, color2, colorlist, closeA, closeB, closebuf, touched;
     std::vector<int> color_off;
     int prec = 0;
+    bool onesided64 = false;   // PM_RETRI pass in FP64 (the mixed path's algorithm, FP64 arithmetic)
     DevBuf vcnt, vptr, vel, adjcnt, xadj, adj;
     DevBuf visited, vvisited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
@@ -473,8 +474,9 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
         if ((probs[i].is_dg != 0) != S.dg) return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the ansatz");
     if (S.dg && n > 1) return fail(NLFEM_ERR_UNSUPPORTED, "DG problems assemble one at a time (no batches)");
     S.prec = probs[0].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64;
+    S.onesided64 = probs[0].precision == NLFEM_PREC_FP64_ONESIDED;
     for (int i = 1; i < n; i++)
-        if ((probs[i].precision == NLFEM_PREC_MIXED ? PREC_MIX : PREC_F64) != S.prec)
+        if (probs[i].precision != probs[0].precision)
             return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the precision");
     int r = make_rule(probs[0], system, S.rule);
     if (r) return r;
@@ -498,6 +500,12 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
         S.pmode = PM_COLORED;
         if (S.prec == PREC_MIX && S.dim == 2 && all_retri && !any_zeta) S.pmode = PM_RETRI;
         if (S.prec == PREC_MIX && all_bary && !any_singular && !any_zeta) S.pmode = PM_BARY;
+        if (S.onesided64) {
+            if (!(S.dim == 2 && all_retri && !any_zeta))
+                return fail(NLFEM_ERR_UNSUPPORTED, "precision \"fp64-onesided\" covers the 2D retriangulate rule "
+                                                   "without domain-decomposition weights");
+            S.pmode = PM_RETRI;
+        }
     }
     const int dV = S.dV, dim = S.dim;
     ENS(S.T64, sizeof(long long) * S.nE * dV);
@@ -1163,29 +1171,30 @@ static int run_pair_blocks(Session &S, long long n, const long *pairs, int close
     return d2h(S, ret, S.keepcnt.get<int>(), (size_t)n);
 }
 
-static PassRule make_pass_rule(const Rule &r, int dim) {
-    PassRule pr;
+template <typename R>
+static PassRuleT<R> make_pass_rule(const Rule &r, int dim) {
+    PassRuleT<R> pr;
     memset(&pr, 0, sizeof(pr));
     const int dV = dim + 1, NS = dV * (dV + 1) / 2;
     for (int k = 0; k < r.nPx; k++) {
-        pr.dxf[k] = (float)r.dx[k];
+        pr.dxf[k] = (R)r.dx[k];
         int t = 0;
         for (int a = 0; a < dV; a++) {
-            pr.cx[dV * k + a] = (float)(r.dx[k] * r.psix[dV * k + a]);
-            for (int b = a; b < dV; b++) pr.cxx[NS * k + t++] = (float)(r.dx[k] * r.psix[dV * k + a] * r.psix[dV * k + b]);
+            pr.cx[dV * k + a] = (R)(r.dx[k] * r.psix[dV * k + a]);
+            for (int b = a; b < dV; b++) pr.cxx[NS * k + t++] = (R)(r.dx[k] * r.psix[dV * k + a] * r.psix[dV * k + b]);
         }
     }
     double insum[1 + 4 + 10] = {0}, mom[6] = {0};
     for (int i = 0; i < r.nPy; i++) {
-        for (int c = 0; c < dim; c++) pr.pyf[dim * i + c] = (float)r.Py[dim * i + c];
+        for (int c = 0; c < dim; c++) pr.pyf[dim * i + c] = (R)r.Py[dim * i + c];
         int t = 0;
         insum[0] += r.dy[i];
         for (int a = 0; a < dV; a++) {
-            pr.cy[dV * i + a] = (float)(r.dy[i] * r.psiy[dV * i + a]);
+            pr.cy[dV * i + a] = (R)(r.dy[i] * r.psiy[dV * i + a]);
             insum[1 + a] += r.dy[i] * r.psiy[dV * i + a];
             for (int b = a; b < dV; b++) {
                 insum[1 + dV + t] += r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b];
-                pr.cyy[NS * i + t++] = (float)(r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b]);
+                pr.cyy[NS * i + t++] = (R)(r.dy[i] * r.psiy[dV * i + a] * r.psiy[dV * i + b]);
             }
         }
         if (dim == 2) {
@@ -1194,8 +1203,8 @@ static PassRule make_pass_rule(const Rule &r, int dim) {
             mom[3] += w * px * px; mom[4] += w * px * py; mom[5] += w * py * py;
         }
     }
-    for (int q = 0; q < 1 + 4 + 10; q++) pr.insum[q] = (float)insum[q];
-    for (int q = 0; q < 6; q++) pr.mom[q] = (float)mom[q];
+    for (int q = 0; q < 1 + 4 + 10; q++) pr.insum[q] = (R)insum[q];
+    for (int q = 0; q < 6; q++) pr.mom[q] = (R)mom[q];
     return pr;
 }
 
@@ -1234,7 +1243,9 @@ static int run_close(Session &S) {
 // first), so every problem goes through the same code as its single assembly and the batch matrices
 // equal the single ones bit for bit. A contribution outside the fixed-point range sets err[5]; the
 // pass is then redone with a unit 2^16 times coarser.
-typedef void (*OneSidedKernel)(MixArgs, Rule, PassRule);
+template <typename PR>
+using OneSidedKernelT = void (*)(MixArgs, Rule, PR);
+typedef OneSidedKernelT<PassRule> OneSidedKernel;
 // Kernel class of a problem for the one-sided passes: 0 constant kernel (closed forms), 1 other
 // regular kernel, 2 singular kernel with Duffy close pairs.
 static int kernel_class(const ProbParams &q) {
@@ -1242,12 +1253,13 @@ static int kernel_class(const ProbParams &q) {
     return duffy_close(q) ? 2 : 1;
 }
 
-static int run_pass_one_sided(Session &S, const PassArgs &pa, const PassRule &pr, const OneSidedKernel *kfn,
+template <typename PR>
+static int run_pass_one_sided(Session &S, const PassArgs &pa, const PR &pr, const OneSidedKernelT<PR> *kfn,
                               int threads, size_t smem) {
     const long long nnz = S.nnz_struct;
     int ncls[3] = {0, 0, 0};
     for (const ProbParams &q : S.hprm) ncls[kernel_class(q)]++;
-    struct Launch { OneSidedKernel k; const int *list; int count; int per_sm; };
+    struct Launch { OneSidedKernelT<PR> k; const int *list; int count; int per_sm; };
     Launch L[3];
     int nl = 0;
     for (int c = 0; c < 3; c++)
@@ -1355,10 +1367,17 @@ static int run_passes(Session &S) {
     a.zptr = S.zptr.get<long long>(); a.zidx = S.zidx.get<long long>();
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
-    const PassRule pr = make_pass_rule(S.rule, DIM);
+    const PassRule pr = make_pass_rule<float>(S.rule, DIM);
+    if (S.pmode == PM_RETRI && S.onesided64) {
+        const PassRuleT<double> pr64 = make_pass_rule<double>(S.rule, DIM);
+        const OneSidedKernelT<PassRuleT<double>> k[3] = {k_pass_mix2d<MIX_CONST, double>, k_pass_mix2d<MIX_REGULAR, double>,
+                                                        k_pass_mix2d<MIX_SINGULAR, double>};
+        return run_pass_one_sided(S, a, pr64, k, MIX_THREADS, mix_warp_bytes<double>(S.rule.nPx) * MIX_WARPS);
+    }
     if (S.pmode == PM_RETRI) {
-        const OneSidedKernel k[3] = {k_pass_mix2d<MIX_CONST>, k_pass_mix2d<MIX_REGULAR>, k_pass_mix2d<MIX_SINGULAR>};
-        return run_pass_one_sided(S, a, pr, k, MIX_THREADS, mix_warp_bytes(S.rule.nPx) * MIX_WARPS);
+        const OneSidedKernel k[3] = {k_pass_mix2d<MIX_CONST, float>, k_pass_mix2d<MIX_REGULAR, float>,
+                                     k_pass_mix2d<MIX_SINGULAR, float>};
+        return run_pass_one_sided(S, a, pr, k, MIX_THREADS, mix_warp_bytes<float>(S.rule.nPx) * MIX_WARPS);
     }
     if (S.pmode == PM_BARY) {   // no singular kernels here
         const OneSidedKernel k[3] = {k_pass_bary<DIM, true>, k_pass_bary<DIM, false>, k_pass_bary<DIM, false>};

@@ -16,8 +16,9 @@ reference raises it (output dimension mismatch, bad arma header) and ``NlfemErro
 reference would abort the process.
 
 Extra configuration keys (absent from the reference): ``"precision"``: ``"fp64"`` (default,
-the reference's arithmetic) or ``"mixed"`` (FP32 quadrature with FP64 cut geometry and FP64
-accumulation).
+the reference's arithmetic), ``"mixed"`` (FP32 quadrature with FP64 cut geometry and FP64
+accumulation), or ``"fp64-onesided"`` (the mixed path's algorithm in FP64 arithmetic, 2D
+retriangulate only: it separates what the precision costs from what the algorithm saves).
 """
 import ctypes
 import os
@@ -39,6 +40,8 @@ __all__ = ["stiffnessMatrix", "loadVector", "stiffnessMatrix_fromArray", "meshFr
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _lp = ctypes.POINTER(ctypes.c_long)
+_PRECISIONS = {"fp64": _lib.NLFEM_PREC_FP64, "mixed": _lib.NLFEM_PREC_MIXED,
+               "fp64-onesided": _lib.NLFEM_PREC_FP64_ONESIDED}
 _ip = ctypes.POINTER(ctypes.c_int)
 
 
@@ -138,9 +141,9 @@ class _Problem:
             c.forcing = self._s(load["function"])
             c.fractional_s = -1.0
         prec = conf.get("precision", "fp64")
-        if prec not in ("fp64", "mixed"):
-            raise ValueError("configuration['precision'] must be 'fp64' or 'mixed'")
-        c.precision = _lib.NLFEM_PREC_MIXED if prec == "mixed" else _lib.NLFEM_PREC_FP64
+        if prec not in _PRECISIONS:
+            raise ValueError("configuration['precision'] must be 'fp64', 'mixed' or 'fp64-onesided'")
+        c.precision = _PRECISIONS[prec]
         c.verbose = int(conf.get("verbose", 0))
         # domain decomposition (nlfem.pyx:204-214): mesh["nZeta"] > 0 with the element -> subdomain
         # indicator mesh["ZetaIndicator"] (scipy CSR)

@@ -833,3 +833,39 @@ def test_session_graph_replay_bitwise(nl, case):
                 assert same_pattern(A, B) and np.array_equal(A.data, B.data)
     finally:
         s2.close()
+
+
+@pytest.mark.parametrize("n,delta,kern,jit,close", [(32, 0.1, "constant", 0.0, None), (24, 0.12, "parabola", 0.2, None),
+                                                    (20, 0.15, "constant", 0.2, None),
+                                                    (12, 0.2, "fractional", 0.1, "fractional")])
+def test_fp64_onesided_matches_oracle(nl, orc, n, delta, kern, jit, close):
+    """The mixed path's algorithm in FP64 arithmetic (precision "fp64-onesided"): one-sided pass,
+    closed forms, fixed-point sums with a unit of 2^-52 of the entry scale. It meets the FP64 bar
+    against the oracle (1e-12), and its pattern is the reference's."""
+    m = square_mesh(n, delta, jitter=jit, seed=n)
+    k = {"function": kern, "horizon": delta, "outputdim": 1}
+    if kern == "fractional":
+        k["fractional_s"] = 0.4
+        c = conf2d(rule="16", close=close, deg=3)
+    else:
+        c = conf2d()
+    A = nl.stiffnessMatrix(m, k, dict(c, precision="fp64-onesided"))
+    B = orc.assemble(m, k, c)["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < 1e-12 and mx < 1e-12, (fro, mx)
+    # deterministic, like every fixed-point path
+    A2 = nl.stiffnessMatrix(m, k, dict(c, precision="fp64-onesided"))
+    assert np.array_equal(A.data, A2.data)
+
+
+def test_fp64_onesided_refusals(nl):
+    from nlfem_gb300._lib import NlfemError
+    m = cube_mesh(3, 0.2)
+    from nlfem_gb300 import quadrules
+    P, w = quadrules.keast11()
+    c = {"ansatz": "CG", "approxBalls": {"method": "baryCenter"},
+         "quadrature": {"outer": {"points": P, "weights": w}, "inner": {"points": P, "weights": w}},
+         "precision": "fp64-onesided"}
+    with pytest.raises(NlfemError, match="2D retriangulate"):
+        nl.stiffnessMatrix(m, {"function": "constant3D", "horizon": 0.2, "outputdim": 1}, c)

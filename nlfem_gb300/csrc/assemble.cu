@@ -21,6 +21,7 @@
 #include "passes.cuh"
 #include "passes_mix.cuh"
 #include "passes_bary.cuh"
+#include "passes_vec.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -897,6 +898,7 @@ __global__ void k_forcing(const double *__restrict__ EC, const double *__restric
                           const int *__restrict__ labT, const int *__restrict__ T32,
                           const int *__restrict__ labV, const int *__restrict__ eprob,
                           const ProbParams *__restrict__ probs, long long nE, Rule rule,
+                          const long long *__restrict__ zptr, const long long *__restrict__ zidx,
                           unsigned long long *__restrict__ facc, unsigned *__restrict__ tiny) {
     constexpr int dV = DIM + 1;
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -913,18 +915,21 @@ __global__ void k_forcing(const double *__restrict__ EC, const double *__restric
 #pragma unroll
         for (int a = 0; a < dV; a++) termf[a] += rule.psix[dV * i + a] * fv * adet[e] * rule.dx[i];
     }
+    // domain decomposition: 1 / zeta of the element with itself (Cassemble.cpp:901-908)
+    const double w = P.zeta ? zeta_weight(zptr, zidx, e, e) : 1.0;
 #pragma unroll
     for (int a = 0; a < dV; a++) {
         int v = T32[e * dV + a];
-        if (labV[v] > 0) fx_atomic_add(&facc[2 * (long long)v], termf[a], P.scale_exp, &tiny[v]);
+        if (labV[v] > 0) fx_atomic_add(&facc[2 * (long long)v], termf[a] * w, P.scale_exp, &tiny[v]);
     }
 }
-__global__ void k_forcing_finish(const unsigned long long *__restrict__ facc, long long nV,
+// Load vector entries r = od v + o from their fixed-point sums.
+__global__ void k_forcing_finish(const unsigned long long *__restrict__ facc, long long K, int od,
                                  const int *__restrict__ vprob, const ProbParams *__restrict__ probs,
                                  double *__restrict__ fd) {
-    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    fd[v] = fx_to_double(facc[2 * v], facc[2 * v + 1], probs[vprob[v]].scale_exp);
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= K) return;
+    fd[r] = fx_to_double(facc[2 * r], facc[2 * r + 1], probs[vprob[r / od]].scale_exp);
 }
 
 // ------------------------------------------------------------------ geometry debug hooks

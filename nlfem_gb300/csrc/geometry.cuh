@@ -188,16 +188,22 @@ __device__ __forceinline__ bool xtoRef(const double *E, const double *y, double 
 // ------------------------------------------------------------------- model (model.cpp)
 // KER_LABELED .. KER_CONSTTRUNC depend on the elements' labels or on absolute positions: FP64
 // passes only.
+// KER_CONSTFIELD .. KER_MICROFIELD3D are matrix-valued (outdim 2, 2, 3): the vector path only.
 enum KernelId {
     KER_CONSTANT = 0, KER_PARABOLA = 1, KER_FRACTIONAL = 2, KER_CONSTANT3D = 3,
-    KER_LABELED = 4, KER_NOTCH = 5, KER_LABELEDNOTCH = 6, KER_LABELEDVALVE = 7, KER_CONSTTRUNC = 8
+    KER_LABELED = 4, KER_NOTCH = 5, KER_LABELEDNOTCH = 6, KER_LABELEDVALVE = 7, KER_CONSTTRUNC = 8,
+    KER_CONSTFIELD = 9, KER_MICROFIELD = 10, KER_MICROFIELD3D = 11
 };
 // MTH_RETRI_UNSYMM .. MTH_NOTRUNC: 2D, FP64 passes only.
 enum MethodId {
     MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2, MTH_RETRI_UNSYMM = 3, MTH_SUBSET = 4,
     MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7, MTH_WEAKSING = 8
 };
-enum LoadId { LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2 };
+// LOAD_LINEARFIELD .. LOAD_BOTHFIELD are vector-valued (outdim 2, except LOAD_LINEARFIELD3D: 3).
+enum LoadId {
+    LOAD_LINEAR = 0, LOAD_LINEAR3D = 1, LOAD_CONSTANT = 2, LOAD_GAUSSIAN = 3, LOAD_JUMP = 4, LOAD_TENSORSIN = 5,
+    LOAD_LINEARFIELD = 6, LOAD_LINEARFIELD3D = 7, LOAD_RIGHTFIELD = 8, LOAD_DOWNFIELD = 9, LOAD_BOTHFIELD = 10
+};
 
 // Per-problem parameters (one entry per independent assembly).
 struct ProbParams {
@@ -277,13 +283,53 @@ __device__ __forceinline__ float kernel_f32(const ProbParams &P, float z0, float
     }
 }
 
-// Load functions (model.cpp:201-203, 240-242, 259-261)
+// Scalar load functions (model.cpp:201-203, 240-261). gaussian and tensorsin call CUDA's exp and
+// sin, which may differ from the host's in the last bit.
 __device__ __forceinline__ double load_f64(int load, const double *x) {
     switch (load) {
     case LOAD_LINEAR: return -2. * (x[1] + 1.);
     case LOAD_LINEAR3D: return -2. * (x[1] + 2.);
+    case LOAD_GAUSSIAN: {
+        const double a = x[0] * x[0], b = x[1] * x[1];
+        return -4. * (a + b - 1.) * exp(-a - b);
+    }
+    case LOAD_JUMP: return (x[0] + x[1] - 0.5 > -1e-15) ? -4. : 4.;   // EPSILON of mathhelpers.h:11
+    case LOAD_TENSORSIN: return 32. * (M_PI * M_PI) * sin(x[0] * M_PI * 4) * sin(x[1] * M_PI * 4);
     default: return 1.0;
     }
+}
+
+// Vector load functions (model.cpp:204-238): the components f_o(x).
+__device__ __forceinline__ void load_vec_f64(int load, const double *x, double *f) {
+    const double c = M_PI / 2.0;
+    switch (load) {
+    case LOAD_LINEARFIELD: f[0] = -c * (1.0 + 2 * x[0]); f[1] = -c * x[1]; break;
+    case LOAD_LINEARFIELD3D:
+        f[0] = -c * (1.0 + 2 * x[0]) * x[1] * x[1]; f[1] = -c * x[1] * x[1]; f[2] = -c * x[2] * x[1] * x[1]; break;
+    case LOAD_RIGHTFIELD: f[0] = 1.0e-1; f[1] = 0.0; break;
+    case LOAD_DOWNFIELD: f[0] = 0.0; f[1] = -M_PI * 2; break;
+    case LOAD_BOTHFIELD: f[0] = -M_PI; f[1] = -M_PI * 2; break;
+    default: f[0] = load_f64(load, x); break;
+    }
+}
+
+// Matrix-valued kernels (model.cpp:140-191), kv[OD * aOut + bOut] of z = x - y; P.kc holds
+// 4 / (pi delta^4) (constantField) or 3 / delta^3 (the microelastic fields).
+template <int OD>
+__device__ __forceinline__ void kernel_field_f64(const ProbParams &P, const double *x, const double *y, double *kv) {
+    if (P.kernel == KER_CONSTFIELD) {   // [k(0,0), k(0,1), k(1,0), k(1,1)] = [c, 0, c, 0]
+        kv[0] = P.kc; kv[1] = 0.0; kv[2] = P.kc; kv[3] = 0.0;
+        return;
+    }
+    double z[3] = {0, 0, 0}, r2 = 0;
+#pragma unroll
+    for (int i = 0; i < OD; i++) { z[i] = x[i] - y[i]; r2 += z[i] * z[i]; }
+    const double r = sqrt(r2);
+    const double cd = P.kc * (1.0 / (r * r * r));
+#pragma unroll
+    for (int i = 0; i < OD; i++)
+#pragma unroll
+        for (int j = 0; j < OD; j++) kv[OD * i + j] = cd * z[i] * z[j];
 }
 
 }  // namespace nlg

@@ -73,6 +73,9 @@ static int kernel_id(const char *s) {
     if (k == "labeledNotch") return KER_LABELEDNOTCH;
     if (k == "labeledValve") return KER_LABELEDVALVE;
     if (k == "constantTruncated") return KER_CONSTTRUNC;
+    if (k == "constantField") return KER_CONSTFIELD;
+    if (k == "linearPrototypeMicroelasticField") return KER_MICROFIELD;
+    if (k == "linearPrototypeMicroelasticField3D") return KER_MICROFIELD3D;
     return -1;
 }
 static int method_id(const char *s) {
@@ -93,7 +96,21 @@ static int load_id(const char *s) {
     if (k == "linear") return LOAD_LINEAR;
     if (k == "linear3D") return LOAD_LINEAR3D;
     if (k == "constant") return LOAD_CONSTANT;
+    if (k == "gaussian") return LOAD_GAUSSIAN;
+    if (k == "jump") return LOAD_JUMP;
+    if (k == "tensorsin") return LOAD_TENSORSIN;
+    if (k == "linearField") return LOAD_LINEARFIELD;
+    if (k == "linearField3D") return LOAD_LINEARFIELD3D;
+    if (k == "constantRightField") return LOAD_RIGHTFIELD;
+    if (k == "constantDownField") return LOAD_DOWNFIELD;
+    if (k == "constantBothField") return LOAD_BOTHFIELD;
     return -1;
+}
+// Number of components of a kernel's or a forcing's values (model.cpp:140-191, 204-238).
+static int kernel_outdim(int k) { return k == KER_MICROFIELD3D ? 3 : (k >= KER_CONSTFIELD ? 2 : 1); }
+static int load_outdim(int l) {
+    if (l == LOAD_LINEARFIELD3D) return 3;
+    return l >= LOAD_LINEARFIELD ? 2 : 1;
 }
 
 // Quadrature rule and the basis function check (Cassemble.cpp:509-517, checks.cpp:36-47).
@@ -159,7 +176,7 @@ static int set_fx_unit(ProbParams &P, int widen) {
 static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     memset(&P, 0, sizeof(P));
     if (p.dim != 2 && p.dim != 3) return fail(NLFEM_ERR_INVALID, "Dimension is not equal to 2 or 3.");
-    if (p.outdim != 1) return fail(NLFEM_ERR_UNSUPPORTED, "only outdim = 1 is implemented");
+    if (p.outdim < 1 || p.outdim > 3) return fail(NLFEM_ERR_INVALID, "outdim must be 1, 2 or 3");
     if (p.is_dg && (long long)(p.dim + 1) * p.nE >= (1LL << 31)) return fail(NLFEM_ERR_UNSUPPORTED, "mesh too large for DG");
     if (p.nE <= 0 || p.nV <= 0 || !p.elements || !p.elementLabels || !p.vertices || !p.vertexLabels)
         return fail(NLFEM_ERR_INVALID, "empty or missing mesh arrays");
@@ -179,7 +196,24 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "The fractional and fractional_weakSingular integration routines are meant for close elements only.");
         std::string kn(p.kernel);
         const bool proto = kn == "linearPrototypeMicroelastic";
-        P.singular = (kn == "fractional") || proto;   // Cassemble.cpp:89-94
+        P.singular = (kn == "fractional") || proto || P.kernel == KER_MICROFIELD;   // Cassemble.cpp:89-94
+        if (kernel_outdim(P.kernel) != p.outdim)
+            return fail(NLFEM_ERR_INVALID, std::string("kernel ") + kn + " has " + std::to_string(kernel_outdim(P.kernel)) +
+                                               " output components, outdim is " + std::to_string(p.outdim));
+        if (p.outdim > 1) {   // vector-valued kernels: the FP64 vector path
+            if (p.dim != (P.kernel == KER_MICROFIELD3D ? 3 : 2))
+                return fail(NLFEM_ERR_INVALID, std::string("kernel ") + kn + " needs a " +
+                                                   (P.kernel == KER_MICROFIELD3D ? "3D" : "2D") + " mesh");
+            if (p.precision != NLFEM_PREC_FP64)
+                return fail(NLFEM_ERR_UNSUPPORTED, "vector-valued kernels run on the fp64 path only (precision \"fp64\")");
+            if (p.is_dg) return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with vector-valued kernels is not implemented");
+            if (p.nZeta > 0)
+                return fail(NLFEM_ERR_UNSUPPORTED, "domain-decomposition weights with vector-valued kernels are not implemented");
+            if ((P.remote != MTH_RETRIANGULATE && P.remote != MTH_BARYCENTER) ||
+                (P.close != MTH_RETRIANGULATE && P.close != MTH_BARYCENTER && P.close != MTH_FRACTIONAL && P.close != MTH_WEAKSING))
+                return fail(NLFEM_ERR_UNSUPPORTED, "vector-valued kernels take retriangulate or baryCenter (remote) and "
+                                                   "those or fractional / weakSingular (close)");
+        }
         if (proto && p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, "kernel linearPrototypeMicroelastic is implemented for 2D meshes only");
         if (duffy_close(P) && (p.tensorGaussDegree <= 0 || !p.Pg || !p.dg))
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
@@ -224,18 +258,27 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             P.kc = 4 / (M_PI * pow(p.sqdelta, 2));
             break;
         case KER_CONSTTRUNC: P.kc = 4 / (M_PI * pow(p.sqdelta, 2)); break;                 // model.cpp:30-42
+        case KER_CONSTFIELD: P.kc = 4. / (M_PI * pow(p.sqdelta, 2)); break;                // model.cpp:182-191
+        case KER_MICROFIELD: case KER_MICROFIELD3D:                                        // model.cpp:140-180
+            P.kc = 3.0 / pow(P.delta, 3);
+            P.expo = 1.0;   // |k| ~ c / |z|: for the fixed-point scale
+            break;
         }
         P.kc_f = (float)P.kc;
         P.expo_f = (float)P.expo;
     } else {
         P.load = load_id(p.forcing);
         if (P.load < 0) return fail(NLFEM_ERR_UNSUPPORTED, std::string("unknown forcing: ") + (p.forcing ? p.forcing : "(null)"));
+        if (load_outdim(P.load) != p.outdim)
+            return fail(NLFEM_ERR_INVALID, std::string("forcing ") + p.forcing + " has " + std::to_string(load_outdim(P.load)) +
+                                               " components, outdim is " + std::to_string(p.outdim));
+        if (p.outdim > 1 && p.is_dg) return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with vector forcings is not implemented");
     }
     P.bridges = 0;
     if (p.elementLabels)
         for (long e = 0; e < p.nE && !P.bridges; e++) P.bridges = p.elementLabels[e] == 0;
     P.zeta = 0;
-    if (system && p.nZeta > 0) {   // the device reads the indicator rows by these pointers
+    if (p.nZeta > 0) {   // the device reads the indicator rows by these pointers
         if (!p.zeta_indices || !p.zeta_indptr) return fail(NLFEM_ERR_INVALID, "nZeta > 0 without the zeta indicator");
         if (p.zeta_indptr[0] != 0) return fail(NLFEM_ERR_INVALID, "zeta indicator: row pointers must start at 0");
         for (long e = 0; e < p.nE; e++)
@@ -261,7 +304,8 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         double kmax = P.kc;
         if (P.kernel == KER_PARABOLA) kmax = P.kc * p.sqdelta;
         if (P.kernel == KER_LABELED) kmax = std::max(P.kc, P.kc2);
-        if (P.kernel == KER_FRACTIONAL) kmax = P.kc / pow(std::min(h, P.delta), P.expo);
+        if (P.kernel == KER_FRACTIONAL || P.kernel == KER_MICROFIELD || P.kernel == KER_MICROFIELD3D)
+            kmax = P.kc / pow(std::min(h, P.delta), P.expo);
         mag = fabs(kmax) * el * std::max(ball, el);
     } else {
         double fm = 1.0;
@@ -307,7 +351,7 @@ static double duffy_traffo(int c, int t, double *al) {
 // ---------------------------------------------------------------- session
 // How the quadrature pass adds into the matrix: colored two-sided passes (FP64, and mixed rules
 // without a one-sided kernel), or one persistent one-sided pass with fixed-point atomics.
-enum { PM_COLORED = 0, PM_RETRI = 1, PM_BARY = 2 };
+enum { PM_COLORED = 0, PM_RETRI = 1, PM_BARY = 2, PM_VEC = 3 };
 
 struct Session {
     int dim = 2, dV = 3, nProb = 0;
@@ -341,6 +385,7 @@ struct Session {
     long long po_cap = 0, t_nnz = 0;
     DevBuf sv_vec, sv_part;                 // CG solve: f, g, b, x, r, p, Ap; dot partials
     DevBuf zptr, zidx;                      // domain-decomposition indicator (element -> subdomains)
+    DevBuf vacc, vtiny;                     // vector path: 128-bit sums per expanded slot
     DevBuf kclist;                          // elements grouped by kernel class (pass launches)
     // Discontinuous Galerkin: after the pair search, dg_swap_in swaps the row space to the element
     // DOFs dV e + a (the identity table, every row kept, K = dV nE rows). T32, labV, vprob, vptr,
@@ -355,7 +400,8 @@ struct Session {
     // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
     // mesh has the same element and vertex counts (an overflow falls back to two passes)
     long long hint_pat_cap = 0, hint_po_cap = 0, hint_nE = -1, hint_nV = -1;
-    int pmode = 0;                          // PM_COLORED, PM_RETRI or PM_BARY
+    int pmode = 0;                          // PM_COLORED, PM_RETRI, PM_BARY or PM_VEC
+    int od = 1;                             // outdim: rows od v + i (PM_VEC when od > 1)
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
     bool replay = false;
     long long nadj = 0, htot = 0;
@@ -373,7 +419,7 @@ struct Session {
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                 &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
-                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx,
+                &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx, &vacc, &vtiny,
                 &dgT32, &dglabV, &dgvprob, &dgvptr, &dgvel};
     }
     ~Session() {
@@ -478,6 +524,9 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
     for (int i = 1; i < n; i++)
         if (probs[i].precision != probs[0].precision)
             return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the precision");
+    S.od = probs[0].outdim;
+    for (int i = 1; i < n; i++)
+        if (probs[i].outdim != S.od) return fail(NLFEM_ERR_UNSUPPORTED, "all problems of a batch must share the outdim");
     int r = make_rule(probs[0], system, S.rule);
     if (r) return r;
     for (int i = 1; i < n; i++) {
@@ -500,6 +549,7 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
         S.pmode = PM_COLORED;
         if (S.prec == PREC_MIX && S.dim == 2 && all_retri && !any_zeta) S.pmode = PM_RETRI;
         if (S.prec == PREC_MIX && all_bary && !any_singular && !any_zeta) S.pmode = PM_BARY;
+        if (S.od > 1) S.pmode = PM_VEC;
         if (S.onesided64) {
             if (!(S.dim == 2 && all_retri && !any_zeta))
                 return fail(NLFEM_ERR_UNSUPPORTED, "precision \"fp64-onesided\" covers the 2D retriangulate rule "
@@ -1038,7 +1088,7 @@ static int run_pattern_bm(Session &S, int words, int threads) {
                                                     S.pscratch.get<int>(), S.cols.get<int>()); ++S.nlaunch;
             CK(cudaGetLastError());
             S.stats.nnz_structural = (long)S.nnz_struct;
-            if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
+            if (S.pmode == PM_RETRI || S.pmode == PM_BARY) return run_slot_maps<DIM>(S);
             return NLFEM_OK;
         }
         a.scratch = nullptr; a.cap = 0; a.cursor = nullptr; a.rowoff = nullptr; a.ovf = nullptr;
@@ -1056,7 +1106,7 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     S.pat_cap = S.nnz_struct;   // the next assembly builds the pattern in one pass
     ENS(S.rowoff, sizeof(long long) * (nV + 1));
     ENS(S.pscratch, sizeof(int) * (S.pat_cap + 1));
-    if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
+    if (S.pmode == PM_RETRI || S.pmode == PM_BARY) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
 
@@ -1094,7 +1144,7 @@ static int run_pattern(Session &S) {
     k_row_sort_global<<<S.nSM * 4, 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.cols.get<int>(), cap); ++S.nlaunch;
     CK(cudaGetLastError());
     S.stats.nnz_structural = (long)S.nnz_struct;
-    if (S.pmode != PM_COLORED) return run_slot_maps<DIM>(S);
+    if (S.pmode == PM_RETRI || S.pmode == PM_BARY) return run_slot_maps<DIM>(S);
     return NLFEM_OK;
 }
 
@@ -1340,6 +1390,62 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PR &pr, cons
     return fail(NLFEM_ERR_NUMERIC, "contribution outside the fixed-point range (non-finite value?)");
 }
 
+// Vector-valued kernels: one thread per ordered pair, FP64 blocks, 128-bit fixed-point sums in the
+// expanded slots (od^2 per structural entry).
+template <int DIM>
+static int run_pass_vec(Session &S) {
+    const long long nslot = (long long)S.od * S.od * S.nnz_struct;
+    ENS(S.vacc, sizeof(unsigned long long) * 2 * (nslot + 1));
+    ENS(S.vtiny, sizeof(unsigned) * (nslot + 1));
+    CK(cudaMemsetAsync(S.vacc.p, 0, sizeof(unsigned long long) * 2 * (nslot + 1), S.st));
+    CK(cudaMemsetAsync(S.vtiny.p, 0, sizeof(unsigned) * (nslot + 1), S.st));
+    unsigned long long *cnt = S.counters.get<unsigned long long>();
+    VecArgs a;
+    memset(&a, 0, sizeof(a));
+    a.pA = S.pA.get<int>(); a.pB = S.pB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
+    a.probs = S.prm.get<ProbParams>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    a.acc = S.vacc.get<unsigned long long>(); a.tiny = S.vtiny.get<unsigned>(); a.P = S.P; a.err = S.err.get<int>();
+    a.n_close = cnt + 4; a.n_subtri = cnt + 5;
+    Duffy d;
+    memset(&d, 0, sizeof(d));
+    if (S.duffy_nPg) d = duffy_view(S);
+    if (S.P > 0) {
+        if (DIM == 2 && S.od == 2) k_quad_vec<2, 2><<<grid_for(S.P, 128), 128, 0, S.st>>>(a, S.rule, d);
+        else if (DIM == 3 && S.od == 3) k_quad_vec<3, 3><<<grid_for(S.P, 128), 128, 0, S.st>>>(a, S.rule, d);
+        else return fail(NLFEM_ERR_UNSUPPORTED, "vector-valued kernels: outdim 2 in 2D or 3 in 3D");
+        ++S.nlaunch;
+    }
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+// Finish of the vector path: expanded rows od v + i, exact zeros dropped.
+static int run_finish_vec(Session &S) {
+    const long long K = (long long)S.od * S.nV;
+    ENS(S.keepcnt, sizeof(int) * (K + 1));
+    ENS(S.fptr, sizeof(long long) * (K + 1));
+    const unsigned grid = (unsigned)grid_for(K * 32, 256);
+    if (S.od == 2)
+        k_vec_finish_count<2><<<grid, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.nV, S.labV.get<int>(), S.vacc.get<unsigned long long>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.keepcnt.get<int>());
+    else
+        k_vec_finish_count<3><<<grid, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.nV, S.labV.get<int>(), S.vacc.get<unsigned long long>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.keepcnt.get<int>());
+    ++S.nlaunch;
+    int r = scan_excl<int>(S, S.keepcnt.get<int>(), K, S.fptr.get<long long>());
+    if (r) return r;
+    r = d2h(S, &S.nnz, S.fptr.get<long long>() + K, 1);
+    if (r) return r;
+    ENS(S.fcols, sizeof(int) * (S.nnz + 1));
+    ENS(S.fvals, sizeof(double) * (S.nnz + 1));
+    if (S.od == 2)
+        k_vec_finish_compact<2><<<grid, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.nV, S.labV.get<int>(), S.cols.get<int>(), S.vacc.get<unsigned long long>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
+    else
+        k_vec_finish_compact<3><<<grid, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.nV, S.labV.get<int>(), S.cols.get<int>(), S.vacc.get<unsigned long long>(), S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fptr.get<long long>(), S.fcols.get<int>(), S.fvals.get<double>());
+    ++S.nlaunch;
+    CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
 template <int DIM>
 static int run_passes(Session &S) {
     constexpr int dV = DIM + 1;
@@ -1367,6 +1473,7 @@ static int run_passes(Session &S) {
     a.zptr = S.zptr.get<long long>(); a.zidx = S.zidx.get<long long>();
     a.n_subtri = cnt + 5; a.n_amb = cnt + 6; a.n_close = cnt + 4; a.n_in = cnt + 12; a.n_cut = cnt + 13;
     a.touched = S.prec == PREC_MIX && S.pmode == PM_COLORED ? S.touched.get<unsigned char>() : nullptr;
+    if (S.pmode == PM_VEC) return run_pass_vec<DIM>(S);
     const PassRule pr = make_pass_rule<float>(S.rule, DIM);
     if (S.pmode == PM_RETRI && S.onesided64) {
         const PassRuleT<double> pr64 = make_pass_rule<double>(S.rule, DIM);
@@ -1401,6 +1508,7 @@ static int run_passes(Session &S) {
 }
 
 static int run_finish(Session &S) {
+    if (S.pmode == PM_VEC) return run_finish_vec(S);
     const long long nV = S.nV;
     ENS(S.keepcnt, sizeof(int) * (nV + 1));
     ENS(S.fptr, sizeof(long long) * (nV + 1));
@@ -1513,7 +1621,7 @@ static int run_system_graph_t(Session &S) {
         S.gexec = nullptr;
     }
     if ((r = run_system_t<DIM>(S))) return r;
-    if (S.pmode == PM_COLORED) return NLFEM_OK;
+    if (S.pmode == PM_COLORED || S.pmode == PM_VEC) return NLFEM_OK;
     const nlfem_stats keep = S.stats;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal));
@@ -1543,14 +1651,22 @@ static int run_forcing_t(Session &S) {
     int r;
     if ((r = run_prep<DIM>(S))) return r;
     if (S.dg && (r = dg_swap_in(S))) return r;
-    const long long nV = S.nV;
-    ENS(S.facc, sizeof(unsigned long long) * 2 * (nV + 1));
-    ENS(S.ftiny, sizeof(unsigned) * (nV + 1));
-    ENS(S.fd, sizeof(double) * (nV + 1));
-    CK(cudaMemsetAsync(S.facc.p, 0, sizeof(unsigned long long) * 2 * (nV + 1), S.st));
-    CK(cudaMemsetAsync(S.ftiny.p, 0, sizeof(unsigned) * (nV + 1), S.st));
-    k_forcing<DIM><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>()); ++S.nlaunch;
-    k_forcing_finish<<<grid_for(nV, 256), 256, 0, S.st>>>(S.facc.get<unsigned long long>(), nV, S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fd.get<double>()); ++S.nlaunch;
+    const long long nV = S.nV, K = (long long)S.od * nV;
+    ENS(S.facc, sizeof(unsigned long long) * 2 * (K + 1));
+    ENS(S.ftiny, sizeof(unsigned) * (K + 1));
+    ENS(S.fd, sizeof(double) * (K + 1));
+    CK(cudaMemsetAsync(S.facc.p, 0, sizeof(unsigned long long) * 2 * (K + 1), S.st));
+    CK(cudaMemsetAsync(S.ftiny.p, 0, sizeof(unsigned) * (K + 1), S.st));
+    const long long *zp = S.zptr.get<long long>(), *zi = S.zidx.get<long long>();
+    if (S.od == 1) {
+        k_forcing<DIM><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, zp, zi, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>());
+    } else if (S.od == 2) {
+        k_forcing_vec<DIM, 2><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, zp, zi, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>());
+    } else {
+        k_forcing_vec<DIM, 3><<<grid_for(S.nE, 128), 128, 0, S.st>>>(S.EC.get<double>(), S.adet.get<double>(), S.labT.get<int>(), S.T32.get<int>(), S.labV.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), S.nE, S.rule, zp, zi, S.facc.get<unsigned long long>(), S.ftiny.get<unsigned>());
+    }
+    ++S.nlaunch;
+    k_forcing_finish<<<grid_for(K, 256), 256, 0, S.st>>>(S.facc.get<unsigned long long>(), K, S.od, S.vprob.get<int>(), S.prm.get<ProbParams>(), S.fd.get<double>()); ++S.nlaunch;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(S.st));
     return NLFEM_OK;
@@ -1634,7 +1750,7 @@ static void host_release_free() {
 }
 
 static int download32(Session &S, int i, nlfem_csr32 *out) {
-    const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
+    const long long r0 = (long long)S.od * S.voff[i], nrows = (long long)S.od * (S.voff[i + 1] - S.voff[i]);
     long long b[2];
     int r = d2h(S, &b[0], S.fptr.get<long long>() + r0, 1);
     if (r) return r;
@@ -1668,7 +1784,7 @@ static int download32(Session &S, int i, nlfem_csr32 *out) {
 }
 
 static int download(Session &S, int i, nlfem_csr *out) {
-    const long long r0 = S.voff[i], nrows = S.voff[i + 1] - S.voff[i];
+    const long long r0 = (long long)S.od * S.voff[i], nrows = (long long)S.od * (S.voff[i + 1] - S.voff[i]);
     long long b[2];
     int r = d2h(S, &b[0], S.fptr.get<long long>() + r0, 1);
     if (r) return r;
@@ -2038,7 +2154,7 @@ int nlfem_load_vector(const nlfem_problem *prob, double *fd) {
     r = session_init(S, prob, 1, false);
     if (!r) r = session_upload(S, prob);
     if (!r) r = (S.dim == 2) ? run_forcing_t<2>(S) : run_forcing_t<3>(S);
-    if (!r) r = d2h(S, fd, S.fd.get<double>(), (size_t)S.nV);
+    if (!r) r = d2h(S, fd, S.fd.get<double>(), (size_t)S.od * S.nV);
     return r;
 }
 

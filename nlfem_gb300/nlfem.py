@@ -147,7 +147,7 @@ class _Problem:
         c.verbose = int(conf.get("verbose", 0))
         # domain decomposition (nlfem.pyx:204-214): mesh["nZeta"] > 0 with the element -> subdomain
         # indicator mesh["ZetaIndicator"] (scipy CSR)
-        nZeta = int(mesh.get("nZeta", 0) or 0) if system else 0
+        nZeta = int(mesh.get("nZeta", 0) or 0)
         if nZeta > 0:
             Z = mesh["ZetaIndicator"]
             c.zeta_indices = self._l(np.asarray(Z.indices)).ctypes.data_as(_lp)

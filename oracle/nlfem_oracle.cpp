@@ -1547,6 +1547,8 @@ oracle_result *oracle_par_assemble(
                 else aAdx = &m.T[m.dV * aTdx];
                 double termf[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
                 double x[3];
+                // domain decomposition: 1 / zeta of the element with itself (Cassemble.cpp:901-908)
+                const double weight = m.nZeta ? 1. / evaluateZeta(m.zeta_indices, m.zeta_indptr, m.nZeta, aTdx, aTdx) : 1.;
                 if (outdim > 1) {                                                  // compute_f, outdim > 1
                     for (int a = 0; a < m.dV * outdim; a++)
                         for (int i = 0; i < nPx; i++) {
@@ -1558,7 +1560,7 @@ oracle_result *oracle_par_assemble(
                             termf[a] += q.psix[m.dV * i + a / outdim] * fo[a % outdim] * aT.absDet * dx[i];
                         }
                     for (int a = 0; a < m.dV * outdim; a++)
-                        if (m.is_dg || m.labV[aAdx[a / outdim]] > 0) fd[outdim * aAdx[a / outdim] + a % outdim] += termf[a] * 1.;
+                        if (m.is_dg || m.labV[aAdx[a / outdim]] > 0) fd[outdim * aAdx[a / outdim] + a % outdim] += termf[a] * weight;
                     continue;
                 }
                 for (int a = 0; a < m.dV; a++) {
@@ -1569,7 +1571,7 @@ oracle_result *oracle_par_assemble(
                     }
                 }
                 for (int a = 0; a < m.dV; a++)
-                    if (m.is_dg || m.labV[aAdx[a]] > 0) fd[aAdx[a]] += termf[a] * 1.;
+                    if (m.is_dg || m.labV[aAdx[a]] > 0) fd[aAdx[a]] += termf[a] * weight;
             }
         }
         r->fd = (double *)malloc(sizeof(double) * K);

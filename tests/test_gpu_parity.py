@@ -416,7 +416,8 @@ def test_weak_singular_close_rule(nl, orc):
         nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="mixed"))
 
 
-@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5"])
+@pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5", "labeled10", "average10",
+                                  "dg10", "weak10", "field8"])
 def test_gpu_matches_committed_fixtures(nl, name):
     """The FP64 path against the committed oracle fixtures (tests/golden/oracle_cases.npz, made by
     tests/golden/make_oracle_golden.py): bit-exact pattern, values within rounding."""
@@ -438,8 +439,8 @@ def test_gpu_matches_committed_fixtures(nl, name):
     fro, mx = rel_errors(A, B)
     tol = 1e-11 if name == "frac12" else FP64_TOL
     assert fro < tol and mx < tol, (fro, mx)
-    if name == "cube5":
-        f = nl.loadVector(dict(mesh), load, conf)
+    if load is not None:
+        f = nl.loadVector(dict(mesh, outdim=int(kernel.get("outputdim", 1))), load, conf)
         g = fx[f"{name}.f"]
         np.testing.assert_allclose(f, g, rtol=1e-13, atol=1e-15 * np.abs(g).max())
 
@@ -869,3 +870,97 @@ def test_fp64_onesided_refusals(nl):
          "precision": "fp64-onesided"}
     with pytest.raises(NlfemError, match="2D retriangulate"):
         nl.stiffnessMatrix(m, {"function": "constant3D", "horizon": 0.2, "outputdim": 1}, c)
+
+
+
+FIELD_CASES = {
+    # constantField (model.cpp:182-191), retriangulate with caps, jittered
+    "constfield": (lambda: square_mesh(12, 0.15, jitter=0.2, seed=21), {"function": "constantField", "horizon": 0.15, "outputdim": 2},
+                   lambda: conf2d()),
+    # the microelastic field kernel, singular: close pairs by the fractional Duffy rule
+    "microfield_frac": (lambda: square_mesh(8, 0.2, jitter=0.1, seed=22),
+                        {"function": "linearPrototypeMicroelasticField", "horizon": 0.2, "outputdim": 2, "fractional_s": -0.5},
+                        lambda: conf2d(rule="16", close="fractional", deg=3)),
+    # the same with the weakSingular close rule
+    "microfield_weak": (lambda: square_mesh(8, 0.2, jitter=0.1, seed=23),
+                        {"function": "linearPrototypeMicroelasticField", "horizon": 0.2, "outputdim": 2, "fractional_s": -0.5},
+                        lambda: conf2d(rule="16", close="weakSingular", deg=3)),
+    # 2D barycenter rule with the constant field kernel
+    "constfield_bary": (lambda: square_mesh(10, 0.2, jitter=0.15, seed=24), {"function": "constantField", "horizon": 0.2, "outputdim": 2},
+                        lambda: conf2d(method="baryCenter")),
+    # 3D microelastic field kernel, barycenter (not singular in the reference's lookup); the inner
+    # rule avoids the outer points, where the kernel is singular
+    "microfield3d": (lambda: cube_mesh(3, 0.1, jitter=0.1, seed=25),
+                     {"function": "linearPrototypeMicroelasticField3D", "horizon": 0.35, "outputdim": 3}, lambda: _conf3d_inner4()),
+}
+
+
+def _conf3d_inner4():
+    pa, pb = 0.5854101966249685, 0.1381966011250105
+    c = conf3d()
+    c["quadrature"]["inner"] = {"points": np.array([[pb, pb, pb], [pa, pb, pb], [pb, pa, pb], [pb, pb, pa]]),
+                                "weights": np.full(4, 1.0 / 24)}
+    return c
+
+
+@pytest.mark.parametrize("case", list(FIELD_CASES))
+def test_vector_kernels_match_oracle(nl, orc, case):
+    """Vector-valued kernels (outdim 2 and 3) on the GPU: the reference's general block indexing
+    (integration.cpp:345-540, 910-1018, 82-288; Cassemble.cpp:721-770) in FP64 with
+    deterministic fixed-point sums. Pattern bit-exact, values within 1e-12 of the oracle (which
+    the reference build pins bit for bit)."""
+    mk, kernel, mkconf = FIELD_CASES[case]
+    m = dict(mk(), outdim=kernel["outputdim"])
+    conf = mkconf()
+    A = nl.stiffnessMatrix(m, kernel, conf)
+    B = orc.assemble(m, kernel, conf)["A"]
+    assert A.shape == B.shape == (m["vertices"].shape[0] * kernel["outputdim"],) * 2
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)
+    A2 = nl.stiffnessMatrix(m, kernel, conf)
+    assert np.array_equal(A.data, A2.data)   # deterministic
+
+
+@pytest.mark.parametrize("load,outdim,dim", [("linearField", 2, 2), ("constantRightField", 2, 2), ("constantDownField", 2, 2),
+                                              ("constantBothField", 2, 2), ("linearField3D", 3, 3), ("gaussian", 1, 2),
+                                              ("jump", 1, 2), ("tensorsin", 1, 2)])
+def test_further_forcings_match_oracle(nl, orc, load, outdim, dim):
+    """The vector forcings and the scalar gaussian / jump / tensorsin (model.cpp:201-258) against
+    the oracle: within 1e-13 (CUDA's exp and sin may differ from the host's in the last bit)."""
+    m = square_mesh(14, 0.1, jitter=0.2, seed=26) if dim == 2 else cube_mesh(3, 0.2, jitter=0.1, seed=27)
+    m = dict(m, outdim=outdim)
+    conf = conf2d() if dim == 2 else conf3d()
+    f = nl.loadVector(m, {"function": load}, conf)
+    g = orc.assemble(m, None, conf, compute="forcing", load={"function": load})["f"]
+    assert f.shape == g.shape == (m["vertices"].shape[0] * outdim,)
+    np.testing.assert_allclose(f, g, rtol=1e-13, atol=1e-14 * np.abs(g).max())
+
+
+def test_load_vector_domain_decomposition(nl, orc):
+    """par_forcing weights each element's contribution by 1 / zeta(aT, aT) (Cassemble.cpp:901-908)."""
+    m = square_mesh(12, 0.1, jitter=0.2, seed=28)
+    nE = m["elements"].shape[0]
+    bx = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
+    rows, cols = [], []
+    for e in range(nE):   # two overlapping subdomains around x = 0.5
+        for z, inside in enumerate((bx[e] < 0.6, bx[e] > 0.4)):
+            if inside:
+                rows.append(e); cols.append(z)
+    Z = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(nE, 2))
+    m = dict(m, nZeta=2, ZetaIndicator=Z)
+    f = nl.loadVector(m, {"function": "linear"}, conf2d())
+    g = orc.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
+    np.testing.assert_allclose(f, g, rtol=1e-13, atol=1e-15 * np.abs(g).max())
+    f0 = nl.loadVector(dict(m, nZeta=0), {"function": "linear"}, conf2d())
+    assert not np.allclose(f, f0)
+
+
+def test_vector_kernel_refusals(nl):
+    from nlfem_gb300._lib import NlfemError
+    m = dict(square_mesh(4, 0.2), outdim=2)
+    k = {"function": "constantField", "horizon": 0.2, "outputdim": 2}
+    with pytest.raises(NlfemError, match="fp64 path only"):
+        nl.stiffnessMatrix(m, k, conf2d(precision="mixed"))
+    with pytest.raises(NlfemError, match="output components"):
+        nl.stiffnessMatrix(dict(m, outdim=1), dict(k, outputdim=1), conf2d())

@@ -117,3 +117,21 @@ def test_retriangulation_equals_reference():
         no, to = oracle.retriangulate_sq(x, TE, sqd, caps)
         assert nr == no
         assert _bitwise(tr, to)
+
+
+def test_load_vector_with_zeta_weights_equals_reference():
+    """par_forcing's 1 / zeta(aT, aT) weight (Cassemble.cpp:901-908) in the restatement."""
+    from oracle import oracle, ref
+    m = square_mesh(12, 0.1, jitter=0.2, seed=44)
+    nE = m["elements"].shape[0]
+    bx = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
+    rows, cols = [], []
+    for e in range(nE):
+        for z, inside in enumerate((bx[e] < 0.6, bx[e] > 0.4)):
+            if inside:
+                rows.append(e); cols.append(z)
+    Z = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(nE, 2))
+    m = dict(m, nZeta=2, ZetaIndicator=Z)
+    fr = ref.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
+    fo = oracle.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
+    assert _bitwise(fr, fo)

@@ -48,7 +48,10 @@ extern "C" {
 /* One assembly problem. Arrays are borrowed host pointers, row-major. */
 typedef struct nlfem_problem {
     int dim;                     /* 2 or 3 */
-    int outdim;                  /* 1 (vector-valued kernels are not implemented) */
+    int outdim;                  /* components of the kernel's / forcing's values: 1; 2 for "constantField",
+                                    "linearPrototypeMicroelasticField" (2D) and the 2D vector forcings;
+                                    3 for "linearPrototypeMicroelasticField3D" and "linearField3D".
+                                    K = outdim nV rows (FP64, continuous P1, no domain decomposition) */
     int is_dg;                   /* 0: continuous P1 (K = nV), 1: discontinuous (K = nE*(dim+1);
                                     FP64, one problem per call, non-singular kernels) */
     long nE, nV;
@@ -63,10 +66,15 @@ typedef struct nlfem_problem {
     double fractional_s;         /* s of the fractional kernel, -1 if unused */
     const char *kernel;          /* "constant", "parabola", "fractional", "linearPrototypeMicroelastic",
                                     "constant3D"; FP64 only, 2D: "labeled", "notch", "labeledNotch",
-                                    "labeledValve", "constantTruncated" */
-    const char *forcing;         /* "linear", "linear3D", "constant" */
+                                    "labeledValve", "constantTruncated"; FP64 only, outdim > 1:
+                                    "constantField", "linearPrototypeMicroelasticField",
+                                    "linearPrototypeMicroelasticField3D" */
+    const char *forcing;         /* "linear", "linear3D", "constant", "gaussian", "jump", "tensorsin";
+                                    outdim 2: "linearField", "constantRightField", "constantDownField",
+                                    "constantBothField"; outdim 3: "linearField3D" */
     const char *method_remote;   /* "retriangulate", "baryCenter"; FP64 only, 2D: "retriangulate_unsymm",
-                                    "subSetBall", "averageBall", "baryCenterRT", "noTruncation" */
+                                    "subSetBall", "averageBall", "baryCenterRT", "noTruncation",
+                                    "exactBall" */
     const char *method_close;    /* singular kernels: "fractional", "weakSingular" (FP64 only), or
                                     NULL (= method_remote) */
     int is_PlacePointOnCap;
@@ -155,6 +163,19 @@ int nlfem_session_assemble(nlfem_session *s);            /* inputs already in HB
  * sequence, later calls launch the graph (falls back to a normal assembly when a capacity check
  * trips). Mixed-precision sessions only; other sessions assemble normally. */
 int nlfem_session_assemble_graph(nlfem_session *s);
+/* Launch-shape autotuner (no counterpart in the reference, whose OpenMP loops have no launch
+ * shape): times the session's assembly with 1, 2, ... blocks per SM (up to the occupancy limit)
+ * for the pair search and for the persistent one-sided quadrature pass, best of reps runs each,
+ * keeps the fastest (ties within 1% go to fewer blocks: less search scratch), records the choice
+ * for the device and configuration class (later sessions of the class start from it; with the
+ * environment variable NLFEM_TUNE_FILE set, records persist in that file), and leaves the
+ * session assembled with it. */
+typedef struct nlfem_tuning {
+    int bfs_blocks_per_sm, pass_blocks_per_sm;   /* chosen (pass: 0 for the colored and vector paths) */
+    int bfs_candidates, pass_candidates;         /* candidates timed: 1 .. n blocks per SM */
+    double bfs_ms[8], pass_ms[8];                /* best phase time (ms) of each candidate */
+} nlfem_tuning;
+int nlfem_session_autotune(nlfem_session *s, int reps, nlfem_tuning *out);
 int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out);
 int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out);
 /* A_Omega u = f_Omega - A_Gamma g by conjugate gradients on problem i's assembled matrix

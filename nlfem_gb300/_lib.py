@@ -48,6 +48,12 @@ class CSR32(ctypes.Structure):
                 ("indices", _ip), ("values", _dp)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("bfs_blocks_per_sm", ctypes.c_int), ("pass_blocks_per_sm", ctypes.c_int),
+                ("bfs_candidates", ctypes.c_int), ("pass_candidates", ctypes.c_int),
+                ("bfs_ms", ctypes.c_double * 8), ("pass_ms", ctypes.c_double * 8)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n_pairs", ctypes.c_long), ("n_candidates", ctypes.c_long),
                 ("n_close", ctypes.c_long), ("nnz_structural", ctypes.c_long),
@@ -90,6 +96,7 @@ def load():
     l.nlfem_session_create.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
     l.nlfem_session_assemble.argtypes = [ctypes.c_void_p]
     l.nlfem_session_assemble_graph.argtypes = [ctypes.c_void_p]
+    l.nlfem_session_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tuning)]
     l.nlfem_session_download.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(CSR)]
     l.nlfem_session_destroy.argtypes = [ctypes.c_void_p]
     l.nlfem_session_destroy.restype = None
@@ -136,7 +143,8 @@ def stats():
 EXPORTED = [
     "nlfem_last_error", "nlfem_device_count", "nlfem_get_stats", "nlfem_stiffness_matrix",
     "nlfem_load_vector", "nlfem_stiffness_batch", "nlfem_csr_free", "nlfem_session_create",
-    "nlfem_session_assemble", "nlfem_session_assemble_graph", "nlfem_session_download", "nlfem_session_destroy",
+    "nlfem_session_assemble", "nlfem_session_assemble_graph", "nlfem_session_autotune", "nlfem_session_download",
+    "nlfem_session_destroy",
     "nlfem_pair_list", "nlfem_pair_blocks", "nlfem_method_retriangulate",
     "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
     "nlfem_par_assemble", "nlfem_load_vector_noalloc", "nlfem_measure_peaks",

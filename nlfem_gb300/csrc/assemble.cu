@@ -215,10 +215,11 @@ __device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method,
             if (xbaryInside<DIM>(&xs[DIM * k], b, P.sqdelta)) return true;
         return false;
     }
-    if (DIM == 2) {
+    if (DIM == 2) {   // retriangulate, retriangulate_unsymm; exactBall: the polygon without cap points
         double R[18];
+        const int caps = method == MTH_EXACT ? 0 : P.caps;
         for (int k = 0; k < nPx; k++)
-            if (xretriangulate(&xs[2 * k], Eb, P.sqdelta, P.caps, R) >= 3) return true;
+            if (xretriangulate(&xs[2 * k], Eb, P.sqdelta, caps, R) >= 3) return true;
     }
     return false;
 }

@@ -141,6 +141,95 @@ __device__ __forceinline__ int xretriangulate(const double *xc, const double *TE
     return Rdx;
 }
 
+// placePointCapCenter (integration.cpp:1300-1351): the circular segment of B_delta(xc) cut off by
+// the chord (ypred, ycur); its centroid goes to cap if it lies in the triangle, and its area is
+// returned (0 otherwise). acos, sin and pow are CUDA's: they may differ from the host's in the
+// last bit.
+__device__ __forceinline__ double xcap_center(const double *ypred, const double *ycur, const double *xc, double sqdelta,
+                                              const double *TE, const double *na, const double *nb, const double *nc,
+                                              double orientation, double *cap) {
+    const double p1[2] = {xadd(xc[0], xmul(ypred[0], -1.0)), xadd(xc[1], xmul(ypred[1], -1.0))};
+    const double p2[2] = {xadd(xc[0], xmul(ycur[0], -1.0)), xadd(xc[1], xmul(ycur[1], -1.0))};
+    const double alpha = 0.5 * acos(xdiv(xdot2(p1[0], p1[1], p2[0], p2[1]), sqdelta));
+    // rightNormal(ycur, ypred, orientation) (mathhelpers.cpp:74-78)
+    const double s0 = xmul(xsub(ypred[1], ycur[1]), orientation), s1 = xmul(xsub(ycur[0], ypred[0]), orientation);
+    const double scaling = (4 * sqrt(sqdelta) * pow(sin(alpha), 3)) / (3 * (2 * alpha - sin(2 * alpha))) *
+                           sqrt(1. / xdot2(s0, s1, s0, s1));
+    const double y[2] = {xadd(xc[0], xmul(s0, scaling)), xadd(xc[1], xmul(s1, scaling))};
+    if (xinTriangle(y, TE, na, nb, nc)) {
+        cap[0] = y[0];
+        cap[1] = y[1];
+        return (sqdelta / 2) * (2 * alpha - sin(2 * alpha));
+    }
+    return 0.0;
+}
+
+// method_exact (integration.cpp:1632-1761): the polygon of B_delta(xc) and the triangle without
+// cap points (R, n points, as method_retriangulate without caps) and up to three circular
+// segments: centroids in caps, areas in capw, their number in *ncaps. A segment counts when its
+// area is not within 1e-15 of zero (double_eq, mathhelpers.cpp:370-373).
+__device__ __forceinline__ int xmethod_exact(const double *xc, const double *TE, double sqdelta, double *R,
+                                             double *caps, double *capw, int *ncaps) {
+    int Rdx = 0, nc_ = 0;
+    bool is_onEdge = false;
+    const double orientation = -xsignDet2(TE);
+    double na[2], nb[2], nc[2];
+    na[0] = xmul(xsub(TE[3], TE[1]), orientation); na[1] = xmul(xsub(TE[0], TE[2]), orientation);
+    nb[0] = xmul(xsub(TE[5], TE[3]), orientation); nb[1] = xmul(xsub(TE[2], TE[4]), orientation);
+    nc[0] = xmul(xsub(TE[1], TE[5]), orientation); nc[1] = xmul(xsub(TE[4], TE[0]), orientation);
+#pragma unroll 1
+    for (int k = 0; k < 3; k++) {
+        const double *p = &TE[2 * k];
+        const double *q = &TE[2 * (k == 2 ? 0 : k + 1)];
+        const double a0 = xsub(q[0], xc[0]), a1 = xsub(q[1], xc[1]);
+        const double b0 = xsub(p[0], q[0]), b1 = xsub(p[1], q[1]);
+        if (xsqdist2(p, xc) <= sqdelta) {
+            if (Rdx < 9) { R[2 * Rdx] = p[0]; R[2 * Rdx + 1] = p[1]; Rdx += 1; }
+            is_onEdge = false;
+        }
+        const double ab = xdot2(a0, a1, b0, b1);
+        const double aa = xdot2(a0, a1, a0, a1);
+        const double bb = xdot2(b0, b1, b0, b1);
+        const double aad = xsub(aa, sqdelta);
+        const double v = xsub(xmul(ab, ab), xmul(aad, bb));
+        if (v >= 0) {
+            const double term1 = xdiv(-ab, bb);
+            const double term2 = xdiv(xsqrt(v), bb);
+            double lam1, lam2;
+            if (term1 > 0) {
+                lam1 = xadd(term1, term2);
+                lam2 = xdiv(xmul(xdiv(1.0, lam1), aad), bb);
+            } else {
+                lam2 = xsub(term1, term2);
+                lam1 = xdiv(xmul(xdiv(1.0, lam2), aad), bb);
+            }
+#pragma unroll 1
+            for (int qi = 0; qi < 2; qi++) {
+                const double lam = qi ? lam2 : lam1;
+                bool ok = (0 <= lam) && (lam <= 1);
+                if (qi) {
+                    const double dl = xsub(lam1, lam2);
+                    ok = ok && (xmul(dl, dl) > 0);
+                }
+                if (!ok) continue;
+                const double y[2] = {xadd(xmul(lam, b0), q[0]), xadd(xmul(lam, b1), q[1])};
+                if (is_onEdge && nc_ < 3) {
+                    capw[nc_] = xcap_center(&R[2 * (Rdx - 1)], y, xc, sqdelta, TE, na, nb, nc, orientation, &caps[2 * nc_]);
+                    nc_ += !(fabs(capw[nc_]) < 1e-15);
+                }
+                if (Rdx < 9) { R[2 * Rdx] = y[0]; R[2 * Rdx + 1] = y[1]; Rdx += 1; }
+                is_onEdge = true;
+            }
+        }
+    }
+    if (is_onEdge && nc_ < 3) {
+        capw[nc_] = xcap_center(&R[2 * (Rdx - 1)], &R[0], xc, sqdelta, TE, na, nb, nc, orientation, &caps[2 * nc_]);
+        nc_ += !(fabs(capw[nc_]) < 1e-15);
+    }
+    *ncaps = nc_;
+    return Rdx;
+}
+
 // baryCenter(dim, E) (mathhelpers.cpp:184-196) and method_baryCenter (integration.cpp:1262-1280):
 // true iff |x - bary(T)|^2 <= delta^2.
 template <int DIM>
@@ -197,7 +286,7 @@ enum KernelId {
 // MTH_RETRI_UNSYMM .. MTH_NOTRUNC: 2D, FP64 passes only.
 enum MethodId {
     MTH_RETRIANGULATE = 0, MTH_BARYCENTER = 1, MTH_FRACTIONAL = 2, MTH_RETRI_UNSYMM = 3, MTH_SUBSET = 4,
-    MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7, MTH_WEAKSING = 8
+    MTH_AVERAGE = 5, MTH_BARY_RT = 6, MTH_NOTRUNC = 7, MTH_WEAKSING = 8, MTH_EXACT = 9
 };
 // LOAD_LINEARFIELD .. LOAD_BOTHFIELD are vector-valued (outdim 2, except LOAD_LINEARFIELD3D: 3).
 enum LoadId {

@@ -89,6 +89,7 @@ static int method_id(const char *s) {
     if (k == "averageBall") return MTH_AVERAGE;
     if (k == "baryCenterRT") return MTH_BARY_RT;
     if (k == "noTruncation") return MTH_NOTRUNC;
+    if (k == "exactBall") return MTH_EXACT;
     return -1;
 }
 static int load_id(const char *s) {
@@ -229,7 +230,7 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, std::string("integration method ") +
                         (P.remote >= MTH_RETRI_UNSYMM ? p.method_remote : p.method_close) + " runs on the fp64 path only (precision \"fp64\")");
-        if (P.kernel >= KER_LABELED) {   // label- or position-dependent kernels of 2D meshes
+        if (P.kernel >= KER_LABELED && P.kernel <= KER_CONSTTRUNC) {   // label- or position-dependent kernels of 2D meshes
             if (p.dim != 2) return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " is implemented for 2D meshes only");
             if (p.precision != NLFEM_PREC_FP64)
                 return fail(NLFEM_ERR_UNSUPPORTED, std::string("kernel ") + p.kernel + " runs on the fp64 path only (precision \"fp64\")");
@@ -402,6 +403,8 @@ struct Session {
     long long hint_pat_cap = 0, hint_po_cap = 0, hint_nE = -1, hint_nV = -1;
     int pmode = 0;                          // PM_COLORED, PM_RETRI, PM_BARY or PM_VEC
     int od = 1;                             // outdim: rows od v + i (PM_VEC when od > 1)
+    int tune_bfs = 0, tune_pass = 0;        // blocks per SM of the search / persistent pass (0: occupancy)
+    int used_bfs = 0, used_pass = 0;        // what the last assembly launched
     // graph replay: the stages run without host reads, on the sizes of the previous assembly
     bool replay = false;
     long long nadj = 0, htot = 0;
@@ -775,7 +778,10 @@ static int run_bfs(Session &S) {
     auto kfn = S.prec == PREC_MIX ? k_bfs<DIM, PREC_MIX> : k_bfs<DIM, PREC_F64>;
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BFS_THREADS, 0));
-    const int nblocks = S.nSM * std::max(per_sm, 1);
+    per_sm = std::max(per_sm, 1);
+    if (S.tune_bfs > 0) per_sm = std::min(per_sm, S.tune_bfs);   // autotuned (nlfem_session_autotune)
+    S.used_bfs = per_sm;
+    const int nblocks = S.nSM * per_sm;
     const int nwarps = nblocks * BFS_WARPS;
     if (S.qcap == 0) S.qcap = std::min<long long>(S.maxNE + 1, 8192);
     if (S.pool_cap == 0) {
@@ -1339,6 +1345,8 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PR &pr, cons
         CK(cudaFuncSetAttribute(L[i].k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&L[i].per_sm, L[i].k, threads, smem));
         if (L[i].per_sm < 1) return fail(NLFEM_ERR_UNSUPPORTED, "quadrature rule too large for the pass's shared memory");
+        if (S.tune_pass > 0) L[i].per_sm = std::min(L[i].per_sm, S.tune_pass);   // autotuned
+        S.used_pass = std::max(i ? S.used_pass : 0, L[i].per_sm);
     }
     MixArgs ma;
     ma.p = pa;
@@ -2010,6 +2018,115 @@ static int session_solve(Session &S, int i, const double *f, const double *g, do
 }
 }  // namespace nlg
 
+// ---------------------------------------------------------------- autotuner
+// The launch shape of the two persistent kernels of an assembly, the pair search (one warp per
+// outer element) and the one-sided quadrature pass (warps over a global element counter), is the
+// number of blocks per SM, at most the occupancy limit. nlfem_session_autotune times each
+// candidate on the session's own workload (CUDA events of the phase, best of reps assemblies),
+// keeps the fastest (on a tie within 1%, the smaller one: fewer warps need less search scratch),
+// and records it per device and configuration class; later sessions of the same class start from
+// the recorded shape. With NLFEM_TUNE_FILE set, the records are read from and written to that file.
+static std::mutex g_tune_mu;
+static std::map<std::string, int> g_tune;
+static bool g_tune_loaded = false;
+
+static std::string tune_key(const Session &S, const char *stage) {
+    cudaDeviceProp prop;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string name = "gpu";
+    if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) name = std::string(prop.name) + "/" + std::to_string(prop.multiProcessorCount);
+    else cudaGetLastError();
+    int kc = 0;
+    for (const ProbParams &q : S.hprm) kc |= 1 << kernel_class(q);
+    for (char &c : name) if (c == ' ') c = '_';
+    return name + "|" + stage + "|d" + std::to_string(S.dim) + "|m" + std::to_string(S.pmode) + "|p" +
+           std::to_string(S.prec) + (S.onesided64 ? "o" : "") + "|k" + std::to_string(kc);
+}
+
+static void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = getenv("NLFEM_TUNE_FILE");
+    if (!path || !path[0]) return;
+    FILE *f = fopen(path, "r");
+    if (!f) return;
+    char key[512];
+    int v;
+    while (fscanf(f, "%511s %d", key, &v) == 2) g_tune[key] = v;
+    fclose(f);
+}
+
+static void tune_save_locked() {
+    const char *path = getenv("NLFEM_TUNE_FILE");
+    if (!path || !path[0]) return;
+    FILE *f = fopen(path, "w");
+    if (!f) return;
+    for (auto &e : g_tune) fprintf(f, "%s %d\n", e.first.c_str(), e.second);
+    fclose(f);
+}
+
+// A new session of a configuration class that was tuned before starts from the recorded shapes.
+static void tune_apply(Session &S) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    tune_load_locked();
+    auto b = g_tune.find(tune_key(S, "bfs"));
+    if (b != g_tune.end()) S.tune_bfs = b->second;
+    auto p = g_tune.find(tune_key(S, "pass"));
+    if (p != g_tune.end()) S.tune_pass = p->second;
+}
+
+static int session_autotune(Session &S, int reps, nlfem_tuning *out) {
+    if (reps < 1) reps = 1;
+    memset(out, 0, sizeof(*out));
+    if (S.gexec) { cudaGraphExecDestroy(S.gexec); S.gexec = nullptr; }   // shapes are baked into a graph
+    int r;
+    // the search
+    int best = 0;
+    double best_ms = 1e300;
+    for (int b = 1; b <= 8; b++) {
+        S.tune_bfs = b;
+        double t = 1e300;
+        for (int i = 0; i < reps; i++) {
+            if ((r = run_system(S))) return r;
+            t = std::min(t, S.stats.ms_bfs);
+        }
+        if (S.used_bfs < b) break;   // beyond the occupancy limit: the same shape as b - 1
+        out->bfs_ms[b - 1] = t;
+        out->bfs_candidates = b;
+        if (t < best_ms * 0.99) { best_ms = t; best = b; }
+    }
+    S.tune_bfs = best;
+    out->bfs_blocks_per_sm = best;
+    // the persistent quadrature pass (one-sided modes only)
+    if (S.pmode == PM_RETRI || S.pmode == PM_BARY) {
+        best = 0;
+        best_ms = 1e300;
+        for (int b = 1; b <= 8; b++) {
+            S.tune_pass = b;
+            double t = 1e300;
+            for (int i = 0; i < reps; i++) {
+                if ((r = run_system(S))) return r;
+                t = std::min(t, S.stats.ms_quad);
+            }
+            if (S.used_pass < b) break;
+            out->pass_ms[b - 1] = t;
+            out->pass_candidates = b;
+            if (t < best_ms * 0.99) { best_ms = t; best = b; }
+        }
+        S.tune_pass = best;
+        out->pass_blocks_per_sm = best;
+    }
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        tune_load_locked();
+        g_tune[tune_key(S, "bfs")] = S.tune_bfs;
+        if (S.pmode == PM_RETRI || S.pmode == PM_BARY) g_tune[tune_key(S, "pass")] = S.tune_pass;
+        tune_save_locked();
+    }
+    return run_system(S);   // the session's matrix, assembled with the chosen shapes
+}
+
 extern "C" {
 
 const char *nlfem_last_error(void) { return g_err.c_str(); }
@@ -2050,6 +2167,7 @@ int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out)
     nlfem_session *s = new nlfem_session();
     s->probs.assign(probs, probs + n);
     r = session_init(s->S, probs, n, true);
+    if (!r) tune_apply(s->S);
     if (!r) r = session_upload(s->S, probs);
     if (!r) { cudaError_t e = cudaStreamSynchronize(s->S.st); if (e != cudaSuccess) r = fail(NLFEM_ERR_CUDA, cudaGetErrorString(e)); }
     if (r) { delete s; return r; }
@@ -2060,6 +2178,11 @@ int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out)
 int nlfem_session_assemble(nlfem_session *s) {
     if (!s) return fail(NLFEM_ERR_INVALID, "null session");
     return run_system(s->S);
+}
+
+int nlfem_session_autotune(nlfem_session *s, int reps, nlfem_tuning *out) {
+    if (!s || !out) return fail(NLFEM_ERR_INVALID, "null argument");
+    return session_autotune(s->S, reps, out);
 }
 
 int nlfem_session_assemble_graph(nlfem_session *s) {

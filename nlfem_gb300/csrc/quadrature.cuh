@@ -357,6 +357,52 @@ __device__ __noinline__ void rule_notrunc_prime(const ProbParams &P, const Rule 
     }
 }
 
+// integrate_exact, "exactBall" (integration.cpp:706-907): per outer point the polygon of
+// method_exact (fan sub-triangles, the inner rule on each) plus its circular segments, each at its
+// centroid with its area as weight; weight 2, no prime blocks. The blocks leave out |aT|.
+__device__ int rule_exact(const ProbParams &P, const Rule &rule, const double *Ea, const double *Eb,
+                          int la, int lb, double *L, double *N, unsigned &nsub, int *err) {
+    int interacts = 0;
+    for (int k = 0; k < rule.nPx; k++) {
+        double x[2], R[18], caps[6], capw[3];
+        int ncaps = 0;
+        xtoPhys<2>(Ea, &rule.Px[2 * k], x);
+        const int n = xmethod_exact(x, Eb, P.sqdelta, R, caps, capw, &ncaps);
+        interacts |= n >= 3;
+        double iL = 0, iN[3] = {0, 0, 0};
+        for (int r = 0; r + 2 < n; r++) {
+            nsub++;
+            const double tri[6] = {R[0], R[1], R[2 * r + 2], R[2 * r + 3], R[2 * r + 4], R[2 * r + 5]};
+            const double rTdet = xabsDet2(tri);
+            for (int i = 0; i < rule.nPy; i++) {
+                double y[2];
+                y[0] = (tri[2] - tri[0]) * rule.Py[2 * i] + (tri[4] - tri[0]) * rule.Py[2 * i + 1] + tri[0];
+                y[1] = (tri[3] - tri[1]) * rule.Py[2 * i] + (tri[5] - tri[1]) * rule.Py[2 * i + 1] + tri[1];
+                iL += kernel_f64<2>(P, x, la, y, lb, err) * rule.dy[i] * rTdet;
+                double ref[2];
+                if (!xtoRef(Eb, y, ref)) atomicOr(&err[4], 1);
+                const double kp = kernel_f64<2>(P, y, lb, x, la, err);
+                const double psi[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
+                for (int b = 0; b < 3; b++) iN[b] += psi[b] * kp * rule.dy[i] * rTdet;
+            }
+        }
+        for (int c = 0; c < ncaps; c++) {
+            iL += kernel_f64<2>(P, x, la, &caps[2 * c], lb, err) * capw[c];
+            double ref[2];
+            if (!xtoRef(Eb, &caps[2 * c], ref)) atomicOr(&err[4], 1);
+            const double kp = kernel_f64<2>(P, &caps[2 * c], lb, x, la, err);
+            const double psi[3] = {1.0 - ref[0] - ref[1], ref[0], ref[1]};
+            for (int b = 0; b < 3; b++) iN[b] += psi[b] * kp * capw[c];
+        }
+        for (int a = 0; a < 3; a++) {
+            const double pa = 2.0 * rule.psix[3 * k + a];
+            for (int b = a; b < 3; b++) L[sym_idx<3>(a, b)] += pa * rule.psix[3 * k + b] * rule.dx[k] * iL;
+            for (int b = 0; b < 3; b++) N[3 * a + b] += pa * rule.dx[k] * iN[b];
+        }
+    }
+    return interacts;
+}
+
 // Out of line: the rules are rare, and inlined they would take registers from the passes' common
 // paths.
 __device__ __noinline__ int rule_out_f64(const ProbParams &P, int method, const Rule &rule, const double *Ea, const double *Eb,
@@ -366,6 +412,7 @@ __device__ __noinline__ int rule_out_f64(const ProbParams &P, int method, const 
     case MTH_SUBSET: case MTH_AVERAGE: return rule_subset(P, rule, Ea, Eb, adetb, la, lb, L, N, nsub, err);
     case MTH_BARY_RT: return rule_baryrt(P, rule, Ea, Eb, adetb, la, lb, L, N, nsub, err);
     case MTH_NOTRUNC: nsub += rule.nPx; rule_notrunc_out(P, rule, Ea, Eb, adetb, la, lb, L, N, err); return 1;
+    case MTH_EXACT: return rule_exact(P, rule, Ea, Eb, la, lb, L, N, nsub, err);
     }
     return 0;
 }

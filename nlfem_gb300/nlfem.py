@@ -333,6 +333,16 @@ class Session:
         _lib.check(fn(self.h))
         return _lib.stats()
 
+    def autotune(self, reps=2):
+        """Times 1, 2, ... blocks per SM for the pair search and the persistent quadrature pass on
+        this session's workload, keeps the fastest for the session (and for later sessions of the
+        same device and configuration class), and leaves the matrices assembled with it. Returns
+        {"bfs": chosen, "pass": chosen, "bfs_ms": [...], "pass_ms": [...]}."""
+        t = _lib.Tuning()
+        _lib.check(self.lib.nlfem_session_autotune(self.h, int(reps), ctypes.byref(t)))
+        return {"bfs": t.bfs_blocks_per_sm, "pass": t.pass_blocks_per_sm,
+                "bfs_ms": list(t.bfs_ms[:t.bfs_candidates]), "pass_ms": list(t.pass_ms[:t.pass_candidates])}
+
     def download(self, i=0):
         out32 = _lib.CSR32()
         code = self.lib.nlfem_session_download32(self.h, i, ctypes.byref(out32))

@@ -417,7 +417,7 @@ def test_weak_singular_close_rule(nl, orc):
 
 
 @pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5", "labeled10", "average10",
-                                  "dg10", "weak10", "field8"])
+                                  "exact8", "dg10", "weak10", "field8"])
 def test_gpu_matches_committed_fixtures(nl, name):
     """The FP64 path against the committed oracle fixtures (tests/golden/oracle_cases.npz, made by
     tests/golden/make_oracle_golden.py): bit-exact pattern, values within rounding."""
@@ -964,3 +964,50 @@ def test_vector_kernel_refusals(nl):
         nl.stiffnessMatrix(m, k, conf2d(precision="mixed"))
     with pytest.raises(NlfemError, match="output components"):
         nl.stiffnessMatrix(dict(m, outdim=1), dict(k, outputdim=1), conf2d())
+
+
+
+@pytest.mark.parametrize("n,delta,kern,jit", [(10, 0.1, "constant", 0.15), (14, 0.12, "parabola", 0.2), (9, 0.25, "constant", 0.0)])
+def test_exact_ball_matches_oracle(nl, orc, n, delta, kern, jit):
+    """exactBall (integration.cpp:706-907, 1300-1351, 1632-1761) on the FP64 path: the polygon
+    without cap points plus up to three circular segments at their centroids. The pair search takes
+    the polygon's interaction test. Within 1e-12 of the oracle (CUDA's acos / sin / pow may differ
+    from the host's in the last bit)."""
+    m = square_mesh(n, delta, jitter=jit, seed=n + 40)
+    k = {"function": kern, "horizon": delta, "outputdim": 1}
+    c = conf2d(method="exactBall")
+    A = nl.stiffnessMatrix(m, k, c)
+    B = orc.assemble(m, k, c)["A"]
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)
+    pairs = orc.assemble(m, k, c, want_pairs=True)["pairs"]
+    sel = pairs[np.random.Generator(np.random.PCG64(n)).choice(len(pairs), min(300, len(pairs)), replace=False)]
+    g, gr = nl.pair_blocks(m, k, c, sel)
+    o, orr = orc.pair_blocks(m, k, c, sel)
+    np.testing.assert_array_equal(gr != 0, orr != 0)
+    np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
+
+
+def test_autotune_keeps_the_matrix(nl):
+    """The launch-shape autotuner (nlfem_session_autotune) times 1, 2, ... blocks per SM of the
+    pair search and the persistent pass and keeps the fastest; the shapes change no bit of the
+    matrix (fixed-point sums, per-element search order)."""
+    m = square_mesh(48, 0.1, jitter=0.2, seed=61)
+    k = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    s = nl.Session([(m, k, conf2d(precision="mixed"))])
+    try:
+        s.assemble()
+        A0 = s.download(0)
+        t = s.autotune(reps=1)
+        A1 = s.download(0)
+        assert t["bfs"] >= 1 and len(t["bfs_ms"]) >= 1
+        assert t["pass"] >= 1 and len(t["pass_ms"]) >= 1
+        assert all(x > 0 for x in t["bfs_ms"] + t["pass_ms"])
+        assert np.array_equal(A0.indptr, A1.indptr) and np.array_equal(A0.indices, A1.indices)
+        assert np.array_equal(A0.data, A1.data)
+        s.assemble(graph=True)   # a graph captured after tuning replays the tuned shapes
+        s.assemble(graph=True)
+        assert np.array_equal(s.download(0).data, A0.data)
+    finally:
+        s.close()

@@ -6,12 +6,15 @@
  *   par_evaluateMass      <- include/Cassemble.h:202-204 (include/Cassemble.pxd:27-29)
  *   method_retriangulate  <- include/Cassemble.h:62-64   (include/Cassemble.pxd:32-34)
  *   toRef                 <- include/Cassemble.h:68      (include/Cassemble.pxd:38)
- *   toPhys                <- include/Cassemble.h:70      (include/Cassemble.pxd:39)
+ *   toPhys                <- include/Cassemble.h:69-70   (include/Cassemble.pxd:39)
  *   solve2x2              <- include/Cassemble.h:71      (include/Cassemble.pxd:40)
+ *   method_retriangulateInfty <- include/Cassemble.h:65-67 (include/Cassemble.pxd:35-37): exported
+ *                            so that the reference's module links; it aborts (no L-infinity ball)
  *
  * Like the reference they abort() on invalid input; the C ABI in nlfem_gpu.h returns status
- * codes instead. The computation runs on the GPU. method_retriangulateInfty (Cassemble.pxd:35-37)
- * is not exported: the L-infinity ball has no GPU implementation yet.
+ * codes instead. The computation runs on the GPU. include/Cassemble.h carries the reference's
+ * header name and includes this file, so the reference's cython/nlfem.pyx compiles against this
+ * library unchanged (nlfem_gb300/dropin.py).
  */
 #ifndef NLFEM_CASSEMBLE_COMPAT_H
 #define NLFEM_CASSEMBLE_COMPAT_H
@@ -39,6 +42,9 @@ int method_retriangulate(const double *xCenter, const double *TE, double sqdelta
                          double *reTriangleList, int isPlacePointOnCap);
 void toRef(const double *E, const double *phys_x, double *ref_p);
 void toPhys(const double *E, const double *p, int dim, double *out_x);
+void toPhys(const double *E, const double *p, double *out_x);
+int method_retriangulateInfty(const double *xCenter, const double *TE, double sqdelta,
+                              double *reTriangleList, int isPlacePointOnCap);
 void solve2x2(const double *A, const double *b, double *x);
 
 #endif

@@ -160,6 +160,20 @@ void toPhys(const double *E, const double *p, int dim, double *out_x) {
     die_on(nlfem_toPhys(E, p, dim, out_x), "toPhys");
 }
 
+// The 2D overload toPhys(E, p, out) (Cassemble.h:69, mathhelpers.cpp:210-215).
+void toPhys(const double *E, const double *p, double *out_x) {
+    die_on(nlfem_toPhys(E, p, 2, out_x), "toPhys");
+}
+
+// method_retriangulateInfty (Cassemble.h:65-67, Cassemble.pxd:35-37): the reference triangulates the
+// L-infinity ball with CGAL; this library has no L-infinity ball, so the call aborts with a message,
+// as the reference aborts on an option it lacks. It is exported so that modules compiled against
+// the reference's Cassemble.pxd (which declares it) link unchanged.
+int method_retriangulateInfty(const double *, const double *, double, double *, int) {
+    fprintf(stderr, "ERROR in method_retriangulateInfty: the L-infinity ball is not implemented in this library\n");
+    abort();
+}
+
 void solve2x2(const double *A, const double *b, double *x) {
     die_on(nlfem_solve2x2(A, b, x), "solve2x2");
 }

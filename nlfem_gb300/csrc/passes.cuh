@@ -119,6 +119,8 @@ struct PassArgs {
     const int *list;            // elements of this color
     int count;
     const int *T32, *labV, *eprob, *labT;
+    const int *Tv;              // vertex table of the close-pair test (T32, except under DG: T32 then
+                                // holds the element DOFs, which no two elements share)
     const double *EC, *adet;
     const float *EChi, *EClo;   // double-float split of EC
     const float *adetf;         // |det| in FP32
@@ -659,8 +661,13 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                 bool done = false;
                 if (DIM == 2 && frac_close) {
                     bool close = (bT == T);
-                    for (int i = 0; i < dV; i++)
-                        for (int j = 0; j < dV; j++) close |= (tv[i] == bv[j]);
+                    if (a.Tv == a.T32) {
+                        for (int i = 0; i < dV; i++)
+                            for (int j = 0; j < dV; j++) close |= (tv[i] == bv[j]);
+                    } else {
+                        for (int i = 0; i < dV; i++)
+                            for (int j = 0; j < dV; j++) close |= (a.Tv[(long long)T * dV + i] == a.Tv[(long long)bT * dV + j]);
+                    }
                     if (close) {
                         nclose++;
                         const long long cs = close_slot(a.xadj, a.adj, T, bT);
@@ -761,8 +768,13 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
                     bool done = false;
                     if (frac_close) {
                         bool close = (aT == T);
-                        for (int i = 0; i < 3; i++)
-                            for (int j = 0; j < 3; j++) close |= (tv[i] == av[j]);
+                        if (a.Tv == a.T32) {
+                            for (int i = 0; i < 3; i++)
+                                for (int j = 0; j < 3; j++) close |= (tv[i] == av[j]);
+                        } else {
+                            for (int i = 0; i < 3; i++)
+                                for (int j = 0; j < 3; j++) close |= (a.Tv[(long long)T * 3 + i] == a.Tv[(long long)aT * 3 + j]);
+                        }
                         if (close) {
                             const long long cs = close_slot(a.xadj, a.adj, aT, T);
                             if (cs < 0) { atomicOr(&a.err[3], 1); }

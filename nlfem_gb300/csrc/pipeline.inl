@@ -223,8 +223,6 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         if (P.singular && P.close == MTH_WEAKSING && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, "the weakSingular close rule runs on the fp64 path only (precision \"fp64\")");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
-        if (p.is_dg && P.singular)   // the close-pair rule needs vertex sharing across element DOFs
-            return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz with singular kernels (close-pair rule) is not implemented");
         if (p.is_dg && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz runs on the fp64 path only (precision \"fp64\")");
         if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision != NLFEM_PREC_FP64)
@@ -1276,7 +1274,9 @@ static int run_close(Session &S) {
     k_close_pairs<<<grid_for(nE, 256), 256, 0, S.st>>>(S.xadj.get<long long>(), S.adj.get<int>(), S.labT.get<int>(), S.eprob.get<int>(), S.prm.get<ProbParams>(), nE, S.closeA.get<int>(), S.closeB.get<int>()); ++S.nlaunch;
     QuadArgs a;
     memset(&a, 0, sizeof(a));
-    a.pA = S.closeA.get<int>(); a.pB = S.closeB.get<int>(); a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>();
+    // under DG the rows are element DOFs (S.T32) and the close pairs are found on the vertices
+    a.pA = S.closeA.get<int>(); a.pB = S.closeB.get<int>(); a.T32 = S.dg_rows ? S.dgT32.get<int>() : S.T32.get<int>();
+    a.labV = S.labV.get<int>();
     a.labT = S.labT.get<int>();
     a.eprob = S.eprob.get<int>(); a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>();
     a.probs = S.prm.get<ProbParams>(); a.P = nslot; a.err = S.err.get<int>();
@@ -1472,6 +1472,7 @@ static int run_passes(Session &S) {
     PassArgs a;
     memset(&a, 0, sizeof(a));
     a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>(); a.eprob = S.eprob.get<int>(); a.labT = S.labT.get<int>();
+    a.Tv = S.dg_rows ? S.dgT32.get<int>() : a.T32;
     a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>(); a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
     a.adetf = S.adetf.get<float>();
     a.probs = S.prm.get<ProbParams>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();

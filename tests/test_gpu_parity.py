@@ -330,6 +330,32 @@ def test_dg_matches_oracle(nl, orc, kname, method):
     assert np.abs(S - C.toarray()).max() <= 1e-12 * abs(C).max()
 
 
+@pytest.mark.parametrize("close,kname", [("fractional", "fractional"), ("weakSingular", "linearPrototypeMicroelastic")])
+def test_dg_singular_kernels(nl, orc, close, kname):
+    """DG with a singular kernel: the close pairs (sharing a vertex) take the Duffy rule, found on
+    the vertex table while the rows are element DOFs (Cassemble.cpp:580-585, integration.cpp:82-288);
+    against the oracle, and summed over the vertex copies against the CG assembly."""
+    m = square_mesh(8, 0.2, jitter=0.1, seed=16)
+    s = 0.4 if kname == "fractional" else -0.5
+    k = {"function": kname, "horizon": 0.2, "outputdim": 1, "fractional_s": s}
+    c = _conf_dg()
+    c["closeElements"] = close
+    c["quadrature"]["tensorGaussDegree"] = 3
+    A = nl.stiffnessMatrix(dict(m), k, c)
+    B = orc.assemble(m, k, c)["A"]
+    nE, nV = m["elements"].shape[0], m["vertices"].shape[0]
+    assert A.shape == (3 * nE, 3 * nE)
+    assert same_pattern(A, B)
+    fro, mx = rel_errors(A, B)
+    assert fro < 1e-11 and mx < 1e-11, (fro, mx)
+    cc = dict(c, ansatz="CG")
+    C = nl.stiffnessMatrix(dict(m), k, cc)
+    P = sp.csr_matrix((np.ones(3 * nE), (np.arange(3 * nE), m["elements"].ravel())), shape=(3 * nE, nV))
+    S = (P.T @ A @ P).toarray()
+    S[m["vertexLabels"] <= 0] = 0
+    assert np.abs(S - C.toarray()).max() <= 1e-11 * abs(C).max()
+
+
 def test_dg_load_vector(nl, orc):
     m = square_mesh(12, 0.1, jitter=0.2, seed=15)
     f = nl.loadVector(dict(m), {"function": "linear"}, _conf_dg())
@@ -364,12 +390,6 @@ def test_dg_refusals(nl):
     m = square_mesh(6, 0.1)
     with pytest.raises(NlfemError, match="fp64 path only"):
         nl.stiffnessMatrix(dict(m), KC, _conf_dg(precision="mixed"))
-    kf = {"function": "fractional", "horizon": 0.1, "outputdim": 1, "fractional_s": 0.4}
-    cf = _conf_dg()
-    cf["closeElements"] = "fractional"
-    cf["quadrature"]["tensorGaussDegree"] = 3
-    with pytest.raises(NlfemError, match="singular kernels"):
-        nl.stiffnessMatrix(dict(m), kf, cf)
     with pytest.raises(NlfemError, match="one at a time"):
         nl.stiffnessMatrix_batch([(dict(m), KC, _conf_dg()), (dict(m), KC, _conf_dg())])
 

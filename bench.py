@@ -64,9 +64,12 @@ def vs_reference(mats, dg):
     sampled rows; the worst over the problems of a batch."""
     from nlfem_gb300 import digest
     digests, meta = dg
-    res = [digest.compare(A, digests[f"p{i}"]) for i, A in enumerate(mats)]
+    res = [digest.compare(A, digests[f"p{i}"]) for i, A in enumerate(mats) if f"p{i}" in digests]
+    if not res:
+        return None
     return {"pattern_identical": all(r["pattern_identical"] for r in res),
-            "fro_est": max(r["fro_est"] for r in res), "max_rows": max(r["max_rows"] for r in res)}
+            "fro_est": max(r["fro_est"] for r in res), "max_rows": max(r["max_rows"] for r in res),
+            "problems_compared": len(res)}
 
 
 def config_dict(args, extra, problems):

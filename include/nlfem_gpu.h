@@ -124,6 +124,8 @@ typedef struct nlfem_stats {
     long n_items_in;     /* one-sided mixed passes: (pair, outer point) items whose ball holds the
                             inner element (retriangulate) or its barycenter (baryCenter) */
     long n_items_cut;    /* one-sided mixed retriangulate pass: items whose ball cuts the element */
+    long slot_map;       /* one-sided passes: matrix slots found by 1 window-rank bitmaps (rows whose
+                            column numbers span a narrow range), 2 per-row hash tables, 0 neither */
 } nlfem_stats;
 
 const char *nlfem_last_error(void);

@@ -258,15 +258,23 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
     }
     if (DIM != 2) return false;
     const F2 p[3] = {f2(pb[0], pb[1]), f2(pb[2], pb[3]), f2(pb[4], pb[5])};
+    // First the cheap certain answer from every outer point: one vertex strictly inside and none
+    // on the sphere means both edges through it cross once, so the polygon has at least three
+    // points. Only when no point gives it does any point need its polygon; points whose ball
+    // clears the triangle are skipped.
+    unsigned cut = 0;   // outer points whose ball may cut the triangle
     for (int k = 0; k < nPx; k++) {
         const F2 x = f2(xsf[2 * k], xsf[2 * k + 1]);
         const F2 Q[3] = {p[0] - x, p[1] - x, p[2] - x};
         const float d0 = dot(Q[0], Q[0]), d1 = dot(Q[1], Q[1]), d2 = dot(Q[2], Q[2]);
         const bool clear = (d0 < sqlo || d0 > sqhi) && (d1 < sqlo || d1 > sqhi) && (d2 < sqlo || d2 > sqhi);
-        // one vertex strictly inside and none on the sphere: both edges through it cross once,
-        // so the polygon has at least three points
         if (clear && (d0 < sqlo || d1 < sqlo || d2 < sqlo)) return true;
-        if (fclassify(Q, P.sqdelta_f) == CLS_OUT) continue;
+        if (fclassify(Q, P.sqdelta_f) != CLS_OUT) cut |= 1u << k;
+    }
+    for (; cut; cut &= cut - 1) {
+        const int k = __ffs(cut) - 1;
+        const F2 x = f2(xsf[2 * k], xsf[2 * k + 1]);
+        const F2 Q[3] = {p[0] - x, p[1] - x, p[2] - x};
         F2 R[9];
         bool amb = false;
         const int n = fretriangulate(Q, P.sqdelta_f, P.caps, R, amb);
@@ -309,15 +317,31 @@ __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, 
     return interacts_filtered<DIM>(P, method, xs, xsf, nPx, Eb, pb, namb);
 }
 
+// One warp per outer element aT: breadth-first search over the vertex-sharing element graph from
+// aT, through the elements that interact with aT (Cassemble.cpp:597-660).
+//   * A group of up to 32 queued elements loads all its vertices at once; each vertex is
+//     expanded the first time the search meets it (per-warp vertex stamps).
+//   * Each fresh vertex lists its incident elements, BFS_UNROLL entries per lane loaded together;
+//     they are then checked one step at a time against the per-warp element stamps (a plain load
+//     and store: an element is met from each of its vertices in quick succession, so the stamp is
+//     usually in L1). Lanes holding the same element in a step keep only the lowest.
+//   * Fresh candidates collect in a per-warp buffer and are tested 32 at a time.
+// Without a singular kernel the walk order does not change the result (the connected component
+// of aT among interacting elements and label-0 bridges), so the queue is consumed in groups of
+// 32 with no level barrier. With one, the candidates found from aT itself (the elements sharing a
+// vertex with it) take the close rule and are all tested before the walk goes on.
+constexpr int BFS_UNROLL = 4;
+
 // 3D searches (barycenter tests, no polygon geometry) fit 64 registers and gain from the doubled
 // residency; the 2D retriangulate test needs more.
 template <int DIM, int PREC>
 __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a, Rule rule) {
     constexpr int dV = DIM + 1;
+    constexpr int U = BFS_UNROLL;
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
     __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];
-    __shared__ int s_buf[BFS_WARPS][64];   // candidates waiting for the interaction test
-    __shared__ int s_vbuf[BFS_WARPS][32 * (DIM + 1)];   // fresh vertices of a frontier group
+    __shared__ int s_buf[BFS_WARPS][32 * U + 32];       // candidates waiting for the interaction test
+    __shared__ int s_vbuf[BFS_WARPS][32 * (DIM + 1)];   // fresh vertices of a queue group
     unsigned namb = 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;   // at most BFS_WARPS
@@ -359,27 +383,39 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
             queue[0] = (int)aT;
         }
         self_pair = __shfl_sync(FULL, self_pair, 0);
-        __syncwarp();   // aT's visited mark before any lane tests a candidate
+        __syncwarp();   // aT's stamp and queue entry before any lane reads them
         cand_local += (lane == 0);
         long long qhead = 0, qtail = 1;
-        int level = 0;
         bool overflow = false;
-        while (qhead < qtail) {
-            const long long lvl_end = qtail;
-            const int method = (P.singular && level == 0) ? P.close : P.remote;
-            int nbuf = 0;
-            // Frontier groups of 32 elements. The neighbours of an element are the elements
-            // incident to its vertices (vertex-sharing adjacency, as the reference's dual graph
-            // with ncommon = 1), so a vertex needs expanding only once per search: the elements
-            // incident to it are seen the first time, whichever dequeued element holds it. The
-            // set of visited elements is the same as the element-wise walk's.
-            for (long long g = qhead; g < lvl_end; g += 32) {
-                int sn = g + lane < lvl_end ? queue[g + lane] : -1;
+        int nbuf = 0;
+        bool lvl0 = true;   // expanding aT itself
+        // tests the last cnt (<= 32) buffered candidates and queues those that interact
+        auto test_batch = [&](int cnt) {
+            const int b = lane < cnt ? buf[nbuf - cnt + lane] : -1;
+            __syncwarp();   // read before later appends reuse the slots
+            nbuf -= cnt;
+            const int method = (P.singular && lvl0) ? P.close : P.remote;
+            bool pair = false;
+            if (b >= 0) {
+                pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
+                cand_local++;
+            }
+            queue_push(pair, b, queue, a.qcap, qtail, overflow);
+        };
+        for (;;) {
+            const long long avail = qtail - qhead;
+            if (avail > 0 && (avail >= 32 || nbuf == 0 || lvl0)) {
+                const int gn = (int)(avail < 32 ? avail : 32);
+                int sn = lane < gn ? queue[qhead + lane] : -1;
+                qhead += gn;
                 if (sn < -1) sn = -sn - 2;   // label-0 bridge stored as -(e+2)
+                int vv[dV];
+#pragma unroll
+                for (int r = 0; r < dV; r++) vv[r] = sn >= 0 ? a.T32[(long long)sn * dV + r] : -1;
                 int nv = 0;
 #pragma unroll
                 for (int r = 0; r < dV; r++) {
-                    int v = sn >= 0 ? a.T32[(long long)sn * dV + r] : -1;
+                    int v = vv[r];
                     const unsigned same = __match_any_sync(FULL, v);
                     if ((__ffs(same) - 1) != lane) v = -1;
                     bool fresh = false;
@@ -390,69 +426,51 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
                     const unsigned m = __ballot_sync(FULL, fresh);
                     if (fresh) vbuf[nv + __popc(m & lanemask_lt())] = v;
                     nv += __popc(m);
-                    __syncwarp();
+                    __syncwarp();   // the stamps of this round before the next round's loads
                 }
                 for (int c0 = 0; c0 < nv; c0 += 32) {
                     const int v = c0 + lane < nv ? vbuf[c0 + lane] : -1;
                     long long beg = 0;
                     int deg = 0;
                     if (v >= 0) { beg = a.vptr[v]; deg = (int)(a.vptr[v + 1] - beg); }
-                    // each lane walks its own vertex's incident elements
                     const int maxdeg = (int)__reduce_max_sync(FULL, (unsigned)deg);
-                    int cand_next = deg > 0 ? a.vel[beg] : -1;   // the list runs one step ahead
-                    for (int jn = 0; jn < maxdeg; jn++) {
-                        int cand = cand_next;
-                        cand_next = jn + 1 < deg ? a.vel[beg + jn + 1] : -1;
-                        const int lab = (P.bridges && cand >= 0) ? a.labT[cand] : 1;   // before the visited store
-                        // lanes holding the same candidate: the lowest one takes it, so the queue
-                        // order (and every order derived from it) does not depend on atomic timing
-                        const unsigned same = __match_any_sync(FULL, cand);
-                        if ((__ffs(same) - 1) != lane) cand = -1;
-                        // the visited array is private to this warp and the candidates of one step
-                        // are distinct, so a plain load and store suffice (steps are ordered by the
-                        // warp synchronisations below; the load may hit L1)
-                        bool fresh = false;
-                        if (cand >= 0) {
-                            fresh = visited[cand - eoff] != stamp;
-                            if (fresh) visited[cand - eoff] = stamp;
+                    for (int j0 = 0; j0 < maxdeg; j0 += U) {
+                        int cand[U];
+#pragma unroll
+                        for (int u = 0; u < U; u++) cand[u] = j0 + u < deg ? a.vel[beg + j0 + u] : -1;
+#pragma unroll
+                        for (int u = 0; u < U; u++) {
+                            int c = cand[u];
+                            const int lb = (P.bridges && c >= 0) ? a.labT[c] : 1;
+                            // lanes holding the same element: the lowest takes it
+                            const unsigned same = __match_any_sync(FULL, c);
+                            if ((__ffs(same) - 1) != lane) c = -1;
+                            bool fresh = false;
+                            if (c >= 0) {
+                                fresh = visited[c - eoff] != stamp;
+                                if (fresh) visited[c - eoff] = stamp;
+                            }
+                            const bool bridge = fresh && lb == 0;
+                            queue_push(bridge, -(c + 2), queue, a.qcap, qtail, overflow);
+                            const bool totest = fresh && !bridge;
+                            const unsigned m = __ballot_sync(FULL, totest);
+                            if (totest) buf[nbuf + __popc(m & lanemask_lt())] = c;
+                            nbuf += __popc(m);
+                            __syncwarp();   // this step's stamps before the next step's loads
                         }
-                        const bool bridge = fresh && lab == 0;
-                        queue_push(bridge, -(cand + 2), queue, a.qcap, qtail, overflow);
-                        // candidates to test are compacted, so the test runs on full warps
-                        const bool totest = fresh && !bridge;
-                        const unsigned m = __ballot_sync(FULL, totest);
-                        if (totest) buf[nbuf + __popc(m & lanemask_lt())] = cand;
-                        nbuf += __popc(m);
-                        __syncwarp();
-                        if (nbuf >= 32) {
-                            const int b = buf[lane];
-                            const bool pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
-                            cand_local++;
-                            queue_push(pair, b, queue, a.qcap, qtail, overflow);
-                            const int rest = nbuf - 32;
-                            const int v2 = lane < rest ? buf[32 + lane] : 0;
-                            __syncwarp();
-                            if (lane < rest) buf[lane] = v2;
-                            nbuf = rest;
-                            __syncwarp();
-                        }
+                        while (nbuf >= 32) test_batch(32);
                     }
                 }
-                if (__any_sync(FULL, overflow)) break;
-            }
-            if (nbuf > 0 && !__any_sync(FULL, overflow)) {
-                const int b = lane < nbuf ? buf[lane] : -1;
-                bool pair = false;
-                if (b >= 0) {
-                    pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
-                    cand_local++;
+                if (lvl0) {   // the close candidates are tested before the walk goes on
+                    while (nbuf > 0) test_batch(nbuf < 32 ? nbuf : 32);
+                    lvl0 = false;
                 }
-                queue_push(pair, b, queue, a.qcap, qtail, overflow);
-                __syncwarp();
+            } else if (nbuf > 0) {
+                test_batch(nbuf < 32 ? nbuf : 32);
+            } else {
+                break;
             }
             if (__any_sync(FULL, overflow)) break;
-            qhead = lvl_end;
-            level++;
         }
         overflow = __any_sync(FULL, overflow);
         if (overflow) {
@@ -554,8 +572,14 @@ struct RowArgs {
     int *ovf;                  // set when the scratch is too small
     // bitmap kernel sources: mode 0, the vertices of the pairs of the elements at the row's
     // vertex (rows of vertices with label > 0, or of every vertex with all_rows); mode 1, the
-    // union of a given row (srcoff / srccnt / srccols) and a given transposed row (tptr / tcols)
+    // union of a given row (srcoff / srccnt / srccols) and a given transposed row (tptr / tcols);
+    // mode 2, the same rows as mode 0 for one-sided passes (out-pairs only) as the union of the
+    // rows' elements' vertex lists (vpool / vseg_start / vseg_cnt: mode 0 run over elements, each
+    // element its own row, lists its partners' vertices and its own)
     int mode, all_rows;
+    const int *vpool;
+    const long long *vseg_start;
+    const int *vseg_cnt;
     const long long *srcoff;
     const int *srccnt, *srccols;
     const long long *tptr;
@@ -623,6 +647,9 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
     unsigned *bm = s_bm + (size_t)(threadIdx.x >> 5) * words;
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    // the bitmap is cleared once here; each row clears the words it touched when it is done
+    for (int i = lane; i < words; i += 32) bm[i] = 0u;
+    __syncwarp();
     for (long long u = gw; u < a.nV; u += nw) {
         if (!a.all_rows && a.labV[u] <= 0) {
             if (pass != 1 && lane == 0) a.rowcnt[u] = 0;
@@ -631,9 +658,6 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         }
         const ProbParams &P = a.probs[a.vprob[u]];
         const int voff = P.vert_off;
-        const int wu = (P.nV + 31) >> 5;
-        for (int i = lane; i < wu; i += 32) bm[i] = 0u;
-        __syncwarp();
         int lo = 0x7fffffff, hi = -1;
         if (a.mode == 1) {   // union of a row and its transposed row
             const long long o = a.srcoff[u];
@@ -651,7 +675,20 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
                 hi = max(hi, v);
             }
         }
-        for (long long t = a.mode == 1 ? a.vptr[u + 1] : a.vptr[u]; t < a.vptr[u + 1]; t++) {
+        if (a.mode == 2) {   // union of the vertex lists of the elements at u
+            for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
+                const int T = a.vel[t];
+                const long long b = a.vseg_start[T];
+                const int n = a.vseg_cnt[T];
+                for (int i = lane; i < n; i += 32) {
+                    const int v = a.vpool[b + i] - voff;
+                    atomicOr(&bm[v >> 5], 1u << (v & 31));
+                    lo = min(lo, v);
+                    hi = max(hi, v);
+                }
+            }
+        }
+        for (long long t = a.mode != 0 ? a.vptr[u + 1] : a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
             const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
             const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
@@ -704,6 +741,9 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
                 }
             }
             __syncwarp();
+            if (hi >= 0)
+                for (int wi = (lo >> 5) + lane; wi <= (hi >> 5); wi += 32) bm[wi] = 0u;
+            __syncwarp();
             continue;
         }
         long long w = pass ? a.rowptr[u] : 0;
@@ -726,7 +766,17 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         }
         if (pass == 0 && lane == 0) a.rowcnt[u] = (int)w;
         __syncwarp();
+        if (hi >= 0)
+            for (int wi = (lo >> 5) + lane; wi <= (hi >> 5); wi += 32) bm[wi] = 0u;
+        __syncwarp();
     }
+}
+
+// Identity incidence (row e holds element e alone): rows of the bitmap kernel over elements.
+__global__ void k_iota(long long n, long long *__restrict__ ptr, int *__restrict__ idx) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= n) ptr[i] = i;
+    if (i < n) idx[i] = (int)i;
 }
 
 // Transposed rows of the out-pair rows (warp per source row u, its entries in the scratch):

@@ -263,6 +263,9 @@ struct PassRuleT {
     // py^2) over the reference triangle.
     R insum[1 + 4 + 10];
     R mom[6];
+    // sums over the outer points of cxx (upper triangle), cx and dxf, in that order: an outer
+    // element's folds when every outer point's ball contains the partner (constant kernels)
+    R xsum[10 + 4 + 1];
 };
 typedef PassRuleT<float> PassRule;
 

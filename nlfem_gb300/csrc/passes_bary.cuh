@@ -28,7 +28,8 @@ struct BaryWarp {
     float pc[32][DIM * (DIM + 1)];      // partner element, local coordinates
     float prt[32];                      // partner |det|
     long long rhb[DIM + 1], rrb[DIM + 1];   // T's rows: hash table start, CSR row start
-    unsigned rmask[DIM + 1];            // T's rows: hash capacity - 1 (0xffffffff: no row)
+    unsigned rmask[DIM + 1];            // T's rows: slot map size field (0xffffffff: no row), see RowHash
+    int rlo[DIM + 1];                   // T's rows: first window word (window-rank map)
 };
 template <int DIM>
 struct BaryEntry {   // one partner vertex of a batch and its integer sums over T's rows
@@ -96,10 +97,12 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             RowHash h;
             h.hb = h.rb = 0;
             h.mask = 0xffffffffu;
+            h.lo = 0;
             if (keepmask & (1u << lane)) h = row_hash(sm, a.T32[(long long)T * dV + lane]);
             W.rhb[lane] = h.hb;
             W.rrb[lane] = h.rb;
             W.rmask[lane] = h.mask;
+            W.rlo[lane] = h.lo;
         }
         const ProbParams P = a.probs[a.eprob[T]];
         const double *ET64 = &a.EC[(long long)T * DIM * dV];
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             for (int w = lane; w < dV * nent; w += 32) {
                 const int e = w / dV, r = w - dV * e;
                 RowHash h;
-                h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
+                h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
                 if (h.mask == 0xffffffffu) continue;   // T's vertex r has no row
                 const long long s = slot_find_row(sm, h, slist[e].col);
                 if (s < 0) miss = true;
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
         if (lane < dV * dV) {
             const int r = lane / dV, c = lane % dV;
             RowHash h;
-            h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
+            h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
             if (h.mask != 0xffffffffu) {
                 long long d = 0;
                 const int si = r <= c ? sym_idx<dV>(r, c) : sym_idx<dV>(c, r);

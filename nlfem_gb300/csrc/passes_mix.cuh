@@ -106,6 +106,8 @@ template <> struct Ar<double> {
 constexpr int MIX_WARPS = 4;
 constexpr int MIX_THREADS = 32 * MIX_WARPS;
 constexpr int RES_N = 10;   // per item: innerLocal, innerNonloc[3], inner termLocalPrime sums[6]
+constexpr int SCAT_U = 1;   // slot lookups per lane whose first accesses are issued together (more
+                            // unrolling overflows the instruction cache of this kernel)
 
 // Per-warp shared scratch; nPx-dependent arrays follow the struct in dynamic shared memory:
 // the outer points of T (FP64, exact; FP32 relative to T's vertex 0), the item results and the
@@ -115,8 +117,9 @@ struct MixWarp {
     R pc[32][6];            // partner element, local coordinates
     R prt[32];              // partner |det|
     int pid[32];            // partner element
-    long long rhb[3], rrb[3];   // T's rows: hash table start, CSR row start
-    unsigned rmask[3];          // T's rows: hash capacity - 1 (0xffffffff: no row)
+    long long rhb[3], rrb[3];   // T's rows: slot map start, CSR row start
+    unsigned rmask[3];          // T's rows: slot map size field (0xffffffff: no row), see RowHash
+    int rlo[3];                 // T's rows: first window word (window-rank map)
     int tvs[3];                 // T's vertices
 };
 // One column group of a batch: the partner vertex and the integer sums of its three rows
@@ -303,6 +306,20 @@ __device__ __forceinline__ int build_list(const unsigned char *mycls, int nPx, i
     return n;
 }
 
+// The same from a bit mask of the lane's outer points (bit k: item (k, lane) is in the list).
+__device__ __forceinline__ int build_list_mask(unsigned mask, int nPx, unsigned short *list) {
+    const int lane = threadIdx.x & 31;
+    int n = 0;
+    for (int k = 0; k < nPx; k++) {
+        const bool mine = (mask >> k) & 1u;
+        const unsigned m = __ballot_sync(FULL, mine);
+        if (mine) list[n + __popc(m & lanemask_lt())] = (unsigned short)(k * 32 + lane);
+        n += __popc(m);
+    }
+    __syncwarp();
+    return n;
+}
+
 // a[i] for i in {0, 1, 2} as register selects (no dynamic indexing of register arrays)
 template <typename X>
 __device__ __forceinline__ X sel3(const X *v, int i) {
@@ -374,7 +391,6 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
     bool bad = false;   // a contribution outside the fixed-point range (reported at the end)
     bool miss = false;  // a matrix slot not found (reported at the end)
     unsigned nsub = 0, namb = 0, nclose = 0, nitin = 0, nitcut = 0;
-    unsigned char mycls[MAXQ];
     for (;;) {
         int idx = 0;
         if (lane == 0) idx = atomicAdd(ma.work, 1);
@@ -395,10 +411,12 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             RowHash h;
             h.hb = h.rb = 0;
             h.mask = 0xffffffffu;
+            h.lo = 0;
             if (keepmask & (1u << lane)) h = row_hash(sm, u);
             W.rhb[lane] = h.hb;
             W.rrb[lane] = h.rb;
             W.rmask[lane] = h.mask;
+            W.rlo[lane] = h.lo;
             W.tvs[lane] = u;
         }
         const ProbParams P = a.probs[a.eprob[T]];
@@ -446,35 +464,26 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             for (int j = 0; j < 6; j++) W.pc[lane][j] = pc[j];
             W.prt[lane] = F32 ? (R)a.adetf[part] : (R)a.adet[part];
             W.pid[lane] = part;
-            R inv[RES_N];   // constant kernel: an inside item's sums
-            if (CK) {
-                const R kr = A::kc(P) * W.prt[lane];
-#pragma unroll
-                for (int q = 0; q < RES_N; q++) inv[q] = kr * pr.insum[q];
-            }
+            // classes as bit masks over the outer points: inm (ball contains the partner), cutm
+            // (ball cuts it). Only cut items (and, for other kernels, inside items) write their
+            // sums into res; the fold reads res for those items only.
+            unsigned inm = 0, cutm = 0;
             for (int k = 0; k < nPx; k++) {
-                unsigned char c = CLS_OUT;
+                int c = CLS_OUT;
                 if (act && !close) {
                     const V x = xf[k];
                     const V Q[3] = {A::v(pc[0] - x.x, pc[1] - x.y), A::v(pc[2] - x.x, pc[3] - x.y), A::v(pc[4] - x.x, pc[5] - x.y)};
-                    c = (unsigned char)A::cls(Q, sqf);
+                    c = A::cls(Q, sqf);
                 }
-                mycls[k] = c;
-                nitin += c == CLS_IN;
-                nitcut += c == CLS_CUT;
-                R *rr = &res[(lane * nPx + k) * RES_N];
-                if (CK && c == CLS_IN) {
-                    nsub++;
-#pragma unroll
-                    for (int q = 0; q < RES_N; q++) rr[q] = inv[q];
-                } else {
-#pragma unroll
-                    for (int q = 0; q < RES_N; q++) rr[q] = R(0);
-                }
+                inm |= (unsigned)(c == CLS_IN) << k;
+                cutm |= (unsigned)(c == CLS_CUT) << k;
             }
+            nitin += __popc(inm);
+            nitcut += __popc(cutm);
+            if (CK) nsub += __popc(inm);
             __syncwarp();
-            const int nin = CK ? 0 : build_list(mycls, nPx, CLS_IN, lst);
-            const int ncut = build_list(mycls, nPx, CLS_CUT, lst + 32 * nPx);
+            const int nin = CK ? 0 : build_list_mask(inm, nPx, lst);
+            const int ncut = build_list_mask(cutm, nPx, lst + 32 * nPx);
             for (int c0 = 0; c0 < nin; c0 += 32) {
                 if (c0 + lane < nin) {
                     const int it = lst[c0 + lane];
@@ -502,6 +511,13 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
             for (int i = 0; i < 9; i++) nx[i] = mx[i] = 0;
 #pragma unroll
             for (int i = 0; i < 6; i++) lpx[i] = lx[i] = 0;
+            // constant kernel: a pair with every outer point inside takes the precomputed sums
+            // (lanefull), so its blocks do not depend on the other pairs of its batch; when that
+            // holds for every active pair (a warp vote, taken here where all lanes are present)
+            // the outer-point loop is skipped
+            const unsigned fullm = nPx >= 32 ? 0xffffffffu : (1u << nPx) - 1u;
+            const bool lanefull = CK && inm == fullm;
+            const bool allin = CK && __all_sync(FULL, !act || close || lanefull);
             if (act) {
                 if (close) {
                     nclose++;
@@ -527,20 +543,58 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 } else {
                     R L[6] = {0, 0, 0, 0, 0, 0}, N[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
                     R LP[6] = {0, 0, 0, 0, 0, 0};
-                    for (int k = 0; k < nPx; k++) {
-                        const R *rr = &res[(lane * nPx + k) * RES_N];
-                        const R dk = pr.dxf[k];
+                    // the outer-point loop is warp-uniform (the rule's constants are read at one
+                    // address per warp); each lane adds the items its classes select
+                    R Axx[6] = {0, 0, 0, 0, 0, 0}, Ax[3] = {0, 0, 0}, Ad = 0;   // inside items (constant kernel)
+                    if (lanefull) {   // every item inside: the rule's sums over all outer points
 #pragma unroll
-                        for (int ab = 0; ab < 6; ab++) L[ab] = A::fm(pr.cxx[6 * k + ab], rr[0], L[ab]);
+                        for (int ab = 0; ab < 6; ab++) Axx[ab] = pr.xsum[ab];
+#pragma unroll
+                        for (int r = 0; r < 3; r++) Ax[r] = pr.xsum[6 + r];
+                        Ad = pr.xsum[9];
+                    }
+                    if (!allin) {
+                        for (int k = 0; k < nPx; k++) {
+                            if (lanefull) continue;
+                            if (CK && ((inm >> k) & 1u)) {
+#pragma unroll
+                                for (int ab = 0; ab < 6; ab++) Axx[ab] += pr.cxx[6 * k + ab];
+#pragma unroll
+                                for (int r = 0; r < 3; r++) Ax[r] += pr.cx[3 * k + r];
+                                Ad += pr.dxf[k];
+                                continue;
+                            }
+                            if (!(((inm | cutm) >> k) & 1u)) continue;
+                            const R *rr = &res[(lane * nPx + k) * RES_N];
+                            const R dk = pr.dxf[k];
+#pragma unroll
+                            for (int ab = 0; ab < 6; ab++) L[ab] = A::fm(pr.cxx[6 * k + ab], rr[0], L[ab]);
+#pragma unroll
+                            for (int r = 0; r < 3; r++) {
+                                const R c = pr.cx[3 * k + r];
+                                N[3 * r + 0] = A::fm(c, rr[1], N[3 * r + 0]);
+                                N[3 * r + 1] = A::fm(c, rr[2], N[3 * r + 1]);
+                                N[3 * r + 2] = A::fm(c, rr[3], N[3 * r + 2]);
+                            }
+#pragma unroll
+                            for (int ab = 0; ab < 6; ab++) LP[ab] = A::fm(dk, rr[4 + ab], LP[ab]);
+                        }
+                    }
+                    if (CK) {   // an inside item's sums are kc |b| times the rule's element sums
+                        R inv[RES_N];
+                        const R kr = A::kc(P) * W.prt[lane];
+#pragma unroll
+                        for (int q = 0; q < RES_N; q++) inv[q] = kr * pr.insum[q];
+#pragma unroll
+                        for (int ab = 0; ab < 6; ab++) L[ab] = A::fm(Axx[ab], inv[0], L[ab]);
 #pragma unroll
                         for (int r = 0; r < 3; r++) {
-                            const R c = pr.cx[3 * k + r];
-                            N[3 * r + 0] = A::fm(c, rr[1], N[3 * r + 0]);
-                            N[3 * r + 1] = A::fm(c, rr[2], N[3 * r + 1]);
-                            N[3 * r + 2] = A::fm(c, rr[3], N[3 * r + 2]);
+                            N[3 * r + 0] = A::fm(Ax[r], inv[1], N[3 * r + 0]);
+                            N[3 * r + 1] = A::fm(Ax[r], inv[2], N[3 * r + 1]);
+                            N[3 * r + 2] = A::fm(Ax[r], inv[3], N[3 * r + 2]);
                         }
 #pragma unroll
-                        for (int ab = 0; ab < 6; ab++) LP[ab] = A::fm(dk, rr[4 + ab], LP[ab]);
+                        for (int ab = 0; ab < 6; ab++) LP[ab] = A::fm(Ad, inv[4 + ab], LP[ab]);
                     }
 #pragma unroll
                     for (int i = 0; i < 6; i++) lx[i] = A::fx(L[i] * rTT, P, bad);
@@ -598,26 +652,46 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                 nent += __popc(m);
             }
             __syncwarp();
-            for (int w = lane; w < 3 * nent; w += 32) {
-                const int e = w / 3, r = w - 3 * e;
-                const int col = slist[e].col;
-                const long long sn = slist[e].v[r], sq = slist[e].v[3 + r];
-                const bool keepc = a.labV[col] > 0;
-                RowHash h;
-                h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r];
-                if (h.mask != 0xffffffffu) {
-                    const long long s = slot_find_row(sm, h, col);
-                    if (s < 0) { miss = true; continue; }
-                    red_add(ma.valsN, s, -sn);
-                    if (anyclose && keepc && sq != sn) {
-                        const int tp = sm.tpos[s];
-                        if (tp < 0) miss = true;
-                        else red_add(vals, sm.rowptr[col] + tp, sn - sq);
+            // (row, column) lookups, SCAT_U per lane at a time: the first memory access of each is
+            // issued before any is examined, so their latencies overlap
+            const int nit = 3 * nent;
+            for (int w0 = 0; w0 < nit; w0 += 32 * SCAT_U) {
+                SlotProbe pb[SCAT_U];
+#pragma unroll
+                for (int u = 0; u < SCAT_U; u++) {
+                    const int w = w0 + lane + 32 * u;
+                    pb[u].e = HEMPTY;
+                    pb[u].i = 0;
+                    if (w < nit) {
+                        const int e = w / 3, r = w - 3 * e;
+                        RowHash h;
+                        h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
+                        pb[u] = slot_probe_begin(sm, h, slist[e].col);
                     }
-                } else if (keepc) {
-                    const long long q = slot_find(sm, col, W.tvs[r]);
-                    if (q < 0) miss = true;
-                    else red_add(vals, q, -sq);
+                }
+#pragma unroll
+                for (int u = 0; u < SCAT_U; u++) {
+                    const int w = w0 + lane + 32 * u;
+                    if (w >= nit) continue;
+                    const int e = w / 3, r = w - 3 * e;
+                    const int col = slist[e].col;
+                    const long long sn = slist[e].v[r], sq = slist[e].v[3 + r];
+                    RowHash h;
+                    h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
+                    if (h.mask != 0xffffffffu) {
+                        const long long s = slot_probe_end(sm, h, col, pb[u]);
+                        if (s < 0) { miss = true; continue; }
+                        red_add(ma.valsN, s, -sn);
+                        if (anyclose && sq != sn && a.labV[col] > 0) {
+                            const int tp = sm.tpos[s];
+                            if (tp < 0) miss = true;
+                            else red_add(vals, sm.rowptr[col] + tp, sn - sq);
+                        }
+                    } else if (a.labV[col] > 0) {
+                        const long long q = slot_find(sm, col, W.tvs[r]);
+                        if (q < 0) miss = true;
+                        else red_add(vals, q, -sq);
+                    }
                 }
             }
             __syncwarp();

@@ -378,6 +378,13 @@ struct Session {
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
     DevBuf out64a, out64b;
     DevBuf hcap, hptr, htab, tpos, dslot;   // slot maps of the one-sided passes
+    DevBuf rwords, rbase, rlo, rankmap;      // window-rank slot map (slots.cuh)
+    // one-sided passes: per element, the vertices of its partners and its own (row patterns)
+    DevBuf eid_ptr, eid, vp_cnt, vp_off, vp_ptr, vp_scratch;
+    long long vp_cap = 0;
+    bool vlists = false;
+    bool use_rank = false;
+    long long rtot = 0;
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
     DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
     DevBuf po_cnt, po_off, po_ptr, po_scratch, tcnt, tptr, tcols;   // transposed pattern construction
@@ -398,7 +405,7 @@ struct Session {
     long long pat_cap = 0;
     // one-shot calls: the previous call's pattern size, used as the scratch capacity when the
     // mesh has the same element and vertex counts (an overflow falls back to two passes)
-    long long hint_pat_cap = 0, hint_po_cap = 0, hint_nE = -1, hint_nV = -1;
+    long long hint_pat_cap = 0, hint_po_cap = 0, hint_vp_cap = 0, hint_nE = -1, hint_nV = -1;
     int pmode = 0;                          // PM_COLORED, PM_RETRI, PM_BARY or PM_VEC
     int od = 1;                             // outdim: rows od v + i (PM_VEC when od > 1)
     int tune_bfs = 0, tune_pass = 0;        // blocks per SM of the search / persistent pass (0: occupancy)
@@ -419,7 +426,7 @@ struct Session {
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
                 &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
-                &hcap, &hptr, &htab, &tpos, &dslot, &pscratch, &rowoff, &kclist, &valsN, &elp,
+                &hcap, &hptr, &htab, &tpos, &dslot, &rwords, &rbase, &rlo, &rankmap, &eid_ptr, &eid, &vp_cnt, &vp_off, &vp_ptr, &vp_scratch, &pscratch, &rowoff, &kclist, &valsN, &elp,
                 &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx, &vacc, &vtiny,
                 &dgT32, &dglabV, &dgvprob, &dgvptr, &dgvel};
     }
@@ -806,6 +813,7 @@ static int run_bfs(Session &S) {
         CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 8, S.st));
         CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
         BfsArgs a;
+        memset(&a, 0, sizeof(a));
         a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>();
         a.EC = S.EC.get<double>();
         a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
@@ -945,6 +953,9 @@ static SlotMap slot_map(Session &S) {
     m.rowptr = S.rowptr.get<long long>();
     m.hptr = S.hptr.get<long long>();
     m.htab = S.htab.get<unsigned long long>();
+    m.rank = S.use_rank ? S.rankmap.get<uint2>() : nullptr;
+    m.rbase = S.rbase.get<long long>();
+    m.rlo = S.rlo.get<int>();
     m.tpos = S.tpos.get<int>();
     m.dslot = S.dslot.get<int>();
     return m;
@@ -957,14 +968,32 @@ static int run_slot_maps(Session &S) {
     const long long nV = S.nV, nE = S.nE, nnz = S.nnz_struct;
     ENS(S.hcap, sizeof(long long) * (nV + 1));
     ENS(S.hptr, sizeof(long long) * (nV + 1));
-    k_hash_cap<<<grid_for(nV, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.hcap.get<long long>()); ++S.nlaunch;
-    int r = scan_excl<long long>(S, S.hcap.get<long long>(), nV, S.hptr.get<long long>());
+    // window rank when the rows' column windows take at most RANK_WORDS_PER_NNZ words per stored
+    // entry together, hash tables otherwise (the choice of the first assembly holds in replays)
+    ENS(S.rwords, sizeof(long long) * (nV + 1));
+    ENS(S.rbase, sizeof(long long) * (nV + 1));
+    ENS(S.rlo, sizeof(int) * (nV + 1));
+    k_rank_words<<<grid_for(nV, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV,
+                                                      S.rwords.get<long long>(), S.rlo.get<int>()); ++S.nlaunch;
+    int r = scan_excl<long long>(S, S.rwords.get<long long>(), nV, S.rbase.get<long long>());
     if (r) return r;
-    r = d2h(S, &S.htot, S.hptr.get<long long>() + nV, 1);
+    r = d2h(S, &S.rtot, S.rbase.get<long long>() + nV, 1);
     if (r) return r;
-    ENS(S.htab, sizeof(unsigned long long) * (S.htot + 1));
-    CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (S.htot + 1), S.st));
-    k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
+    if (!S.replay) S.use_rank = S.rtot <= (long long)RANK_WORDS_PER_NNZ * std::max<long long>(nnz, 1);
+    if (S.use_rank) {
+        ENS(S.rankmap, sizeof(uint2) * (S.rtot + 1));
+        k_rank_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.rbase.get<long long>(),
+                                                 S.rlo.get<int>(), S.rankmap.get<uint2>()); ++S.nlaunch;
+    } else {
+        k_hash_cap<<<grid_for(nV, 256), 256, 0, S.st>>>(S.rowptr.get<long long>(), nV, S.hcap.get<long long>()); ++S.nlaunch;
+        r = scan_excl<long long>(S, S.hcap.get<long long>(), nV, S.hptr.get<long long>());
+        if (r) return r;
+        r = d2h(S, &S.htot, S.hptr.get<long long>() + nV, 1);
+        if (r) return r;
+        ENS(S.htab, sizeof(unsigned long long) * (S.htot + 1));
+        CK(cudaMemsetAsync(S.htab.p, 0xff, sizeof(unsigned long long) * (S.htot + 1), S.st));
+        k_hash_fill<<<S.nSM * 8, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), nV, S.hptr.get<long long>(), S.htab.get<unsigned long long>()); ++S.nlaunch;
+    }
     if (S.pmode != PM_RETRI) {   // the barycenter pass writes its own rows only: no mirror slots
         CK(cudaGetLastError());
         return NLFEM_OK;
@@ -977,6 +1006,65 @@ static int run_slot_maps(Session &S) {
     k_tpos<<<S.nSM * 8, 256, 0, S.st>>>(m, S.cols.get<int>(), S.labV.get<int>(), nV, S.tpos.get<int>(), S.err.get<int>()); ++S.nlaunch;
     k_dslot<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(m, S.T32.get<int>(), S.labV.get<int>(), nE, S.dslot.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
+    return NLFEM_OK;
+}
+
+// Rows written in one bitmap pass into a scratch at an atomic cursor (pass 2), its capacity the
+// previous assembly's total; with no capacity yet, or after an overflow, the rows are counted
+// first (pass 0). Counters[cursor] and err[ovf] are the pass's cursor and overflow flag.
+template <int DIM>
+static int run_rows_direct(Session &S, RowArgs o, long long nrows, DevBuf &cnt, DevBuf &off, DevBuf &ptr,
+                           DevBuf &scratch, long long &cap, int cursor_i, int ovf_i, int words, int threads,
+                           unsigned grid, size_t smem) {
+    ENS(cnt, sizeof(int) * (nrows + 1));
+    ENS(off, sizeof(long long) * (nrows + 1));
+    ENS(ptr, sizeof(long long) * (nrows + 1));
+    o.rowptr = nullptr; o.cols = nullptr;
+    o.rowcnt = cnt.get<int>();
+    o.rowoff = off.get<long long>();
+    unsigned long long *cursor = S.counters.get<unsigned long long>() + cursor_i;
+    int *ovf = S.err.get<int>() + ovf_i;
+    int r;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        if (cap == 0) {   // count the rows first
+            o.scratch = nullptr; o.cap = 0; o.cursor = nullptr; o.ovf = nullptr;
+            k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 0, words); ++S.nlaunch;
+            if ((r = scan_excl<int>(S, cnt.get<int>(), nrows, ptr.get<long long>()))) return r;
+            long long tot = 0;
+            if ((r = d2h(S, &tot, ptr.get<long long>() + nrows, 1))) return r;
+            cap = tot + 1;
+        }
+        ENS(scratch, sizeof(int) * (cap + 1));
+        CK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), S.st));
+        CK(cudaMemsetAsync(ovf, 0, sizeof(int), S.st));
+        o.scratch = scratch.get<int>(); o.cap = cap; o.cursor = cursor; o.ovf = ovf;
+        k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 2, words); ++S.nlaunch;
+        int of = 0;
+        if ((r = d2h(S, &of, ovf, 1))) return r;
+        if (!of) return NLFEM_OK;
+        if (attempt == 1) return fail(NLFEM_ERR_CUDA, "internal: row scratch overflow after a recount");
+        cap = 0;
+    }
+    return NLFEM_OK;
+}
+
+// Per element, the vertices of its partners and its own (none without a partner): the bitmap
+// kernel in mode 0 over elements, each element the only member of its own row. The one-sided
+// passes' row patterns are then unions of these lists (mode 2).
+template <int DIM>
+static int run_elem_vlists(Session &S, const RowArgs &a, int words, int threads, unsigned grid, size_t smem) {
+    const long long nE = S.nE;
+    ENS(S.eid_ptr, sizeof(long long) * (nE + 1));
+    ENS(S.eid, sizeof(int) * (nE + 1));
+    k_iota<<<grid_for(nE + 1, 256), 256, 0, S.st>>>(nE, S.eid_ptr.get<long long>(), S.eid.get<int>()); ++S.nlaunch;
+    RowArgs o = a;
+    o.in_ptr = nullptr;
+    o.all_rows = 1;
+    o.mode = 0;
+    o.vptr = S.eid_ptr.get<long long>(); o.vel = S.eid.get<int>(); o.vprob = S.eprob.get<int>(); o.nV = nE;
+    int r = run_rows_direct<DIM>(S, o, nE, S.vp_cnt, S.vp_off, S.vp_ptr, S.vp_scratch, S.vp_cap, 15, 11,
+                                 words, threads, grid, smem);
+    if (r) return r;
     return NLFEM_OK;
 }
 
@@ -995,33 +1083,10 @@ static int run_pattern_transposed(Session &S, RowArgs &a, int words, int threads
     RowArgs o = a;
     o.in_ptr = nullptr;
     o.all_rows = 1;
-    o.mode = 0;
-    o.rowptr = nullptr; o.cols = nullptr;
-    o.rowcnt = S.po_cnt.get<int>();
-    o.rowoff = S.po_off.get<long long>();
-    unsigned long long *cursor = S.counters.get<unsigned long long>() + 14;
-    int *ovf = S.err.get<int>() + 10;
-    int r;
-    for (int attempt = 0; attempt < 2; attempt++) {
-        if (S.po_cap == 0) {   // count the rows first
-            o.scratch = nullptr; o.cap = 0; o.cursor = nullptr; o.ovf = nullptr;
-            k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 0, words); ++S.nlaunch;
-            if ((r = scan_excl<int>(S, S.po_cnt.get<int>(), nV, S.po_ptr.get<long long>()))) return r;
-            long long tot = 0;
-            if ((r = d2h(S, &tot, S.po_ptr.get<long long>() + nV, 1))) return r;
-            S.po_cap = tot + 1;
-        }
-        ENS(S.po_scratch, sizeof(int) * (S.po_cap + 1));
-        CK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), S.st));
-        CK(cudaMemsetAsync(ovf, 0, sizeof(int), S.st));
-        o.scratch = S.po_scratch.get<int>(); o.cap = S.po_cap; o.cursor = cursor; o.ovf = ovf;
-        k_row_pattern_bm<DIM><<<grid, threads, smem, S.st>>>(o, 2, words); ++S.nlaunch;
-        int of = 0;
-        if ((r = d2h(S, &of, ovf, 1))) return r;
-        if (!of) break;
-        if (attempt == 1) return fail(NLFEM_ERR_CUDA, "internal: out-pair row scratch overflow after a recount");
-        S.po_cap = 0;
-    }
+    o.mode = S.vlists ? 2 : 0;
+    int r = run_rows_direct<DIM>(S, o, nV, S.po_cnt, S.po_off, S.po_ptr, S.po_scratch, S.po_cap, 14, 10,
+                                 words, threads, grid, smem);
+    if (r) return r;
     ENS(S.tcnt, sizeof(int) * (nV + 1));
     ENS(S.tptr, sizeof(long long) * (nV + 1));
     CK(cudaMemsetAsync(S.tcnt.p, 0, sizeof(int) * (nV + 1), S.st));
@@ -1065,6 +1130,15 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     if (S.hint_nE == S.nE && S.hint_nV == S.nV) {   // one-shot calls: the previous call's sizes
         if (S.pat_cap == 0) S.pat_cap = S.hint_pat_cap;
         if (S.po_cap == 0) S.po_cap = S.hint_po_cap;
+        if (S.vp_cap == 0) S.vp_cap = S.hint_vp_cap;
+    }
+    // the one-sided passes' rows (out-pairs only) are unions of per-element vertex lists
+    S.vlists = S.pmode == PM_RETRI || S.pmode == PM_BARY;
+    if (S.vlists) {
+        int r = run_elem_vlists<DIM>(S, a, words, threads, grid, smem);
+        if (r) return r;
+        a.vpool = S.vp_scratch.get<int>(); a.vseg_start = S.vp_off.get<long long>(); a.vseg_cnt = S.vp_cnt.get<int>();
+        if (S.pmode == PM_BARY) a.mode = 2;
     }
     if (S.pmode == PM_RETRI) {
         int r = run_pattern_transposed<DIM>(S, a, words, threads, grid, smem);
@@ -1259,6 +1333,16 @@ static PassRuleT<R> make_pass_rule(const Rule &r, int dim) {
     }
     for (int q = 0; q < 1 + 4 + 10; q++) pr.insum[q] = (R)insum[q];
     for (int q = 0; q < 6; q++) pr.mom[q] = (R)mom[q];
+    double xsum[10 + 4 + 1] = {0};
+    for (int k = 0; k < r.nPx; k++) {
+        int t = 0;
+        for (int a = 0; a < dV; a++) {
+            xsum[NS + a] += r.dx[k] * r.psix[dV * k + a];
+            for (int b = a; b < dV; b++) xsum[t++] += r.dx[k] * r.psix[dV * k + a] * r.psix[dV * k + b];
+        }
+        xsum[NS + dV] += r.dx[k];
+    }
+    for (int q = 0; q < NS + dV + 1; q++) pr.xsum[q] = (R)xsum[q];
     return pr;
 }
 
@@ -1588,6 +1672,7 @@ static int run_system_post(Session &S) {
     if ((r = d2h(S, &ncl[5], S.counters.get<unsigned long long>() + 12, 2))) return r;
     S.stats.n_items_in = (long)ncl[5];
     S.stats.n_items_cut = (long)ncl[6];
+    S.stats.slot_map = (S.pmode == PM_RETRI || S.pmode == PM_BARY) ? (S.use_rank ? 1 : 2) : 0;
     S.stats.n_candidates = (long)ncl[4];
     S.stats.n_close = (long)ncl[0];
     S.stats.n_subtri = (long)ncl[1];
@@ -1620,9 +1705,9 @@ static int run_system_graph_t(Session &S) {
         const long long launches = S.nlaunch;
         CK(cudaGraphLaunch(S.gexec, S.st));
         CK(cudaStreamSynchronize(S.st));
-        int he[11];
-        if ((r = d2h(S, he, S.err.get<int>(), 11))) return r;
-        if (!he[0] && !he[1] && !he[5] && !he[6] && !he[10]) {
+        int he[12];
+        if ((r = d2h(S, he, S.err.get<int>(), 12))) return r;
+        if (!he[0] && !he[1] && !he[5] && !he[6] && !he[10] && !he[11]) {
             S.nlaunch = launches;
             return run_system_post(S);
         }
@@ -1864,6 +1949,7 @@ static void cache_take(Session &S) {
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
     S.hint_pat_cap = g_cache->hint_pat_cap;
     S.hint_po_cap = g_cache->hint_po_cap;
+    S.hint_vp_cap = g_cache->hint_vp_cap;
     S.hint_nE = g_cache->hint_nE;
     S.hint_nV = g_cache->hint_nV;
     delete g_cache;
@@ -1881,6 +1967,7 @@ static void cache_give(Session &S) {
     for (size_t i = 0; i < to.size(); i++) std::swap(*to[i], *from[i]);
     g_cache->hint_pat_cap = S.pat_cap;
     g_cache->hint_po_cap = S.po_cap;
+    g_cache->hint_vp_cap = S.vp_cap;
     g_cache->hint_nE = S.nE;
     g_cache->hint_nV = S.nV;
 }

@@ -1,7 +1,7 @@
 """Digests of the REFERENCE's own assembly of each full-size workload: tests/golden/digest_*.npz.
 
 Usage (needs the reference checkout; it is compiled by oracle/ref.mk against oracle/refshim/):
-    python tests/golden/make_ref_digests.py <reference checkout> [workload ...] [--threads N]
+    python tests/golden/make_ref_digests.py <reference checkout> [workload ...] [--threads N] [--resume]
 workloads: c2 (delta 0.1), c2d05 (delta 0.05), c3, c4, c5 (default: all).
 
 Each file holds, per problem, the digest of nlfem_gb300/digest.py (pattern hash, Frobenius norm,
@@ -29,7 +29,10 @@ def path_of(key):
     return os.path.join(HERE, f"digest_{key}.npz")
 
 
-def make(key, threads):
+def make(key, threads, resume=False):
+    """Assembles every problem of the workload with the reference and writes the digest file.
+    With resume, problems already in an existing file are kept, and the file is rewritten after
+    each problem, so a long batch (c5) can be stopped and continued."""
     from nlfem_gb300 import digest, workloads
     from oracle import ref
     from make_oracle_golden import input_hash
@@ -37,7 +40,12 @@ def make(key, threads):
     probs, rec = workloads.problems(name, "fp64", delta=delta)
     batch = len(probs) > 1
     digests, secs = {}, 0.0
+    if resume and os.path.exists(path_of(key)):
+        digests, old = digest.load(path_of(key))
+        secs = float(old.get("ref_seconds", 0.0))
     for i, (mesh, kernel, conf) in enumerate(probs):
+        if f"p{i}" in digests:
+            continue
         t0 = time.time()
         r = ref.assemble(mesh, kernel, conf, nthreads=threads)
         secs += r["seconds"]
@@ -50,10 +58,20 @@ def make(key, threads):
         digests[f"p{i}"] = d
         print(f"{key} problem {i}: K={int(d['K'])} nnz={int(d['nnz'])} {r['seconds']:.1f}s "
               f"(total {time.time() - t0:.1f}s)", flush=True)
-    meta = {"workload": rec["workload"], "problems": len(probs), "ref_seconds": secs, "ref_threads": threads,
-            "source": "reference src/*.cpp compiled by oracle/ref.mk against oracle/refshim"}
-    digest.save(path_of(key), digests, meta)
+        if resume:
+            _save(key, digests, rec, probs, secs, threads)
+    _save(key, digests, rec, probs, secs, threads)
     print("wrote", path_of(key), os.path.getsize(path_of(key)), "bytes", flush=True)
+
+
+def _save(key, digests, rec, probs, secs, threads):
+    from nlfem_gb300 import digest
+    meta = {"workload": rec["workload"], "problems": len(probs), "problems_done": len(digests),
+            "ref_seconds": secs, "ref_threads": threads,
+            "source": "reference src/*.cpp compiled by oracle/ref.mk against oracle/refshim"}
+    tmp = path_of(key) + ".tmp.npz"
+    digest.save(tmp, digests, meta)
+    os.replace(tmp, path_of(key))
 
 
 def main():
@@ -61,11 +79,12 @@ def main():
     ap.add_argument("reference", help="path of the reference checkout (its src/ and include/)")
     ap.add_argument("workloads", nargs="*", default=list(WORKLOADS))
     ap.add_argument("--threads", type=int, default=os.cpu_count())
+    ap.add_argument("--resume", action="store_true", help="keep the problems of an existing file; save after each")
     a = ap.parse_args()
     from oracle import ref
     ref.build(a.reference)
     for key in a.workloads:
-        make(key, a.threads)
+        make(key, a.threads, a.resume)
 
 
 if __name__ == "__main__":

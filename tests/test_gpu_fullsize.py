@@ -11,7 +11,8 @@ workloads here, in both precisions:
 * mixed path: both <= 1e-6;
 * load vector: <= 1e-12 (max entry, relative).
 C5's FP64 check covers every eighth problem (its batch matrices equal the single assemblies bit
-for bit, a property the parity tests check); the mixed check covers all 64.
+for bit, a property the parity tests check); the mixed check covers all 64. A batch digest may hold
+only the first problems of the batch (meta problems_done); the checks cover the problems it holds.
 """
 import os
 import sys
@@ -53,6 +54,7 @@ def test_workload_matches_reference(gpu, key):
         idx = list(range(len(probs)))
         if precision == "fp64" and len(probs) > 1:
             idx = idx[::8]
+        idx = [i for i in idx if f"p{i}" in digests]   # a batch digest may be partial (problems_done)
         for i in idx:
             mesh, kernel, conf = probs[i]
             d = digests[f"p{i}"]

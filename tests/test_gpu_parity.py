@@ -1031,3 +1031,33 @@ def test_autotune_keeps_the_matrix(nl):
         assert np.array_equal(s.download(0).data, A0.data)
     finally:
         s.close()
+
+
+def test_mixed_slot_maps_window_rank_and_hash(nl, orc):
+    """The one-sided pass finds matrix slots with window-rank bitmaps when the rows span narrow
+    ranges of vertex numbers (a row-by-row numbering) and with per-row hash tables otherwise (here:
+    a random vertex numbering). Both give the same matrix, bit for bit after renumbering, and
+    both match the oracle within the mixed tolerance."""
+    from nlfem_gb300 import _lib, meshes
+    v, e, l = meshes.regular_square(64, 0.03, jitter=0.2, seed=21)
+    m = meshes.mesh_dict(v, e, l)
+    k = {"function": "constant", "horizon": 0.03, "outputdim": 1}
+    c = conf2d(precision="mixed")
+    A = nl.stiffnessMatrix(dict(m), k, c)
+    assert _lib.stats()["slot_map"] == 1
+    nV = v.shape[0]
+    perm = np.random.default_rng(3).permutation(nV)   # vertex i becomes vertex perm[i]
+    v2 = np.empty_like(v)
+    v2[perm] = v
+    m2 = meshes.mesh_dict(v2, perm[e], l)
+    B = nl.stiffnessMatrix(m2, k, c)
+    assert _lib.stats()["slot_map"] == 2
+    Ac = A.tocoo()   # renumbered entry by entry: slots that cancelled to zero stay stored
+    A2 = sp.csr_matrix((Ac.data, (perm[Ac.row], perm[Ac.col])), shape=(nV, nV))
+    A2.sort_indices(); B.sort_indices()
+    assert same_pattern(A2, B)
+    np.testing.assert_array_equal(A2.data, B.data)
+    C = orc.assemble(m, k, conf2d())["A"]
+    assert same_pattern(A, C)
+    fro, mx = rel_errors(A, C)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)

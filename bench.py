@@ -34,10 +34,16 @@ import numpy as np
 
 METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel err"
 
-# DRAM traffic (read + write bytes) of the one k_pass_mix2d launch of a C2 assembly (n = 256,
-# delta = 0.1), from an ncu capture of that launch (dram__bytes_read.sum + dram__bytes_write.sum);
-# None for workloads not captured. Reported as roofline.traffic with its source.
-PASS_TRAFFIC_BYTES = {("c2", 256, 0.1): 5.32e9 + 1.07e9}
+# DRAM traffic (read + write bytes) per pair of the k_pass_mix2d<0> launch, from an ncu capture of
+# that launch on the 2D constant-kernel workload at n = 128 (2.56e7 pairs: 187.0 MB read, 34.6 MB
+# written); the pass streams its pair list and reuses the mesh from L2, so the traffic grows with
+# the pairs. Reported as roofline.traffic (scaled to this run's pairs) with its source.
+PASS_TRAFFIC_PER_PAIR = {"c2": (187.021e6 + 34.574e6) / 25573871}
+# Algorithmic bytes of the pair search: per candidate the element's stamp (4 B), its incidence entry
+# (4 B), its 12 FP32 coordinates (48 B) and, per 3 candidates, a vertex's stamp and incidence range
+# (about 4 B): 60 B; per pair its queue and pool entries (8 B).
+SEARCH_BYTES_PER_CANDIDATE = 60
+SEARCH_BYTES_PER_PAIR = 8
 
 
 def workload(args, precision):
@@ -70,6 +76,20 @@ def vs_reference(mats, dg):
     return {"pattern_identical": all(r["pattern_identical"] for r in res),
             "fro_est": max(r["fro_est"] for r in res), "max_rows": max(r["max_rows"] for r in res),
             "problems_compared": len(res)}
+
+
+def search_roofline(st):
+    """The pair search against HBM: its algorithmic bytes (SEARCH_BYTES_PER_CANDIDATE per tested
+    candidate, SEARCH_BYTES_PER_PAIR per pair) over the device time of the search phase (vertex
+    incidence, search, pair compaction)."""
+    hbm = measured_peaks().get("hbm_gbs")
+    ms = st["ms_bfs"]
+    nbytes = SEARCH_BYTES_PER_CANDIDATE * st["n_candidates"] + SEARCH_BYTES_PER_PAIR * st["n_pairs"]
+    gbs = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else None
+    return {"bound": "hbm", "kernel": "k_bfs (one warp per outer element)", "candidates": int(st["n_candidates"]),
+            "algorithmic_bytes": int(nbytes), "ms": ms, "achieved": gbs, "peak": hbm, "unit": "GB/s",
+            "frac": (gbs / hbm) if (gbs and hbm) else None,
+            "note": "latency bound (dependent stamp and incidence loads per step), not bandwidth bound"}
 
 
 def config_dict(args, extra, problems):
@@ -363,15 +383,18 @@ def run_gpu(args, rank=0, world=1, dist=None):
                      "quadrature+scatter": st["ms_quad"], "finish": st["ms_finish"]},
         "roofline": {"bound": "fp32", "kernel": kname,
                      "achieved": achieved, "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
-                     "traffic": PASS_TRAFFIC_BYTES.get((args.workload, extra.get("n"), extra.get("delta"))),
-                     "traffic_source": "ncu DRAM bytes of this kernel's launch at n=256, delta=0.1 (not measured "
-                                       "in this run)",
+                     "traffic": (PASS_TRAFFIC_PER_PAIR[args.workload] * st["n_pairs"]
+                                 if args.workload in PASS_TRAFFIC_PER_PAIR else None),
+                     "traffic_source": "ncu DRAM bytes of this kernel's launch on the 2D constant-kernel workload "
+                                       "at n=128 (2.56e7 pairs), scaled by this run's pairs (not measured in this "
+                                       "run)",
                      "note": "achieved = flops of the algorithm that ran for the step (FLOP model in "
                              "bench.algorithmic_flops: the reference's inner-point loops, or their closed forms "
                              "for constant kernels; FP64 close pairs not counted) / device time of the "
                              "quadrature phase; peak = FP32 FMA throughput measured in this run (of measured); "
                              "CUDA-core bound path with no GEMM-shaped work, so neither the tensor-core nor the "
                              "HBM peak applies"},
+        "search": search_roofline(st),
         "peaks_measured": {"fp32_tflops": peak32, "fp64_tflops": peak64,
                            "hbm_gbs": measured_peaks().get("hbm_gbs")},
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -773,7 +773,7 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
 }
 
 // Identity incidence (row e holds element e alone): rows of the bitmap kernel over elements.
-__global__ void k_iota(long long n, long long *__restrict__ ptr, int *__restrict__ idx) {
+__global__ void k_iota_rows(long long n, long long *__restrict__ ptr, int *__restrict__ idx) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i <= n) ptr[i] = i;
     if (i < n) idx[i] = (int)i;

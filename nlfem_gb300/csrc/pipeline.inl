@@ -366,6 +366,7 @@ struct Session {
     cudaEvent_t ev[8];
     // inputs
     DevBuf T64, labT64, V, labV64, eoffd, voffd, prm, duffy;
+    DevBuf duffyf;   // FP32 Duffy tables of the mixed close-pair rule: points (float4), weights
     // derived
     DevBuf T32, labT, eprob, EC, adet, labV, vprob, EChi, EClo, adetf;
     DevBuf color, color2, colorlist, closeA, closeB, closebuf, touched;
@@ -420,7 +421,7 @@ struct Session {
     nlfem_stats stats;
     // every device buffer of the session, in a fixed order
     std::vector<DevBuf *> buffers() {
-        return {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &T32, &labT, &eprob,
+        return {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &duffyf, &T32, &labT, &eprob,
                 &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited, &vvisited,
                 &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
@@ -622,6 +623,21 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
             h.insert(h.end(), p.dg, p.dg + nPg);
             ENS(S.duffy, sizeof(double) * h.size());
             CK(cudaMemcpyAsync(S.duffy.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, S.st));
+            // FP32 copies for the mixed path: per case the points and the weights tdet * dg
+            std::vector<float> hf;
+            {
+                size_t o = 0;
+                const double *dg = &h[h.size() - nPg];
+                for (int c = 0; c < 3; c++) {
+                    const size_t np = (size_t)nTr[c] * nPg;
+                    for (size_t i = 0; i < np * 4; i++) hf.push_back((float)h[o + i]);
+                    for (size_t i = 0; i < np; i++) hf.push_back((float)(h[o + np * 4 + i] * dg[i % nPg]));
+                    while (hf.size() % 4) hf.push_back(0.f);   // the next case's float4 points stay 16-byte aligned
+                    o += np * 4 + np + np * 4 + np;
+                }
+            }
+            ENS(S.duffyf, sizeof(float) * hf.size());
+            CK(cudaMemcpyAsync(S.duffyf.p, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice, S.st));
             CK(cudaStreamSynchronize(S.st));
         }
     }
@@ -1056,7 +1072,7 @@ static int run_elem_vlists(Session &S, const RowArgs &a, int words, int threads,
     const long long nE = S.nE;
     ENS(S.eid_ptr, sizeof(long long) * (nE + 1));
     ENS(S.eid, sizeof(int) * (nE + 1));
-    k_iota<<<grid_for(nE + 1, 256), 256, 0, S.st>>>(nE, S.eid_ptr.get<long long>(), S.eid.get<int>()); ++S.nlaunch;
+    k_iota_rows<<<grid_for(nE + 1, 256), 256, 0, S.st>>>(nE, S.eid_ptr.get<long long>(), S.eid.get<int>()); ++S.nlaunch;
     RowArgs o = a;
     o.in_ptr = nullptr;
     o.all_rows = 1;
@@ -1242,6 +1258,12 @@ static Duffy duffy_view(const Session &S) {
     }
     d.dg = h + o;
     d.nPg = nPg;
+    const float *f = S.duffyf.get<float>();
+    size_t of = 0;
+    for (int c = 0; c < 3; c++) {
+        d.alf[c] = reinterpret_cast<const float4 *>(f + of); of += (size_t)nTr[c] * nPg * 4;
+        d.wf[c] = f + of; of += ((size_t)nTr[c] * nPg + 3) / 4 * 4;
+    }
     return d;
 }
 

@@ -30,6 +30,8 @@ struct Duffy {
     const double *alphaU[3];  // the points with xi kept (weakSingular basis functions)
     const double *tdetW[3];   // xi^(1 - 2s) (weakSingular)
     const double *dg;         // [k]
+    const float4 *alf[3];     // FP32 copies of alpha (mixed path)
+    const float *wf[3];       // FP32 tdet * dg (mixed path)
 };
 
 struct QuadArgs {
@@ -586,6 +588,84 @@ __device__ __forceinline__ void close_accumulate(const ProbParams &P, const Duff
     }
 }
 
+// The same sum on the mixed path with FP32 arithmetic throughout the point loop (FP64 runs at
+// 1/64 of the FP32 rate here). The pair's first vertex is shared (the join puts the common vertices
+// first), so x - y = al0 a0 + al1 a1 - al2 b0 - al3 b1 with the edge vectors a, b of both elements
+// from that vertex; the edge vectors enter as FP32 hi + lo parts, which keeps x - y accurate to a
+// few units of 2^-24 of its size (the canceled Duffy maps keep |x - y| of the order of the
+// edges). The power r2^h, h = -(d+2s)/2, takes the exact binary exponent of r2 = m 2^E:
+// r2^h = 2^I 2^(t - I + h log2 m), t = h E, I = floor(t), with h split into hh (12 significant
+// bits, so hh E is exact) and hl, so only arguments in [-2, 2] reach exp2f and log2f. Each
+// summand w kc dAB ker pxy pxy^T is added with Kahan compensation; the lanes' sums are combined in
+// FP64 by the caller.
+template <int NEQ>
+__device__ __forceinline__ void close_accumulate_f32(const ProbParams &P, const Duffy &d, int c, int nT,
+                                                     const double *EA, const double *EB, double dAB, double *M) {
+    constexpr int NL = 6 - NEQ, SH = 3 - NEQ;
+    const int lane = threadIdx.x & 31;
+    const int total = nT * d.nPg;
+    const float4 *alf = d.alf[c];
+    const float *wf = d.wf[c];
+    const double ae[4] = {EA[2] - EA[0], EA[4] - EA[0], EA[3] - EA[1], EA[5] - EA[1]};
+    const double be[4] = {EB[2] - EB[0], EB[4] - EB[0], EB[3] - EB[1], EB[5] - EB[1]};
+    float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        ah[i] = (float)ae[i]; al[i] = (float)(ae[i] - (double)ah[i]);
+        bh[i] = (float)be[i]; bl[i] = (float)(be[i] - (double)bh[i]);
+    }
+    const double hexp = -0.5 * P.expo;
+    const float hh = (float)(ldexp(rint(ldexp(hexp, 8)), -8));   // 8 fraction bits, |h| < 16: exact products with E
+    const float hl = (float)(hexp - (double)hh);
+    const float hf = (float)hexp;
+    const float kcd = (float)(P.kc * dAB);
+    float Mf[21], Mc[21];
+#pragma unroll
+    for (int q = 0; q < 21; q++) Mf[q] = Mc[q] = 0.f;
+    for (int idx = lane; idx < total; idx += 32) {
+        const float4 a4 = alf[idx];
+        const float w = wf[idx];
+        float z0 = fmaf(a4.x, ah[0], fmaf(a4.y, ah[1], fmaf(-a4.z, bh[0], -a4.w * bh[1])));
+        float z1 = fmaf(a4.x, ah[2], fmaf(a4.y, ah[3], fmaf(-a4.z, bh[2], -a4.w * bh[3])));
+        z0 = fmaf(a4.x, al[0], fmaf(a4.y, al[1], fmaf(-a4.z, bl[0], fmaf(-a4.w, bl[1], z0))));
+        z1 = fmaf(a4.x, al[2], fmaf(a4.y, al[3], fmaf(-a4.z, bl[2], fmaf(-a4.w, bl[3], z1))));
+        const float r2 = fmaf(z0, z0, z1 * z1);
+        int E;
+        const float m = frexpf(r2, &E);
+        const float t = hh * (float)E;   // exact
+        const float I = floorf(t);
+        const float g = fmaf(hf, log2f(m), fmaf(hl, (float)E, t - I));
+        const float ker = ldexpf(exp2f(g), (int)I);
+        const float px[3] = {1.f - a4.x - a4.y, a4.x, a4.y};
+        const float py[3] = {1.f - a4.z - a4.w, a4.z, a4.w};
+        float v[NL];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (i < NEQ) {
+                v[i] = px[i] - py[i];
+            } else {
+                v[i] = px[i];
+                v[i + SH] = -py[i];
+            }
+        }
+        const float bf = ker * w * kcd;
+#pragma unroll
+        for (int aa = 0; aa < NL; aa++) {
+            const float fa = bf * v[aa];
+#pragma unroll
+            for (int b = aa; b < NL; b++) {
+                const int q = sym_idx<6>(aa, b);
+                const float y = fmaf(fa, v[b], -Mc[q]);
+                const float tt = Mf[q] + y;
+                Mc[q] = (tt - Mf[q]) - y;
+                Mf[q] = tt;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 21; q++) M[q] = (double)Mf[q] - (double)Mc[q];
+}
+
 // integrate_weakSingular (integration.cpp:82-185), the lanes taking the (map, Gauss point) items
 // in turn: the kernel at the canceled points (as in the fractional rule), the basis functions at
 // the points with xi kept, the weight xi^(1 - 2s). W holds termLocal and termLocalPrime (upper
@@ -701,9 +781,15 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     double M[21];
 #pragma unroll
     for (int i = 0; i < 21; i++) M[i] = 0.0;
-    if (nEqual == 1) close_accumulate<1, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
-    else if (nEqual == 2) close_accumulate<2, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
-    else close_accumulate<3, FAST>(P, d, c, nT, EA, EB, dA * dB, M);
+    if (FAST) {
+        if (nEqual == 1) close_accumulate_f32<1>(P, d, c, nT, EA, EB, dA * dB, M);
+        else if (nEqual == 2) close_accumulate_f32<2>(P, d, c, nT, EA, EB, dA * dB, M);
+        else close_accumulate_f32<3>(P, d, c, nT, EA, EB, dA * dB, M);
+    } else {
+        if (nEqual == 1) close_accumulate<1, false>(P, d, c, nT, EA, EB, dA * dB, M);
+        else if (nEqual == 2) close_accumulate<2, false>(P, d, c, nT, EA, EB, dA * dB, M);
+        else close_accumulate<3, false>(P, d, c, nT, EA, EB, dA * dB, M);
+    }
 #pragma unroll
     for (int i = 0; i < 21; i++) M[i] = warp_sum(M[i]);
     for (int aa = 0; aa < nLocal; aa++)

@@ -258,12 +258,36 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
     }
     if (DIM != 2) return false;
     const F2 p[3] = {f2(pb[0], pb[1]), f2(pb[2], pb[3]), f2(pb[4], pb[5])};
-    // First the cheap certain answer from every outer point: one vertex strictly inside and none
-    // on the sphere means both edges through it cross once, so the polygon has at least three
-    // points. Only when no point gives it does any point need its polygon; points whose ball
-    // clears the triangle are skipped.
-    unsigned cut = 0;   // outer points whose ball may cut the triangle
+    // First, per outer point, the disc around the triangle's centroid through its farthest vertex:
+    // a ball holding that disc holds the triangle (the polygon is the triangle itself: three
+    // points), and a ball missing it misses the triangle. Both with the squared-distance margin.
+    const F2 cen = f2((p[0].x + p[1].x + p[2].x) * (1.f / 3.f), (p[0].y + p[1].y + p[2].y) * (1.f / 3.f));
+    float rb2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) { const F2 w = p[i] - cen; rb2 = fmaxf(rb2, dot(w, w)); }
+    const float rb = sqrtf(rb2) * (1.f + 8.f * U32), dl = sqrtf(P.sqdelta_f);
+    const float din = dl - rb;
+    const float sq_in = din > 0.f ? din * din * (1.f - MARG_D) : -1.f;
+    const float sq_out = (dl + rb) * (dl + rb) * (1.f + MARG_D);
+    unsigned und = 0;   // outer points the disc test leaves open
+    int kn = 0;
+    float dn = 3.0e38f;
     for (int k = 0; k < nPx; k++) {
+        const F2 q = cen - f2(xsf[2 * k], xsf[2 * k + 1]);
+        const float dc = dot(q, q);
+        if (dc < sq_in) return true;
+        if (dc > sq_out) continue;
+        und |= 1u << k;
+        if (dc < dn) { dn = dc; kn = k; }
+    }
+    if (!und) return false;
+    // Then the cheap certain answer, nearest point first: one vertex strictly inside and none on
+    // the sphere means both edges through it cross once, so the polygon has at least three
+    // points. Only when no point gives it does any point need its polygon.
+    unsigned cut = 0;   // outer points whose ball may cut the triangle
+    for (unsigned rest = und, first = 1; rest; first = 0) {
+        const int k = first ? kn : __ffs(rest) - 1;
+        rest &= ~(1u << k);
         const F2 x = f2(xsf[2 * k], xsf[2 * k + 1]);
         const F2 Q[3] = {p[0] - x, p[1] - x, p[2] - x};
         const float d0 = dot(Q[0], Q[0]), d1 = dot(Q[1], Q[1]), d2 = dot(Q[2], Q[2]);

@@ -299,9 +299,8 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
         const int k = __ffs(cut) - 1;
         const F2 x = f2(xsf[2 * k], xsf[2 * k + 1]);
         const F2 Q[3] = {p[0] - x, p[1] - x, p[2] - x};
-        F2 R[9];
         bool amb = false;
-        const int n = fretriangulate(Q, P.sqdelta_f, P.caps, R, amb);
+        const int n = fretriangulate(Q, P.sqdelta_f, P.caps, nullptr, amb);   // the count only
         if (!amb) {
             if (n >= 3) return true;
             continue;
@@ -581,6 +580,7 @@ __global__ void k_in_fill(const int *__restrict__ pA, const int *__restrict__ pB
 struct RowArgs {
     const int *T32, *labT, *labV, *vprob, *vel, *pB, *inA;
     const long long *vptr, *out_ptr, *in_ptr;
+    const int *out_cnt;        // out-pair counts when the out-lists are pool segments (see PassArgs)
     const ProbParams *probs;
     long long nV;
     unsigned *marks;       // nwarps * mstride
@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(256) k_row_pattern(RowArgs a, int pass) {
         const long long rbase = a.cols ? a.rowptr[u] : 0;
         for (long long t = a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
-            const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
+            const long long ob = a.out_ptr[T], oe = a.out_cnt ? ob + a.out_cnt[T] : a.out_ptr[T + 1];
             const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
             if (oe == ob && ie == ib) continue;
             const long long nEl = 1 + (oe - ob) + (ie - ib);
@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(256) k_row_pattern_bm(RowArgs a, int pass, int
         }
         for (long long t = a.mode != 0 ? a.vptr[u + 1] : a.vptr[u]; t < a.vptr[u + 1]; t++) {
             const int T = a.vel[t];
-            const long long ob = a.out_ptr[T], oe = a.out_ptr[T + 1];
+            const long long ob = a.out_ptr[T], oe = a.out_cnt ? ob + a.out_cnt[T] : a.out_ptr[T + 1];
             const long long ib = a.in_ptr ? a.in_ptr[T] : 0, ie = a.in_ptr ? a.in_ptr[T + 1] : 0;
             if (oe == ob && ie == ib) continue;
             const int nout = (int)(oe - ob), nEl = 1 + nout + (int)(ie - ib);

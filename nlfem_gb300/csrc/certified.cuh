@@ -68,7 +68,7 @@ struct FPoly {
 
 __device__ __forceinline__ void fpush(FPoly &Y, const FPt &p, bool &amb) {
     if (Y.n >= 9) { amb = true; return; }
-    Y.R[Y.n] = p.y;
+    if (Y.R) Y.R[Y.n] = p.y;   // null R: the count only
     if (Y.n == 0) Y.first = p;
     Y.last = p;
     Y.n++;
@@ -99,7 +99,8 @@ __device__ __forceinline__ void fplace_cap(FPoly &Y, const FPt &a, const FPt &b,
 
 // FP32 method_retriangulate with the triangle P given relative to the ball center. Returns the
 // polygon point count (sub-triangles: fan (R0, R[j+1], R[j+2])); amb = true when a decision was
-// within its margin (the result must then be recomputed in FP64).
+// within its margin (the result must then be recomputed in FP64). With R null only the count is
+// kept (the interaction test of the pair search).
 __device__ __forceinline__ int fretriangulate(const F2 *P, float sq, int caps, F2 *R, bool &amb,
                                               unsigned *why = nullptr) {
     FPoly Y;

@@ -126,6 +126,8 @@ struct PassArgs {
     const float *adetf;         // |det| in FP32
     const ProbParams *probs;
     const long long *out_ptr, *in_ptr;
+    const int *out_cnt;         // out-pair counts when the out-lists are the search's pool segments
+                                // (out_ptr = segment starts, pB = the pool); null: out_ptr[T + 1] ends
     const int *pB, *inA;
     const long long *rowptr;
     const int *cols;

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
         idx = __shfl_sync(FULL, idx, 0);
         if (idx >= a.count) break;
         const int T = a.list ? a.list[idx] : idx;
-        const long long lb = a.out_ptr[T], le = a.out_ptr[T + 1];
+        const long long lb = a.out_ptr[T], le = a.out_cnt ? lb + a.out_cnt[T] : a.out_ptr[T + 1];
         if (lb == le || a.labT[T] == 0) continue;
         int tv[dV];
         unsigned keepmask = 0;

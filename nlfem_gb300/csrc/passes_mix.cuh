@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         idx = __shfl_sync(FULL, idx, 0);
         if (idx >= a.count) break;
         const int T = a.list ? a.list[idx] : idx;
-        const long long lb = a.out_ptr[T], le = a.out_ptr[T + 1];
+        const long long lb = a.out_ptr[T], le = a.out_cnt ? lb + a.out_cnt[T] : a.out_ptr[T + 1];
         if (lb == le || a.labT[T] == 0) continue;
         int tv[3];
         unsigned keepmask = 0;   // bit r: the row of T's vertex r exists

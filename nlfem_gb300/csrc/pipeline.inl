@@ -385,6 +385,8 @@ struct Session {
     long long vp_cap = 0;
     bool vlists = false;
     bool use_rank = false;
+    bool pairs_pool = false;        // out-lists are the search's pool segments (run_pairs)
+    bool want_pair_arrays = false;  // the pair-list hook asks for aT-major pA / pB
     long long rtot = 0;
     DevBuf pscratch, rowoff;                // single-pass pattern (capacity from the last assembly)
     DevBuf valsN, elp;                      // one-sided retriangulate pass: own-row termNonloc, LP blocks
@@ -883,6 +885,18 @@ static int pattern_bitmap_threads(const Session &S) {
 template <int DIM>
 static int run_pairs(Session &S) {
     const long long nE = S.nE;
+    // The one-sided passes and their bitmap pattern read each element's partners where the search
+    // left them (its segment of the pool: seg_start, seg_cnt), so the pairs are held once (4 B
+    // each). The other paths, and the pair-list hook, get aT-major arrays pA, pB and out_ptr.
+    S.pairs_pool = !S.want_pair_arrays &&
+                   (S.pmode == PM_BARY || S.pmode == PM_RETRI) && pattern_bitmap_threads(S);
+    if (S.pairs_pool) {
+        int r = d2h(S, &S.P, reinterpret_cast<long long *>(S.counters.get<unsigned long long>()), 1);   // pool cursor
+        if (r) return r;
+        S.stats.n_pairs = (long)S.P;
+        CK(cudaGetLastError());
+        return NLFEM_OK;
+    }
     ENS(S.out_ptr, sizeof(long long) * (nE + 1));
     int r = scan_excl<int>(S, S.seg_cnt.get<int>(), nE, S.out_ptr.get<long long>());
     if (r) return r;
@@ -1133,6 +1147,7 @@ static int run_pattern_bm(Session &S, int words, int threads) {
     a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.labV = S.labV.get<int>();
     a.vprob = S.vprob.get<int>(); a.vel = S.vel.get<int>(); a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>();
     a.vptr = S.vptr.get<long long>(); a.out_ptr = S.out_ptr.get<long long>();
+    if (S.pairs_pool) { a.pB = S.pool.get<int>(); a.out_ptr = S.seg_start.get<long long>(); a.out_cnt = S.seg_cnt.get<int>(); }
     a.in_ptr = S.pmode == PM_BARY ? nullptr : S.in_ptr.get<long long>();   // rows of one-sided rules: out-pairs only
     a.probs = S.prm.get<ProbParams>(); a.nV = nV;
     a.marks = nullptr; a.mstride = 0;
@@ -1583,6 +1598,7 @@ static int run_passes(Session &S) {
     a.adetf = S.adetf.get<float>();
     a.probs = S.prm.get<ProbParams>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
     a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();
+    if (S.pairs_pool) { a.pB = S.pool.get<int>(); a.out_ptr = S.seg_start.get<long long>(); a.out_cnt = S.seg_cnt.get<int>(); }
     a.vals = S.vals.get<double>(); a.xadj = S.xadj.get<long long>(); a.adj = S.adj.get<int>();
     a.closebuf = S.closebuf.get<double>(); a.err = S.err.get<int>();
     a.zptr = S.zptr.get<long long>(); a.zidx = S.zidx.get<long long>();
@@ -2397,6 +2413,7 @@ int nlfem_pair_list(const nlfem_problem *prob, long *n_pairs, long **pairs) {
     int r = nlfem_session_create(prob, 1, &s);
     if (r) return r;
     Session &S = s->S;
+    S.want_pair_arrays = true;
     r = S.dim == 2 ? (run_prep<2>(S) || run_dual<2>(S) || run_bfs<2>(S) || run_pairs<2>(S))
                    : (run_prep<3>(S) || run_dual<3>(S) || run_bfs<3>(S) || run_pairs<3>(S));
     if (r) { r = g_err.empty() ? NLFEM_ERR_CUDA : r; nlfem_session_destroy(s); return r ? r : NLFEM_ERR_CUDA; }

@@ -1061,3 +1061,27 @@ def test_mixed_slot_maps_window_rank_and_hash(nl, orc):
     assert same_pattern(A, C)
     fro, mx = rel_errors(A, C)
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_far_component_capacity_retries(nl, orc, prec):
+    """The search sizes its pair pool from the mesh's mean element size. A far-away extra triangle
+    inflates the bounding box, so that estimate is far too small and the pool overflows: the
+    search reruns with the size it counted. The pairs and the matrix are those of the oracle."""
+    from nlfem_gb300 import meshes
+    v, e, l = meshes.regular_square(32, 0.3, jitter=0.1, seed=31)
+    nV = v.shape[0]
+    v2 = np.vstack([v, [[50.0, 50.0], [50.01, 50.0], [50.0, 50.01]]])
+    e2 = np.vstack([e, [[nV, nV + 1, nV + 2]]])
+    l2 = np.concatenate([l, [1]])
+    m = meshes.mesh_dict(v2, e2, l2)
+    k = {"function": "constant", "horizon": 0.3, "outputdim": 1}
+    A = nl.stiffnessMatrix(dict(m), k, conf2d(precision=prec))
+    ref = orc.assemble(m, k, conf2d(), want_pairs=True)
+    got = nl.pair_list(m, k, conf2d(precision=prec))
+    rp = ref["pairs"][np.lexsort((ref["pairs"][:, 1], ref["pairs"][:, 0]))]
+    np.testing.assert_array_equal(got, rp)
+    assert same_pattern(A, ref["A"])
+    fro, mx = rel_errors(A, ref["A"])
+    tol = MIX_TOL if prec == "mixed" else FP64_TOL
+    assert fro < tol and mx < tol, (fro, mx)

@@ -14,9 +14,10 @@
 
 namespace nlg {
 
-// Margins, relative to the magnitude of each decision's operands. The FP32 rounding error of every
-// tested quantity is a few units of 2^-24 of that magnitude (coordinates are local to the ball
-// center, built from double-float differences), so each margin is at least 256 times larger.
+// Margins, relative to the magnitude of each decision's operands. The FP32 rounding error of a
+// tested quantity is a bounded number of units of 2^-24 of that magnitude (coordinates are local
+// to the outer element, built from double-float differences); each margin is 256 or more such
+// units, and the bound for the vertex tests is written out below MIX_MAX_H_OVER_DELTA.
 // Which roots of |q + l (p - q) - x|^2 = delta^2 lie in [0, 1] is fixed by the signs of its values
 // at 0 and 1 (vertex distances, MARG_D) and of the discriminant (MARG_V, flagged only when the
 // tangent point lies near the segment); MARG_L additionally guards the computed roots.
@@ -35,6 +36,19 @@ __device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2{a.x + b.x, a.y +
 __device__ __forceinline__ float dot(F2 a, F2 b) { return fmaf(a.x, b.x, a.y * b.y); }
 
 constexpr float U32 = 5.9604645e-8f;      // 2^-24
+
+// Error bound of the squared distances the vertex tests compare (u = 2^-24). Coordinates are local
+// to the outer element T's first vertex: an outer point lies within h (T's diameter) of it, and a
+// candidate element's vertices within delta + 3h (h the largest diameter). A vertex offset is the
+// FP32 difference of double-float (hi + lo) pairs, |error| <= 2.01 u (delta + 3h); the outer point's
+// offset is one FP32 rounding, <= u h; their difference Q adds u |Q|. At |Q| ~ delta the squared
+// distance Q.Q (one FMA, 2u) is then off by at most
+//   2 delta (u delta + 2.01 u (delta + 3.5 h)) + 2 u delta^2 = u delta^2 (8.02 + 14.07 h / delta),
+// below MARG_D delta^2 = 256 u delta^2 while h <= 17.6 delta. The mixed path therefore refuses
+// meshes with an element diameter above MIX_MAX_H_OVER_DELTA delta. The bounding-disc tests of the
+// pair search (centroid distance against (delta +- r)^2) have the same bound divided by
+// (1 + r / delta)^2, with r inflated by 8u.
+constexpr double MIX_MAX_H_OVER_DELTA = 16.0;
 
 // inTriangle with margin: y carries a position error bound ey; a sign test is ambiguous when its
 // value is within twice the bound on its error.

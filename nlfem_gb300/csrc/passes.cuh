@@ -605,6 +605,10 @@ __global__ void __launch_bounds__(PASS_THREADS) k_pass(PassArgs a, Rule rule, Pa
             any |= keep[r];
         }
         if (!any || a.labT[T] == 0) continue;
+        // an element without any pair (a ball smaller than the element can stay strictly inside
+        // it, which the retriangulation counts as no polygon) adds nothing, and its row pattern
+        // holds none of its columns
+        if (a.out_ptr[T] == a.out_ptr[T + 1] && (!a.in_ptr || a.in_ptr[T] == a.in_ptr[T + 1])) continue;
         const ProbParams P = a.probs[a.eprob[T]];
         // rows of T's vertices: column lists in shared memory when they fit
         RowView rows[dV];

@@ -296,6 +296,31 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     for (int j = 0; j < p.dim; j++) vol *= std::max(hi[j] - lo[j], 1e-300);
     const double el = vol / (double)p.nE;
     P.el = el;
+    // The one-sided passes decide their geometry with margins (certified.cuh; 2^-40 for the FP64
+    // instance). The rounding of coordinates local to an outer element grows with the element
+    // size relative to the ball: the FP32 vertex tests stay inside their margin while every element
+    // diameter is at most MIX_MAX_H_OVER_DELTA times delta (the FP64 ones up to 512 delta).
+    if (system && (p.precision == NLFEM_PREC_MIXED || p.precision == NLFEM_PREC_FP64_ONESIDED)) {
+        const int dV = p.dim + 1;
+        double hmax2 = 0;
+        for (long e = 0; e < p.nE; e++)
+            for (int a = 0; a < dV; a++)
+                for (int b = a + 1; b < dV; b++) {
+                    const long va = p.elements[e * dV + a], vb = p.elements[e * dV + b];
+                    if (va < 0 || vb < 0 || va >= p.nV || vb >= p.nV) continue;   // rejected by the mesh checks
+                    double d2 = 0;
+                    for (int j = 0; j < p.dim; j++) {
+                        const double d = p.vertices[va * p.dim + j] - p.vertices[vb * p.dim + j];
+                        d2 += d * d;
+                    }
+                    hmax2 = std::max(hmax2, d2);
+                }
+        const double lim = p.precision == NLFEM_PREC_MIXED ? MIX_MAX_H_OVER_DELTA : 512.0;
+        if (hmax2 > lim * lim * p.sqdelta)
+            return fail(NLFEM_ERR_UNSUPPORTED, std::string("precision \"") + (p.precision == NLFEM_PREC_MIXED ? "mixed" : "fp64-onesided") +
+                        "\" needs elements no larger than " + std::to_string((int)lim) +
+                        " times the horizon (the margins of its geometry tests); precision \"fp64\" has no such bound");
+    }
     double mag;
     if (system) {
         const double h = pow(el, 1.0 / p.dim);

@@ -1085,3 +1085,21 @@ def test_far_component_capacity_retries(nl, orc, prec):
     fro, mx = rel_errors(A, ref["A"])
     tol = MIX_TOL if prec == "mixed" else FP64_TOL
     assert fro < tol and mx < tol, (fro, mx)
+
+
+def test_mixed_refuses_elements_far_larger_than_the_horizon(nl, orc):
+    """The margins of the mixed path's FP32 geometry hold while every element is at most 16 times
+    the horizon (certified.cuh); beyond that the mixed precision is refused and FP64 runs. With a
+    horizon this small, a ball around an element's own quadrature point stays inside the element,
+    which the retriangulation counts as no polygon, so some elements have no pair at all."""
+    from nlfem_gb300._lib import NlfemError
+    m = square_mesh(8, 0.005, jitter=0.1, seed=33)
+    k = {"function": "constant", "horizon": 0.005, "outputdim": 1}
+    with pytest.raises(NlfemError, match="no larger than 16 times the horizon"):
+        nl.stiffnessMatrix(dict(m), k, conf2d(precision="mixed"))
+    A = nl.stiffnessMatrix(dict(m), k, conf2d())
+    B = orc.assemble(m, k, conf2d())["A"]
+    assert same_pattern(A, B)
+    if B.nnz:
+        fro, mx = rel_errors(A, B)
+        assert fro < FP64_TOL and mx < FP64_TOL, (fro, mx)

@@ -231,7 +231,7 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
                                                    const float *xsf, int nPx, const double *Eb,
                                                    const float *pb, unsigned &namb) {
     if (P.full_search) return true;
-    if (method == MTH_FRACTIONAL) return true;   // the mixed path takes no weakSingular rule
+    if (method == MTH_FRACTIONAL || method == MTH_WEAKSING) return true;   // close rules: every candidate
     const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
     if (method == MTH_BARYCENTER) {
         float bf[DIM];

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         long long D[6];   // termLocal of T's pairs, integer sums
 #pragma unroll
         for (int i = 0; i < 6; i++) D[i] = 0;
-        const bool frac_close = KIND == MIX_SINGULAR && P.singular && P.close == MTH_FRACTIONAL;
+        const bool frac_close = KIND == MIX_SINGULAR && duffy_close(P);   // fractional or weakSingular close blocks
         const R sqf = A::sqd(P);
         int part_next = lb + lane < le ? a.pB[lb + lane] : T;   // partners one batch ahead
         for (long long p0 = lb; p0 < le; p0 += 32) {

@@ -220,12 +220,13 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "You chose an integration routing for singular kernels, but no quadrature rule for it.");
         if ((P.close == MTH_FRACTIONAL || P.close == MTH_WEAKSING) && p.dim != 2)
             return fail(NLFEM_ERR_UNSUPPORTED, "fractional and weakSingular close pairs are 2D only");
-        if (P.singular && P.close == MTH_WEAKSING && p.precision != NLFEM_PREC_FP64)
-            return fail(NLFEM_ERR_UNSUPPORTED, "the weakSingular close rule runs on the fp64 path only (precision \"fp64\")");
+        if (P.singular && P.close == MTH_WEAKSING && p.precision == NLFEM_PREC_FP64_ONESIDED)
+            return fail(NLFEM_ERR_UNSUPPORTED, "precision \"fp64-onesided\" takes the fractional close rule only");
         if (p.dim == 2 && (P.kernel == KER_CONSTANT3D)) return fail(NLFEM_ERR_INVALID, "constant3D kernel needs a 3D mesh");
         if (p.is_dg && p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, "the DG ansatz runs on the fp64 path only (precision \"fp64\")");
-        if ((P.remote >= MTH_RETRI_UNSYMM || P.close >= MTH_RETRI_UNSYMM) && p.precision != NLFEM_PREC_FP64)
+        if ((P.remote >= MTH_RETRI_UNSYMM || (P.close >= MTH_RETRI_UNSYMM && P.close != MTH_WEAKSING)) &&
+            p.precision != NLFEM_PREC_FP64)
             return fail(NLFEM_ERR_UNSUPPORTED, std::string("integration method ") +
                         (P.remote >= MTH_RETRI_UNSYMM ? p.method_remote : p.method_close) + " runs on the fp64 path only (precision \"fp64\")");
         if (P.kernel >= KER_LABELED && P.kernel <= KER_CONSTTRUNC) {   // label- or position-dependent kernels of 2D meshes
@@ -659,7 +660,10 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
                     const size_t np = (size_t)nTr[c] * nPg;
                     for (size_t i = 0; i < np * 4; i++) hf.push_back((float)h[o + i]);
                     for (size_t i = 0; i < np; i++) hf.push_back((float)(h[o + np * 4 + i] * dg[i % nPg]));
-                    while (hf.size() % 4) hf.push_back(0.f);   // the next case's float4 points stay 16-byte aligned
+                    while (hf.size() % 4) hf.push_back(0.f);   // the next float4 points stay 16-byte aligned
+                    for (size_t i = 0; i < np * 4; i++) hf.push_back((float)h[o + np * 5 + i]);   // alphaU
+                    for (size_t i = 0; i < np; i++) hf.push_back((float)(h[o + np * 9 + i] * dg[i % nPg]));   // tdetW dg
+                    while (hf.size() % 4) hf.push_back(0.f);
                     o += np * 4 + np + np * 4 + np;
                 }
             }
@@ -1303,6 +1307,8 @@ static Duffy duffy_view(const Session &S) {
     for (int c = 0; c < 3; c++) {
         d.alf[c] = reinterpret_cast<const float4 *>(f + of); of += (size_t)nTr[c] * nPg * 4;
         d.wf[c] = f + of; of += ((size_t)nTr[c] * nPg + 3) / 4 * 4;
+        d.alfU[c] = reinterpret_cast<const float4 *>(f + of); of += (size_t)nTr[c] * nPg * 4;
+        d.wfW[c] = f + of; of += ((size_t)nTr[c] * nPg + 3) / 4 * 4;
     }
     return d;
 }

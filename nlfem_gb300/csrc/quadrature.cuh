@@ -32,6 +32,8 @@ struct Duffy {
     const double *dg;         // [k]
     const float4 *alf[3];     // FP32 copies of alpha (mixed path)
     const float *wf[3];       // FP32 tdet * dg (mixed path)
+    const float4 *alfU[3];    // FP32 copies of alphaU (mixed weakSingular rule)
+    const float *wfW[3];      // FP32 tdetW * dg (mixed weakSingular rule)
 };
 
 struct QuadArgs {
@@ -702,6 +704,67 @@ __device__ __forceinline__ void weak_accumulate(const ProbParams &P, const Duffy
     }
 }
 
+// The weakSingular sums on the mixed path, in FP32 as close_accumulate_f32 (the same x - y and
+// power), with the basis functions at the points with xi kept and the weight xi^(1 - 2s).
+__device__ __forceinline__ void weak_accumulate_f32(const ProbParams &P, const Duffy &d, int c, int nT,
+                                                    const double *EA, const double *EB, double dAB, double *W) {
+    const int lane = threadIdx.x & 31;
+    const int total = nT * d.nPg;
+    const float4 *alf = d.alf[c], *alu = d.alfU[c];
+    const float *wf = d.wfW[c];
+    const double ae[4] = {EA[2] - EA[0], EA[4] - EA[0], EA[3] - EA[1], EA[5] - EA[1]};
+    const double be[4] = {EB[2] - EB[0], EB[4] - EB[0], EB[3] - EB[1], EB[5] - EB[1]};
+    float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        ah[i] = (float)ae[i]; al[i] = (float)(ae[i] - (double)ah[i]);
+        bh[i] = (float)be[i]; bl[i] = (float)(be[i] - (double)bh[i]);
+    }
+    const double hexp = -0.5 * P.expo;
+    const float hh = (float)(ldexp(rint(ldexp(hexp, 8)), -8));
+    const float hl = (float)(hexp - (double)hh);
+    const float hf = (float)hexp;
+    const float kcd = (float)(P.kc * dAB);
+    float Wf[21], Wc[21];
+#pragma unroll
+    for (int q = 0; q < 21; q++) Wf[q] = Wc[q] = 0.f;
+    auto add = [&](int q, float v) {   // Kahan step
+        const float y = v - Wc[q];
+        const float t = Wf[q] + y;
+        Wc[q] = (t - Wf[q]) - y;
+        Wf[q] = t;
+    };
+    for (int idx = lane; idx < total; idx += 32) {
+        const float4 a4 = alf[idx], u4 = alu[idx];
+        float z0 = fmaf(a4.x, ah[0], fmaf(a4.y, ah[1], fmaf(-a4.z, bh[0], -a4.w * bh[1])));
+        float z1 = fmaf(a4.x, ah[2], fmaf(a4.y, ah[3], fmaf(-a4.z, bh[2], -a4.w * bh[3])));
+        z0 = fmaf(a4.x, al[0], fmaf(a4.y, al[1], fmaf(-a4.z, bl[0], fmaf(-a4.w, bl[1], z0))));
+        z1 = fmaf(a4.x, al[2], fmaf(a4.y, al[3], fmaf(-a4.z, bl[2], fmaf(-a4.w, bl[3], z1))));
+        const float r2 = fmaf(z0, z0, z1 * z1);
+        int E;
+        const float m = frexpf(r2, &E);
+        const float t = hh * (float)E;
+        const float I = floorf(t);
+        const float g = fmaf(hf, log2f(m), fmaf(hl, (float)E, t - I));
+        const float f = ldexpf(exp2f(g), (int)I) * wf[idx] * kcd;
+        const float px[3] = {1.f - u4.x - u4.y, u4.x, u4.y};
+        const float py[3] = {1.f - u4.z - u4.w, u4.z, u4.w};
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float fx = f * px[i], fy = f * py[i];
+#pragma unroll
+            for (int j = i; j < 3; j++) {
+                add(sym_idx<3>(i, j), fx * px[j]);
+                add(6 + sym_idx<3>(i, j), fy * py[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 3; j++) add(12 + 3 * i + j, fx * py[j]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 21; q++) W[q] = (double)Wf[q] - (double)Wc[q];
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int lane = threadIdx.x & 31;
@@ -741,11 +804,12 @@ __global__ void __launch_bounds__(128) k_quad_close(QuadArgs a, Duffy d) {
     const int nT = (nEqual == 1) ? 2 : (nEqual == 2 ? 5 : 6);
     double acc[36];
     for (int i = 0; i < 36; i++) acc[i] = 0;
-    if (!FAST && P.close == MTH_WEAKSING) {
+    if (P.close == MTH_WEAKSING) {
         double W[21];
 #pragma unroll
         for (int i = 0; i < 21; i++) W[i] = 0.0;
-        weak_accumulate(P, d, c, nT, EA, EB, dA * dB, W);
+        if (FAST) weak_accumulate_f32(P, d, c, nT, EA, EB, dA * dB, W);
+        else weak_accumulate(P, d, c, nT, EA, EB, dA * dB, W);
 #pragma unroll
         for (int i = 0; i < 21; i++) W[i] = warp_sum(W[i]);
         // termLocal[argA a][argA b], termLocalPrime[argB a][argB b], termNonloc and

@@ -432,8 +432,13 @@ def test_weak_singular_close_rule(nl, orc):
     g, _ = nl.pair_blocks(m, kp, cw, np.array(pairs), close=True)
     o, _ = orc.pair_blocks(m, kp, cw, np.array(pairs), method="weakSingular")
     np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-12 * np.abs(o).max())
-    with pytest.raises(NlfemError, match="fp64 path only"):
-        nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="mixed"))
+    # the mixed path: FP32 Duffy rule (weakSingular form) for the close pairs, within the mixed bound
+    Am = nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="mixed"))
+    assert same_pattern(Am, B)
+    fro, mx = rel_errors(Am, B)
+    assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
+    with pytest.raises(NlfemError, match="fractional close rule only"):
+        nl.stiffnessMatrix(dict(m), kp, conf2d(rule="16", close="weakSingular", deg=3, precision="fp64-onesided"))
 
 
 @pytest.mark.parametrize("name", ["config1", "tangent", "parabola20", "frac12", "cube5", "labeled10", "average10",

@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
 #pragma unroll
                         for (int i = 0; i < 3; i++)
 #pragma unroll
-                            for (int j = i; j < 3; j++) lx[sym_idx<3>(i, j)] = fx64d(cb[3 * i + j], P.fx_mul, bad);
+                            for (int j = i + 1; j < 3; j++) lx[sym_idx<3>(i, j)] = fx64d(cb[3 * i + j], P.fx_mul, bad);
 #pragma unroll
                         for (int i = 0; i < 9; i++) {
                             nx[i] = fx64d(cb[9 + i], P.fx_mul, bad);    // termNonloc [T vertex][b vertex]
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
 #pragma unroll
                         for (int i = 0; i < 3; i++)
 #pragma unroll
-                            for (int j = i; j < 3; j++) lpx[sym_idx<3>(i, j)] = fx64d(cb[18 + 3 * i + j], P.fx_mul, bad);
+                            for (int j = i + 1; j < 3; j++) lpx[sym_idx<3>(i, j)] = fx64d(cb[18 + 3 * i + j], P.fx_mul, bad);
                     }
                 } else {
                     R L[6] = {0, 0, 0, 0, 0, 0}, N[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -597,18 +597,25 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                         for (int ab = 0; ab < 6; ab++) LP[ab] = A::fm(Ad, inv[4 + ab], LP[ab]);
                     }
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lx[i] = A::fx(L[i] * rTT, P, bad);
+                    for (int i = 0; i < 6; i++)   // the diagonal entries come from the row sums (k_sym_add)
+                        if (i != 0 && i != 3 && i != 5) lx[i] = A::fx(L[i] * rTT, P, bad);
 #pragma unroll
                     for (int i = 0; i < 9; i++) mx[i] = nx[i] = A::fx(N[i] * rTT, P, bad);
 #pragma unroll
-                    for (int i = 0; i < 6; i++) lpx[i] = A::fx(LP[i] * rTT, P, bad);
+                    for (int i = 0; i < 6; i++)
+                        if (i != 0 && i != 3 && i != 5) lpx[i] = A::fx(LP[i] * rTT, P, bad);
                 }
-                balance_rows<3>(lx, nx, lpx, mx);
+                // Only off-diagonal entries of the matrix are accumulated: every kept row of the
+                // assembled operator sums to zero (for kernels of |x - y| each pair's blocks do, the
+                // basis functions summing to one), so k_sym_add sets each diagonal entry to minus
+                // its row's off-diagonal sum. The integers are those a per-pair balance of the
+                // block diagonals would give, so the matrix is the same bit for bit.
 #pragma unroll
                 for (int i = 0; i < 6; i++) D[i] += lx[i];
-                // termLocalPrime into the partner's block accumulator
-#pragma unroll
-                for (int q = 0; q < 6; q++) red_add(ma.elp, (long long)part * 6 + q, lpx[q]);
+                // termLocalPrime (off-diagonal part) into the partner's block accumulator
+                red_add(ma.elp, (long long)part * 6 + 1, lpx[1]);
+                red_add(ma.elp, (long long)part * 6 + 2, lpx[2]);
+                red_add(ma.elp, (long long)part * 6 + 4, lpx[4]);
             }
             // termNonloc into A[T, b] (minus sign): lanes sharing a partner vertex add their
             // integers, the first of them lists the sums (over the item results, read by now); then
@@ -675,6 +682,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
                     if (w >= nit) continue;
                     const int e = w / 3, r = w - 3 * e;
                     const int col = slist[e].col;
+                    if (col == W.tvs[r]) continue;   // the matrix diagonal: from the row sum
                     const long long sn = slist[e].v[r], sq = slist[e].v[3 + r];
                     RowHash h;
                     h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
@@ -701,7 +709,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
         for (int i = 0; i < 6; i++)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) D[i] += (long long)__shfl_xor_sync(FULL, (unsigned long long)D[i], o);
-        if (lane < 9) {
+        if (lane < 9 && lane / 3 != lane % 3) {   // off-diagonal entries (the diagonal: k_sym_add)
             const int r = lane / 3, c = lane % 3;
             const int s = sm.dslot[(long long)T * 9 + lane];
             const int si = r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r);
@@ -733,7 +741,8 @@ __global__ void __launch_bounds__(MIX_THREADS, 4) k_pass_mix2d(MixArgs ma, Rule 
 // Symmetric completion of the one-sided retriangulate pass: every slot (t, v) adds the
 // termNonloc sums of the transposed slot (v, t) when v has a row. Integer sums, so the completed
 // matrix is exactly symmetric in these contributions, as the reference's A[b, T] -= termNonlocPrime
-// = termNonloc^T (kernels of |x - y|) makes it. One warp per row.
+// = termNonloc^T (kernels of |x - y|) makes it. Then the row's diagonal entry is set to minus the
+// sum of its other entries, which the pass left out (every kept row sums to zero). One warp per row.
 __global__ void k_sym_add(const long long *__restrict__ rowptr, const int *__restrict__ cols,
                           const int *__restrict__ tpos, const long long *__restrict__ valsN, long long nrows,
                           long long *__restrict__ vals) {
@@ -742,12 +751,18 @@ __global__ void k_sym_add(const long long *__restrict__ rowptr, const int *__res
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long t = gw; t < nrows; t += nw) {
         const long long b = rowptr[t], e = rowptr[t + 1];
+        long long off = 0, dslot = -1;
         for (long long s = b + lane; s < e; s += 32) {
+            if (cols[s] == (int)t) { dslot = s; continue; }
             long long v = valsN[s];
             const int tp = tpos[s];
             if (tp >= 0) v += valsN[rowptr[cols[s]] + tp];
-            vals[s] += v;
+            v += vals[s];
+            vals[s] = v;
+            off += v;
         }
+        off = (long long)warp_sum((unsigned long long)off);
+        if (dslot >= 0) vals[dslot] = -off;   // the row sums to zero
     }
 }
 
@@ -769,6 +784,7 @@ __global__ void k_elem_blocks(const long long *__restrict__ elp, const int *__re
     for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int c = 0; c < 3; c++) {
+            if (r == c) continue;   // the diagonal comes from the row sum (k_sym_add)
             const int s = dslot[e * 9 + 3 * r + c];
             if (s >= 0) red_add(vals, s, b[r <= c ? sym_idx<3>(r, c) : sym_idx<3>(c, r)]);
             else if (labV[T32[e * 3 + r]] > 0) atomicOr(&err[3], 1);

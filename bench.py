@@ -360,7 +360,11 @@ def run_gpu(args, rank=0, world=1, dist=None):
         if len(calls) == 1:
             return [nlfem.stiffnessMatrix(*calls[0])]
         return nlfem.stiffnessMatrix_batch(calls)
-    e2e_call()
+    # two warm-up calls: results come back in pinned host blocks that the library pools, and a
+    # caller holding the previous result while the next call runs uses two of them; the first two
+    # calls allocate them (cudaMallocHost of the matrix size), later calls reuse them
+    Bs = e2e_call()
+    Bs = e2e_call()
     e2e_t, e2e_p, d2h = [], 0, 0
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize()
@@ -397,7 +401,9 @@ def run_gpu(args, rank=0, world=1, dist=None):
         "search": search_roofline(st),
         "peaks_measured": {"fp32_tflops": peak32, "fp64_tflops": peak64,
                            "hbm_gbs": measured_peaks().get("hbm_gbs")},
-        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "note": "nlfem.stiffnessMatrix from pinned host mesh arrays to a host scipy CSR, two warm-up "
+                        "calls (the pooled pinned result blocks), the previous result held during each call"},
         "clocks": clocks,
         "gpu_launches": launches,
     }

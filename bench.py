@@ -38,7 +38,7 @@ METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel e
 # that launch on the 2D constant-kernel workload at n = 128 (2.56e7 pairs: 187.0 MB read, 34.6 MB
 # written); the pass streams its pair list and reuses the mesh from L2, so the traffic grows with
 # the pairs. Reported as roofline.traffic (scaled to this run's pairs) with its source.
-PASS_TRAFFIC_PER_PAIR = {"c2": (187.021e6 + 34.574e6) / 25573871}
+PASS_TRAFFIC_PER_PAIR = {"c2": (187.713e6 + 35.046e6) / 25573871}
 # Algorithmic bytes of the pair search: per candidate the element's stamp (4 B), its incidence entry
 # (4 B), its 12 FP32 coordinates (48 B) and, per 3 candidates, a vertex's stamp and incidence range
 # (about 4 B): 60 B; per pair its queue and pool entries (8 B).

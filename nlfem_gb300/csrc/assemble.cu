@@ -50,7 +50,7 @@ __global__ void k_prep_elements(const long long *__restrict__ T64, const long lo
                                 int *__restrict__ T32, int *__restrict__ labT, int *__restrict__ eprob,
                                 double *__restrict__ EC, double *__restrict__ adet,
                                 float *__restrict__ EChi, float *__restrict__ EClo,
-                                float *__restrict__ adetf) {
+                                float *__restrict__ adetf, float *__restrict__ BCf) {
     constexpr int dV = DIM + 1;
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nE) return;
@@ -69,6 +69,18 @@ __global__ void k_prep_elements(const long long *__restrict__ T64, const long lo
             EChi[e * DIM * dV + DIM * k + j] = hi;
             EClo[e * DIM * dV + DIM * k + j] = (float)(E[DIM * k + j] - (double)hi);
         }
+    }
+    {   // barycenter (mathhelpers.cpp:184-196), split like the vertex coordinates
+        double b[DIM];
+        xbary<DIM>(E, b);
+        float *o = &BCf[e * BC_STRIDE<DIM>];
+#pragma unroll
+        for (int j = 0; j < DIM; j++) {
+            const float hi = (float)b[j];
+            o[j] = hi;
+            o[BC_STRIDE<DIM> / 2 + j] = (float)(b[j] - (double)hi);
+        }
+        if (DIM == 3) { o[3] = 0.f; o[7] = 0.f; }
     }
     long long l = lab64[e];
     labT[e] = (int)(l > 2147483647LL ? 2147483647LL : (l < -2147483647LL ? -2147483647LL : l));
@@ -167,6 +179,7 @@ struct BfsArgs {
     const int *T32, *labT, *eprob;
     const double *EC;
     const float *EChi, *EClo;
+    const float *BCf;        // barycenters, double-float (BC_STRIDE floats per element)
     unsigned long long *n_amb;
     const ProbParams *probs;
     long long nE;
@@ -224,6 +237,37 @@ __device__ __forceinline__ bool interacts_exact(const ProbParams &P, int method,
     return false;
 }
 
+// method_baryCenter for some outer point (integrate_baryCenter's doesInteract) with the FP32
+// barycenter offset bf; the exact FP64 test decides the points within the squared-distance margin.
+// oc holds the outer points' centroid and the radius ro of a sphere around it holding them all: a
+// barycenter farther than delta + ro from the centroid is outside every ball (checked with the
+// squared-distance margin, ro inflated by 8u).
+template <int DIM>
+__device__ __forceinline__ bool bary_filtered(const ProbParams &P, const double *xs, const float *xsf, int nPx,
+                                              const double *Eb, const float *bf, const float *oc, unsigned &namb) {
+    const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
+    {
+        float dc = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; j++) { const float d = bf[j] - oc[j]; dc = fmaf(d, d, dc); }
+        const float R = sqrtf(P.sqdelta_f) + oc[3];
+        if (dc > R * R * (1.f + MARG_D)) return false;
+    }
+    double b64[DIM];
+    bool have_b64 = false;
+    for (int k = 0; k < nPx; k++) {
+        float d2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; j++) { float d = xsf[DIM * k + j] - bf[j]; d2 = fmaf(d, d, d2); }
+        if (d2 < sqlo) return true;
+        if (d2 > sqhi) continue;
+        namb++;
+        if (!have_b64) { xbary<DIM>(Eb, b64); have_b64 = true; }
+        if (xbaryInside<DIM>(&xs[DIM * k], b64, P.sqdelta)) return true;
+    }
+    return false;
+}
+
 // The same predicate with the certified FP32 geometry (certified.cuh); the exact FP64 routine
 // runs only for outer points whose FP32 decisions are within their margins.
 template <int DIM>
@@ -233,29 +277,6 @@ __device__ __forceinline__ bool interacts_filtered(const ProbParams &P, int meth
     if (P.full_search) return true;
     if (method == MTH_FRACTIONAL || method == MTH_WEAKSING) return true;   // close rules: every candidate
     const float sqlo = P.sqdelta_f * (1.f - MARG_D), sqhi = P.sqdelta_f * (1.f + MARG_D);
-    if (method == MTH_BARYCENTER) {
-        float bf[DIM];
-#pragma unroll
-        for (int j = 0; j < DIM; j++) {
-            float s = pb[j];
-#pragma unroll
-            for (int i = 1; i <= DIM; i++) s += pb[DIM * i + j];
-            bf[j] = s / (float)(DIM + 1);
-        }
-        double b64[DIM];
-        bool have_b64 = false;
-        for (int k = 0; k < nPx; k++) {
-            float d2 = 0.f;
-#pragma unroll
-            for (int j = 0; j < DIM; j++) { float d = xsf[DIM * k + j] - bf[j]; d2 = fmaf(d, d, d2); }
-            if (d2 < sqlo) return true;
-            if (d2 > sqhi) continue;
-            namb++;
-            if (!have_b64) { xbary<DIM>(Eb, b64); have_b64 = true; }
-            if (xbaryInside<DIM>(&xs[DIM * k], b64, P.sqdelta)) return true;
-        }
-        return false;
-    }
     if (DIM != 2) return false;
     const F2 p[3] = {f2(pb[0], pb[1]), f2(pb[2], pb[3]), f2(pb[4], pb[5])};
     // First, per outer point, the disc around the triangle's centroid through its farthest vertex:
@@ -329,10 +350,16 @@ __device__ __forceinline__ void queue_push(bool push, int val, int *queue, long 
 template <int DIM, int PREC>
 __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, int method, const double *xs,
                                          const float *xsf, int nPx, const float *ohi, const float *olo,
-                                         const double *Ea, int b, unsigned &namb) {
+                                         const double *Ea, int b, const float *oc, unsigned &namb) {
     constexpr int dV = DIM + 1;
     const double *Eb = &a.EC[(long long)b * DIM * dV];
     if (PREC == PREC_F64) return interacts_exact<DIM>(P, method, xs, nPx, Ea, Eb);
+    if (method == MTH_BARYCENTER && !P.full_search) {
+        float bf[DIM];
+        bary_offset<DIM>(a.BCf, b, ohi, olo, bf);
+        return bary_filtered<DIM>(P, xs, xsf, nPx, Eb, bf, oc, namb);
+    }
+    if (DIM != 2) return P.full_search || method == MTH_FRACTIONAL || method == MTH_WEAKSING;
     float pb[DIM * dV];
 #pragma unroll
     for (int j = 0; j < DIM * dV; j++)
@@ -363,6 +390,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
     constexpr int U = BFS_UNROLL;
     __shared__ double s_x[BFS_WARPS][MAXQ * DIM];
     __shared__ float s_xf[BFS_WARPS][MAXQ * DIM];
+    __shared__ float s_oc[BFS_WARPS][4];                // outer points' centroid and enclosing radius
     __shared__ int s_buf[BFS_WARPS][32 * U + 32];       // candidates waiting for the interaction test
     __shared__ int s_vbuf[BFS_WARPS][32 * (DIM + 1)];   // fresh vertices of a queue group
     unsigned namb = 0;
@@ -398,6 +426,24 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
             for (int j = 0; j < DIM; j++) xsf[DIM * k + j] = (float)(xs[DIM * k + j] - Ea[j]);
         }
         __syncwarp();
+        if (PREC != PREC_F64 && lane == 0) {
+            float c[DIM], r2 = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; j++) {
+                float t = 0.f;
+                for (int k = 0; k < rule.nPx; k++) t += xsf[DIM * k + j];
+                c[j] = t / (float)rule.nPx;
+                s_oc[wib][j] = c[j];
+            }
+            for (int k = 0; k < rule.nPx; k++) {
+                float d2 = 0.f;
+#pragma unroll
+                for (int j = 0; j < DIM; j++) { const float d = xsf[DIM * k + j] - c[j]; d2 = fmaf(d, d, d2); }
+                r2 = fmaxf(r2, d2);
+            }
+            s_oc[wib][3] = sqrtf(r2) * (1.f + 8.f * U32);
+        }
+        __syncwarp();
         // (aT, aT): the first candidate of the first dequeued element (Cassemble.cpp:621)
         bool self_pair = false;
         if (lane == 0) {
@@ -420,7 +466,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
             const int method = (P.singular && lvl0) ? P.close : P.remote;
             bool pair = false;
             if (b >= 0) {
-                pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, namb);
+                pair = bfs_test<DIM, PREC>(a, P, method, xs, xsf, rule.nPx, ohi, olo, Ea, b, s_oc[wib], namb);
                 cand_local++;
             }
             queue_push(pair, b, queue, a.qcap, qtail, overflow);

@@ -39,8 +39,9 @@ constexpr float U32 = 5.9604645e-8f;      // 2^-24
 
 // Error bound of the squared distances the vertex tests compare (u = 2^-24). Coordinates are local
 // to the outer element T's first vertex: an outer point lies within h (T's diameter) of it, and a
-// candidate element's vertices within delta + 3h (h the largest diameter). A vertex offset is the
-// FP32 difference of double-float (hi + lo) pairs, |error| <= 2.01 u (delta + 3h); the outer point's
+// candidate element's vertices within delta + 3h (h the largest diameter). A vertex offset (and a
+// barycenter offset, from the barycenter's own double-float pair) is the FP32 difference of
+// double-float (hi + lo) pairs, |error| <= 2.01 u (delta + 3h); the outer point's
 // offset is one FP32 rounding, <= u h; their difference Q adds u |Q|. At |Q| ~ delta the squared
 // distance Q.Q (one FMA, 2u) is then off by at most
 //   2 delta (u delta + 2.01 u (delta + 3.5 h)) + 2 u delta^2 = u delta^2 (8.02 + 14.07 h / delta),

@@ -242,6 +242,29 @@ __device__ __forceinline__ void xbary(const double *E, double *b) {
         b[j] = xdiv(s, (double)(DIM + 1));
     }
 }
+// Per-element barycenter as a double-float pair, for the FP32 barycenter tests: DIM hi floats at
+// offset 0 and DIM lo floats at offset BC_STRIDE / 2 (3D pads each half to four floats).
+template <int DIM>
+constexpr int BC_STRIDE = DIM == 2 ? 4 : 8;
+
+// Offset of element b's barycenter from the outer element's first vertex (ohi + olo), in FP32:
+// the difference of two double-float pairs, like the vertex offsets.
+template <int DIM>
+__device__ __forceinline__ void bary_offset(const float *BCf, long long b, const float *ohi, const float *olo,
+                                            float *bf) {
+    const float4 *q = reinterpret_cast<const float4 *>(BCf + b * BC_STRIDE<DIM>);
+    if (DIM == 2) {
+        const float4 v = q[0];
+        bf[0] = (v.x - ohi[0]) + (v.z - olo[0]);
+        bf[1] = (v.y - ohi[1]) + (v.w - olo[1]);
+    } else {
+        const float4 h = q[0], l = q[1];
+        bf[0] = (h.x - ohi[0]) + (l.x - olo[0]);
+        bf[1] = (h.y - ohi[1]) + (l.y - olo[1]);
+        bf[DIM - 1] = (h.z - ohi[DIM - 1]) + (l.z - olo[DIM - 1]);
+    }
+}
+
 template <int DIM>
 __device__ __forceinline__ bool xbaryInside(const double *x, const double *b, double sqdelta) {
     double d = xsub(x[0], b[0]);

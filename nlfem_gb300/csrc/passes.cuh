@@ -123,6 +123,7 @@ struct PassArgs {
                                 // holds the element DOFs, which no two elements share)
     const double *EC, *adet;
     const float *EChi, *EClo;   // double-float split of EC
+    const float *BCf;           // barycenters, double-float (BC_STRIDE floats per element)
     const float *adetf;         // |det| in FP32
     const ProbParams *probs;
     const long long *out_ptr, *in_ptr;

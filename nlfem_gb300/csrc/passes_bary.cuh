@@ -129,25 +129,20 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             const bool act = p < le;
             const int part = part_next;
             part_next = p + 32 < le ? a.pB[p + 32] : T;
-            float pc[DIM * dV];
+            if (!CK) {   // the inner quadrature needs the partner's vertices
 #pragma unroll
-            for (int j = 0; j < DIM * dV; j++)
-                pc[j] = (a.EChi[(long long)part * DIM * dV + j] - ohi[j % DIM]) + (a.EClo[(long long)part * DIM * dV + j] - olo[j % DIM]);
-#pragma unroll
-            for (int j = 0; j < DIM * dV; j++) W.pc[lane][j] = pc[j];
+                for (int j = 0; j < DIM * dV; j++)
+                    W.pc[lane][j] = (a.EChi[(long long)part * DIM * dV + j] - ohi[j % DIM]) +
+                                    (a.EClo[(long long)part * DIM * dV + j] - olo[j % DIM]);
+            }
             W.prt[lane] = a.adetf[part];
             float bf[DIM];
-#pragma unroll
-            for (int j = 0; j < DIM; j++) {
-                float s = pc[j];
-#pragma unroll
-                for (int i = 1; i < dV; i++) s += pc[DIM * i + j];
-                bf[j] = s / (float)dV;
-            }
+            bary_offset<DIM>(a.BCf, part, ohi, olo, bf);
             // owner: which outer points see the partner's barycenter inside the ball
             bool have_b64 = false;
             double b64[DIM];
             float inv[RN];   // constant kernel: an item's sums
+            unsigned inm = 0;   // constant kernel: outer points whose ball holds the barycenter
             if (CK) {
                 const float kr = P.kc_f * W.prt[lane];
 #pragma unroll
@@ -169,14 +164,13 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                         c = xbaryInside<DIM>(&W.x64[DIM * k], b64, P.sqdelta) ? 1 : 0;
                     }
                 }
-                mycls[k] = c;
                 nitin += c;
-                float *rr = &res[(lane * nPx + k) * RN];
-                if (CK && c) {
-                    nsub++;
-#pragma unroll
-                    for (int q = 0; q < RN; q++) rr[q] = inv[q];
+                if (CK) {
+                    inm |= (unsigned)c << k;
+                    nsub += c;
                 } else {
+                    mycls[k] = c;
+                    float *rr = &res[(lane * nPx + k) * RN];
 #pragma unroll
                     for (int q = 0; q < RN; q++) rr[q] = 0.f;
                 }
@@ -231,7 +225,34 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                 for (int i = 0; i < NS; i++) L[i] = 0.f;
 #pragma unroll
                 for (int i = 0; i < dV * dV; i++) N[i] = 0.f;
-                for (int k = 0; k < nPx; k++) {
+                if (CK) {   // every item's sums are inv: the folds are inv times the mask's rule sums
+                    float sx[NS], cxs[dV];
+                    if (inm == (nPx == 32 ? 0xffffffffu : (1u << nPx) - 1u)) {
+#pragma unroll
+                        for (int i = 0; i < NS; i++) sx[i] = pr.xsum[i];
+#pragma unroll
+                        for (int r = 0; r < dV; r++) cxs[r] = pr.xsum[NS + r];
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < NS; i++) sx[i] = 0.f;
+#pragma unroll
+                        for (int r = 0; r < dV; r++) cxs[r] = 0.f;
+                        for (unsigned mm = inm; mm; mm &= mm - 1) {
+                            const int k = __ffs(mm) - 1;
+#pragma unroll
+                            for (int i = 0; i < NS; i++) sx[i] += pr.cxx[NS * k + i];
+#pragma unroll
+                            for (int r = 0; r < dV; r++) cxs[r] += pr.cx[dV * k + r];
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < NS; i++) L[i] = sx[i] * inv[0];
+#pragma unroll
+                    for (int r = 0; r < dV; r++)
+#pragma unroll
+                        for (int t = 0; t < dV; t++) N[dV * r + t] = cxs[r] * inv[1 + t];
+                }
+                for (int k = 0; k < (CK ? 0 : nPx); k++) {
                     const float *rr = &res[(lane * nPx + k) * RN];
 #pragma unroll
                     for (int s = 0; s < NS; s++) L[s] = fmaf(pr.cxx[NS * k + s], rr[0], L[s]);

@@ -395,6 +395,7 @@ struct Session {
     DevBuf duffyf;   // FP32 Duffy tables of the mixed close-pair rule: points (float4), weights
     // derived
     DevBuf T32, labT, eprob, EC, adet, labV, vprob, EChi, EClo, adetf;
+    DevBuf BCf;   // element barycenters as double-float pairs (BC_STRIDE floats per element)
     DevBuf color, color2, colorlist, closeA, closeB, closebuf, touched;
     std::vector<int> color_off;
     int prec = 0;
@@ -454,7 +455,7 @@ struct Session {
                 &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
-                &EChi, &EClo, &adetf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
+                &EChi, &EClo, &adetf, &BCf, &color, &color2, &colorlist, &closeA, &closeB, &closebuf, &touched,
                 &hcap, &hptr, &htab, &tpos, &dslot, &rwords, &rbase, &rlo, &rankmap, &eid_ptr, &eid, &vp_cnt, &vp_off, &vp_ptr, &vp_scratch, &pscratch, &rowoff, &kclist, &valsN, &elp,
                 &po_cnt, &po_off, &po_ptr, &po_scratch, &tcnt, &tptr, &tcols, &sv_vec, &sv_part, &zptr, &zidx, &vacc, &vtiny,
                 &dgT32, &dglabV, &dgvprob, &dgvptr, &dgvel};
@@ -764,6 +765,7 @@ static int run_prep(Session &S) {
     ENS(S.EChi, sizeof(float) * nE * DIM * dV);
     ENS(S.adetf, sizeof(float) * nE);
     ENS(S.EClo, sizeof(float) * nE * DIM * dV);
+    ENS(S.BCf, sizeof(float) * nE * BC_STRIDE<DIM>);
     ENS(S.labV, sizeof(int) * nV);
     ENS(S.vprob, sizeof(int) * nV);
     ENS(S.counters, sizeof(unsigned long long) * 16);
@@ -773,7 +775,7 @@ static int run_prep(Session &S) {
     k_prep_elements<DIM><<<grid_for(nE, 256), 256, 0, S.st>>>(
         S.T64.get<long long>(), S.labT64.get<long long>(), S.V.get<double>(), S.eoffd.get<int>(),
         S.voffd.get<int>(), S.nProb, nE, S.T32.get<int>(), S.labT.get<int>(), S.eprob.get<int>(),
-        S.EC.get<double>(), S.adet.get<double>(), S.EChi.get<float>(), S.EClo.get<float>(), S.adetf.get<float>()); ++S.nlaunch;
+        S.EC.get<double>(), S.adet.get<double>(), S.EChi.get<float>(), S.EClo.get<float>(), S.adetf.get<float>(), S.BCf.get<float>()); ++S.nlaunch;
     k_prep_vertices<<<grid_for(nV, 256), 256, 0, S.st>>>(S.labV64.get<long long>(), S.voffd.get<int>(),
         S.nProb, nV, S.labV.get<int>(), S.vprob.get<int>()); ++S.nlaunch;
     CK(cudaGetLastError());
@@ -863,7 +865,7 @@ static int run_bfs(Session &S) {
         memset(&a, 0, sizeof(a));
         a.T32 = S.T32.get<int>(); a.labT = S.labT.get<int>(); a.eprob = S.eprob.get<int>();
         a.EC = S.EC.get<double>();
-        a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
+        a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>(); a.BCf = S.BCf.get<float>();
         a.probs = S.prm.get<ProbParams>(); a.nE = nE;
         a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;
         a.vptr = S.vptr.get<long long>(); a.vel = S.vel.get<int>();
@@ -1625,7 +1627,7 @@ static int run_passes(Session &S) {
     memset(&a, 0, sizeof(a));
     a.T32 = S.T32.get<int>(); a.labV = S.labV.get<int>(); a.eprob = S.eprob.get<int>(); a.labT = S.labT.get<int>();
     a.Tv = S.dg_rows ? S.dgT32.get<int>() : a.T32;
-    a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>(); a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>();
+    a.EC = S.EC.get<double>(); a.adet = S.adet.get<double>(); a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>(); a.BCf = S.BCf.get<float>();
     a.adetf = S.adetf.get<float>();
     a.probs = S.prm.get<ProbParams>(); a.out_ptr = S.out_ptr.get<long long>(); a.in_ptr = S.in_ptr.get<long long>();
     a.pB = S.pB.get<int>(); a.inA = S.inA.get<int>(); a.rowptr = S.rowptr.get<long long>(); a.cols = S.cols.get<int>();

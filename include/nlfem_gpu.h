@@ -187,6 +187,12 @@ int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out);
  * iterations); *iterations receives the count. Deterministic. */
 int nlfem_session_solve(nlfem_session *s, int i, const double *f, const double *g, double rtol, int maxit,
                         double *u, int *iterations);
+/* Testing hook of the pair search's visited stamps: sets every search warp's 16-bit stamp epoch
+ * (the next outer element a warp takes uses epoch + 1; after 0xffff the warp clears its stamps
+ * and starts again at 1). Needs one assembly of the session first (NLFEM_ERR_INVALID before).
+ * The epoch must lie above every epoch a warp used since it last cleared its stamps (stale stamps
+ * would otherwise read as visited). */
+int nlfem_session_set_search_epoch(nlfem_session *s, unsigned epoch);
 void nlfem_session_destroy(nlfem_session *s);
 
 /* The interacting pairs (aT, bT) of the BFS, sorted by (aT, bT). Free *pairs with free(). */

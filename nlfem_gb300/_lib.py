@@ -99,6 +99,7 @@ def load():
     l.nlfem_session_assemble_graph.argtypes = [ctypes.c_void_p]
     l.nlfem_session_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tuning)]
     l.nlfem_session_download.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(CSR)]
+    l.nlfem_session_set_search_epoch.argtypes = [ctypes.c_void_p, ctypes.c_uint]
     l.nlfem_session_destroy.argtypes = [ctypes.c_void_p]
     l.nlfem_session_destroy.restype = None
     l.nlfem_pair_list.argtypes = [P, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(_lp)]
@@ -145,7 +146,7 @@ EXPORTED = [
     "nlfem_last_error", "nlfem_device_count", "nlfem_get_stats", "nlfem_stiffness_matrix",
     "nlfem_load_vector", "nlfem_stiffness_batch", "nlfem_csr_free", "nlfem_session_create",
     "nlfem_session_assemble", "nlfem_session_assemble_graph", "nlfem_session_autotune", "nlfem_session_download",
-    "nlfem_session_destroy",
+    "nlfem_session_destroy", "nlfem_session_set_search_epoch",
     "nlfem_pair_list", "nlfem_pair_blocks", "nlfem_method_retriangulate",
     "nlfem_retriangulate_batch", "nlfem_retriangulate_certified_batch", "nlfem_toRef", "nlfem_toPhys", "nlfem_solve2x2",
     "nlfem_par_assemble", "nlfem_load_vector_noalloc", "nlfem_measure_peaks",

@@ -183,12 +183,17 @@ struct BfsArgs {
     unsigned long long *n_amb;
     const ProbParams *probs;
     long long nE;
-    unsigned *visited;       // nwarps * vstride
+    // Per-warp visited stamps (16-bit): a warp marks what it has met for its current outer element
+    // with that element's epoch, a per-warp counter kept across launches in epoch[]. Nothing is
+    // cleared between outer elements or assemblies; when a warp's counter wraps, the warp clears
+    // its own stamps.
+    unsigned short *visited;   // nwarps * vstride: elements
     long long vstride;
-    const long long *vptr;   // vertex -> incident elements (sorted)
+    const long long *vptr;     // vertex -> incident elements (sorted)
     const int *vel;
-    unsigned *vvisited;      // nwarps * vvstride: vertices whose incident elements were seen
+    unsigned short *vvisited;  // nwarps * vvstride: vertices whose incident elements were seen
     long long vvstride;
+    unsigned *epoch;           // nwarps: the last epoch each warp used
     int *queue;              // nwarps * qcap
     long long qcap;
     int *pool;               // pool of bT per aT segment
@@ -197,6 +202,7 @@ struct BfsArgs {
     long long *seg_start;
     int *seg_cnt;
     unsigned long long *n_cand;
+    unsigned long long *work;   // next outer element to hand out (chunks of BFS_CHUNK)
     int *err;                // [0] queue overflow, [1] pool overflow, [2] bad method
     long long *qneed;
 };
@@ -381,6 +387,10 @@ __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, 
 // 32 with no level barrier. With one, the candidates found from aT itself (the elements sharing a
 // vertex with it) take the close rule and are all tested before the walk goes on.
 constexpr int BFS_UNROLL = 4;
+// Outer elements are handed out in chunks of consecutive indices: neighbouring elements (in a mesh
+// numbered with any locality) meet largely the same candidates, so the warp's stamps of the
+// previous element are still in cache for the next one.
+constexpr int BFS_CHUNK = 8;
 
 // 3D searches (barycenter tests, no polygon geometry) fit 64 registers and gain from the doubled
 // residency; the 2D retriangulate test needs more.
@@ -397,15 +407,25 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;   // at most BFS_WARPS
     const long long gw = (long long)blockIdx.x * wpb + wib;
-    const long long nw = (long long)gridDim.x * wpb;
-    unsigned *visited = a.visited + gw * a.vstride;
-    unsigned *vvis = a.vvisited + gw * a.vvstride;
+    unsigned short *visited = a.visited + gw * a.vstride;
+    unsigned short *vvis = a.vvisited + gw * a.vvstride;
+    unsigned ep = a.epoch[gw];
     int *vbuf = s_vbuf[wib];
     int *buf = s_buf[wib];
     int *queue = a.queue + gw * a.qcap;
     double *xs = s_x[wib];
     unsigned long long cand_local = 0;
-    for (long long aT = gw; aT < a.nE; aT += nw) {
+    long long cnext = 0, cend = 0;   // the warp's current chunk of consecutive outer elements
+    for (;;) {
+        if (cnext == cend) {
+            unsigned long long c0 = 0;
+            if (lane == 0) c0 = atomicAdd(a.work, (unsigned long long)BFS_CHUNK);
+            c0 = __shfl_sync(FULL, c0, 0);
+            if (c0 >= (unsigned long long)a.nE) break;
+            cnext = (long long)c0;
+            cend = cnext + BFS_CHUNK < a.nE ? cnext + BFS_CHUNK : a.nE;
+        }
+        const long long aT = cnext++;
         const int lab = a.labT[aT];
         if (lab == 0) {
             if (lane == 0) { a.seg_cnt[aT] = 0; a.seg_start[aT] = 0; }
@@ -414,7 +434,14 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
         const ProbParams P = a.probs[a.eprob[aT]];
         const long long eoff = P.elem_off;
         const long long voff = P.vert_off;
-        const unsigned stamp = (unsigned)aT + 1u;   // unique over all problems
+        ep = (ep + 1u) & 0xffffu;
+        if (ep == 0u) {   // the 16-bit epochs wrapped: clear this warp's stamps
+            for (long long i = lane; i < a.vstride; i += 32) visited[i] = 0;
+            for (long long i = lane; i < a.vvstride; i += 32) vvis[i] = 0;
+            __syncwarp();
+            ep = 1u;
+        }
+        const unsigned short stamp = (unsigned short)ep;
         const double *Ea = &a.EC[aT * DIM * dV];
         float ohi[DIM], olo[DIM];
 #pragma unroll
@@ -587,6 +614,7 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
             }
         }
     }
+    if (lane == 0) a.epoch[gw] = ep;
     cand_local = warp_sum(cand_local);
     if (lane == 0 && cand_local) atomicAdd(a.n_cand, cand_local);
     namb = warp_sum(namb);

@@ -401,6 +401,8 @@ struct Session {
     int prec = 0;
     bool onesided64 = false;   // PM_RETRI pass in FP64 (the mixed path's algorithm, FP64 arithmetic)
     DevBuf vcnt, vptr, vel, adjcnt, xadj, adj;
+    DevBuf stamp_epoch;   // per-warp stamp epochs of the search
+    long long stamp_layout[3] = {0, 0, 0};   // warps, element and vertex stride the stamps were laid out for
     DevBuf visited, vvisited, queue, pool, seg_start, seg_cnt, out_ptr, pA, pB, incnt, in_ptr, inA;
     DevBuf marks, rowcnt, rowptr, cols, acc, tiny, vals, keepcnt, fptr, fcols, fvals;
     DevBuf closelist, scan_tmp, counters, err, facc, ftiny, fd;
@@ -451,7 +453,7 @@ struct Session {
     // every device buffer of the session, in a fixed order
     std::vector<DevBuf *> buffers() {
         return {&T64, &labT64, &V, &labV64, &eoffd, &voffd, &prm, &duffy, &duffyf, &T32, &labT, &eprob,
-                &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited, &vvisited,
+                &EC, &adet, &labV, &vprob, &vcnt, &vptr, &vel, &adjcnt, &xadj, &adj, &visited, &vvisited, &stamp_epoch,
                 &queue, &pool, &seg_start, &seg_cnt, &out_ptr, &pA, &pB, &incnt, &in_ptr, &inA,
                 &marks, &rowcnt, &rowptr, &cols, &acc, &tiny, &vals, &keepcnt, &fptr, &fcols,
                 &fvals, &closelist, &scan_tmp, &counters, &err, &facc, &ftiny, &fd, &out64a, &out64b,
@@ -850,15 +852,30 @@ static int run_bfs(Session &S) {
         }
         S.pool_cap = std::max<long long>((long long)(1.1 * est), 1 << 20);
     }
-    ENS(S.visited, sizeof(unsigned) * (size_t)nwarps * S.maxNE);
-    ENS(S.vvisited, sizeof(unsigned) * (size_t)nwarps * S.maxNV);
+    {   // stamps: zeroed only when first laid out (a new layout or a larger buffer)
+        const size_t be = sizeof(unsigned short) * (size_t)nwarps * S.maxNE;
+        const size_t bv = sizeof(unsigned short) * (size_t)nwarps * S.maxNV;
+        const size_t bw = sizeof(unsigned) * (size_t)nwarps;
+        const bool relayout = be > S.visited.cap || bv > S.vvisited.cap || bw > S.stamp_epoch.cap ||
+                              S.stamp_layout[0] != nwarps || S.stamp_layout[1] != S.maxNE ||
+                              S.stamp_layout[2] != S.maxNV;
+        ENS(S.visited, be);
+        ENS(S.vvisited, bv);
+        ENS(S.stamp_epoch, bw);
+        if (relayout) {
+            CK(cudaMemsetAsync(S.visited.p, 0, be, S.st));
+            CK(cudaMemsetAsync(S.vvisited.p, 0, bv, S.st));
+            CK(cudaMemsetAsync(S.stamp_epoch.p, 0, bw, S.st));
+            S.stamp_layout[0] = nwarps;
+            S.stamp_layout[1] = S.maxNE;
+            S.stamp_layout[2] = S.maxNV;
+        }
+    }
     ENS(S.seg_start, sizeof(long long) * (nE + 1));
     ENS(S.seg_cnt, sizeof(int) * (nE + 1));
     for (int attempt = 0; attempt < 8; attempt++) {
         ENS(S.queue, sizeof(int) * (size_t)nwarps * S.qcap);
         ENS(S.pool, sizeof(int) * (size_t)S.pool_cap);
-        CK(cudaMemsetAsync(S.visited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNE, S.st));
-        CK(cudaMemsetAsync(S.vvisited.p, 0, sizeof(unsigned) * (size_t)nwarps * S.maxNV, S.st));
         CK(cudaMemsetAsync(S.counters.p, 0, sizeof(unsigned long long) * 8, S.st));
         CK(cudaMemsetAsync(S.err.p, 0, sizeof(int) * 4, S.st));
         BfsArgs a;
@@ -867,9 +884,10 @@ static int run_bfs(Session &S) {
         a.EC = S.EC.get<double>();
         a.EChi = S.EChi.get<float>(); a.EClo = S.EClo.get<float>(); a.BCf = S.BCf.get<float>();
         a.probs = S.prm.get<ProbParams>(); a.nE = nE;
-        a.visited = S.visited.get<unsigned>(); a.vstride = S.maxNE;
+        a.visited = S.visited.get<unsigned short>(); a.vstride = S.maxNE;
+        a.epoch = S.stamp_epoch.get<unsigned>();
         a.vptr = S.vptr.get<long long>(); a.vel = S.vel.get<int>();
-        a.vvisited = S.vvisited.get<unsigned>(); a.vvstride = S.maxNV;
+        a.vvisited = S.vvisited.get<unsigned short>(); a.vvstride = S.maxNV;
         a.queue = S.queue.get<int>(); a.qcap = S.qcap;
         a.pool = S.pool.get<int>(); a.pool_cap = S.pool_cap;
         unsigned long long *cnt = S.counters.get<unsigned long long>();
@@ -877,6 +895,7 @@ static int run_bfs(Session &S) {
         a.seg_start = S.seg_start.get<long long>(); a.seg_cnt = S.seg_cnt.get<int>();
         a.err = S.err.get<int>();
         a.n_amb = cnt + 7;
+        a.work = cnt + 3;
         kfn<<<nblocks, BFS_THREADS, 0, S.st>>>(a, S.rule);
         ++S.nlaunch;
         CK(cudaGetLastError());
@@ -2363,6 +2382,17 @@ int nlfem_session_download(nlfem_session *s, int i, nlfem_csr *out) {
 }
 
 void nlfem_session_destroy(nlfem_session *s) { delete s; }
+
+int nlfem_session_set_search_epoch(nlfem_session *s, unsigned epoch) {
+    if (!s) return fail(NLFEM_ERR_INVALID, "null session");
+    Session &S = s->S;
+    const long long nw = S.stamp_layout[0];
+    if (nw <= 0) return fail(NLFEM_ERR_INVALID, "no pair search has run in this session");
+    std::vector<unsigned> h((size_t)nw, epoch & 0xffffu);
+    CK(cudaMemcpyAsync(S.stamp_epoch.p, h.data(), sizeof(unsigned) * (size_t)nw, cudaMemcpyHostToDevice, S.st));
+    CK(cudaStreamSynchronize(S.st));
+    return NLFEM_OK;
+}
 
 // One-shot session on the cached buffers of the previous one-shot call.
 static int session_create_cached(const nlfem_problem *probs, int n, nlfem_session **out) {

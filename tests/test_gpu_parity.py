@@ -819,6 +819,31 @@ def test_mixed_3d_deterministic_and_fp64_pattern(nl):
     assert fro < MIX_TOL and mx < MIX_TOL, (fro, mx)
 
 
+@pytest.mark.parametrize("case", ["retri2d", "bary3d"])
+def test_search_stamp_epochs(nl, case):
+    """The pair search's 16-bit per-warp stamp epochs: later assemblies of a session reuse the
+    stamps uncleared, and a warp whose epoch wraps clears its own stamps; every assembly, normal
+    or replayed from the graph, gives the first one's matrix bit for bit."""
+    from nlfem_gb300 import _lib
+    if case == "retri2d":
+        probs = [(square_mesh(40, 0.1, jitter=0.2, seed=11), KC, conf2d(precision="mixed"))]
+    else:
+        probs = [(cube_mesh(8, 0.1, jitter=0.1, seed=12), {"function": "constant3D", "horizon": 0.2, "outputdim": 1},
+                  conf3d(precision="mixed"))]
+    s = nl.Session(probs)
+    try:
+        assert s.lib.nlfem_session_set_search_epoch(s.h, 5) != 0   # no search has run yet
+        s.assemble()
+        ref = s.download(0)
+        for ep, graph in ((0xfffe, False), (0xfff9, False), (0xfffd, True), (0xfffe, True)):
+            _lib.check(s.lib.nlfem_session_set_search_epoch(s.h, ep))
+            s.assemble(graph=graph)
+            A = s.download(0)
+            assert same_pattern(A, ref) and np.array_equal(A.data, ref.data), (ep, graph)
+    finally:
+        s.close()
+
+
 @pytest.mark.parametrize("case", ["retri_batch", "bary3d", "fractional"])
 def test_session_graph_replay_bitwise(nl, case):
     if case == "retri_batch":

@@ -382,6 +382,7 @@ def run_gpu(args, rank=0, world=1, dist=None):
         "config": config_dict(args, extra, problems),
         "pairs_per_step": int(st["n_pairs"]), "nnz": int(sum(A.nnz for A in A_mixed)),
         "nnz_structural": int(st["nnz_structural"]), "close_pairs": int(st["n_close"]),
+        "device_bytes": int(st["dev_bytes"]),
         "fp64_fallbacks": int(st["n_ambiguous"]), "subtriangles": int(st["n_subtri"]),
         "phase_ms": {"dual+bfs+pairs+color": st["ms_bfs"], "pattern": st["ms_pattern"],
                      "quadrature+scatter": st["ms_quad"], "finish": st["ms_finish"]},

@@ -126,6 +126,7 @@ typedef struct nlfem_stats {
     long n_items_cut;    /* one-sided mixed retriangulate pass: items whose ball cuts the element */
     long slot_map;       /* one-sided passes: matrix slots found by 1 window-rank bitmaps (rows whose
                             column numbers span a narrow range), 2 per-row hash tables, 0 neither */
+    long dev_bytes;      /* device memory the session's buffers hold after the assembly */
 } nlfem_stats;
 
 const char *nlfem_last_error(void);

@@ -62,7 +62,7 @@ class Stats(ctypes.Structure):
                 ("ms_pattern", ctypes.c_double), ("ms_quad", ctypes.c_double),
                 ("ms_finish", ctypes.c_double), ("n_launches", ctypes.c_long),
                 ("n_items_in", ctypes.c_long), ("n_items_cut", ctypes.c_long),
-                ("slot_map", ctypes.c_long)]
+                ("slot_map", ctypes.c_long), ("dev_bytes", ctypes.c_long)]
 
 
 class NlfemError(RuntimeError):

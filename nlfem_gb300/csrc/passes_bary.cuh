@@ -10,9 +10,9 @@
 // Per batch of 32 pairs, the owner lane tests its pair's outer points (FP32 distance with a
 // certified margin, exact FP64 test inside the margin), the (pair, point) items whose ball
 // contains the barycenter are compacted and integrated 32 at a time over the full inner element,
-// and the owner lane folds them in a fixed order. Each pair's integer blocks are balanced so its
-// rows sum to exactly zero (balance_rows). Lanes sharing a partner vertex add their integers;
-// all lanes then share the slot lookups in T's rows.
+// and the owner lane folds them in a fixed order. Only off-diagonal entries are accumulated; the
+// matrix rows sum to zero, and k_row_diag sets the diagonal entries from the row sums. Lanes sharing
+// a partner vertex add their integers; all lanes then share the slot lookups in T's rows.
 #pragma once
 #include "passes_mix.cuh"
 
@@ -30,6 +30,7 @@ struct BaryWarp {
     long long rhb[DIM + 1], rrb[DIM + 1];   // T's rows: hash table start, CSR row start
     unsigned rmask[DIM + 1];            // T's rows: slot map size field (0xffffffff: no row), see RowHash
     int rlo[DIM + 1];                   // T's rows: first window word (window-rank map)
+    int tvs[DIM + 1];                   // T's vertices
 };
 template <int DIM>
 struct BaryEntry {   // one partner vertex of a batch and its integer sums over T's rows
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
             W.rrb[lane] = h.rb;
             W.rmask[lane] = h.mask;
             W.rlo[lane] = h.lo;
+            W.tvs[lane] = a.T32[(long long)T * dV + lane];
         }
         const ProbParams P = a.probs[a.eprob[T]];
         const double *ET64 = &a.EC[(long long)T * DIM * dV];
@@ -263,14 +265,18 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                         for (int t = 0; t < dV; t++) N[dV * r + t] = fmaf(c, rr[1 + t], N[dV * r + t]);
                     }
                 }
-                long long lx[NS];
+                // off-diagonal entries only: every kept row sums to zero (each pair's blocks do),
+                // so k_row_diag sets each diagonal entry to minus its row's other entries, the same
+                // integer a per-pair balance of the block diagonals would give
 #pragma unroll
-                for (int i = 0; i < NS; i++) lx[i] = fx64(2.f * L[i] * rTT, P.fx_mul, bad);
+                for (int r = 0; r < dV; r++)
+#pragma unroll
+                    for (int c = r + 1; c < dV; c++) {
+                        const int i = sym_idx<dV>(r, c);
+                        D[i] += fx64(2.f * L[i] * rTT, P.fx_mul, bad);
+                    }
 #pragma unroll
                 for (int i = 0; i < dV * dV; i++) nx[i] = fx64(2.f * N[i] * rTT, P.fx_mul, bad);
-                balance_rows<dV>(lx, nx, nullptr, nullptr);
-#pragma unroll
-                for (int i = 0; i < NS; i++) D[i] += lx[i];
             }
             // termNonloc into A[T, b] (minus sign): group sums per partner vertex, shared lookups
             __syncwarp();
@@ -322,6 +328,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
                 RowHash h;
                 h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
                 if (h.mask == 0xffffffffu) continue;   // T's vertex r has no row
+                if (slist[e].col == W.tvs[r]) continue;   // the matrix diagonal: from the row sum
                 const long long s = slot_find_row(sm, h, slist[e].col);
                 if (s < 0) miss = true;
                 else red_add(vals, s, -slist[e].v[r]);
@@ -333,7 +340,7 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
         for (int i = 0; i < NS; i++)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) D[i] += (long long)__shfl_xor_sync(FULL, (unsigned long long)D[i], o);
-        if (lane < dV * dV) {
+        if (lane < dV * dV && lane / dV != lane % dV) {   // off-diagonal entries of T's block
             const int r = lane / dV, c = lane % dV;
             RowHash h;
             h.hb = W.rhb[r]; h.rb = W.rrb[r]; h.mask = W.rmask[r]; h.lo = W.rlo[r];
@@ -359,6 +366,26 @@ __global__ void __launch_bounds__(BARY_THREADS) k_pass_bary(MixArgs ma, Rule rul
         if (nsub && a.n_subtri) atomicAdd(a.n_subtri, (unsigned long long)nsub);
         if (namb && a.n_amb) atomicAdd(a.n_amb, (unsigned long long)namb);
         if (nitin && a.n_in) atomicAdd(a.n_in, (unsigned long long)nitin);
+    }
+}
+
+// Completion of the barycenter pass: each row's diagonal entry becomes minus the sum of its other
+// entries (the pass left it out; every kept row sums to zero, rows the pass did not write stay
+// zero). One warp per row.
+__global__ void k_row_diag(const long long *__restrict__ rowptr, const int *__restrict__ cols, long long nrows,
+                           long long *__restrict__ vals) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long t = gw; t < nrows; t += nw) {
+        const long long b = rowptr[t], e = rowptr[t + 1];
+        long long off = 0, dslot = -1;
+        for (long long s = b + lane; s < e; s += 32) {
+            if (cols[s] == (int)t) dslot = s;
+            else off += vals[s];
+        }
+        off = (long long)warp_sum((unsigned long long)off);
+        if (dslot >= 0) vals[dslot] = -off;
     }
 }
 

@@ -326,38 +326,6 @@ __device__ __forceinline__ X sel3(const X *v, int i) {
     return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]);
 }
 
-// Exact row balance of one pair's integer blocks. For kernels of |x - y|, sum_c termLocal[r][c]
-// = sum_c termNonloc[r][c] and sum_c' termLocalPrime[c][c'] = sum_r termNonlocPrime[r][c] hold
-// in exact arithmetic (the basis functions sum to one). The diagonal entries take the rounding,
-// so each of the pair's rows sums to exactly zero and the assembled operator annihilates
-// constants exactly, as the FP64 reference does to rounding.
-template <int dV>
-__device__ __forceinline__ void balance_rows(long long *lx, const long long *nx, long long *lpx,
-                                             const long long *mx) {
-#pragma unroll
-    for (int r = 0; r < dV; r++) {
-        long long s = 0;
-#pragma unroll
-        for (int c = 0; c < dV; c++) s += nx[dV * r + c];
-#pragma unroll
-        for (int c = 0; c < dV; c++)
-            if (c != r) s -= lx[c < r ? sym_idx<dV>(c, r) : sym_idx<dV>(r, c)];
-        lx[sym_idx<dV>(r, r)] = s;
-    }
-    if (lpx) {
-#pragma unroll
-        for (int c = 0; c < dV; c++) {
-            long long s = 0;
-#pragma unroll
-            for (int r = 0; r < dV; r++) s += mx[dV * r + c];
-#pragma unroll
-            for (int q = 0; q < dV; q++)
-                if (q != c) s -= lpx[q < c ? sym_idx<dV>(q, c) : sym_idx<dV>(c, q)];
-            lpx[sym_idx<dV>(c, c)] = s;
-        }
-    }
-}
-
 __device__ __forceinline__ long long shfl64(long long v, int src) {
     return (long long)__shfl_sync(FULL, (unsigned long long)v, src);
 }

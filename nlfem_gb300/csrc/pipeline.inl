@@ -1557,6 +1557,11 @@ static int run_pass_one_sided(Session &S, const PassArgs &pa, const PR &pr, cons
             k_sym_add<<<S.nSM * 16, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), S.tpos.get<int>(), ma.valsN, S.nV, vals); ++S.nlaunch;
             CK(cudaGetLastError());
         }
+        if (S.pmode == PM_BARY) {   // the diagonal entries from the row sums
+            k_row_diag<<<S.nSM * 16, 256, 0, S.st>>>(S.rowptr.get<long long>(), S.cols.get<int>(), S.nV,
+                                                     reinterpret_cast<long long *>(S.vals.p)); ++S.nlaunch;
+            CK(cudaGetLastError());
+        }
         if (S.replay) return NLFEM_OK;   // the overflow flag is checked after the replay
         int ovf = 0;
         int r = d2h(S, &ovf, S.err.get<int>() + 5, 1);
@@ -1773,6 +1778,11 @@ static int run_system_post(Session &S) {
     S.stats.ms_finish = t[3];
     S.stats.ms_total = t[0] + t[1] + t[2] + t[3];
     S.stats.n_launches = (long)S.nlaunch;
+    {
+        size_t held = 0;
+        for (DevBuf *b : S.buffers()) held += b->cap;
+        S.stats.dev_bytes = (long)held;
+    }
     g_stats = S.stats;
     return NLFEM_OK;
 }

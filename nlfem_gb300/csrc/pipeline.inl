@@ -42,8 +42,8 @@ static int ensure(DevBuf &b, size_t bytes, bool no_grow) {
     if (bytes <= b.cap) return NLFEM_OK;
     // a captured sequence cannot allocate; the run before the capture sizes every buffer
     if (no_grow) return fail(NLFEM_ERR_CUDA, "internal: a buffer would grow during graph capture");
+    size_t want = std::max(bytes, (size_t)(b.cap + b.cap / 4));   // a regrown buffer gets 25% headroom
     b.release();
-    size_t want = std::max(bytes, (size_t)(b.cap + b.cap / 4));
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
         cudaGetLastError();

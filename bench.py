@@ -39,11 +39,19 @@ METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel e
 # written); the pass streams its pair list and reuses the mesh from L2, so the traffic grows with
 # the pairs. Reported as roofline.traffic (scaled to this run's pairs) with its source.
 PASS_TRAFFIC_PER_PAIR = {"c2": (187.713e6 + 35.046e6) / 25573871}
-# Algorithmic bytes of the pair search: per candidate the element's stamp (4 B), its incidence entry
-# (4 B), its 12 FP32 coordinates (48 B) and, per 3 candidates, a vertex's stamp and incidence range
-# (about 4 B): 60 B; per pair its queue and pool entries (8 B).
-SEARCH_BYTES_PER_CANDIDATE = 60
+# Algorithmic bytes of the pair search per tested candidate: its 16-bit visited stamp (2 B), its
+# incidence entry (4 B), a share of a vertex's stamp and incidence range (about 4 B) and the
+# geometry its interaction test reads (the element's coordinates as double-float pairs for the
+# retriangulate test, its barycenter's for the barycenter test); per pair, its queue and pool
+# entries (8 B).
+SEARCH_STAMP_BYTES, SEARCH_INCIDENCE_BYTES = 2 + 4, 4
+SEARCH_GEOMETRY_BYTES = {("retriangulate", 2): 2 * 6 * 4, ("baryCenter", 2): 2 * 2 * 4, ("baryCenter", 3): 2 * 3 * 4}
 SEARCH_BYTES_PER_PAIR = 8
+
+
+def search_bytes_per_candidate(conf, dim):
+    geo = SEARCH_GEOMETRY_BYTES.get((conf["approxBalls"]["method"], dim), 2 * (dim + 1) * dim * 4)
+    return SEARCH_STAMP_BYTES + SEARCH_INCIDENCE_BYTES + geo
 
 
 def workload(args, precision):
@@ -78,16 +86,17 @@ def vs_reference(mats, dg):
             "problems_compared": len(res)}
 
 
-def search_roofline(st):
-    """The pair search against HBM: its algorithmic bytes (SEARCH_BYTES_PER_CANDIDATE per tested
+def search_roofline(st, conf, dim):
+    """The pair search against HBM: its algorithmic bytes (search_bytes_per_candidate per tested
     candidate, SEARCH_BYTES_PER_PAIR per pair) over the device time of the search phase (vertex
     incidence, search, pair compaction)."""
     hbm = measured_peaks().get("hbm_gbs")
     ms = st["ms_bfs"]
-    nbytes = SEARCH_BYTES_PER_CANDIDATE * st["n_candidates"] + SEARCH_BYTES_PER_PAIR * st["n_pairs"]
+    per_cand = search_bytes_per_candidate(conf, dim)
+    nbytes = per_cand * st["n_candidates"] + SEARCH_BYTES_PER_PAIR * st["n_pairs"]
     gbs = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else None
     return {"bound": "hbm", "kernel": "k_bfs (one warp per outer element)", "candidates": int(st["n_candidates"]),
-            "algorithmic_bytes": int(nbytes), "ms": ms, "achieved": gbs, "peak": hbm, "unit": "GB/s",
+            "bytes_per_candidate": per_cand, "algorithmic_bytes": int(nbytes), "ms": ms, "achieved": gbs, "peak": hbm, "unit": "GB/s",
             "frac": (gbs / hbm) if (gbs and hbm) else None,
             "note": "latency bound (dependent stamp and incidence loads per step), not bandwidth bound"}
 
@@ -399,7 +408,7 @@ def run_gpu(args, rank=0, world=1, dist=None):
                              "quadrature phase; peak = FP32 FMA throughput measured in this run (of measured); "
                              "CUDA-core bound path with no GEMM-shaped work, so neither the tensor-core nor the "
                              "HBM peak applies"},
-        "search": search_roofline(st),
+        "search": search_roofline(st, conf0, int(problems[0][0]["vertices"].shape[1])),
         "peaks_measured": {"fp32_tflops": peak32, "fp64_tflops": peak64,
                            "hbm_gbs": measured_peaks().get("hbm_gbs")},
         "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

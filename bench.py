@@ -34,11 +34,16 @@ import numpy as np
 
 METRIC = "element-pair quadratures/s: mixed vs FP64 on one GB300 at <=1e-6 rel err"
 
-# DRAM traffic (read + write bytes) per pair of the k_pass_mix2d<0> launch, from an ncu capture of
-# that launch on the 2D constant-kernel workload at n = 128 (2.56e7 pairs: 187.0 MB read, 34.6 MB
-# written); the pass streams its pair list and reuses the mesh from L2, so the traffic grows with
-# the pairs. Reported as roofline.traffic (scaled to this run's pairs) with its source.
-PASS_TRAFFIC_PER_PAIR = {"c2": (187.713e6 + 35.046e6) / 25573871}
+# DRAM traffic (read + write bytes) per pair of the quadrature pass, from an ncu capture of one
+# launch on a smaller case of the workload: k_pass_mix2d<0> on the 2D constant-kernel workload at
+# n = 128 (2.56e7 pairs: 187.7 MB read, 35.0 MB written), k_pass_bary<3> on the 3D one at n = 24
+# (2.59e7 pairs: 143.7 MB read, 8.2 MB written). The passes stream their pair lists and reuse the
+# mesh from L2, so the traffic grows with the pairs. Reported as roofline.traffic (scaled to this
+# run's pairs) with its source.
+PASS_TRAFFIC = {
+    "c2": ((187.713e6 + 35.046e6) / 25573871, "k_pass_mix2d<0> on the 2D constant-kernel workload at n=128 (2.56e7 pairs)"),
+    "c4": ((143.728e6 + 8.242e6) / 25852104, "k_pass_bary<3> on the 3D constant-kernel workload at n=24 (2.59e7 pairs)"),
+}
 # Algorithmic bytes of the pair search per tested candidate: its 16-bit visited stamp (2 B), its
 # incidence entry (4 B), a share of a vertex's stamp and incidence range (about 4 B) and the
 # geometry its interaction test reads (the element's coordinates as double-float pairs for the
@@ -397,11 +402,12 @@ def run_gpu(args, rank=0, world=1, dist=None):
                      "quadrature+scatter": st["ms_quad"], "finish": st["ms_finish"]},
         "roofline": {"bound": "fp32", "kernel": kname,
                      "achieved": achieved, "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
-                     "traffic": (PASS_TRAFFIC_PER_PAIR[args.workload] * st["n_pairs"]
-                                 if args.workload in PASS_TRAFFIC_PER_PAIR else None),
-                     "traffic_source": "ncu DRAM bytes of this kernel's launch on the 2D constant-kernel workload "
-                                       "at n=128 (2.56e7 pairs), scaled by this run's pairs (not measured in this "
-                                       "run)",
+                     "traffic": (PASS_TRAFFIC[args.workload][0] * st["n_pairs"]
+                                 if args.workload in PASS_TRAFFIC and args.delta == 0.1 else None),
+                     "traffic_source": ("ncu DRAM bytes of one launch of " + PASS_TRAFFIC[args.workload][1] +
+                                        ", scaled by this run's pairs (not measured in this run)"
+                                        if args.workload in PASS_TRAFFIC and args.delta == 0.1 else
+                                        "no ncu capture of this workload's pass"),
                      "note": "achieved = flops of the algorithm that ran for the step (FLOP model in "
                              "bench.algorithmic_flops: the reference's inner-point loops, or their closed forms "
                              "for constant kernels; FP64 close pairs not counted) / device time of the "

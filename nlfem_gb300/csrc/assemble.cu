@@ -387,9 +387,9 @@ __device__ __forceinline__ bool bfs_test(const BfsArgs &a, const ProbParams &P, 
 // 32 with no level barrier. With one, the candidates found from aT itself (the elements sharing a
 // vertex with it) take the close rule and are all tested before the walk goes on.
 constexpr int BFS_UNROLL = 4;
-// Outer elements are handed out in chunks of consecutive indices: neighbouring elements (in a mesh
-// numbered with any locality) meet largely the same candidates, so the warp's stamps of the
-// previous element are still in cache for the next one.
+// Outer elements are handed out in chunks of consecutive indices (at most BFS_CHUNK, fewer near
+// the end): neighbouring elements (in a mesh numbered with any locality) meet largely the same
+// candidates, so the warp's stamps of the previous element are still in cache for the next one.
 constexpr int BFS_CHUNK = 8;
 
 // 3D searches (barycenter tests, no polygon geometry) fit 64 registers and gain from the doubled
@@ -419,11 +419,22 @@ __global__ void __launch_bounds__(BFS_THREADS, DIM == 3 ? 4 : 2) k_bfs(BfsArgs a
     for (;;) {
         if (cnext == cend) {
             unsigned long long c0 = 0;
-            if (lane == 0) c0 = atomicAdd(a.work, (unsigned long long)BFS_CHUNK);
+            long long ch = 1;
+            if (lane == 0) {
+                // guided: chunks shrink to one element as the work runs out, so warps finish
+                // together (an element costs a warp about a millisecond at C2); the counter read
+                // may be stale, which only changes a chunk's size
+                const long long rem = a.nE - (long long)*(volatile unsigned long long *)a.work;
+                const long long nw = (long long)gridDim.x * wpb;
+                ch = rem / (2 * nw);
+                ch = ch < 1 ? 1 : (ch > BFS_CHUNK ? BFS_CHUNK : ch);
+                c0 = atomicAdd(a.work, (unsigned long long)ch);
+            }
             c0 = __shfl_sync(FULL, c0, 0);
+            ch = __shfl_sync(FULL, ch, 0);
             if (c0 >= (unsigned long long)a.nE) break;
             cnext = (long long)c0;
-            cend = cnext + BFS_CHUNK < a.nE ? cnext + BFS_CHUNK : a.nE;
+            cend = cnext + ch < a.nE ? cnext + ch : a.nE;
         }
         const long long aT = cnext++;
         const int lab = a.labT[aT];

@@ -191,8 +191,8 @@ int nlfem_session_solve(nlfem_session *s, int i, const double *f, const double *
 /* Testing hook of the pair search's visited stamps: sets every search warp's 16-bit stamp epoch
  * (the next outer element a warp takes uses epoch + 1; after 0xffff the warp clears its stamps
  * and starts again at 1). Needs one assembly of the session first (NLFEM_ERR_INVALID before).
- * The epoch must lie above every epoch a warp used since it last cleared its stamps (stale stamps
- * would otherwise read as visited). */
+ * The epoch must lie above every epoch any warp used since it last cleared its stamps (stale
+ * stamps would otherwise read as visited): move it forward once, then let assemblies run. */
 int nlfem_session_set_search_epoch(nlfem_session *s, unsigned epoch);
 void nlfem_session_destroy(nlfem_session *s);
 

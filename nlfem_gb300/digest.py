@@ -1,8 +1,8 @@
 """Digests of assembled matrices: compact, size-independent fingerprints for full-size checks.
 
-A full-size stiffness matrix (C2: 7.75e7 entries) is too large to keep as a fixture, so the
-reference assembly of each workload is stored as a digest (tests/golden/digest_*.npz), and a
-matrix assembled elsewhere is compared with it:
+A full-size stiffness matrix (7.75e7 entries for 2·256² triangles at delta = 0.1) is too large to
+keep as a fixture, so the reference assembly of each workload is stored as a digest
+(tests/golden/digest_*.npz), and a matrix assembled elsewhere is compared with it:
 * pattern: SHA-256 of the sorted CSR row pointers and column indices (int64) - bit-exact check;
 * fro / maxabs: Frobenius norm and largest |entry| of the reference matrix;
 * Au: the reference matrix applied to a seeded Gaussian vector u. For a difference D of two

@@ -10,7 +10,7 @@ workloads here, in both precisions:
   max-entry error over the sampled rows <= 1e-12 (rounding only: the GPU sums in another order);
 * mixed path: both <= 1e-6;
 * load vector: <= 1e-12 (max entry, relative).
-C5's FP64 check covers every eighth problem (its batch matrices equal the single assemblies bit
+The 64-problem batch's FP64 check covers every eighth problem (its batch matrices equal the single assemblies bit
 for bit, a property the parity tests check); the mixed check covers all 64. A batch digest may hold
 only the first problems of the batch (meta problems_done); the checks cover the problems it holds.
 """

@@ -3,7 +3,8 @@
  * Drop-in boundary for nlfem's assembly path. Every entry point takes plain pointers and
  * sizes (row-major, int64 indices as the reference's `long`), returns an nlfem status code
  * instead of aborting, and runs its arithmetic on the GPU (sm_103a). No CPU fallback exists:
- * without a usable CUDA device every compute entry point returns NLFEM_ERR_CUDA.
+ * without a usable CUDA device every compute entry point returns NLFEM_ERR_CUDA (after the host
+ * checks of its problems, which report a refused configuration as such on any machine).
  *
  * Reference interfaces replaced (cagau/nlfem):
  *   nlfem_par_assemble        <- par_assemble         include/Cassemble.h:125-140,

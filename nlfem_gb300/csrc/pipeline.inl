@@ -174,6 +174,18 @@ static int set_fx_unit(ProbParams &P, int widen) {
     return NLFEM_OK;
 }
 
+// Number of subdomains elements a and b share: the sorted-merge intersection of their indicator
+// rows (evaluateZeta, mathhelpers.cpp:19-37).
+static long zeta_common(const long *idx, const long *ptr, long a, long b) {
+    long i = ptr[a], ie = ptr[a + 1], j = ptr[b], je = ptr[b + 1], n = 0;
+    while (i < ie && j < je) {
+        if (idx[i] < idx[j]) i++;
+        else if (idx[j] < idx[i]) j++;
+        else { n++; i++; j++; }
+    }
+    return n;
+}
+
 static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
     memset(&P, 0, sizeof(P));
     if (p.dim != 2 && p.dim != 3) return fail(NLFEM_ERR_INVALID, "Dimension is not equal to 2 or 3.");
@@ -197,6 +209,14 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
             return fail(NLFEM_ERR_INVALID, "The fractional and fractional_weakSingular integration routines are meant for close elements only.");
         std::string kn(p.kernel);
         const bool proto = kn == "linearPrototypeMicroelastic";
+        // chk_Conf (checks.cpp:105-113)
+        if (P.close == MTH_FRACTIONAL && p.is_dg)
+            return fail(NLFEM_ERR_INVALID, "The fractional integration routine cannot be used for DG ansatz spaces. Try "
+                                           "using the weakSingular integration routine if your singularity is of degree "
+                                           "2+2s for s<=0.5.");
+        if ((proto || kn == "linearPrototypeMicroelasticField") && p.fractional_s != -0.5)
+            return fail(NLFEM_ERR_INVALID, "The fractional_s corresponding to the linearPrototypeMicroelastic kernels is "
+                                           "s=-0.5, as 2+2s = 1. Please set fractional_s.");
         P.singular = (kn == "fractional") || proto || P.kernel == KER_MICROFIELD;   // Cassemble.cpp:89-94
         if (kernel_outdim(P.kernel) != p.outdim)
             return fail(NLFEM_ERR_INVALID, std::string("kernel ") + kn + " has " + std::to_string(kernel_outdim(P.kernel)) +
@@ -283,6 +303,13 @@ static int make_params(const nlfem_problem &p, bool system, ProbParams &P) {
         if (p.zeta_indptr[0] != 0) return fail(NLFEM_ERR_INVALID, "zeta indicator: row pointers must start at 0");
         for (long e = 0; e < p.nE; e++)
             if (p.zeta_indptr[e + 1] < p.zeta_indptr[e]) return fail(NLFEM_ERR_INVALID, "zeta indicator: decreasing row pointers");
+        if (system) {   // chk_Mesh (checks.cpp:74-84): the first 20 elements share a subdomain pairwise
+            const long m = std::min<long>(p.nE, 20);
+            for (long k = 0; k < m; k++)
+                for (long j = 0; j < m; j++)
+                    if (zeta_common(p.zeta_indices, p.zeta_indptr, k, j) == 0)
+                        return fail(NLFEM_ERR_INVALID, "Some rows Zeta(k).dot(Zeta(j)) evaluate to zero.");
+        }
         P.zeta = 1;
     }
     // fixed-point scale: typical magnitude of an entry
@@ -523,12 +550,11 @@ static int d2h(Session &S, T *host, const T *dev, size_t n) {
     return NLFEM_OK;
 }
 
+static int device_ok();
+
+// Host checks of the problems first (they need no device, so a configuration error is reported as
+// such on any machine), then the device: stream, events, uploads.
 static int session_init(Session &S, const nlfem_problem *probs, int n, bool system) {
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&S.nSM, cudaDevAttrMultiProcessorCount, dev));
-    CK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
-    for (int i = 0; i < 8; i++) CK(cudaEventCreate(&S.ev[i]));
     S.system = system;
     S.nProb = n;
     S.dim = probs[0].dim;
@@ -596,6 +622,15 @@ static int session_init(Session &S, const nlfem_problem *probs, int n, bool syst
                                                    "without domain-decomposition weights");
             S.pmode = PM_RETRI;
         }
+    }
+    r = device_ok();
+    if (r) return r;
+    {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&S.nSM, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
+        for (int i = 0; i < 8; i++) CK(cudaEventCreate(&S.ev[i]));
     }
     const int dV = S.dV, dim = S.dim;
     ENS(S.T64, sizeof(long long) * S.nE * dV);
@@ -2350,11 +2385,9 @@ int nlfem_session_download32(nlfem_session *s, int i, nlfem_csr32 *out) {
 
 int nlfem_session_create(const nlfem_problem *probs, int n, nlfem_session **out) {
     if (!probs || n <= 0 || !out) return fail(NLFEM_ERR_INVALID, "no problems");
-    int r = device_ok();
-    if (r) return r;
     nlfem_session *s = new nlfem_session();
     s->probs.assign(probs, probs + n);
-    r = session_init(s->S, probs, n, true);
+    int r = session_init(s->S, probs, n, true);
     if (!r) tune_apply(s->S);
     if (!r) r = session_upload(s->S, probs);
     if (!r) { cudaError_t e = cudaStreamSynchronize(s->S.st); if (e != cudaSuccess) r = fail(NLFEM_ERR_CUDA, cudaGetErrorString(e)); }
@@ -2407,12 +2440,10 @@ int nlfem_session_set_search_epoch(nlfem_session *s, unsigned epoch) {
 // One-shot session on the cached buffers of the previous one-shot call.
 static int session_create_cached(const nlfem_problem *probs, int n, nlfem_session **out) {
     if (!probs || n <= 0 || !out) return fail(NLFEM_ERR_INVALID, "no problems");
-    int r = device_ok();
-    if (r) return r;
     nlfem_session *s = new nlfem_session();
     cache_take(s->S);
     s->probs.assign(probs, probs + n);
-    r = session_init(s->S, probs, n, true);
+    int r = session_init(s->S, probs, n, true);
     if (!r) r = session_upload(s->S, probs);
     if (r) { cache_give(s->S); delete s; return r; }
     *out = s;
@@ -2470,10 +2501,8 @@ int nlfem_stiffness_matrix(const nlfem_problem *prob, nlfem_csr *out) {
 
 int nlfem_load_vector(const nlfem_problem *prob, double *fd) {
     if (!prob || !fd) return fail(NLFEM_ERR_INVALID, "null argument");
-    int r = device_ok();
-    if (r) return r;
     Session S;
-    r = session_init(S, prob, 1, false);
+    int r = session_init(S, prob, 1, false);
     if (!r) r = session_upload(S, prob);
     if (!r) r = (S.dim == 2) ? run_forcing_t<2>(S) : run_forcing_t<3>(S);
     if (!r) r = d2h(S, fd, S.fd.get<double>(), (size_t)S.od * S.nV);

@@ -46,6 +46,17 @@ def cube_mesh(n, delta=0.1, jitter=0.0, seed=0):
     return meshes.mesh_dict(v, e, l)
 
 
+def labeled_mesh(n=14, seed=5):
+    """Omega split into labels 3 (x0 < 0.5) and 4, the layer -1, all moved by -0.5 so that the
+    notch {x1 = 0, x0 > 0} cuts the right half. Every label pair is a case of the labeled kernel
+    (10 lx + ly in {-11, -7, -6, 9, 29, 33, 34, 39, 43, 44}); 3 + 4 = 7 closes labeledNotch."""
+    from nlfem_gb300 import meshes
+    v, e, l = meshes.regular_square(n, 0.1, jitter=0.1, seed=seed)
+    bx = v[e].mean(axis=1)[:, 0]
+    lab = np.where(l > 0, np.where(bx < 0.5, 3, 4), -1)
+    return meshes.mesh_dict(v - 0.5, e, lab)
+
+
 def rel_errors(A, B):
     """Relative Frobenius and max-entry errors of A against the reference B."""
     D = (A - B).tocsr()

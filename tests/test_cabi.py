@@ -69,12 +69,52 @@ def test_evaluate_mass_no_cpu_fallback_and_checks(lib):
 
 
 def test_invalid_configuration_is_reported(lib):
+    """The problems' host checks run before device discovery: a configuration error has its own
+    code on any machine."""
     from nlfem_gb300 import nlfem, _lib
-    if lib.nlfem_device_count() == 0:
-        pytest.skip("configuration checks run after device discovery")
     m = square_mesh(4)
-    with pytest.raises(_lib.NlfemError):
+    with pytest.raises(_lib.NlfemError) as e:
         nlfem.stiffnessMatrix(m, {"function": "nope", "horizon": 0.1, "outputdim": 1}, conf2d())
+    assert e.value.code == 4
+    with pytest.raises(_lib.NlfemError) as e:   # chk_Conf: 3D takes the barycenter rule only
+        from conftest import cube_mesh
+        nlfem.stiffnessMatrix(cube_mesh(2), {"function": "constant3D", "horizon": 0.3, "outputdim": 1}, conf2d())
+    assert e.value.code == 1
+
+
+def _zeta(m, rows):
+    import scipy.sparse as sp
+    indptr = np.cumsum([0] + [len(r) for r in rows])
+    m = dict(m)
+    m["nZeta"] = 2
+    m["ZetaIndicator"] = sp.csr_matrix((np.ones(indptr[-1]), np.concatenate(rows).astype(np.int64), indptr),
+                                       shape=(len(rows), 2))
+    return m
+
+
+def test_zeta_subdomain_check(lib):
+    """chk_Mesh (checks.cpp:74-84): the first 20 elements must share a subdomain pairwise, or the
+    reference aborts; here the library refuses with NLFEM_ERR_INVALID and the reference's words,
+    before it looks for a device. The load vector has no such check (the reference runs chk_Mesh
+    for the system only)."""
+    from nlfem_gb300 import nlfem, _lib
+    m = square_mesh(6, 0.1)
+    nE = m["elements"].shape[0]
+    ker = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    split = [[0] if e % 2 == 0 else [1] for e in range(nE)]   # elements 0 and 1 share none
+    with pytest.raises(_lib.NlfemError, match="Zeta") as e:
+        nlfem.stiffnessMatrix(_zeta(m, split), ker, conf2d())
+    assert e.value.code == 1
+    late = [[0, 1] if e < 20 else ([0] if e % 2 == 0 else [1]) for e in range(nE)]   # only later elements split
+    ok = [_zeta(m, late), dict(m)]
+    if lib.nlfem_device_count() == 0:
+        for mm in ok:
+            with pytest.raises(_lib.NlfemError) as e:
+                nlfem.stiffnessMatrix(mm, ker, conf2d())
+            assert e.value.code == 2   # past the host checks: no device
+        with pytest.raises(_lib.NlfemError) as e:
+            nlfem.loadVector(_zeta(m, split), {"function": "linear"}, conf2d())
+        assert e.value.code == 2
 
 
 def test_outdim_mismatch_raises_valueerror():
@@ -83,3 +123,23 @@ def test_outdim_mismatch_raises_valueerror():
     m["outdim"] = 2
     with pytest.raises(ValueError):
         nlfem.stiffnessMatrix(m, {"function": "constant", "horizon": 0.1, "outputdim": 1}, conf2d())
+
+
+def test_reference_configuration_checks(lib):
+    """chk_Conf (checks.cpp:105-113), where the reference aborts: the fractional close rule with the
+    DG ansatz, and the prototype microelastic kernels with fractional_s other than -0.5. Refused
+    with NLFEM_ERR_INVALID before any device work."""
+    from nlfem_gb300 import nlfem, _lib
+    m = square_mesh(4, 0.2)
+    frac = {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4}
+    c = conf2d(close="fractional", deg=3)
+    c["ansatz"] = "DG"
+    with pytest.raises(_lib.NlfemError, match="cannot be used for DG") as e:
+        nlfem.stiffnessMatrix(dict(m), frac, c)
+    assert e.value.code == 1
+    for name, od in (("linearPrototypeMicroelastic", 1), ("linearPrototypeMicroelasticField", 2)):
+        k = {"function": name, "horizon": 0.2, "outputdim": od, "fractional_s": 0.4}
+        mm = dict(m, outdim=od)
+        with pytest.raises(_lib.NlfemError, match="Please set fractional_s") as e:
+            nlfem.stiffnessMatrix(mm, k, conf2d(close="fractional", deg=3))
+        assert e.value.code == 1

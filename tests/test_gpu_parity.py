@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from conftest import conf2d, conf3d, square_mesh, cube_mesh, rel_errors, same_pattern
+from conftest import conf2d, conf3d, square_mesh, cube_mesh, labeled_mesh, rel_errors, same_pattern
 
 pytestmark = pytest.mark.gpu
 
@@ -159,10 +159,11 @@ def test_mixed_no_caps(nl, orc):
 def test_domain_decomposition_weights(nl, orc, prec):
     """Domain decomposition (Cassemble.cpp:649-657): every pair's blocks weighted by 1 / the number
     of subdomains its elements share. Two subdomains overlap in a strip wider than the ball, so
-    every interacting pair shares one."""
+    every interacting pair shares one; the first 20 elements lie in both (chk_Mesh, checks.cpp:74-84,
+    requires them to share one pairwise)."""
     m = square_mesh(14, 0.1, jitter=0.1, seed=8)
     x = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
-    rows = [[0] if xi < 0.3 else ([1] if xi > 0.7 else [0, 1]) for xi in x]
+    rows = [[0, 1] if e < 20 else ([0] if xi < 0.3 else ([1] if xi > 0.7 else [0, 1])) for e, xi in enumerate(x)]
     indptr = np.cumsum([0] + [len(r) for r in rows])
     Z = sp.csr_matrix((np.ones(indptr[-1]), np.concatenate(rows), indptr), shape=(len(rows), 2))
     m["nZeta"] = 2
@@ -194,15 +195,7 @@ def test_pair_blocks_match_oracle(nl, orc):
 LABEL_KERNELS = ["labeled", "notch", "labeledNotch", "labeledValve", "constantTruncated"]
 
 
-def _labeled_mesh(n=14, seed=5):
-    """Omega split into labels 3 (x0 < 0.5) and 4, the layer -1, all moved by -0.5 so that the
-    notch {x1 = 0, x0 > 0} cuts the right half. Every label pair is a case of the labeled kernel
-    (10 lx + ly in {-11, -7, -6, 9, 29, 33, 34, 39, 43, 44}); 3 + 4 = 7 closes labeledNotch."""
-    from nlfem_gb300 import meshes
-    v, e, l = meshes.regular_square(n, 0.1, jitter=0.1, seed=seed)
-    bx = v[e].mean(axis=1)[:, 0]
-    lab = np.where(l > 0, np.where(bx < 0.5, 3, 4), -1)
-    return meshes.mesh_dict(v - 0.5, e, lab)
+_labeled_mesh = labeled_mesh
 
 
 @pytest.mark.parametrize("name,method", [(k, "retriangulate") for k in LABEL_KERNELS] + [("labeledValve", "baryCenter"), ("notch", "baryCenter")])
@@ -330,11 +323,12 @@ def test_dg_matches_oracle(nl, orc, kname, method):
     assert np.abs(S - C.toarray()).max() <= 1e-12 * abs(C).max()
 
 
-@pytest.mark.parametrize("close,kname", [("fractional", "fractional"), ("weakSingular", "linearPrototypeMicroelastic")])
+@pytest.mark.parametrize("close,kname", [("weakSingular", "fractional"), ("weakSingular", "linearPrototypeMicroelastic")])
 def test_dg_singular_kernels(nl, orc, close, kname):
-    """DG with a singular kernel: the close pairs (sharing a vertex) take the Duffy rule, found on
-    the vertex table while the rows are element DOFs (Cassemble.cpp:580-585, integration.cpp:82-288);
-    against the oracle, and summed over the vertex copies against the CG assembly."""
+    """DG with a singular kernel: the close pairs (sharing a vertex) take the weakSingular Duffy rule
+    (the reference refuses the fractional rule for DG, checks.cpp:105-107), found on the vertex
+    table while the rows are element DOFs (Cassemble.cpp:580-585, integration.cpp:82-185); against
+    the oracle, and summed over the vertex copies against the CG assembly."""
     m = square_mesh(8, 0.2, jitter=0.1, seed=16)
     s = 0.4 if kname == "fractional" else -0.5
     k = {"function": kname, "horizon": 0.2, "outputdim": 1, "fractional_s": s}

@@ -21,7 +21,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from conftest import conf2d, conf3d, cube_mesh, same_pattern, square_mesh
+from conftest import conf2d, conf3d, cube_mesh, labeled_mesh, same_pattern, square_mesh
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
@@ -135,3 +135,88 @@ def test_load_vector_with_zeta_weights_equals_reference():
     fr = ref.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
     fo = oracle.assemble(m, None, conf2d(), compute="forcing", load={"function": "linear"})["f"]
     assert _bitwise(fr, fo)
+
+
+def test_zeta_weighted_matrix_equals_reference():
+    """The system's 1 / zeta(aT, bT) weights (Cassemble.cpp:648-657) in the restatement, on the
+    domain decomposition of the GPU test (two subdomains overlapping in a strip wider than the
+    ball; the first 20 elements in both, as chk_Mesh requires)."""
+    from oracle import oracle, ref
+    m = square_mesh(14, 0.1, jitter=0.1, seed=8)
+    x = m["vertices"][m["elements"]].mean(axis=1)[:, 0]
+    rows = [[0, 1] if e < 20 else ([0] if xi < 0.3 else ([1] if xi > 0.7 else [0, 1])) for e, xi in enumerate(x)]
+    indptr = np.cumsum([0] + [len(r) for r in rows])
+    Z = sp.csr_matrix((np.ones(indptr[-1]), np.concatenate(rows), indptr), shape=(len(rows), 2))
+    m = dict(m, nZeta=2, ZetaIndicator=Z)
+    kc = {"function": "constant", "horizon": 0.1, "outputdim": 1}
+    R = ref.assemble(m, kc, conf2d())["A"]
+    O = oracle.assemble(m, kc, conf2d())["A"]
+    R.sort_indices(); O.sort_indices()
+    assert same_pattern(R, O)
+    assert _bitwise(R.data, O.data)
+
+
+def _bridges():
+    from nlfem_gb300.meshes import mesh_dict
+    m = square_mesh(14, 0.1, jitter=0.1, seed=5)
+    lab = m["elementLabels"].copy()
+    lab[40:60] = 0
+    return mesh_dict(m["vertices"], m["elements"], lab)
+
+
+def _dg(close, kname, s):
+    c = conf2d(close=close, deg=3)
+    c["ansatz"] = "DG"
+    return (square_mesh(8, 0.2, jitter=0.1, seed=16), {"function": kname, "horizon": 0.2, "outputdim": 1, "fractional_s": s}, c)
+
+
+def _field(kname, conf, seed, s=None):
+    k = {"function": kname, "horizon": 0.2, "outputdim": 2}
+    if s is not None:
+        k["fractional_s"] = s
+    return (square_mesh(8, 0.2, jitter=0.1, seed=seed), k, conf)
+
+
+WIDENED = {
+    # label-0 elements searched through, never paired (Cassemble.cpp:611-633)
+    "bridges": lambda: (_bridges(), {"function": "constant", "horizon": 0.1, "outputdim": 1}, conf2d()),
+    "bary2d": lambda: (square_mesh(14, 0.15, jitter=0.2, seed=4), {"function": "parabola", "horizon": 0.15, "outputdim": 1},
+                       conf2d(method="baryCenter")),
+    "fullsearch": lambda: (square_mesh(10, 0.1, jitter=0.1, seed=3), {"function": "constant", "horizon": 0.1, "outputdim": 1},
+                           dict(conf2d(), is_fullConnectedComponentSearch=1)),
+    "weaksing": lambda: (square_mesh(8, 0.2, jitter=0.1, seed=6),
+                         {"function": "fractional", "horizon": 0.2, "outputdim": 1, "fractional_s": 0.4},
+                         conf2d(close="weakSingular", deg=3)),
+    "prototype": lambda: (square_mesh(8, 0.2, jitter=0.1, seed=6),
+                          {"function": "linearPrototypeMicroelastic", "horizon": 0.2, "outputdim": 1, "fractional_s": -0.5},
+                          conf2d(close="fractional", deg=3)),
+    "dg_weak_fractional": lambda: _dg("weakSingular", "fractional", 0.4),
+    "dg_weak_prototype": lambda: _dg("weakSingular", "linearPrototypeMicroelastic", -0.5),
+    "field_weak": lambda: _field("linearPrototypeMicroelasticField", conf2d(close="weakSingular", deg=3), 23, -0.5),
+    "constfield_bary": lambda: _field("constantField", conf2d(method="baryCenter"), 24),
+}
+for _r in ("retriangulate_unsymm", "subSetBall", "averageBall", "baryCenterRT", "noTruncation"):
+    WIDENED["rule_" + _r] = (lambda r: lambda: (square_mesh(12, 0.12, jitter=0.15, seed=17),
+                                                {"function": "parabola", "horizon": 0.12, "outputdim": 1},
+                                                conf2d(method=r)))(_r)
+for _k in ("labeled", "notch", "labeledNotch", "labeledValve", "constantTruncated"):
+    WIDENED["kernel_" + _k] = (lambda k: lambda: (labeled_mesh(10, 6), {"function": k, "horizon": 0.1, "outputdim": 1},
+                                                  conf2d()))(_k)
+
+
+@pytest.mark.parametrize("case", sorted(WIDENED))
+def test_widened_rows_equal_reference(case):
+    """The restatement against the reference's own C++ on every configuration beyond the headline
+    rules that the GPU tests compare with it: label-0 bridges, the 2D barycenter rule, the full
+    component search, the weakSingular close rule, the prototype microelastic kernel, DG with
+    singular kernels, vector-valued kernels, the further ball rules and the label- and
+    position-dependent kernels. Bit for bit, single-threaded."""
+    from oracle import oracle, ref
+    mesh, kernel, conf = WIDENED[case]()
+    if int(kernel.get("outputdim", 1)) > 1:
+        mesh = dict(mesh, outdim=int(kernel["outputdim"]))
+    R = ref.assemble(mesh, kernel, conf)["A"]
+    O = oracle.assemble(mesh, kernel, conf)["A"]
+    R.sort_indices(); O.sort_indices()
+    assert same_pattern(R, O)
+    assert _bitwise(R.data, O.data)
